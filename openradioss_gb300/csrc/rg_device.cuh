@@ -1,0 +1,143 @@
+// Device-side data structures shared by the kernels of the explicit cycle.
+//
+// Layout in HBM (structure of arrays, one context = one model):
+//   nodes  : dbl4 X4[n] = {x, y, z, MS},  dbl4 V4[n] = {vx, vy, vz, code}
+//            dbl4 D4[n] = {dx, dy, dz, 0}; shells add VR4 = {vrx, vry, vrz, IN}
+//            -- one 32-byte sector per node record, read with two 16-byte loads.
+//   hexa   : int32 NC[8][NE] and IADS[8][NE] (0-based), state arrays
+//            SIG[6][NE], EINT, RHO, QVIS, OFF, VOL0, PLA, EPSD, EHOU.
+//   slots  : FSKY[LSKY] = {fx, fy, fz, sti} (dbl4 in the FP64 form, float4
+//            in the mixed form), FSKYR[LSKY] = {mx, my, mz, stir} for shells.
+//   skyline: ADSKY[n+1] (0-based) -- node n sums slots ADSKY[n]..ADSKY[n+1]-1
+//            in that order, the PARITH/ON order of ASSPAR4.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rg_constants.h"
+
+namespace rg {
+
+// 32-byte aligned node / slot records (one DRAM sector each).
+typedef double4_32a dbl4;
+__host__ __device__ __forceinline__ dbl4 mk4(double x, double y, double z,
+                                             double w) {
+  dbl4 t;
+  t.x = x;
+  t.y = y;
+  t.z = z;
+  t.w = w;
+  return t;
+}
+
+// RESOL time-step scalars, resident on the device so that cycles chain
+// without host round trips (engine/source/engine/resol.F:2721-2722, 6123,
+// 6352, 6494-6497).
+struct Time {
+  double tt, dt1, dt2, dt12, dt2old, dtmx;
+  double dt2t;       // element/nodal minimum of the current cycle
+  double dtmin;      // error threshold (0 = none)
+  int ncycle, neltst, status, pad;
+};
+
+struct NodeView {
+  dbl4 *X4;   // x y z MS
+  dbl4 *V4;   // vx vy vz code(as double)
+  dbl4 *D4;   // dx dy dz -
+  dbl4 *VR4;  // vrx vry vrz IN (shell models only)
+  dbl4 *DR4;  // unused slot, kept for alignment of the record set
+  int numnod;
+};
+
+// Per-block partial minimum of the element time step.
+struct DtPartials {
+  double *dt;
+  int *el;  // user id of the element attaining it (-1 none)
+};
+
+__device__ __forceinline__ dbl4 ld4(const dbl4 *__restrict__ p) { return *p; }
+__device__ __forceinline__ void st4(dbl4 *__restrict__ p, dbl4 v) { *p = v; }
+
+// Block-level (min dt, element) reduction; ties keep the larger element
+// order key (the last element attaining the minimum in sequential order).
+__device__ __forceinline__ void dt_pair_min(double &d, int &k, double d2,
+                                            int k2) {
+  if (d2 < d || (d2 == d && k2 > k)) {
+    d = d2;
+    k = k2;
+  }
+}
+
+template <int NT>
+__device__ __forceinline__ void block_dt_min(double d, int k, double *out_d,
+                                             int *out_k) {
+  __shared__ double sd[NT / 32];
+  __shared__ int sk[NT / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    double d2 = __shfl_down_sync(0xffffffffu, d, o);
+    int k2 = __shfl_down_sync(0xffffffffu, k, o);
+    dt_pair_min(d, k, d2, k2);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sd[w] = d;
+    sk[w] = k;
+  }
+  __syncthreads();
+  if (w == 0) {
+    d = l < NT / 32 ? sd[l] : RG_EP30;
+    k = l < NT / 32 ? sk[l] : -1;
+    for (int o = 16; o > 0; o >>= 1) {
+      double d2 = __shfl_down_sync(0xffffffffu, d, o);
+      int k2 = __shfl_down_sync(0xffffffffu, k, o);
+      dt_pair_min(d, k, d2, k2);
+    }
+    if (l == 0) {
+      *out_d = d;
+      *out_k = k;
+    }
+  }
+}
+
+// Hexa group parameters (one launch per group of identical material and
+// property; values taken from PM / GEO / mat_param like the reference).
+struct HexaParams {
+  int nft, nel;            // element range in the hexa arrays
+  int mtn;                 // 1 = LAW1, 2 = LAW2
+  int part_off;            // first dt-partial slot of this launch
+  double rho0, g, c1;      // PM(1), PM(22), PM(32)
+  double qh, qa, qb, vns1, vns2;  // GEO(13..17)
+  double dtfac;            // DTFAC1(1)
+  // LAW2 Johnson-Cook (mat_param%uparam / iparam)
+  double ca, cb, cn, epmx, sigm0, cc, epdr, asrate, z3;
+  int icc, vp, israte, pad;
+};
+
+template <typename ER>
+struct HexaArrays {
+  int ne;                  // total hexa count (SoA stride)
+  const int *nc;           // [8][ne] 0-based node numbers
+  const int *iads;         // [8][ne] 0-based slots
+  const int *ngl;          // [ne] user ids
+  ER *sig;                 // [6][ne]
+  double *eint;            // [ne]   (FP64 in both forms: energy accumulator)
+  double *rho;             // [ne]   (FP64 in both forms: volume history)
+  ER *qvis;                // [ne]
+  ER *off;                 // [ne]   OFFG
+  double *vol0;            // [ne]
+  ER *pla, *epsd;          // [ne]   LAW2
+  double *ehou;            // [ne]   accumulated hourglass energy
+};
+
+template <typename ER>
+struct SlotT;
+template <>
+struct SlotT<double> {
+  typedef dbl4 type;
+};
+template <>
+struct SlotT<float> {
+  typedef float4 type;
+};
+
+}  // namespace rg

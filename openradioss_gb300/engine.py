@@ -1,0 +1,201 @@
+"""Python host mirror of the C ABI (include/rg_api.h).
+
+``Engine`` drives one rg_ctx through ctypes: it uploads a
+:class:`openradioss_gb300.model.Model` (the arrays the starter hands to the
+engine), advances explicit cycles on the GPU and reads results back.  Every
+call goes to librg.so; there is no CPU fallback -- if the library or a CUDA
+device is missing, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+
+RG_PREC_FP64 = 0
+RG_PREC_MIXED = 1
+
+ST_NEGVOL = 1
+ST_NAN = 2
+ST_SLOT = 4
+ST_DTMIN = 8
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class RgError(RuntimeError):
+    pass
+
+
+class Engine:
+    """One model resident on one GPU (an rg_ctx)."""
+
+    def __init__(self, model, device=0, precision=RG_PREC_FP64, skyline=None):
+        self.L = _lib.lib()
+        self.model = model
+        self.precision = precision
+        h = C.c_void_p()
+        r = self.L.rg_ctx_create(device, C.byref(h))
+        if r != 0:
+            raise RgError("rg_ctx_create failed (%d): no usable CUDA device %d" % (r, device))
+        self.h = h
+        try:
+            self._setup(model, precision, skyline)
+        except Exception:
+            self.close()
+            raise
+
+    def _chk(self, r, what):
+        if r < 0:
+            raise RgError("%s failed (%d): %s" % (what, r, self.L.rg_last_error(self.h).decode()))
+        return r
+
+    def _setup(self, m, precision, skyline):
+        L = self.L
+        self._chk(L.rg_set_precision(self.h, precision), "rg_set_precision")
+        X = np.ascontiguousarray(m.X.T.reshape(-1), np.float64)
+        V = np.ascontiguousarray(m.V.T.reshape(-1), np.float64)
+        MS = np.ascontiguousarray(m.MS, np.float64)
+        IN = None if m.IN is None else np.ascontiguousarray(m.IN, np.float64)
+        ic = np.ascontiguousarray(m.icodt, np.int32)
+        self._chk(L.rg_mesh_upload(self.h, m.numnod, _p(X), _p(V), _p(MS), _p(IN), _p(ic)),
+                  "rg_mesh_upload")
+        for g in m.hexa:
+            ixs = np.ascontiguousarray(g.ixs.T.reshape(-1), np.int32)
+            self._chk(L.rg_hexa_group_add(self.h, g.ixs.shape[1], _p(ixs), g.mat["mtn"],
+                                          _p(g.mat["pm"]), _p(g.geo), _p(g.mat["uparam"]),
+                                          _p(g.mat["iparam"]), 4, 1, 0), "rg_hexa_group_add")
+        for g in m.shells:
+            ixc = np.ascontiguousarray(g.ixc.T.reshape(-1), np.int32)
+            thk = np.ascontiguousarray(g.thk, np.float64)
+            self._chk(L.rg_shell_group_add(self.h, g.ixc.shape[1], _p(ixc), g.npt,
+                                           _p(g.mat["pm"]), _p(g.geo), _p(g.mat["uparam"]),
+                                           _p(g.mat["iparam"]), _p(thk), 2, 1),
+                      "rg_shell_group_add")
+        for (p0, nrm, ds) in m.rwalls:
+            self._chk(L.rg_rwall_add(self.h, _p(np.asarray(p0, np.float64)),
+                                     _p(np.asarray(nrm, np.float64)), float(ds)), "rg_rwall_add")
+        if skyline is not None:
+            adsky, iads, iadc = (np.ascontiguousarray(a, np.int32) for a in skyline)
+            self._chk(L.rg_skyline_set(self.h, _p(adsky), _p(iads), _p(iadc)), "rg_skyline_set")
+        self._chk(L.rg_finalize(self.h, m.dtfac_solid, m.dtfac_shell, m.dtmx, m.dt2old),
+                  "rg_finalize")
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.rg_ctx_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- stepping --------------------------------------------------------
+    def cycle(self, n=1, sync=True):
+        self._chk(self.L.rg_cycle(self.h, int(n)), "rg_cycle")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        self._chk(self.L.rg_synchronize(self.h), "rg_synchronize")
+
+    def status(self):
+        return self._chk(self.L.rg_status(self.h), "rg_status")
+
+    def forint_step(self, x, v, dt1, vr=None, f=None, stifn=None):
+        """FORINT-level call with host buffers: x, v as X(3,N) arrays
+        (numpy (N,3) row-major == Fortran (3,N)).  Returns (f, stifn, dt2t,
+        neltst)."""
+        n = self.model.numnod
+        if f is None:
+            f = np.empty((n, 3))
+        if stifn is None:
+            stifn = np.empty(n)
+        dt2t = C.c_double()
+        el = C.c_int()
+        self._chk(self.L.rg_forint_step(self.h, _p(x), _p(v), _p(vr), float(dt1), _p(f),
+                                        _p(stifn), None, None, C.byref(dt2t), C.byref(el)),
+                  "rg_forint_step")
+        return f, stifn, dt2t.value, el.value
+
+    def host_register(self, a):
+        self._chk(self.L.rg_host_register(self.h, _p(a), a.nbytes), "rg_host_register")
+
+    def host_unregister(self, a):
+        self._chk(self.L.rg_host_unregister(self.h, _p(a)), "rg_host_unregister")
+
+    # ---- results -----------------------------------------------------------
+    def nodes(self):
+        n = self.model.numnod
+        out = {k: np.zeros(3 * n) for k in ("X", "V", "D", "VR")}
+        self._chk(self.L.rg_download_nodes(self.h, _p(out["X"]), _p(out["V"]), _p(out["D"]),
+                                           _p(out["VR"])), "rg_download_nodes")
+        return {k: a.reshape(n, 3).T.copy() for k, a in out.items()}
+
+    def forces(self):
+        n = self.model.numnod
+        f, st, fr = np.zeros(3 * n), np.zeros(n), np.zeros(3 * n)
+        self._chk(self.L.rg_download_forces(self.h, _p(f), _p(st), _p(fr)), "rg_download_forces")
+        return dict(F=f.reshape(n, 3).T.copy(), STIFN=st, FR=fr.reshape(n, 3).T.copy())
+
+    def hexa_state(self, which):
+        ne = self.model.numels
+        out = np.zeros(6 * ne if which == 0 else ne)
+        self._chk(self.L.rg_download_hexa_state(self.h, which, _p(out)), "rg_download_hexa_state")
+        return out.reshape(6, ne) if which == 0 else out
+
+    def shell_state(self, which, size):
+        out = np.zeros(size)
+        self._chk(self.L.rg_download_shell_state(self.h, which, _p(out)), "rg_download_shell_state")
+        return out
+
+    def time(self):
+        tt, dt1, dt2 = C.c_double(), C.c_double(), C.c_double()
+        nc, el = C.c_int(), C.c_int()
+        self._chk(self.L.rg_get_time(self.h, C.byref(tt), C.byref(dt1), C.byref(dt2),
+                                     C.byref(nc), C.byref(el)), "rg_get_time")
+        return dict(tt=tt.value, dt1=dt1.value, dt2=dt2.value, ncycle=nc.value, neltst=el.value)
+
+    def energy(self):
+        v = [C.c_double() for _ in range(4)]
+        self._chk(self.L.rg_energy(self.h, *[C.byref(x) for x in v]), "rg_energy")
+        return dict(eint=v[0].value, ekin=v[1].value, ekinr=v[2].value, ehour=v[3].value)
+
+    def skyline(self):
+        m = self.model
+        adsky = np.zeros(m.numnod + 1, np.int32)
+        iads = np.zeros(max(8 * m.numels, 1), np.int32)
+        iadc = np.zeros(max(4 * m.numelc, 1), np.int32)
+        lsky = C.c_int()
+        self._chk(self.L.rg_skyline_get(self.h, _p(adsky), _p(iads), _p(iadc), C.byref(lsky)),
+                  "rg_skyline_get")
+        return adsky, iads[:8 * m.numels], iadc[:4 * m.numelc], lsky.value
+
+    def info(self):
+        a = [C.c_int() for _ in range(4)]
+        b = C.c_ulonglong()
+        self._chk(self.L.rg_info(self.h, *[C.byref(x) for x in a], C.byref(b)), "rg_info")
+        return dict(numnod=a[0].value, numels=a[1].value, numelc=a[2].value, lsky=a[3].value,
+                    device_bytes=b.value)
+
+    def set_timing(self, on):
+        self._chk(self.L.rg_set_timing(self.h, 1 if on else 0), "rg_set_timing")
+
+    def time_cycles(self, n):
+        """Run n cycles between two CUDA events on the context stream and
+        return the device time in ms."""
+        ms = C.c_double()
+        self._chk(self.L.rg_time_cycles(self.h, int(n), C.byref(ms)), "rg_time_cycles")
+        return ms.value
+
+    def kernel_times(self):
+        a = (C.c_double * 4)()
+        self._chk(self.L.rg_kernel_times(self.h, a), "rg_kernel_times")
+        return dict(hexa=a[0], shell=a[1], dt=a[2], node=a[3])

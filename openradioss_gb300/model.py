@@ -1,0 +1,251 @@
+"""Host-side model preparation (the starter's decisions for this path).
+
+Builds, with numpy, the arrays the engine receives from the starter for the
+explicit hot path, in the reference's own layouts:
+
+* nodal coordinates ``X(3,NUMNOD)`` / velocities ``V(3,NUMNOD)`` /
+  masses ``MS(NUMNOD)``;
+* hexa connectivity ``IXS(11,NUMELS)`` = {mat, n1..n8 (1-based), prop,
+  user id} (starter/source/elements/solid/solide/sgrtails.F);
+* shell connectivity ``IXC(7,NUMELC)`` = {mat, n1..n4, prop, user id};
+* material columns ``PM(1:NPROPM)`` and property columns ``GEO(1:NPROPG)``
+  holding the entries the path reads (LAW1: hm_read_mat01.F; LAW2:
+  hm_read_mat02_jc.F90; solid property: hm_read_prop14.F; shell property:
+  hm_read_prop01.F), plus LAW2 ``mat_param%uparam`` / ``iparam``;
+* boundary codes (bit 1/2/4 = fixed x/y/z translation, 8/16/32 rotations).
+
+The synthetic meshes are the workloads the benchmark and the tests run: a
+structured one-point hexa block (bar impact, large block) and a square crash
+box of 4-node shells.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+NPROPM = 128
+NPROPG = 256
+NUPARAM = 16
+NIPARAM = 8
+
+
+# --------------------------------------------------------------------------
+# materials / properties
+# --------------------------------------------------------------------------
+def _g_bulk(young, nu):
+    if nu == 0.5:
+        nu = 0.499  # ZEP499 (hm_read_mat01.F)
+    g = young / (2.0 * (1.0 + nu))
+    c1 = young / (3.0 * (1.0 - 2.0 * nu))
+    return g, c1
+
+
+def law1(rho, young, nu):
+    """/MAT/ELAST (LAW1): PM(1)=rho, PM(20)=E, PM(21)=nu, PM(22)=G, PM(32)=C1."""
+    pm = np.zeros(NPROPM)
+    g, c1 = _g_bulk(young, nu)
+    pm[0] = rho
+    pm[19] = young
+    pm[20] = nu
+    pm[21] = g
+    pm[31] = c1
+    pm[88] = rho  # PM(89) = RHO0
+    return dict(mtn=1, pm=pm, uparam=np.zeros(NUPARAM), iparam=np.zeros(NIPARAM, np.int32))
+
+
+def law2(rho, young, nu, a, b, n, c=0.0, eps0=1.0, epsmax=0.0, sigmax=0.0,
+         m_exp=0.0, vp=0, icc=0, fcut=0.0):
+    """/MAT/PLAS_JOHNS (LAW2, Johnson-Cook) with the reader's defaults
+    (starter/source/materials/mat/mat002/hm_read_mat02_jc.F90:100-135)."""
+    pm = np.zeros(NPROPM)
+    g, bulk = _g_bulk(young, nu)
+    if n == 0.0:
+        n = 1.0
+    if epsmax == 0.0:
+        epsmax = 1e20
+    if sigmax == 0.0:
+        sigmax = 1e20
+    if icc == 0:
+        icc = 1
+    if vp == 0:
+        vp = 2
+    israte = 1
+    if c == 0.0:
+        eps0 = 1.0
+        israte = 0
+    if vp == 1:
+        fcut = 10000.0
+    asrate = 1e20 if fcut == 0.0 else 2.0 * math.pi * fcut
+    if m_exp == 0.0:
+        m_exp = 1.0
+    pm[0] = rho
+    pm[19] = young
+    pm[20] = nu
+    pm[21] = g
+    pm[31] = bulk
+    pm[37], pm[38], pm[39] = a, b, n
+    pm[88] = rho
+    up = np.zeros(NUPARAM)
+    up[:10] = [a, b, n, epsmax, sigmax, c, eps0, 0.0, asrate, m_exp]
+    ip = np.zeros(NIPARAM, np.int32)
+    ip[:4] = [0, icc, vp, israte]
+    return dict(mtn=2, pm=pm, uparam=up, iparam=ip)
+
+
+def solid_prop(qa=1.1, qb=0.05, qh=0.1, dn1=0.0, dn2=0.0):
+    """/PROP/SOLID Isolid=1, Iframe=1 (JCVT=0), Ismstr=4: GEO(13)=QH,
+    GEO(14)=QA, GEO(15)=QB, GEO(16..17) numerical damping."""
+    geo = np.zeros(NPROPG)
+    geo[12], geo[13], geo[14], geo[15], geo[16] = qh, qa, qb, dn1, dn2
+    return geo
+
+
+def shell_prop(thk, npt=5, hm=0.02, hf=0.02, hr=0.02, dm=0.0, ishell=3):
+    """/PROP/SHELL, Ishell=3 style BT with physical-stabilisation-free viscous
+    hourglass: GEO(1)=thickness, GEO(3)=ISMSTR, GEO(13..15)=hm,hf,hr,
+    GEO(16)=dm, NPT through-thickness points."""
+    geo = np.zeros(NPROPG)
+    geo[0] = thk
+    geo[12], geo[13], geo[14], geo[15] = hm, hf, hr, dm
+    geo[37] = 5.0 / 6.0  # shear factor
+    return geo
+
+
+# --------------------------------------------------------------------------
+# meshes
+# --------------------------------------------------------------------------
+def hexa_volumes(X, ixs):
+    """SDERI3 determinant (sderi3.F) of every hexa, FP64, vectorised."""
+    n = ixs[1:9].T - 1
+    x, y, z = X[0][n], X[1][n], X[2][n]
+    d = lambda a, i, j: a[:, i] - a[:, j]
+    x17, x28, x35, x46 = d(x, 6, 0), d(x, 7, 1), d(x, 4, 2), d(x, 5, 3)
+    y17, y28, y35, y46 = d(y, 6, 0), d(y, 7, 1), d(y, 4, 2), d(y, 5, 3)
+    z17, z28, z35, z46 = d(z, 6, 0), d(z, 7, 1), d(z, 4, 2), d(z, 5, 3)
+    j1, j2, j3 = x17 + x28 - x35 - x46, y17 + y28 - y35 - y46, z17 + z28 - z35 - z46
+    j4, j5, j6 = (x17 + x46) + (x28 + x35), (y17 + y46) + (y28 + y35), (z17 + z46) + (z28 + z35)
+    j7, j8, j9 = (x17 + x46) - (x28 + x35), (y17 + y46) - (y28 + y35), (z17 + z46) - (z28 + z35)
+    return (1.0 / 64.0) * (j1 * (j5 * j9 - j6 * j8) + j2 * (j6 * j7 - j4 * j9) + j3 * (j4 * j8 - j5 * j7))
+
+
+@dataclass
+class HexaGroupSpec:
+    ixs: np.ndarray            # (11, nel) int32
+    mat: dict
+    geo: np.ndarray
+
+
+@dataclass
+class ShellGroupSpec:
+    ixc: np.ndarray            # (7, nel) int32
+    mat: dict
+    geo: np.ndarray
+    thk: np.ndarray            # (nel,)
+    npt: int = 5
+
+
+@dataclass
+class Model:
+    """A deck for the hot path: nodes, element groups, conditions."""
+    name: str
+    X: np.ndarray              # (3, numnod) float64
+    V: np.ndarray              # (3, numnod)
+    MS: np.ndarray             # (numnod,)
+    icodt: np.ndarray          # (numnod,) int32
+    hexa: list = field(default_factory=list)
+    shells: list = field(default_factory=list)
+    IN: np.ndarray | None = None
+    rwalls: list = field(default_factory=list)  # (p0[3], n[3], dsearch)
+    dtfac_solid: float = 0.9
+    dtfac_shell: float = 0.9
+    dtmx: float = 1e30
+    dt2old: float = 1e30
+
+    @property
+    def numnod(self):
+        return self.X.shape[1]
+
+    @property
+    def numels(self):
+        return sum(g.ixs.shape[1] for g in self.hexa)
+
+    @property
+    def numelc(self):
+        return sum(g.ixc.shape[1] for g in self.shells)
+
+
+def hexa_block(nx, ny, nz, h, origin=(0.0, 0.0, 0.0)):
+    """Structured block of nx*ny*nz one-point hexas of edge h.  Node order
+    x fastest; element nodes 1-4 on the lower z face counter-clockwise,
+    5-8 above (the reference's brick numbering)."""
+    ix = np.arange(nx + 1)
+    iy = np.arange(ny + 1)
+    iz = np.arange(nz + 1)
+    gz, gy, gx = np.meshgrid(iz, iy, ix, indexing="ij")
+    X = np.stack([origin[0] + h * gx.ravel(), origin[1] + h * gy.ravel(),
+                  origin[2] + h * gz.ravel()]).astype(np.float64)
+    nid = lambda i, j, k: (k * (ny + 1) + j) * (nx + 1) + i
+    ez, ey, ex = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ex, ey, ez = ex.ravel(), ey.ravel(), ez.ravel()
+    conn = np.stack([
+        nid(ex, ey, ez), nid(ex + 1, ey, ez), nid(ex + 1, ey + 1, ez), nid(ex, ey + 1, ez),
+        nid(ex, ey, ez + 1), nid(ex + 1, ey, ez + 1), nid(ex + 1, ey + 1, ez + 1), nid(ex, ey + 1, ez + 1),
+    ]).astype(np.int32)
+    nel = conn.shape[1]
+    ixs = np.zeros((11, nel), np.int32)
+    ixs[0] = 1
+    ixs[1:9] = conn + 1
+    ixs[9] = 1
+    ixs[10] = np.arange(1, nel + 1, dtype=np.int32)
+    return X, ixs
+
+
+def lumped_mass_hexa(X, ixs, rho, ms=None):
+    """SMASS3 (starter/source/elements/solid/solide/smass3.F:92): each node
+    receives rho*V/8 from every hexa, accumulated in element order."""
+    numnod = X.shape[1]
+    if ms is None:
+        ms = np.zeros(numnod)
+    vol = hexa_volumes(X, ixs)
+    m8 = rho * vol * 0.125
+    for k in range(8):
+        np.add.at(ms, ixs[1 + k] - 1, m8)
+    return ms
+
+
+def bar_impact(n=20, h=0.005, v0=10.0, rho=7850.0, young=210e9, nu=0.3,
+               law="law1"):
+    """Steel bar impact: n^3 one-point hexas, edge h, LAW1 elastic, viscous
+    hourglass, the z=0 face fixed, every other node moving at v0 towards it
+    (along the face normal)."""
+    X, ixs = hexa_block(n, n, n, h)
+    mat = law1(rho, young, nu) if law == "law1" else law2(
+        rho, young, nu, 350e6, 275e6, 0.36, c=0.022, eps0=1.0)
+    ms = lumped_mass_hexa(X, ixs, rho)
+    icodt = np.zeros(X.shape[1], np.int32)
+    fixed = X[2] == 0.0
+    icodt[fixed] = 7
+    V = np.zeros_like(X)
+    V[2, ~fixed] = -v0
+    return Model("bar_impact_%d" % n, X, V, ms, icodt,
+                 hexa=[HexaGroupSpec(ixs, mat, solid_prop())])
+
+
+def large_block(n=128, h=0.005, vmean=20.0, vstd=0.5, seed=1, rho=7850.0,
+                young=210e9, nu=0.3, law="law2"):
+    """Large hexa block with Johnson-Cook: n^3 one-point hexas, seeded
+    initial velocity 20 m/s + N(0, 0.5) per node component."""
+    X, ixs = hexa_block(n, n, n, h)
+    mat = law2(rho, young, nu, 350e6, 275e6, 0.36, c=0.022, eps0=1.0) \
+        if law == "law2" else law1(rho, young, nu)
+    ms = lumped_mass_hexa(X, ixs, rho)
+    rng = np.random.default_rng(seed)
+    V = rng.normal(0.0, vstd, size=X.shape)
+    V[2] += -vmean
+    icodt = np.zeros(X.shape[1], np.int32)
+    icodt[X[2] == 0.0] = 7
+    V[:, X[2] == 0.0] = 0.0
+    return Model("large_block_%d" % n, X, V, ms, icodt,
+                 hexa=[HexaGroupSpec(ixs, mat, solid_prop())])

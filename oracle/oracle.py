@@ -1,0 +1,145 @@
+"""ctypes front-end of the CPU oracle -- TEST INFRASTRUCTURE.
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use this module, and only as a checker / reported baseline;
+the product never imports it.  See rg_oracle.cpp for what it restates and
+its parity status (pinned by analytic known-answer tests; unpinned against
+outputs of the reference engine itself).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "librg_oracle.so")
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (g++, -ffp-contract=off)."""
+    if force or not os.path.exists(_LIB):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB)
+        vp = C.c_void_p
+        L.or_model_new.restype = vp
+        L.or_model_new.argtypes = [C.c_int, _dp, _dp, _dp, _ip]
+        L.or_model_free.argtypes = [vp]
+        L.or_hexa_group_add.argtypes = [vp, C.c_int, _ip, C.c_int, _dp, _dp, _dp, _ip,
+                                        C.c_int, C.c_int, C.c_int]
+        L.or_shell_group_add.argtypes = [vp, C.c_int, _ip, C.c_int, _dp, _dp, _dp, _ip,
+                                         _dp, C.c_int, C.c_int]
+        L.or_set_inertia.argtypes = [vp, _dp]
+        L.or_rwall_add.argtypes = [vp, _dp, _dp, C.c_double]
+        L.or_finalize.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+        L.or_get_skyline.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.or_cycle.argtypes = [vp, C.c_int]
+        L.or_get_nodes.argtypes = [vp] + [C.c_void_p] * 7
+        L.or_get_time.argtypes = [vp] + [C.c_void_p] * 5
+        L.or_get_hexa_state.argtypes = [vp, C.c_int, C.c_int, _dp]
+        L.or_energy.argtypes = [vp] + [C.c_void_p] * 4
+        L.or_error.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class OracleModel:
+    """A model stepped by the CPU oracle."""
+
+    def __init__(self, model, nthreads=None):
+        L = lib()
+        self.model = model
+        n = model.numnod
+        X = np.ascontiguousarray(model.X.T.reshape(-1))
+        V = np.ascontiguousarray(model.V.T.reshape(-1))
+        self.h = L.or_model_new(n, X, V, np.ascontiguousarray(model.MS, np.float64),
+                                np.ascontiguousarray(model.icodt, np.int32))
+        for g in model.hexa:
+            r = L.or_hexa_group_add(self.h, g.ixs.shape[1],
+                                    np.ascontiguousarray(g.ixs.T.reshape(-1), np.int32),
+                                    g.mat["mtn"], g.mat["pm"], g.geo, g.mat["uparam"],
+                                    g.mat["iparam"], 4, 1, 0)
+            if r < 0:
+                raise RuntimeError("or_hexa_group_add failed %d" % r)
+        for g in model.shells:
+            r = L.or_shell_group_add(self.h, g.ixc.shape[1],
+                                     np.ascontiguousarray(g.ixc.T.reshape(-1), np.int32),
+                                     g.npt, g.mat["pm"], g.geo, g.mat["uparam"],
+                                     g.mat["iparam"], np.ascontiguousarray(g.thk, np.float64),
+                                     2, 1)
+            if r < 0:
+                raise RuntimeError("or_shell_group_add failed %d" % r)
+        if model.IN is not None:
+            L.or_set_inertia(self.h, np.ascontiguousarray(model.IN, np.float64))
+        for (p0, nrm, ds) in model.rwalls:
+            L.or_rwall_add(self.h, np.asarray(p0, np.float64), np.asarray(nrm, np.float64), ds)
+        nt = nthreads or os.cpu_count() or 1
+        r = L.or_finalize(self.h, model.dtfac_solid, model.dtfac_shell, model.dtmx,
+                          model.dt2old, nt)
+        if r != 0:
+            raise RuntimeError("or_finalize failed %d" % r)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_model_free(self.h)
+            self.h = None
+
+    def cycle(self, n=1):
+        return lib().or_cycle(self.h, n)
+
+    def skyline(self):
+        m = self.model
+        adsky = np.zeros(m.numnod + 1, np.int32)
+        iads = np.zeros(8 * max(m.numels, 1), np.int32)
+        iadc = np.zeros(4 * max(m.numelc, 1), np.int32)
+        lsky = np.zeros(1, np.int32)
+        lib().or_get_skyline(self.h, _ptr(adsky), _ptr(iads), _ptr(iadc), _ptr(lsky))
+        return adsky, iads[:8 * m.numels], iadc[:4 * m.numelc], int(lsky[0])
+
+    def nodes(self):
+        n = self.model.numnod
+        out = {k: np.zeros(3 * n) for k in ("X", "V", "D", "VR", "F", "FR")}
+        out["STIFN"] = np.zeros(n)
+        lib().or_get_nodes(self.h, _ptr(out["X"]), _ptr(out["V"]), _ptr(out["D"]),
+                           _ptr(out["VR"]), _ptr(out["F"]), _ptr(out["STIFN"]),
+                           _ptr(out["FR"]))
+        for k in ("X", "V", "D", "VR", "F", "FR"):
+            out[k] = out[k].reshape(n, 3).T.copy()
+        return out
+
+    def time(self):
+        tt, dt1, dt2 = (np.zeros(1) for _ in range(3))
+        nc, el = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        lib().or_get_time(self.h, _ptr(tt), _ptr(dt1), _ptr(dt2), _ptr(nc), _ptr(el))
+        return dict(tt=tt[0], dt1=dt1[0], dt2=dt2[0], ncycle=int(nc[0]), neltst=int(el[0]))
+
+    def hexa_state(self, which):
+        ne = self.model.numels
+        out = np.zeros(6 * ne if which == 0 else ne)
+        lib().or_get_hexa_state(self.h, 0, which, out)
+        return out.reshape(6, ne) if which == 0 else out
+
+    def energy(self):
+        v = [np.zeros(1) for _ in range(4)]
+        lib().or_energy(self.h, *[_ptr(a) for a in v])
+        return dict(eint=v[0][0], ekin=v[1][0], ekinr=v[2][0], ehour=v[3][0])
+
+    def error(self):
+        return lib().or_error(self.h)

@@ -1,0 +1,1140 @@
+// CPU oracle for the OpenRadioss explicit hot path -- TEST INFRASTRUCTURE.
+//
+// A restatement, routine by routine and in the reference's own expression
+// order, of the Fortran that one explicit cycle runs.  It checks the CUDA
+// product (tests, smoke) and is the timed CPU baseline (bench.py); the
+// product never links or calls it.  Compiled with -ffp-contract=off like the
+// reference's gfortran build (engine/CMake_Compilers/cmake_linux64_gf.txt:163)
+// so that no multiply-add is fused.
+//
+// Parity status: the reference engine cannot be built here (no Fortran
+// compiler; the starter also needs an un-vendored binary library), so this
+// restatement is pinned by analytic known-answer tests, not by outputs of the
+// reference engine -- parity against the reference itself is unpinned.
+//
+// Each block cites the reference file:line it follows (paths relative to the
+// OpenRadioss source tree).
+#include "rg_oracle.h"
+#include "../openradioss_gb300/csrc/rg_constants.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr int MVSIZ = 128;  // group length (engine/share/spe_inc/mvsiz_p.inc)
+
+struct HexaGroup {
+  int nft = 0, nel = 0, mtn = 1;
+  int ismstr = 4, jhbe = 1, jcvt = 0;
+  // material / property values used on the path
+  double rho0 = 0, g = 0, c1 = 0;  // PM(1), PM(22), PM(32)
+  double qh = 0, qa = 0, qb = 0, vns1 = 0, vns2 = 0;  // GEO(13..17)
+  // LAW2 (mat_param%uparam / iparam)
+  double ca = 0, cb = 0, cn = 1, epmx = 0, sigm0 = 0, cc = 0, epdr = 1;
+  double fisokin = 0, asrate = 0, z3 = 1;
+  int iform = 0, icc = 1, vp = 2, israte = 0;
+};
+
+struct ShellGroup;  // shells: rg_oracle_shell.cpp
+
+struct Model {
+  int numnod = 0;
+  std::vector<double> X, V, D, A, AR, VR, DR, STIFN, STIFR, MS, IN;
+  std::vector<double> FLAST, FRLAST;  // assembled forces of the last cycle
+  std::vector<int> icodt;
+
+  // hexa elements (global SoA over all hexa groups)
+  int numels = 0;
+  std::vector<int> ixs;  // 11 * numels, reference layout, 1-based nodes
+  std::vector<HexaGroup> hg;
+  std::vector<double> sig, eint, rho, vol, qvis, offg, pla, epsd, ehou;
+  std::vector<int> iads;  // 8 * numels, 1-based slot numbers
+
+  // skyline
+  std::vector<int> adsky;      // numnod + 1 (1-based values)
+  std::vector<double> fsky;    // 8 * lsky: {fx,fy,fz,mx,my,mz,sti,stir}
+  int lsky = 0;
+
+  // time (RESOL)
+  double tt = 0, dt1 = 0, dt2 = 0, dt12 = 0, dt2old = 0, dtmx = RG_EP30;
+  double dtfac_solid = RG_ZEP9, dtfac_shell = RG_ZEP9;
+  int ncycle = 0, neltst = 0, nthreads = 1;
+  int error = 0;
+  bool finalized = false;
+  double ehour_total = 0;
+};
+
+// ----------------------------------------------------------------------------
+// SFORC3 one-point hexa, JCVT=0, Lagrangian, JHBE=1 (sforc3.F:60-1817).
+// All arrays are local group SoA of length nel <= MVSIZ, as in the Fortran.
+// ----------------------------------------------------------------------------
+struct HexaLocal {
+  int nc[8][MVSIZ];
+  double x[8][MVSIZ], y[8][MVSIZ], z[8][MVSIZ];
+  double vx[8][MVSIZ], vy[8][MVSIZ], vz[8][MVSIZ];
+  double off[MVSIZ], voln[MVSIZ], deltax[MVSIZ];
+  double px[4][MVSIZ], py[4][MVSIZ], pz[4][MVSIZ];
+  double ph[4][3][MVSIZ];  // PXiHj
+  double dxx[MVSIZ], dyy[MVSIZ], dzz[MVSIZ], dxy[MVSIZ], dyx[MVSIZ],
+      dyz[MVSIZ], dzy[MVSIZ], dxz[MVSIZ], dzx[MVSIZ], d4[MVSIZ], d5[MVSIZ],
+      d6[MVSIZ], wxx[MVSIZ], wyy[MVSIZ], wzz[MVSIZ];
+  double dvol[MVSIZ], divde[MVSIZ], amu[MVSIZ], vol_avg[MVSIZ];
+  double s[6][MVSIZ];  // stress before rotation (SOLD)
+  double ssp[MVSIZ], qnew[MVSIZ], ssp_eq[MVSIZ], sti[MVSIZ];
+  double f[3][8][MVSIZ];
+};
+
+void hexa_group(Model &M, const HexaGroup &G, double &dt2t, int &neltst) {
+  HexaLocal L;
+  const int nel = G.nel, nft = G.nft, NE = M.numels;
+  double *SIG = M.sig.data();
+  const double DT1 = M.dt1;
+
+  // SCOOR3 gather (scoor3.F: NC, XD from X, OFF from OFFG, V)
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    for (int k = 0; k < 8; k++) L.nc[k][i] = M.ixs[11 * e + 1 + k] - 1;
+    const double og = M.offg[e];
+    L.off[i] = std::fabs(og);
+    for (int k = 0; k < 8; k++) {
+      const int n = L.nc[k][i];
+      L.x[k][i] = M.X[3 * n + 0];
+      L.y[k][i] = M.X[3 * n + 1];
+      L.z[k][i] = M.X[3 * n + 2];
+      if (og < RG_ZERO) {
+        L.vx[k][i] = L.vy[k][i] = L.vz[k][i] = RG_ZERO;
+      } else {
+        L.vx[k][i] = M.V[3 * n + 0];
+        L.vy[k][i] = M.V[3 * n + 1];
+        L.vz[k][i] = M.V[3 * n + 2];
+      }
+    }
+  }
+
+  // SDERI3 (sderi3.F:32-339): Jacobian, volume, PX/PY/PZ, hourglass PH.
+  for (int i = 0; i < nel; i++) {
+    const double *X1 = &L.x[0][i];
+    (void)X1;
+    double x17 = L.x[6][i] - L.x[0][i], x28 = L.x[7][i] - L.x[1][i];
+    double x35 = L.x[4][i] - L.x[2][i], x46 = L.x[5][i] - L.x[3][i];
+    double y17 = L.y[6][i] - L.y[0][i], y28 = L.y[7][i] - L.y[1][i];
+    double y35 = L.y[4][i] - L.y[2][i], y46 = L.y[5][i] - L.y[3][i];
+    double z17 = L.z[6][i] - L.z[0][i], z28 = L.z[7][i] - L.z[1][i];
+    double z35 = L.z[4][i] - L.z[2][i], z46 = L.z[5][i] - L.z[3][i];
+    double jac1 = x17 + x28 - x35 - x46;
+    double jac2 = y17 + y28 - y35 - y46;
+    double jac3 = z17 + z28 - z35 - z46;
+    double x_17_46 = x17 + x46, x_28_35 = x28 + x35;
+    double y_17_46 = y17 + y46, y_28_35 = y28 + y35;
+    double z_17_46 = z17 + z46, z_28_35 = z28 + z35;
+    double jac4 = x_17_46 + x_28_35, jac5 = y_17_46 + y_28_35,
+           jac6 = z_17_46 + z_28_35;
+    double jac7 = x_17_46 - x_28_35, jac8 = y_17_46 - y_28_35,
+           jac9 = z_17_46 - z_28_35;
+    double j5968 = jac5 * jac9 - jac6 * jac8;
+    double j6749 = jac6 * jac7 - jac4 * jac9;
+    double j4857 = jac4 * jac8 - jac5 * jac7;
+    double det = RG_ONE_OVER_64 * (jac1 * j5968 + jac2 * j6749 + jac3 * j4857);
+    // SCHKJABT3 (solide4/schkjabt3.F), Lagrangian, ISMSTR=4: a non-positive
+    // volume of a live element stops the run (INEG_V=0: element switched off,
+    // MSTOP=1).  Here: the element is switched off and the error is flagged.
+    if (L.off[i] == RG_ZERO) {
+      det = RG_ONE;
+    } else if (det <= RG_ZERO) {
+      det = RG_ONE;
+      L.off[i] = RG_ZERO;
+      M.offg[nft + i] = RG_ZERO;
+      M.error |= 1;
+    }
+    L.voln[i] = det;
+    double dett = RG_ONE_OVER_64 / det;
+    double jaci1 = dett * j5968;
+    double jaci4 = dett * j6749;
+    double jaci7 = dett * j4857;
+    double jaci2 = dett * (jac3 * jac8 - jac2 * jac9);
+    double jaci5 = dett * (jac1 * jac9 - jac3 * jac7);
+    double jaci8 = dett * (jac2 * jac7 - jac1 * jac8);
+    double jaci3 = dett * (jac2 * jac6 - jac3 * jac5);
+    double jaci6 = dett * (jac3 * jac4 - jac1 * jac6);
+    double jaci9 = dett * (jac1 * jac5 - jac2 * jac4);
+    double jac12 = jaci1 + jaci2, jac45 = jaci4 + jaci5, jac78 = jaci7 + jaci8;
+    L.px[0][i] = -jac12 - jaci3;
+    L.py[0][i] = -jac45 - jaci6;
+    L.pz[0][i] = -jac78 - jaci9;
+    L.px[1][i] = -jac12 + jaci3;
+    L.py[1][i] = -jac45 + jaci6;
+    L.pz[1][i] = -jac78 + jaci9;
+    jac12 = jaci1 - jaci2;
+    jac45 = jaci4 - jaci5;
+    jac78 = jaci7 - jaci8;
+    L.px[2][i] = jac12 + jaci3;
+    L.py[2][i] = jac45 + jaci6;
+    L.pz[2][i] = jac78 + jaci9;
+    L.px[3][i] = jac12 - jaci3;
+    L.py[3][i] = jac45 - jaci6;
+    L.pz[3][i] = jac78 - jaci9;
+    // JHBE /= 0: hourglass projections (sderi3.F, three H vectors)
+    const double *xx[8], *yy[8], *zz[8];
+    for (int k = 0; k < 8; k++) {
+      xx[k] = &L.x[k][i];
+      yy[k] = &L.y[k][i];
+      zz[k] = &L.z[k][i];
+    }
+#define XK(k) (*xx[(k)-1])
+#define YK(k) (*yy[(k)-1])
+#define ZK(k) (*zz[(k)-1])
+    double hx, hy, hz;
+    hx = (XK(1) - XK(2) + XK(3) - XK(4) + XK(5) - XK(6) + XK(7) - XK(8));
+    hy = (YK(1) - YK(2) + YK(3) - YK(4) + YK(5) - YK(6) + YK(7) - YK(8));
+    hz = (ZK(1) - ZK(2) + ZK(3) - ZK(4) + ZK(5) - ZK(6) + ZK(7) - ZK(8));
+    for (int k = 0; k < 4; k++)
+      L.ph[k][0][i] = L.px[k][i] * hx + L.py[k][i] * hy + L.pz[k][i] * hz;
+    hx = (XK(1) + XK(2) - XK(3) - XK(4) - XK(5) - XK(6) + XK(7) + XK(8));
+    hy = (YK(1) + YK(2) - YK(3) - YK(4) - YK(5) - YK(6) + YK(7) + YK(8));
+    hz = (ZK(1) + ZK(2) - ZK(3) - ZK(4) - ZK(5) - ZK(6) + ZK(7) + ZK(8));
+    for (int k = 0; k < 4; k++)
+      L.ph[k][1][i] = L.px[k][i] * hx + L.py[k][i] * hy + L.pz[k][i] * hz;
+    hx = (XK(1) - XK(2) - XK(3) + XK(4) - XK(5) + XK(6) + XK(7) - XK(8));
+    hy = (YK(1) - YK(2) - YK(3) + YK(4) - YK(5) + YK(6) + YK(7) - YK(8));
+    hz = (ZK(1) - ZK(2) - ZK(3) + ZK(4) - ZK(5) + ZK(6) + ZK(7) - ZK(8));
+    for (int k = 0; k < 4; k++)
+      L.ph[k][2][i] = L.px[k][i] * hx + L.py[k][i] * hy + L.pz[k][i] * hz;
+#undef XK
+#undef YK
+#undef ZK
+  }
+
+  // SDLEN3 + SLEN (sdlen3.F:39-172, slen.F:30): DELTAX = 4 V / sqrt(max A^2)
+  {
+    static const int face[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                                   {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+    for (int i = 0; i < nel; i++) {
+      double aream = RG_EM20;
+      for (int j = 0; j < 6; j++) {
+        const int a = face[j][0], b = face[j][1], c = face[j][2], d = face[j][3];
+        double x13 = L.x[c][i] - L.x[a][i], x24 = L.x[d][i] - L.x[b][i];
+        double y13 = L.y[c][i] - L.y[a][i], y24 = L.y[d][i] - L.y[b][i];
+        double z13 = L.z[c][i] - L.z[a][i], z24 = L.z[d][i] - L.z[b][i];
+        double fs1 = x13 - x24, ft1 = x13 + x24;
+        double fs2 = y13 - y24, ft2 = y13 + y24;
+        double fs3 = z13 - z24, ft3 = z13 + z24;
+        double e = fs1 * fs1 + fs2 * fs2 + fs3 * fs3;
+        double f = fs1 * ft1 + fs2 * ft2 + fs3 * ft3;
+        double g = ft1 * ft1 + ft2 * ft2 + ft3 * ft3;
+        double area = e * g - f * f;
+        aream = std::max(area, aream);
+      }
+      L.deltax[i] = RG_FOUR * L.voln[i] * RG_ONE / std::sqrt(aream);
+    }
+  }
+
+  // SDEFO3 (sdefo3.F:32-313), JHBE=1, JCVT=0 branch.
+  const double dt1d2 = RG_HALF * DT1;
+  for (int i = 0; i < nel; i++) {
+    double vx17 = L.vx[0][i] - L.vx[6][i], vx28 = L.vx[1][i] - L.vx[7][i];
+    double vx35 = L.vx[2][i] - L.vx[4][i], vx46 = L.vx[3][i] - L.vx[5][i];
+    double vy17 = L.vy[0][i] - L.vy[6][i], vy28 = L.vy[1][i] - L.vy[7][i];
+    double vy35 = L.vy[2][i] - L.vy[4][i], vy46 = L.vy[3][i] - L.vy[5][i];
+    double vz17 = L.vz[0][i] - L.vz[6][i], vz28 = L.vz[1][i] - L.vz[7][i];
+    double vz35 = L.vz[2][i] - L.vz[4][i], vz46 = L.vz[3][i] - L.vz[5][i];
+    const double *PX = nullptr;
+    (void)PX;
+#define P_(a, k) L.a[k][i]
+    L.dxx[i] = P_(px, 0) * vx17 + P_(px, 1) * vx28 + P_(px, 2) * vx35 + P_(px, 3) * vx46;
+    L.dyy[i] = P_(py, 0) * vy17 + P_(py, 1) * vy28 + P_(py, 2) * vy35 + P_(py, 3) * vy46;
+    L.dzz[i] = P_(pz, 0) * vz17 + P_(pz, 1) * vz28 + P_(pz, 2) * vz35 + P_(pz, 3) * vz46;
+    L.dxy[i] = P_(py, 0) * vx17 + P_(py, 1) * vx28 + P_(py, 2) * vx35 + P_(py, 3) * vx46;
+    L.dxz[i] = P_(pz, 0) * vx17 + P_(pz, 1) * vx28 + P_(pz, 2) * vx35 + P_(pz, 3) * vx46;
+    L.dyx[i] = P_(px, 0) * vy17 + P_(px, 1) * vy28 + P_(px, 2) * vy35 + P_(px, 3) * vy46;
+    L.dyz[i] = P_(pz, 0) * vy17 + P_(pz, 1) * vy28 + P_(pz, 2) * vy35 + P_(pz, 3) * vy46;
+    L.dzx[i] = P_(px, 0) * vz17 + P_(px, 1) * vz28 + P_(px, 2) * vz35 + P_(px, 3) * vz46;
+    L.dzy[i] = P_(py, 0) * vz17 + P_(py, 1) * vz28 + P_(py, 2) * vz35 + P_(py, 3) * vz46;
+#undef P_
+    L.d4[i] = L.dxy[i] + L.dyx[i];
+    L.d5[i] = L.dyz[i] + L.dzy[i];
+    L.d6[i] = L.dxz[i] + L.dzx[i];
+    L.wzz[i] = dt1d2 * (L.dyx[i] - L.dxy[i]);
+    L.wyy[i] = dt1d2 * (L.dxz[i] - L.dzx[i]);
+    L.wxx[i] = dt1d2 * (L.dzy[i] - L.dyz[i]);
+  }
+
+  // SRHO3 Lagrangian branch (srho3.F:140-150): VOLO = GBUF%VOL (initial)
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    L.divde[i] = DT1 * (L.dxx[i] + L.dyy[i] + L.dzz[i]);
+    if (M.offg[e] == RG_ZERO && L.voln[i] == RG_ONE) L.voln[i] = M.vol[e];
+    L.dvol[i] = L.voln[i] - (G.rho0 / M.rho[e]) * M.vol[e];
+    M.rho[e] = G.rho0 * (M.vol[e] / L.voln[i]);
+    M.eint[e] = M.eint[e] * M.vol[e];
+  }
+
+  // SROTA3 (srota3.F:40-97): Jaumann rotation; S = stress before rotation
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    for (int c = 0; c < 6; c++) L.s[c][i] = SIG[c * NE + e];
+    const double s1 = L.s[0][i], s2 = L.s[1][i], s3 = L.s[2][i],
+                 s4 = L.s[3][i], s5 = L.s[4][i], s6 = L.s[5][i];
+    const double q1 = RG_TWO * s4 * L.wzz[i];
+    const double q2 = RG_TWO * s6 * L.wyy[i];
+    const double q3 = RG_TWO * s5 * L.wxx[i];
+    SIG[0 * NE + e] = s1 - q1 + q2;
+    SIG[1 * NE + e] = s2 + q1 - q3;
+    SIG[2 * NE + e] = s3 - q2 + q3;
+    SIG[3 * NE + e] = s4 + L.wzz[i] * (s1 - s2) + L.wyy[i] * s5 - L.wxx[i] * s6;
+    SIG[4 * NE + e] = s5 + L.wxx[i] * (s2 - s3) + L.wzz[i] * s6 - L.wyy[i] * s4;
+    SIG[5 * NE + e] = s6 + L.wyy[i] * (s3 - s1) + L.wxx[i] * s4 - L.wzz[i] * s5;
+  }
+
+  // MMAIN prologue (mmain.F90:676-760): VOL_AVG, AMU (LAW1/2), RHOREF=RHO
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    L.vol_avg[i] = L.voln[i] - RG_HALF * L.dvol[i];
+    L.amu[i] = M.rho[e] / G.rho0 - RG_ONE;
+  }
+
+  // ---- material law: deviatoric update + radial return -------------------
+  double dpla[MVSIZ];
+  if (G.mtn == 1) {
+    // M1LAW (m1law.F:35-190) first loop
+    for (int i = 0; i < nel; i++) {
+      const int e = nft + i;
+      const double gg = G.g * L.off[i];
+      const double g1 = DT1 * gg, g2 = RG_TWO * g1;
+      L.ssp[i] = std::sqrt((RG_ONEP333 * gg + G.c1) / G.rho0);
+      double *sg[6];
+      for (int c = 0; c < 6; c++) sg[c] = &SIG[c * NE + e];
+      const double p = -RG_THIRD * (*sg[0] + *sg[1] + *sg[2]);
+      const double dav = -RG_THIRD * (L.dxx[i] + L.dyy[i] + L.dzz[i]);
+      *sg[0] = *sg[0] + p + g2 * (L.dxx[i] + dav);
+      *sg[1] = *sg[1] + p + g2 * (L.dyy[i] + dav);
+      *sg[2] = *sg[2] + p + g2 * (L.dzz[i] + dav);
+      *sg[3] = *sg[3] + g1 * L.d4[i];
+      *sg[4] = *sg[4] + g1 * L.d5[i];
+      *sg[5] = *sg[5] + g1 * L.d6[i];
+    }
+  } else {
+    // M2LAW (m2law.F:38-580), Johnson-Cook, FISOKIN = 0, IFORM = 0, no
+    // thermal (TSTAR = 0), explicit (IMPL_S = 0).
+    const double asrate = std::min(RG_ONE, G.asrate * DT1);
+    for (int i = 0; i < nel; i++) {
+      const int e = nft + i;
+      const double gg = G.g * L.off[i];
+      double *sg[6];
+      for (int c = 0; c < 6; c++) sg[c] = &SIG[c * NE + e];
+      const double p = -RG_THIRD * (*sg[0] + *sg[1] + *sg[2]);
+      const double dav = -RG_THIRD * (L.dxx[i] + L.dyy[i] + L.dzz[i]);
+      const double g1 = DT1 * gg, g2 = RG_TWO * g1;
+      L.ssp[i] = std::sqrt((RG_ONEP333 * gg + G.c1) / G.rho0);
+      *sg[0] = *sg[0] + p + g2 * (L.dxx[i] + dav);
+      *sg[1] = *sg[1] + p + g2 * (L.dyy[i] + dav);
+      *sg[2] = *sg[2] + p + g2 * (L.dzz[i] + dav);
+      *sg[3] = *sg[3] + g1 * L.d4[i];
+      *sg[4] = *sg[4] + g1 * L.d5[i];
+      *sg[5] = *sg[5] + g1 * L.d6[i];
+      double aj2 = RG_HALF * (*sg[0] * *sg[0] + *sg[1] * *sg[1] + *sg[2] * *sg[2]) +
+                   *sg[3] * *sg[3] + *sg[4] * *sg[4] + *sg[5] * *sg[5];
+      aj2 = std::sqrt(RG_THREE * aj2);
+      // MSTRAIN_RATE (mstrain_rate.F), IDEV = VP-2
+      if (G.israte >= 0) {
+        double epsdot;
+        if (G.vp - 2 == 0) {
+          const double e1 = L.dxx[i], e2 = L.dyy[i], e3 = L.dzz[i];
+          const double e4 = RG_HALF * L.d4[i], e5 = RG_HALF * L.d5[i],
+                       e6 = RG_HALF * L.d6[i];
+          const double epsp = e1 * e1 + e2 * e2 + e3 * e3 +
+                              RG_TWO * (e4 * e4 + e5 * e5 + e6 * e6);
+          epsdot = std::sqrt(epsp);
+        } else {
+          const double dv = (L.dxx[i] + L.dyy[i] + L.dzz[i]) * RG_THIRD;
+          const double e1 = L.dxx[i] - dv, e2 = L.dyy[i] - dv, e3 = L.dzz[i] - dv;
+          const double e4 = RG_HALF * L.d4[i], e5 = RG_HALF * L.d5[i],
+                       e6 = RG_HALF * L.d6[i];
+          const double epsp = RG_HALF * (e1 * e1 + e2 * e2 + e3 * e3) +
+                              e4 * e4 + e5 * e5 + e6 * e6;
+          epsdot = std::sqrt(RG_THREE * epsp) / RG_THREE_HALF;
+        }
+        if (G.israte == 0)
+          M.epsd[e] = epsdot;
+        else
+          M.epsd[e] = asrate * epsdot + (RG_ONE - asrate) * M.epsd[e];
+      }
+      double epd = RG_ONE, sigmx = G.sigm0;
+      if (G.cc != RG_ZERO) {
+        if (G.vp == 1) {
+          epd = std::max(M.epsd[e], G.epdr);
+          epd = std::log(epd / G.epdr);
+        } else {
+          epd = std::max(M.epsd[e], RG_EM15);
+          epd = std::log(epd / G.epdr);
+        }
+        const double mt = std::max(RG_EM15, G.z3);
+        epd = std::max(RG_ZERO, epd);
+        epd = (RG_ONE + G.cc * epd) * (RG_ONE - std::pow(RG_ZERO, mt));
+        if (G.icc == 1) sigmx = G.sigm0 * epd;
+      } else {
+        const double mt = std::max(RG_EM15, G.z3);
+        epd = RG_ONE - std::pow(RG_ZERO, mt);
+        if (G.icc == 1) sigmx = G.sigm0 * epd;
+      }
+      const double epxe = M.pla[e];
+      double ak, qh;
+      if (G.cn == RG_ONE) {
+        ak = G.ca + G.cb * epxe;
+        qh = G.cb * epd;
+      } else if (epxe > RG_ZERO) {
+        ak = G.ca + G.cb * std::pow(epxe, G.cn);
+        if (G.cn > RG_ONE)
+          qh = (G.cb * G.cn * std::pow(epxe, G.cn - RG_ONE)) * epd;
+        else
+          qh = (G.cb * G.cn / std::pow(epxe, RG_ONE - G.cn)) * epd;
+      } else {
+        ak = G.ca;
+        qh = RG_ZERO;
+      }
+      ak = ak * epd;
+      if (sigmx < ak) {
+        ak = sigmx;
+        qh = RG_ZERO;
+      }
+      if (epxe > G.epmx) {
+        ak = RG_ZERO;
+        qh = RG_ZERO;
+      }
+      double scale = std::min(RG_ONE, ak / std::max(aj2, RG_EM15));
+      dpla[i] = (RG_ONE - scale) * aj2 / std::max(RG_THREE * gg + qh, RG_EM15);
+      ak = ak + (RG_ONE - G.fisokin) * dpla[i] * qh;
+      scale = std::min(RG_ONE, ak / std::max(aj2, RG_EM15));
+      for (int c = 0; c < 6; c++) *sg[c] = scale * *sg[c];
+      M.pla[e] = epxe + dpla[i];
+    }
+  }
+
+  // MQVISCB (mqviscb.F:44-600): explicit, 3D, one point (FACPG = 1),
+  // VISI = 1, FACQ = 1; VOL = VNEW, VOL0 = initial volume.
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    const double dd = -L.dxx[i] - L.dyy[i] - L.dzz[i];
+    double al = RG_ZERO, ad = RG_ZERO;
+    const double cx = L.ssp[i] + std::sqrt(RG_ZERO);  // VD2 = 0 (Lagrange)
+    if (L.off[i] == RG_ONE) {
+      if (L.voln[i] > RG_ZERO)
+        al = std::pow(L.voln[i], RG_ONE / RG_THREE);
+      else
+        al = RG_ZERO;
+      ad = std::max(RG_ZERO, dd);
+    }
+    const double rhoe = M.rho[e];
+    const double nrho = std::sqrt(rhoe * G.rho0);  // RHOREF = RHO (ISMSTR 4)
+    const double qa = RG_ONE * G.qa, qb = RG_ONE * G.qb;
+    const double cns1 = RG_ONE * G.vns1 * al * nrho * L.ssp[i] * L.off[i];
+    const double cns2 = RG_ONE * G.vns2 * al * nrho * L.ssp[i] * L.off[i];
+    const double qaa = qa * qa * ad;
+    const double vis = RG_ZERO;
+    const double qx = qb * L.ssp[i] + al * qaa +
+                      RG_ONE * RG_TWO * vis / std::max(RG_EM20, rhoe * L.deltax[i]) +
+                      (cns1 + RG_ONE * cns2) / std::max(RG_EM20, rhoe * L.deltax[i]);
+    L.qnew[i] = rhoe * ad * al * (qaa * al + qb * L.ssp[i]);
+    L.ssp_eq[i] = std::max(RG_EM20, qx + std::sqrt(qx * qx + cx * cx));
+    double dtx = L.deltax[i] / L.ssp_eq[i];
+    // STI (ISMSTR /= 1, 11): STI = (RHO/DTX) * (VOL/DTX)
+    L.sti[i] = RG_ZERO;
+    if (!(L.off[i] == RG_ZERO || M.offg[e] < RG_ZERO)) {
+      const double tidt = RG_ONE / dtx;
+      const double trho = rhoe * tidt;
+      const double tvol = L.voln[i] * tidt;
+      L.sti[i] = trho * tvol;
+    }
+    dtx = M.dtfac_solid * dtx;
+    // NODADT = 0: DT2T = min over live elements (mqviscb.F:520-535)
+    if (L.voln[i] > RG_ZERO && (L.off[i] != RG_ZERO && M.offg[e] >= RG_ZERO)) {
+      if (!(dtx > dt2t)) {
+        dt2t = dtx;
+        neltst = e;
+      }
+    }
+  }
+
+  // Law epilogue: pressure, energy, QOLD (m1law.F:170-190, m2law.F:430-460)
+  const double dta = RG_HALF * DT1;
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    double *sg[6];
+    for (int c = 0; c < 6; c++) sg[c] = &SIG[c * NE + e];
+    const double pnew = G.c1 * L.amu[i];
+    *sg[0] = (*sg[0] - pnew) * L.off[i];
+    *sg[1] = (*sg[1] - pnew) * L.off[i];
+    *sg[2] = (*sg[2] - pnew) * L.off[i];
+    *sg[3] = *sg[3] * L.off[i];
+    *sg[4] = *sg[4] * L.off[i];
+    *sg[5] = *sg[5] * L.off[i];
+    double einc;
+    if (G.mtn == 1) {
+      const double p2 = -(L.s[0][i] + *sg[0] + L.s[1][i] + *sg[1] + L.s[2][i] + *sg[2]) *
+                        RG_THIRD;
+      const double e1 = L.dxx[i] * (L.s[0][i] + *sg[0] + p2);
+      const double e2 = L.dyy[i] * (L.s[1][i] + *sg[1] + p2);
+      const double e3 = L.dzz[i] * (L.s[2][i] + *sg[2] + p2);
+      const double e4 = L.d4[i] * (L.s[3][i] + *sg[3]);
+      const double e5 = L.d5[i] * (L.s[4][i] + *sg[4]);
+      const double e6 = L.d6[i] * (L.s[5][i] + *sg[5]);
+      einc = L.vol_avg[i] * (e1 + e2 + e3 + e4 + e5 + e6) * dta -
+             RG_HALF * L.dvol[i] * (M.qvis[e] + L.qnew[i] + p2);
+    } else {
+      const double e1 = L.dxx[i] * (L.s[0][i] + *sg[0]);
+      const double e2 = L.dyy[i] * (L.s[1][i] + *sg[1]);
+      const double e3 = L.dzz[i] * (L.s[2][i] + *sg[2]);
+      const double e4 = L.d4[i] * (L.s[3][i] + *sg[3]);
+      const double e5 = L.d5[i] * (L.s[4][i] + *sg[4]);
+      const double e6 = L.d6[i] * (L.s[5][i] + *sg[5]);
+      einc = L.vol_avg[i] * (e1 + e2 + e3 + e4 + e5 + e6) * dta -
+             RG_HALF * L.dvol[i] * (M.qvis[e] + L.qnew[i]);
+    }
+    M.eint[e] = (M.eint[e] + einc * L.off[i]) / std::max(RG_EM15, M.vol[e]);
+    M.qvis[e] = L.qnew[i];
+  }
+
+  // SMALLB3 (smallb3.F:45): OFF < 1 propagates to OFFG
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    if (L.off[i] < RG_ONE) {
+      if (L.off[i] == RG_ZERO)
+        M.offg[e] = RG_ZERO;
+      else if (M.offg[e] > RG_ONE)
+        M.offg[e] = RG_ONE + L.off[i];
+      else
+        M.offg[e] = L.off[i];
+    }
+  }
+
+  // SHVIS3 (shvis3.F:31-473), IINT=1, JHBE>=1, ISMSTR=4 (not 1, 2).
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    const double caq = RG_FOURTH * L.off[i] * G.qh;
+    double fcl = caq * M.rho[e] * std::pow(L.voln[i], RG_TWO_THIRD);
+    const double fcq = fcl * caq * RG_HUNDRED;
+    fcl = fcl * L.ssp[i];
+    const double *vx = &L.vx[0][0], *vy = &L.vy[0][0], *vz = &L.vz[0][0];
+    (void)vx; (void)vy; (void)vz;
+#define VX(k) L.vx[(k)-1][i]
+#define VY(k) L.vy[(k)-1][i]
+#define VZ(k) L.vz[(k)-1][i]
+#define PH(k, j) L.ph[(k)-1][(j)-1][i]
+    double g[8][3];
+    g[0][0] = RG_ONE - PH(1, 1);
+    g[1][0] = -RG_ONE - PH(2, 1);
+    g[2][0] = RG_ONE - PH(3, 1);
+    g[3][0] = -RG_ONE - PH(4, 1);
+    g[4][0] = RG_ONE + PH(3, 1);
+    g[5][0] = -RG_ONE + PH(4, 1);
+    g[6][0] = RG_ONE + PH(1, 1);
+    g[7][0] = -RG_ONE + PH(2, 1);
+    g[0][1] = RG_ONE - PH(1, 2);
+    g[1][1] = RG_ONE - PH(2, 2);
+    g[2][1] = -RG_ONE - PH(3, 2);
+    g[3][1] = -RG_ONE - PH(4, 2);
+    g[4][1] = -RG_ONE + PH(3, 2);
+    g[5][1] = -RG_ONE + PH(4, 2);
+    g[6][1] = RG_ONE + PH(1, 2);
+    g[7][1] = RG_ONE + PH(2, 2);
+    g[0][2] = RG_ONE - PH(1, 3);
+    g[1][2] = -RG_ONE - PH(2, 3);
+    g[2][2] = -RG_ONE - PH(3, 3);
+    g[3][2] = RG_ONE - PH(4, 3);
+    g[4][2] = -RG_ONE + PH(3, 3);
+    g[5][2] = RG_ONE + PH(4, 3);
+    g[6][2] = RG_ONE + PH(1, 3);
+    g[7][2] = -RG_ONE + PH(2, 3);
+    double hgx[4], hgy[4], hgz[4];
+    for (int m = 0; m < 3; m++) {
+      hgx[m] = g[0][m] * VX(1) + g[1][m] * VX(2) + g[2][m] * VX(3) + g[3][m] * VX(4) +
+               g[4][m] * VX(5) + g[5][m] * VX(6) + g[6][m] * VX(7) + g[7][m] * VX(8);
+      hgy[m] = g[0][m] * VY(1) + g[1][m] * VY(2) + g[2][m] * VY(3) + g[3][m] * VY(4) +
+               g[4][m] * VY(5) + g[5][m] * VY(6) + g[6][m] * VY(7) + g[7][m] * VY(8);
+      hgz[m] = g[0][m] * VZ(1) + g[1][m] * VZ(2) + g[2][m] * VZ(3) + g[3][m] * VZ(4) +
+               g[4][m] * VZ(5) + g[5][m] * VZ(6) + g[6][m] * VZ(7) + g[7][m] * VZ(8);
+    }
+    hgx[3] = VX(1) - VX(2) + VX(3) - VX(4) - VX(5) + VX(6) - VX(7) + VX(8);
+    hgy[3] = VY(1) - VY(2) + VY(3) - VY(4) - VY(5) + VY(6) - VY(7) + VY(8);
+    hgz[3] = VZ(1) - VZ(2) + VZ(3) - VZ(4) - VZ(5) + VZ(6) - VZ(7) + VZ(8);
+    double hx[4], hy[4], hz[4];
+    for (int m = 0; m < 4; m++) {
+      hx[m] = hgx[m] * (fcl + std::fabs(hgx[m]) * fcq);
+      hy[m] = hgy[m] * (fcl + std::fabs(hgy[m]) * fcq);
+      hz[m] = hgz[m] * (fcl + std::fabs(hgz[m]) * fcq);
+    }
+    static const double s4[8] = {-1, 1, -1, 1, 1, -1, 1, -1};
+    for (int k = 0; k < 8; k++) {
+      // F1k = -G k1*HX1 - G k2*HX2 - G k3*HX3 +/- HX4
+      const double *gk = g[k];
+      if (s4[k] < 0) {
+        L.f[0][k][i] = -gk[0] * hx[0] - gk[1] * hx[1] - gk[2] * hx[2] - hx[3];
+        L.f[1][k][i] = -gk[0] * hy[0] - gk[1] * hy[1] - gk[2] * hy[2] - hy[3];
+        L.f[2][k][i] = -gk[0] * hz[0] - gk[1] * hz[1] - gk[2] * hz[2] - hz[3];
+      } else {
+        L.f[0][k][i] = -gk[0] * hx[0] - gk[1] * hx[1] - gk[2] * hx[2] + hx[3];
+        L.f[1][k][i] = -gk[0] * hy[0] - gk[1] * hy[1] - gk[2] * hy[2] + hy[3];
+        L.f[2][k][i] = -gk[0] * hz[0] - gk[1] * hz[1] - gk[2] * hz[2] + hz[3];
+      }
+    }
+    const double ehou =
+        DT1 * (hz[0] * hgz[0] + hz[1] * hgz[1] + hz[2] * hgz[2] + hz[3] * hgz[3] +
+               hx[0] * hgx[0] + hx[1] * hgx[1] + hx[2] * hgx[2] + hx[3] * hgx[3] +
+               hy[0] * hgy[0] + hy[1] * hgy[1] + hy[2] * hgy[2] + hy[3] * hgy[3]);
+    M.ehou[e] += ehou;
+#undef VX
+#undef VY
+#undef VZ
+#undef PH
+  }
+
+  // SFINT3 Lagrangian branch (sfint3.F:257-361): S = (SIG - QVIS) * VOLN
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    const double q = L.qnew[i], v = L.voln[i];
+    const double s1 = (SIG[0 * NE + e] + RG_ZERO - q) * v;
+    const double s2 = (SIG[1 * NE + e] + RG_ZERO - q) * v;
+    const double s3 = (SIG[2 * NE + e] + RG_ZERO - q) * v;
+    const double s4 = (SIG[3 * NE + e] + RG_ZERO) * v;
+    const double s5 = (SIG[4 * NE + e] + RG_ZERO) * v;
+    const double s6 = (SIG[5 * NE + e] + RG_ZERO) * v;
+    // nodes (1,7) (2,8) (3,5) (4,6) share P with opposite sign
+    static const int pa[4] = {0, 1, 2, 3}, pb[4] = {6, 7, 4, 5};
+    for (int j = 0; j < 4; j++) {
+      const double px = L.px[j][i], py = L.py[j][i], pz = L.pz[j][i];
+      double fint = s1 * px + s4 * py + s6 * pz;
+      L.f[0][pa[j]][i] = L.f[0][pa[j]][i] - fint;
+      L.f[0][pb[j]][i] = L.f[0][pb[j]][i] + fint;
+      fint = s2 * py + s4 * px + s5 * pz;
+      L.f[1][pa[j]][i] = L.f[1][pa[j]][i] - fint;
+      L.f[1][pb[j]][i] = L.f[1][pb[j]][i] + fint;
+      fint = s3 * pz + s6 * px + s5 * py;
+      L.f[2][pa[j]][i] = L.f[2][pa[j]][i] - fint;
+      L.f[2][pb[j]][i] = L.f[2][pb[j]][i] + fint;
+    }
+  }
+
+  // SCUMU3P (scumu3p.F:37-664): zero deleted (OFFG<0) elements, STI/4,
+  // write FSKY(1:3,K), FSKY(7,K) at K = IADS(k, e).
+  for (int i = 0; i < nel; i++) {
+    const int e = nft + i;
+    if (M.offg[e] < RG_ZERO)
+      for (int c = 0; c < 3; c++)
+        for (int k = 0; k < 8; k++) L.f[c][k][i] = RG_ZERO;
+    const double sti = RG_FOURTH * L.sti[i];
+    for (int k = 0; k < 8; k++) {
+      const int K = M.iads[8 * e + k] - 1;
+      double *fs = &M.fsky[8 * K];
+      fs[0] = L.f[0][k][i];
+      fs[1] = L.f[1][k][i];
+      fs[2] = L.f[2][k][i];
+      fs[6] = sti;
+    }
+  }
+}
+
+}  // namespace
+
+// shells (rg_oracle_shell.cpp)
+namespace rg_oracle_shell {
+struct Shells;
+Shells *create();
+void destroy(Shells *);
+int group_add(Shells *, int nel, const int *ixc, int npt, const double *pm,
+              const double *geo, const double *uparam, const int *iparam,
+              const double *thk0, int ismstr, int ithk);
+int numelc(const Shells *);
+const int *ixc(const Shells *);
+int *iadc(Shells *);
+void step(Shells *, const double *X, const double *V, const double *VR,
+          double *fsky, double dt1, double dtfac, double &dt2t, int &neltst,
+          int &error, int nthreads);
+void energy(const Shells *, double &eint, double &ehour);
+int rwall_add(Shells *, const double *p0, const double *nrm, double dsearch);
+void rwall_apply(Shells *, int numnod, const double *X, double *V,
+                 const double *A, double dt12);
+}  // namespace rg_oracle_shell
+
+struct OrModelWrap {
+  Model m;
+  rg_oracle_shell::Shells *sh = nullptr;
+  // planar rigid walls
+  struct Wall {
+    double p0[3], n[3], dsearch;
+    std::vector<int> slaves;
+  };
+  std::vector<Wall> walls;
+};
+
+extern "C" {
+
+void *or_model_new(int numnod, const double *x, const double *v,
+                   const double *ms, const int *icodt) {
+  auto *w = new OrModelWrap();
+  Model &M = w->m;
+  M.numnod = numnod;
+  M.X.assign(x, x + 3 * (size_t)numnod);
+  M.V.assign(v, v + 3 * (size_t)numnod);
+  M.D.assign(3 * (size_t)numnod, 0.0);
+  M.A.assign(3 * (size_t)numnod, 0.0);
+  M.AR.assign(3 * (size_t)numnod, 0.0);
+  M.VR.assign(3 * (size_t)numnod, 0.0);
+  M.DR.assign(3 * (size_t)numnod, 0.0);
+  M.FLAST.assign(3 * (size_t)numnod, 0.0);
+  M.FRLAST.assign(3 * (size_t)numnod, 0.0);
+  M.STIFN.assign(numnod, 0.0);
+  M.STIFR.assign(numnod, 0.0);
+  M.MS.assign(ms, ms + numnod);
+  M.IN.assign(numnod, 0.0);
+  M.icodt.assign(numnod, 0);
+  if (icodt) M.icodt.assign(icodt, icodt + numnod);
+  w->sh = rg_oracle_shell::create();
+  return w;
+}
+
+void or_model_free(void *m) {
+  auto *w = (OrModelWrap *)m;
+  if (!w) return;
+  rg_oracle_shell::destroy(w->sh);
+  delete w;
+}
+
+int or_set_inertia(void *m, const double *in) {
+  Model &M = ((OrModelWrap *)m)->m;
+  M.IN.assign(in, in + M.numnod);
+  return 0;
+}
+
+int or_hexa_group_add(void *m, int nel, const int *ixs, int mtn,
+                      const double *pm, const double *geo,
+                      const double *uparam, const int *iparam, int ismstr,
+                      int jhbe, int jcvt) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (M.finalized || nel <= 0) return -1;
+  if (mtn != 1 && mtn != 2) return -2;
+  if (jcvt != 0 || jhbe != 1 || ismstr != 4) return -3;
+  // Split into MVSIZ-long groups like the starter (SGRTAILS).
+  for (int s = 0; s < nel; s += MVSIZ) {
+    HexaGroup G;
+    G.nft = M.numels + s;
+    G.nel = std::min(MVSIZ, nel - s);
+    G.mtn = mtn;
+    G.ismstr = ismstr;
+    G.jhbe = jhbe;
+    G.jcvt = jcvt;
+    G.rho0 = pm[0];
+    G.g = pm[21];
+    G.c1 = pm[31];
+    G.qh = geo[12];
+    G.qa = geo[13];
+    G.qb = geo[14];
+    G.vns1 = geo[15];
+    G.vns2 = geo[16];
+    if (mtn == 2) {
+      G.iform = iparam[0];
+      G.icc = iparam[1];
+      G.vp = iparam[2];
+      G.israte = iparam[3];
+      G.ca = uparam[0];
+      G.cb = uparam[1];
+      G.cn = uparam[2];
+      G.epmx = uparam[3];
+      G.sigm0 = uparam[4];
+      G.cc = uparam[5];
+      G.epdr = uparam[6];
+      G.fisokin = uparam[7];
+      G.asrate = uparam[8];
+      G.z3 = uparam[9];
+      if (G.iform != 0 || G.fisokin != 0.0) return -4;
+    }
+    M.hg.push_back(G);
+  }
+  const size_t old = M.numels;
+  M.numels += nel;
+  M.ixs.insert(M.ixs.end(), ixs, ixs + 11 * (size_t)nel);
+  // element state: initial values (starter): SIG = 0, EINT = 0, RHO = RHO0,
+  // OFF = 1, volume from the initial geometry (computed at finalize).
+  M.eint.resize(M.numels, 0.0);
+  M.rho.resize(M.numels, pm[0]);
+  M.vol.resize(M.numels, 0.0);
+  M.qvis.resize(M.numels, 0.0);
+  M.offg.resize(M.numels, 1.0);
+  M.pla.resize(M.numels, 0.0);
+  M.epsd.resize(M.numels, 0.0);
+  M.ehou.resize(M.numels, 0.0);
+  (void)old;
+  return (int)M.hg.size() - 1;
+}
+
+int or_shell_group_add(void *m, int nel, const int *ixc, int npt,
+                       const double *pm, const double *geo,
+                       const double *uparam, const int *iparam,
+                       const double *thk0, int ismstr, int ithk) {
+  auto *w = (OrModelWrap *)m;
+  if (w->m.finalized) return -1;
+  return rg_oracle_shell::group_add(w->sh, nel, ixc, npt, pm, geo, uparam,
+                                    iparam, thk0, ismstr, ithk);
+}
+
+int or_rwall_add(void *m, const double *p0, const double *nrm, double dsearch) {
+  auto *w = (OrModelWrap *)m;
+  OrModelWrap::Wall W;
+  for (int c = 0; c < 3; c++) {
+    W.p0[c] = p0[c];
+    W.n[c] = nrm[c];
+  }
+  W.dsearch = dsearch;
+  w->walls.push_back(W);
+  return (int)w->walls.size() - 1;
+}
+
+// Initial hexa volume: the SDERI3 determinant of the initial geometry.
+static double hexa_volume(const Model &M, int e) {
+  double x[8], y[8], z[8];
+  for (int k = 0; k < 8; k++) {
+    const int n = M.ixs[11 * e + 1 + k] - 1;
+    x[k] = M.X[3 * n];
+    y[k] = M.X[3 * n + 1];
+    z[k] = M.X[3 * n + 2];
+  }
+  double x17 = x[6] - x[0], x28 = x[7] - x[1], x35 = x[4] - x[2], x46 = x[5] - x[3];
+  double y17 = y[6] - y[0], y28 = y[7] - y[1], y35 = y[4] - y[2], y46 = y[5] - y[3];
+  double z17 = z[6] - z[0], z28 = z[7] - z[1], z35 = z[4] - z[2], z46 = z[5] - z[3];
+  double jac1 = x17 + x28 - x35 - x46, jac2 = y17 + y28 - y35 - y46,
+         jac3 = z17 + z28 - z35 - z46;
+  double jac4 = (x17 + x46) + (x28 + x35), jac5 = (y17 + y46) + (y28 + y35),
+         jac6 = (z17 + z46) + (z28 + z35);
+  double jac7 = (x17 + x46) - (x28 + x35), jac8 = (y17 + y46) - (y28 + y35),
+         jac9 = (z17 + z46) - (z28 + z35);
+  return RG_ONE_OVER_64 * (jac1 * (jac5 * jac9 - jac6 * jac8) +
+                           jac2 * (jac6 * jac7 - jac4 * jac9) +
+                           jac3 * (jac4 * jac8 - jac5 * jac7));
+}
+
+int or_finalize(void *m, double dtfac_solid, double dtfac_shell, double dtmx,
+                double dt2old_init, int nthreads) {
+  auto *w = (OrModelWrap *)m;
+  Model &M = w->m;
+  if (M.finalized) return -1;
+  M.dtfac_solid = dtfac_solid;
+  M.dtfac_shell = dtfac_shell;
+  M.dtmx = dtmx;
+  M.dt2old = dt2old_init;
+  M.nthreads = nthreads > 0 ? nthreads : 1;
+  // sig 6 x numels SoA
+  M.sig.assign(6 * (size_t)M.numels, 0.0);
+  for (int e = 0; e < M.numels; e++) M.vol[e] = hexa_volume(M, e);
+
+  // FILLCNE (starter/source/spmd/domdec2.F:2046-2250): per node, solids in
+  // increasing user-id order (stable), then shells in increasing user-id
+  // order.  W_PON (restart/ddsplit/w_pon.F:581-700) turns CNE positions
+  // into IADS / IADC slot numbers.
+  const int numelc = rg_oracle_shell::numelc(w->sh);
+  const int *ixc = rg_oracle_shell::ixc(w->sh);
+  std::vector<int> cnt(M.numnod + 2, 0);
+  for (int e = 0; e < M.numels; e++)
+    for (int k = 0; k < 8; k++) cnt[M.ixs[11 * e + 1 + k]]++;
+  for (int e = 0; e < numelc; e++)
+    for (int k = 0; k < 4; k++) cnt[ixc[7 * e + 1 + k]]++;
+  M.adsky.assign(M.numnod + 1, 0);
+  M.adsky[0] = 1;
+  for (int n = 1; n <= M.numnod; n++) M.adsky[n] = M.adsky[n - 1] + cnt[n];
+  M.lsky = M.adsky[M.numnod] - 1;
+  std::vector<int> fill(M.adsky.begin(), M.adsky.end() - 1);  // next slot
+  std::vector<int> ord(M.numels);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+    return M.ixs[11 * a + 10] < M.ixs[11 * b + 10];
+  });
+  M.iads.assign(8 * (size_t)M.numels, 0);
+  for (int e : ord)
+    for (int k = 0; k < 8; k++) {
+      const int n = M.ixs[11 * e + 1 + k];
+      M.iads[8 * e + k] = fill[n - 1]++;
+    }
+  std::vector<int> ordc(numelc);
+  std::iota(ordc.begin(), ordc.end(), 0);
+  std::stable_sort(ordc.begin(), ordc.end(), [&](int a, int b) {
+    return ixc[7 * a + 6] < ixc[7 * b + 6];
+  });
+  int *iadc = rg_oracle_shell::iadc(w->sh);
+  for (int e : ordc)
+    for (int k = 0; k < 4; k++) {
+      const int n = ixc[7 * e + 1 + k];
+      iadc[4 * e + k] = fill[n - 1]++;
+    }
+  M.fsky.assign(8 * (size_t)std::max(M.lsky, 1), 0.0);
+
+  // rigid-wall slave nodes (all nodes within dsearch of the plane)
+  for (auto &W : w->walls) {
+    for (int n = 0; n < M.numnod; n++) {
+      double d = (M.X[3 * n] - W.p0[0]) * W.n[0] + (M.X[3 * n + 1] - W.p0[1]) * W.n[1] +
+                 (M.X[3 * n + 2] - W.p0[2]) * W.n[2];
+      if (d <= W.dsearch) W.slaves.push_back(n);
+    }
+  }
+  M.finalized = true;
+  return 0;
+}
+
+int or_get_skyline(void *m, int *adsky, int *iads, int *iadc, int *lsky) {
+  auto *w = (OrModelWrap *)m;
+  Model &M = w->m;
+  if (!M.finalized) return -1;
+  if (adsky) std::copy(M.adsky.begin(), M.adsky.end(), adsky);
+  if (iads) std::copy(M.iads.begin(), M.iads.end(), iads);
+  if (iadc) {
+    const int nc = rg_oracle_shell::numelc(w->sh);
+    std::copy(rg_oracle_shell::iadc(w->sh), rg_oracle_shell::iadc(w->sh) + 4 * nc, iadc);
+  }
+  if (lsky) *lsky = M.lsky;
+  return 0;
+}
+
+// One explicit cycle in RESOL order (engine/source/engine/resol.F).
+int or_cycle(void *m, int ncycle) {
+  auto *w = (OrModelWrap *)m;
+  Model &M = w->m;
+  if (!M.finalized) return -1;
+  const int numnod = M.numnod;
+  const bool rot = rg_oracle_shell::numelc(w->sh) > 0;
+  for (int c = 0; c < ncycle; c++) {
+    // resol.F:2721-2722, 2826: DT1 = DT2, DT2 = 1e6, DT2T = DT2
+    M.dt1 = M.dt2;
+    M.dt2 = RG_EP06;
+    double dt2t = M.dt2;
+    int neltst = 0;
+    // FORINT: element groups (OpenMP over groups, forint.F:339).  Each
+    // group reports the minimum of DTFAC1*DTX and the last element (group
+    // order) attaining it; ties across groups resolve to the larger global
+    // element index, i.e. the sequential-order result of MQVISCB.
+    const int ng = (int)M.hg.size();
+    std::vector<double> gdt(ng, RG_EP06);
+    std::vector<int> gel(ng, -1);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(M.nthreads)
+    for (int g = 0; g < ng; g++) {
+      double d = RG_EP06;
+      int el = -1;
+      hexa_group(M, M.hg[g], d, el);
+      gdt[g] = d;
+      gel[g] = el;
+    }
+    int eidx = -1;
+    for (int g = 0; g < ng; g++)
+      if (gel[g] >= 0 && !(gdt[g] > dt2t)) {
+        dt2t = gdt[g];
+        eidx = gel[g];
+      }
+    if (eidx >= 0) neltst = M.ixs[11 * eidx + 10];
+    if (rot) {
+      int err = 0;
+      double d = dt2t;
+      int el = neltst;
+      rg_oracle_shell::step(w->sh, M.X.data(), M.V.data(), M.VR.data(),
+                            M.fsky.data(), M.dt1, M.dtfac_shell, d, el, err,
+                            M.nthreads);
+      M.error |= err;
+      if (d < dt2t) {
+        dt2t = d;
+        neltst = el;
+      }
+    }
+    // ASSPAR4 (asspar4.F:165-180): fixed-order slot sums
+#pragma omp parallel for schedule(static) num_threads(M.nthreads)
+    for (int n = 0; n < numnod; n++) {
+      double a0 = M.A[3 * n], a1 = M.A[3 * n + 1], a2 = M.A[3 * n + 2];
+      double r0 = M.AR[3 * n], r1 = M.AR[3 * n + 1], r2 = M.AR[3 * n + 2];
+      double st = RG_ZERO, sr = RG_ZERO;
+      for (int k = M.adsky[n] - 1; k < M.adsky[n + 1] - 1; k++) {
+        const double *fs = &M.fsky[8 * k];
+        a0 = a0 + fs[0];
+        a1 = a1 + fs[1];
+        a2 = a2 + fs[2];
+        r0 = r0 + fs[3];
+        r1 = r1 + fs[4];
+        r2 = r2 + fs[5];
+        st = st + fs[6];
+        sr = sr + fs[7];
+      }
+      M.A[3 * n] = a0;
+      M.A[3 * n + 1] = a1;
+      M.A[3 * n + 2] = a2;
+      M.AR[3 * n] = r0;
+      M.AR[3 * n + 1] = r1;
+      M.AR[3 * n + 2] = r2;
+      M.STIFN[n] = st;
+      M.STIFR[n] = sr;
+      M.FLAST[3 * n] = a0;
+      M.FLAST[3 * n + 1] = a1;
+      M.FLAST[3 * n + 2] = a2;
+      M.FRLAST[3 * n] = r0;
+      M.FRLAST[3 * n + 1] = r1;
+      M.FRLAST[3 * n + 2] = r2;
+    }
+    // resol.F:6123-6127, 6352, 6494-6497
+    if (dt2t < M.dt2) {
+      M.dt2 = dt2t;
+      M.neltst = neltst;
+    }
+    M.dt2 = std::min(std::min(M.dt2, RG_SP_1P1 * M.dt2old), M.dtmx);
+    M.dt2old = M.dt2;
+    M.dt12 = RG_HALF * (M.dt1 + M.dt2);
+    // ACCELE (accele.F:66-78)
+#pragma omp parallel for schedule(static) num_threads(M.nthreads)
+    for (int n = 0; n < numnod; n++) {
+      if (M.MS[n] > RG_ZERO) {
+        const double rtmp = RG_ONE / M.MS[n];
+        M.A[3 * n] = M.A[3 * n] * rtmp;
+        M.A[3 * n + 1] = M.A[3 * n + 1] * rtmp;
+        M.A[3 * n + 2] = M.A[3 * n + 2] * rtmp;
+      } else {
+        M.A[3 * n] = M.A[3 * n + 1] = M.A[3 * n + 2] = RG_ZERO;
+      }
+      if (rot) {
+        if (M.IN[n] > RG_ZERO) {
+          const double rtmp = RG_ONE / M.IN[n];
+          M.AR[3 * n] = M.AR[3 * n] * rtmp;
+          M.AR[3 * n + 1] = M.AR[3 * n + 1] * rtmp;
+          M.AR[3 * n + 2] = M.AR[3 * n + 2] * rtmp;
+        } else {
+          M.AR[3 * n] = M.AR[3 * n + 1] = M.AR[3 * n + 2] = RG_ZERO;
+        }
+      }
+      // BCS10 / BCS1V (bcs10.F:31): fixed translational DOFs; code bits
+      // 1 = x, 2 = y, 4 = z; rotational bits 8, 16, 32.
+      const int ic = M.icodt[n];
+      if (ic) {
+        if (ic & 1) M.A[3 * n] = RG_ZERO;
+        if (ic & 2) M.A[3 * n + 1] = RG_ZERO;
+        if (ic & 4) M.A[3 * n + 2] = RG_ZERO;
+        if (ic & 8) M.AR[3 * n] = RG_ZERO;
+        if (ic & 16) M.AR[3 * n + 1] = RG_ZERO;
+        if (ic & 32) M.AR[3 * n + 2] = RG_ZERO;
+      }
+    }
+    // RGWALL (rwall/rgwall.F:33): sliding planar wall, applied on the
+    // velocity that VELOCITY is about to produce.
+    for (auto &W : w->walls) {
+      for (int n : W.slaves) {
+        double vn = (M.V[3 * n] + M.dt12 * M.A[3 * n]) * W.n[0] +
+                    (M.V[3 * n + 1] + M.dt12 * M.A[3 * n + 1]) * W.n[1] +
+                    (M.V[3 * n + 2] + M.dt12 * M.A[3 * n + 2]) * W.n[2];
+        double d = (M.X[3 * n] - W.p0[0]) * W.n[0] + (M.X[3 * n + 1] - W.p0[1]) * W.n[1] +
+                   (M.X[3 * n + 2] - W.p0[2]) * W.n[2];
+        if (d <= RG_ZERO && vn < RG_ZERO) {
+          const double an = vn / M.dt12;
+          M.A[3 * n] = M.A[3 * n] - an * W.n[0];
+          M.A[3 * n + 1] = M.A[3 * n + 1] - an * W.n[1];
+          M.A[3 * n + 2] = M.A[3 * n + 2] - an * W.n[2];
+        }
+      }
+    }
+    // VELOCITY (velocity.F:59-75), DEPLA (displacement.F:68-100)
+#pragma omp parallel for schedule(static) num_threads(M.nthreads)
+    for (int n = 0; n < numnod; n++) {
+      for (int c = 0; c < 3; c++) {
+        M.V[3 * n + c] = M.V[3 * n + c] + M.dt12 * M.A[3 * n + c];
+        M.A[3 * n + c] = RG_ZERO;
+      }
+      if (rot)
+        for (int c = 0; c < 3; c++) {
+          M.VR[3 * n + c] = M.VR[3 * n + c] + M.dt12 * M.AR[3 * n + c];
+          M.AR[3 * n + c] = RG_ZERO;
+        }
+      for (int c = 0; c < 3; c++) {
+        const double vdt = M.dt2 * M.V[3 * n + c];
+        M.D[3 * n + c] = M.D[3 * n + c] + vdt;
+        M.X[3 * n + c] = M.X[3 * n + c] + vdt;
+      }
+    }
+    // resol.F:8603-8611 (double accumulation), NCYCLE + 1
+    M.tt = M.tt + M.dt2;
+    M.ncycle++;
+  }
+  return M.error;
+}
+
+int or_get_nodes(void *m, double *x, double *v, double *d, double *vr,
+                 double *f, double *stifn, double *fr) {
+  Model &M = ((OrModelWrap *)m)->m;
+  const size_t n3 = 3 * (size_t)M.numnod;
+  if (x) std::copy(M.X.begin(), M.X.begin() + n3, x);
+  if (v) std::copy(M.V.begin(), M.V.begin() + n3, v);
+  if (d) std::copy(M.D.begin(), M.D.begin() + n3, d);
+  if (vr) std::copy(M.VR.begin(), M.VR.begin() + n3, vr);
+  if (f) std::copy(M.FLAST.begin(), M.FLAST.begin() + n3, f);
+  if (fr) std::copy(M.FRLAST.begin(), M.FRLAST.begin() + n3, fr);
+  if (stifn) std::copy(M.STIFN.begin(), M.STIFN.end(), stifn);
+  return 0;
+}
+
+int or_get_time(void *m, double *tt, double *dt1, double *dt2, int *ncycle,
+                int *neltst) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (tt) *tt = M.tt;
+  if (dt1) *dt1 = M.dt1;
+  if (dt2) *dt2 = M.dt2;
+  if (ncycle) *ncycle = M.ncycle;
+  if (neltst) *neltst = M.neltst;
+  return 0;
+}
+
+int or_get_hexa_state(void *m, int group, int which, double *out) {
+  Model &M = ((OrModelWrap *)m)->m;
+  (void)group;
+  const int ne = M.numels;
+  switch (which) {
+    case 0:
+      std::copy(M.sig.begin(), M.sig.end(), out);
+      return 0;
+    case 1: std::copy(M.eint.begin(), M.eint.end(), out); return 0;
+    case 2: std::copy(M.rho.begin(), M.rho.end(), out); return 0;
+    case 3: std::copy(M.qvis.begin(), M.qvis.end(), out); return 0;
+    case 4: std::copy(M.offg.begin(), M.offg.end(), out); return 0;
+    case 5: std::copy(M.pla.begin(), M.pla.end(), out); return 0;
+    case 6: std::copy(M.epsd.begin(), M.epsd.end(), out); return 0;
+    case 7: std::copy(M.vol.begin(), M.vol.end(), out); return 0;
+    case 8: std::copy(M.ehou.begin(), M.ehou.end(), out); return 0;
+  }
+  (void)ne;
+  return -1;
+}
+
+int or_energy(void *m, double *eint, double *ekin, double *ekinr,
+              double *ehour) {
+  auto *w = (OrModelWrap *)m;
+  Model &M = w->m;
+  double ei = 0, ek = 0, ekr = 0, eh = 0;
+  for (int e = 0; e < M.numels; e++) {
+    ei += M.eint[e] * M.vol[e];
+    eh += M.ehou[e];
+  }
+  double sei = 0, seh = 0;
+  rg_oracle_shell::energy(w->sh, sei, seh);
+  ei += sei;
+  eh += seh;
+  for (int n = 0; n < M.numnod; n++) {
+    const double v2 = M.V[3 * n] * M.V[3 * n] + M.V[3 * n + 1] * M.V[3 * n + 1] +
+                      M.V[3 * n + 2] * M.V[3 * n + 2];
+    ek += RG_HALF * M.MS[n] * v2;
+    const double w2 = M.VR[3 * n] * M.VR[3 * n] + M.VR[3 * n + 1] * M.VR[3 * n + 1] +
+                      M.VR[3 * n + 2] * M.VR[3 * n + 2];
+    ekr += RG_HALF * M.IN[n] * w2;
+  }
+  if (eint) *eint = ei;
+  if (ekin) *ekin = ek;
+  if (ekinr) *ekinr = ekr;
+  if (ehour) *ehour = eh;
+  return 0;
+}
+
+int or_error(void *m) { return ((OrModelWrap *)m)->m.error; }
+
+}  // extern "C"

@@ -1,0 +1,78 @@
+/*
+ * CPU oracle for the OpenRadioss explicit hot path -- TEST INFRASTRUCTURE.
+ *
+ * This library restates, in plain C++ on the CPU and in FP64, the reference
+ * Fortran routines of one explicit cycle (element forces -> PARITH/ON slot
+ * assembly -> acceleration -> boundary conditions -> velocity ->
+ * displacement -> time step).  It exists only to check the CUDA product and to
+ * time the CPU baseline; the product never links, loads or calls it.
+ *
+ * Parity status: the reference engine cannot be built here (no Fortran
+ * compiler), so this restatement is pinned by analytic known-answer tests
+ * (rigid-body motion, constant-strain patch test, elastic wave speed,
+ * energy conservation, Johnson-Cook uniaxial yield) rather than by outputs of
+ * the reference engine itself.
+ *
+ * Conventions follow the reference: nodal arrays are X(3,NUMNOD) (xyz
+ * interleaved), IXS(11,NUMELS) columns hold {mat, n1..n8 (1-based), prop,
+ * user id}, IXC(7,NUMELC) hold {mat, n1..n4, prop, user id}.
+ */
+#pragma once
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+void *or_model_new(int numnod, const double *x, const double *v,
+                   const double *ms, const int *icodt);
+void or_model_free(void *m);
+
+/* Hexa group (SFORC3 path).  pm / geo are the material / property columns
+ * (PM(1:NPROPM,imat), GEO(1:NPROPG,iprop)); uparam / iparam the LAW2
+ * mat_param%uparam(1:12) / iparam(1:4).  Returns the group index or <0. */
+int or_hexa_group_add(void *m, int nel, const int *ixs, int mtn,
+                      const double *pm, const double *geo,
+                      const double *uparam, const int *iparam, int ismstr,
+                      int jhbe, int jcvt);
+
+/* Belytschko-Tsay shell group (CFORC3 path, LAW2). */
+int or_shell_group_add(void *m, int nel, const int *ixc, int npt,
+                       const double *pm, const double *geo,
+                       const double *uparam, const int *iparam,
+                       const double *thk0, int ismstr, int ithk);
+
+/* Rotational inertia (shell nodes). */
+int or_set_inertia(void *m, const double *in);
+
+/* Planar rigid wall (RGWALL, infinite plane): point, outward normal,
+ * sliding (0) ; slave nodes all nodes with distance < dsearch. */
+int or_rwall_add(void *m, const double *p0, const double *nrm,
+                 double dsearch);
+
+/* Build PARITH/ON tables (FILLCNE order) and finish set-up. */
+int or_finalize(void *m, double dtfac_solid, double dtfac_shell, double dtmx,
+                double dt2old_init, int nthreads);
+
+/* Skyline tables (after finalize): adsky (numnod+1, 1-based like ADSKY),
+ * iads (8*numels), iadc (4*numelc). */
+int or_get_skyline(void *m, int *adsky, int *iads, int *iadc, int *lsky);
+
+int or_cycle(void *m, int ncycle);
+
+/* Nodal results: X, V, D (3*numnod each, any may be NULL); F = assembled
+ * forces of the last cycle (A before division by mass), STIFN. */
+int or_get_nodes(void *m, double *x, double *v, double *d, double *vr,
+                 double *f, double *stifn, double *fr);
+int or_get_time(void *m, double *tt, double *dt1, double *dt2,
+                int *ncycle, int *neltst);
+/* Element state: which = 0 sig(6*nel, c*nel+i), 1 eint, 2 rho, 3 qvis,
+ * 4 offg, 5 pla, 6 epsd, 7 vol0. */
+int or_get_hexa_state(void *m, int group, int which, double *out);
+/* Energies: internal, kinetic (translational), kinetic rotational,
+ * hourglass (accumulated). */
+int or_energy(void *m, double *eint, double *ekin, double *ekinr,
+              double *ehour);
+int or_error(void *m);
+
+#ifdef __cplusplus
+}
+#endif
