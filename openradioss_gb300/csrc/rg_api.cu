@@ -13,6 +13,7 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 using namespace rg;
@@ -469,6 +470,7 @@ int init_hexa_state(rg_ctx *c, HexaArrays<ER> &A) {
   std::vector<double> zd(ne, 0.0);
   for (auto &g : c->hg)
     for (int i = 0; i < g.nel; i++) rho[g.P.nft + i] = g.P.rho0;
+  const bool vol_history = !std::is_same<ER, double>::value;
   // initial volume: SDERI3 determinant of the initial geometry
   for (int e = 0; e < ne; e++) {
     double x[8], y[8], z[8];
@@ -490,7 +492,8 @@ int init_hexa_state(rg_ctx *c, HexaArrays<ER> &A) {
   }
   RG_CUDA(c, cudaMemcpy(A.sig, zero.data(), 6 * (size_t)ne * sizeof(ER), cudaMemcpyHostToDevice));
   RG_CUDA(c, cudaMemcpy(A.eint, zd.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
-  RG_CUDA(c, cudaMemcpy(A.rho, rho.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+  RG_CUDA(c, cudaMemcpy(A.rho, vol_history ? vol.data() : rho.data(), ne * sizeof(double),
+                        cudaMemcpyHostToDevice));
   RG_CUDA(c, cudaMemcpy(A.qvis, zero.data(), ne * sizeof(ER), cudaMemcpyHostToDevice));
   RG_CUDA(c, cudaMemcpy(A.off, one.data(), ne * sizeof(ER), cudaMemcpyHostToDevice));
   RG_CUDA(c, cudaMemcpy(A.vol0, vol.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
@@ -667,6 +670,9 @@ int rg_hexa_group_add(rg_ctx *c, int nel, const int *ixs, int mtn,
   P.vns1 = geo[15];
   P.vns2 = geo[16];
   if (!(P.rho0 > 0.0)) return fail(c, RG_E_ARG, "PM(1) density must be > 0");
+  // M1LAW / M2LAW: SSP = SQRT((ONEP333*G + C1)/RHO0), a group constant at OFF=1
+  P.ssp1 = std::sqrt((RG_ONEP333 * (P.g * 1.0) + P.c1) / P.rho0);
+  P.has_cns = (P.vns1 != 0.0 || P.vns2 != 0.0) ? 1 : 0;
   if (mtn == 2) {
     if (iparam[0] != 0 || uparam[7] != 0.0)
       return fail(c, RG_E_UNSUP, "LAW2: Zerilli or kinematic hardening not supported");
@@ -1074,7 +1080,17 @@ int rg_download_hexa_state(rg_ctx *c, int which, double *out) {
     case 8: src = f64 ? c->h64.ehou : c->h32.ehou; isdouble = true; break;
     default: return fail(c, RG_E_ARG, "unknown hexa state index");
   }
-  if (f64 || isdouble) {
+  if (!f64 && which == 2) {
+    // mixed form keeps the element volume: RHO = RHO0 * VOL0 / VOL
+    std::vector<double> v(ne), v0(ne);
+    RG_CUDA(c, cudaMemcpy(v.data(), c->h32.rho, ne * sizeof(double), cudaMemcpyDeviceToHost));
+    RG_CUDA(c, cudaMemcpy(v0.data(), c->h32.vol0, ne * sizeof(double), cudaMemcpyDeviceToHost));
+    for (auto &g : c->hg)
+      for (int i = 0; i < g.nel; i++) {
+        const int e = g.P.nft + i;
+        out[e] = g.P.rho0 * (v0[e] / v[e]);
+      }
+  } else if (f64 || isdouble) {
     RG_CUDA(c, cudaMemcpy(out, src, cnt * sizeof(double), cudaMemcpyDeviceToHost));
   } else {
     std::vector<float> tmp(cnt);

@@ -249,13 +249,31 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     }
 
     // ---- SRHO3 (Lagrangian) -------------------------------------------------
+    // FP64 form: RHO state, DVOL = VOLN - (RHO0/RHO)*VOL0, RHO = RHO0*VOL0/VOLN.
+    // Mixed form: the FP64 state array holds the volume of the last cycle
+    // instead of the density (same information, RHO = RHO0*VOL0/VOL), so
+    // DVOL is one FP64 subtraction and no FP64 division is needed.
     const double vol0 = A.vol0[e];
-    double rho_old = A.rho[e];
     if (offg == (R)0 && voln == RG_ONE) voln = vol0;
-    const double dvol_d = voln - (P.rho0 / rho_old) * vol0;
-    const double rho_new = P.rho0 * (vol0 / voln);
-    A.rho[e] = rho_new;
-    double eint = A.eint[e] * vol0;
+    double dvol_d, rho_new;
+    R rho_r, amu, dvol_r;
+    if (F64) {
+      const double rho_old = A.rho[e];
+      dvol_d = voln - (P.rho0 / rho_old) * vol0;
+      rho_new = P.rho0 * (vol0 / voln);
+      A.rho[e] = rho_new;
+      rho_r = (R)rho_new;
+      amu = (R)(rho_new / P.rho0 - RG_ONE);
+      dvol_r = (R)dvol_d;
+    } else {
+      const double vold = A.rho[e];
+      dvol_d = voln - vold;
+      A.rho[e] = voln;
+      rho_new = 0.0;
+      rho_r = (R)P.rho0 * ((R)vol0 / volr);
+      amu = (R)(vol0 - voln) / volr;  // RHO/RHO0 - 1 = VOL0/VOLN - 1
+      dvol_r = (R)dvol_d;
+    }
 
     // ---- SROTA3 --------------------------------------------------------------
     R s[6], sg[6];
@@ -274,12 +292,13 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     }
 
     // ---- MMAIN prologue: VOL_AVG, AMU (mmain.F90:676-700) --------------------
-    const double vol_avg_d = voln - RG_HALF * dvol_d;
-    const R amu = (R)(rho_new / P.rho0 - RG_ONE);
+    const R vol_avg_r = volr - (R)RG_HALF * dvol_r;
 
     // ---- material law ----------------------------------------------------------
     const R gg = (R)P.g * off;
-    const R ssp = sqrt(((R)RG_ONEP333 * gg + (R)P.c1) / (R)P.rho0);
+    // sound speed: per-group constant for live elements (OFF = 1)
+    const R ssp = off == (R)RG_ONE ? (R)P.ssp1
+                                   : sqrt(((R)RG_ONEP333 * gg + (R)P.c1) / (R)P.rho0);
     {
       const R g1 = dt1 * gg, g2 = (R)RG_TWO * g1;
       const R p = -(R)RG_THIRD * (sg[0] + sg[1] + sg[2]);
@@ -340,11 +359,10 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
         ak = (R)P.ca + (R)P.cb * epxe;
         qh = (R)P.cb * epd;
       } else if (epxe > (R)0) {
-        ak = (R)P.ca + (R)P.cb * pow(epxe, (R)P.cn);
-        if (P.cn > RG_ONE)
-          qh = ((R)P.cb * (R)P.cn * pow(epxe, (R)(P.cn - RG_ONE))) * epd;
-        else
-          qh = ((R)P.cb * (R)P.cn / pow(epxe, (R)(RG_ONE - P.cn))) * epd;
+        // EPXE**(N-1) = EPXE**N / EPXE: one power evaluation
+        const R pn = pow(epxe, (R)P.cn);
+        ak = (R)P.ca + (R)P.cb * pn;
+        qh = ((R)P.cb * (R)P.cn * (pn / epxe)) * epd;
       } else {
         ak = (R)P.ca;
         qh = (R)0;
@@ -369,35 +387,37 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
 
     // ---- MQVISCB (explicit, 3D, one point) -------------------------------------
     R qnew, sti;
+    const R cbv = F64 ? (R)cbrt(voln) : cbrt(volr);  // VOL**(1/3)
     {
       const R dd = -dxx - dyy - dzz;
       R al = (R)0, ad = (R)0;
       if (off == (R)RG_ONE) {
-        al = voln > RG_ZERO ? (R)cbrt(voln) : (R)0;  // VOL**(1/3)
+        al = voln > RG_ZERO ? cbv : (R)0;
         ad = fmax_((R)0, dd);
       }
-      const R rhoe = (R)rho_new;
-      const R nrho = sqrt(rhoe * (R)P.rho0);
+      const R rhoe = rho_r;
       const R qa = (R)P.qa, qb = (R)P.qb;
-      const R cns1 = (R)P.vns1 * al * nrho * ssp * off;
-      const R cns2 = (R)P.vns2 * al * nrho * ssp * off;
       const R qaa = qa * qa * ad;
-      const R rdx = fmax_((R)RG_EM20, rhoe * deltax);
-      const R qx = qb * ssp + al * qaa + (cns1 + cns2) / rdx;
+      R qx = qb * ssp + al * qaa;
+      if (P.has_cns) {
+        const R nrho = sqrt(rhoe * (R)P.rho0);
+        const R cns1 = (R)P.vns1 * al * nrho * ssp * off;
+        const R cns2 = (R)P.vns2 * al * nrho * ssp * off;
+        qx = qx + (cns1 + cns2) / fmax_((R)RG_EM20, rhoe * deltax);
+      }
       qnew = rhoe * ad * al * (qaa * al + qb * ssp);
       const R ssp_eq = fmax_((R)RG_EM20, qx + sqrt(qx * qx + ssp * ssp));
-      R dtx = deltax / ssp_eq;
+      const R dtx = deltax / ssp_eq;
       sti = (R)0;
       if (!(off == (R)0 || offg < (R)0)) {
         const R tidt = (R)RG_ONE / dtx;
         sti = (rhoe * tidt) * (volr * tidt);
       }
-      const double dtxd = P.dtfac * (double)dtx;
+      const double dtxd = F64 ? P.dtfac * (double)dtx : (double)((R)P.dtfac * dtx);
       if (voln > RG_ZERO && (off != (R)0 && offg >= (R)0)) {
         dtmine = dtxd;
         elmin = e;  // element order key; mapped to the user id by the dt kernel
       }
-      (void)al;
     }
 
     // ---- law epilogue: pressure, energy, QOLD ----------------------------------
@@ -411,7 +431,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
       sg[5] = sg[5] * off;
       const R qold = A.qvis[e];
       const R dta = (R)RG_HALF * dt1;
-      double einc;
+      R ework, qwork;
       if (LAW == 1) {
         const R p2 = -(s[0] + sg[0] + s[1] + sg[1] + s[2] + sg[2]) * (R)RG_THIRD;
         const R e1 = dxx * (s[0] + sg[0] + p2);
@@ -420,8 +440,8 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
         const R e4 = d4 * (s[3] + sg[3]);
         const R e5 = d5 * (s[4] + sg[4]);
         const R e6 = d6 * (s[5] + sg[5]);
-        einc = vol_avg_d * (double)((e1 + e2 + e3 + e4 + e5 + e6) * dta) -
-               RG_HALF * dvol_d * (double)(qold + qnew + p2);
+        ework = (e1 + e2 + e3 + e4 + e5 + e6);
+        qwork = qold + qnew + p2;
       } else {
         const R e1 = dxx * (s[0] + sg[0]);
         const R e2 = dyy * (s[1] + sg[1]);
@@ -429,10 +449,19 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
         const R e4 = d4 * (s[3] + sg[3]);
         const R e5 = d5 * (s[4] + sg[4]);
         const R e6 = d6 * (s[5] + sg[5]);
-        einc = vol_avg_d * (double)((e1 + e2 + e3 + e4 + e5 + e6) * dta) -
-               RG_HALF * dvol_d * (double)(qold + qnew);
+        ework = (e1 + e2 + e3 + e4 + e5 + e6);
+        qwork = qold + qnew;
       }
-      A.eint[e] = (eint + einc * (double)off) / fmax_(RG_EM15, vol0);
+      if (F64) {
+        const double einc = (double)vol_avg_r * (double)ework * (double)dta -
+                            RG_HALF * dvol_d * (double)qwork;
+        const double eint = A.eint[e] * vol0;
+        A.eint[e] = (eint + einc * (double)off) / fmax_(RG_ZERO + RG_EM15, vol0);
+      } else {
+        // EINT += EINC / VOL0: increment in FP32, accumulation in FP64
+        const R einc = vol_avg_r * ework * dta - (R)RG_HALF * dvol_r * qwork;
+        A.eint[e] = A.eint[e] + (double)(einc * off / (R)vol0);
+      }
       A.qvis[e] = qnew;
 #pragma unroll
       for (int c = 0; c < 6; c++) A.sig[c * ne + e] = sg[c];
@@ -451,8 +480,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     R f[3][8];
     {
       const R caq = (R)RG_FOURTH * off * (R)P.qh;
-      const R al = (R)cbrt(voln);
-      R fcl = caq * (R)rho_new * (al * al);  // VOL**(2/3)
+      R fcl = caq * rho_r * (cbv * cbv);  // VOL**(2/3) = (VOL**(1/3))**2
       const R fcq = fcl * caq * (R)RG_HUNDRED;
       fcl = fcl * ssp;
       R g[8][3];

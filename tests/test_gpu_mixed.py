@@ -1,0 +1,44 @@
+"""Mixed form (FP32 element / material, FP64 nodal + energies) against the
+FP64 GPU path: relative error of displacement, peak force and internal
+energy within 1e-4 (the mixed form's stated tolerance)."""
+import numpy as np
+import pytest
+
+from openradioss_gb300 import model as M
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def run(model, prec, ncycle, every):
+    from openradioss_gb300.engine import Engine
+    e = Engine(model, precision=prec)
+    peak, eint = 0.0, []
+    for _ in range(ncycle // every):
+        e.cycle(every)
+        f = e.forces()["F"]
+        peak = max(peak, float(np.max(np.linalg.norm(f, axis=0))))
+        eint.append(e.energy()["eint"])
+    return e, peak, np.array(eint)
+
+
+@pytest.mark.parametrize("wl", ["jc_block", "elastic_bar"])
+def test_mixed_vs_fp64(wl):
+    if wl == "jc_block":
+        m = M.large_block(n=20, seed=1)
+        ncyc = 600
+    else:
+        m = M.bar_impact(n=16)
+        ncyc = 800
+    e64, p64, ei64 = run(m, 0, ncyc, 50)
+    e32, p32, ei32 = run(m, 1, ncyc, 50)
+    d64, d32 = e64.nodes()["D"], e32.nodes()["D"]
+    err_d = np.max(np.abs(d32 - d64)) / np.max(np.abs(d64))
+    err_p = abs(p32 - p64) / p64
+    err_e = np.max(np.abs(ei32 - ei64)) / np.max(np.abs(ei64))
+    print(wl, "displacement %.2e peak force %.2e internal energy %.2e" % (err_d, err_p, err_e))
+    assert err_d < TOL
+    assert err_p < TOL
+    assert err_e < TOL
+    assert e32.status() == 0 and e64.status() == 0
