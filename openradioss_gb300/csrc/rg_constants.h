@@ -41,4 +41,12 @@
 #define RG_ONE_OVER_12  (0x1.5555555555555p-4) /* 0.083333333333333329 */
 #define RG_EM04         (0x1.a36e2eb1c432dp-14) /* 0.0001 */
 #define RG_EP03         (0x1.f400000000000p+9) /* 1000 */
+#define RG_ZEP81        (0x1.9eb851eb851ecp-1) /* 0.81000000000000005 */
+#define RG_ZEP072169    (0x1.279aae6c8f756p-4) /* 0.072169000000000011 */
+#define RG_ONEP414      (0x1.69fbe76c8b439p+0) /* 1.4139999999999999 */
+#define RG_ONE_OVER_9   (0x1.c71c71c71c71cp-4) /* 0.1111111111111111 */
+#define RG_THREE_OVER_4 (0x1.8000000000000p-1) /* 0.75 */
+#define RG_FOUR_OVER_5  (0x1.999999999999ap-1) /* 0.80000000000000004 */
+#define RG_EM07         (0x1.ad7f29abcaf48p-24) /* 9.9999999999999995e-08 */
+#define RG_NINE         (0x1.2000000000000p+3) /* 9 */
 #define RG_SP_1P1       (0x1.19999a0000000p+0) /* 1.1000000238418579: REAL*4 literal 1.1 */

@@ -52,6 +52,7 @@ def lib():
         L.or_get_hexa_state.argtypes = [vp, C.c_int, C.c_int, _dp]
         L.or_energy.argtypes = [vp] + [C.c_void_p] * 4
         L.or_error.argtypes = [vp]
+        L.or_get_shell_state.argtypes = [vp, C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -135,6 +136,11 @@ class OracleModel:
         out = np.zeros(6 * ne if which == 0 else ne)
         lib().or_get_hexa_state(self.h, 0, which, out)
         return out.reshape(6, ne) if which == 0 else out
+
+    def shell_state(self, which, size):
+        out = np.zeros(size)
+        lib().or_get_shell_state(self.h, which, out)
+        return out
 
     def energy(self):
         v = [np.zeros(1) for _ in range(4)]

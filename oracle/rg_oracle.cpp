@@ -660,6 +660,7 @@ void energy(const Shells *, double &eint, double &ehour);
 int rwall_add(Shells *, const double *p0, const double *nrm, double dsearch);
 void rwall_apply(Shells *, int numnod, const double *X, double *V,
                  const double *A, double dt12);
+int get_state(const Shells *, int which, double *out);
 }  // namespace rg_oracle_shell
 
 struct OrModelWrap {
@@ -1019,21 +1020,33 @@ int or_cycle(void *m, int ncycle) {
         if (ic & 32) M.AR[3 * n + 2] = RG_ZERO;
       }
     }
-    // RGWALL (rwall/rgwall.F:33): sliding planar wall, applied on the
-    // velocity that VELOCITY is about to produce.
+    // RGWALL (constraints/general/rwall/rgwall.F:33), fixed infinite plane,
+    // sliding: a slave node whose predicted position X + (V + A*DT12)*DT2 is
+    // on or behind the plane and which does not move away from it loses the
+    // normal components of its acceleration and velocity.
     for (auto &W : w->walls) {
       for (int n : W.slaves) {
-        double vn = (M.V[3 * n] + M.dt12 * M.A[3 * n]) * W.n[0] +
-                    (M.V[3 * n + 1] + M.dt12 * M.A[3 * n + 1]) * W.n[1] +
-                    (M.V[3 * n + 2] + M.dt12 * M.A[3 * n + 2]) * W.n[2];
-        double d = (M.X[3 * n] - W.p0[0]) * W.n[0] + (M.X[3 * n + 1] - W.p0[1]) * W.n[1] +
-                   (M.X[3 * n + 2] - W.p0[2]) * W.n[2];
-        if (d <= RG_ZERO && vn < RG_ZERO) {
-          const double an = vn / M.dt12;
-          M.A[3 * n] = M.A[3 * n] - an * W.n[0];
-          M.A[3 * n + 1] = M.A[3 * n + 1] - an * W.n[1];
-          M.A[3 * n + 2] = M.A[3 * n + 2] - an * W.n[2];
-        }
+        const int n1 = 3 * n, n2 = n1 + 1, n3 = n1 + 2;
+        const double vx = M.V[n1] + M.A[n1] * M.dt12;
+        const double vy = M.V[n2] + M.A[n2] * M.dt12;
+        const double vz = M.V[n3] + M.A[n3] * M.dt12;
+        const double ux = M.X[n1] + vx * M.dt2;
+        const double uy = M.X[n2] + vy * M.dt2;
+        const double uz = M.X[n3] + vz * M.dt2;
+        const double xc = ux - W.p0[0], yc = uy - W.p0[1], zc = uz - W.p0[2];
+        const double dp = xc * W.n[0] + yc * W.n[1] + zc * W.n[2];
+        if (dp > RG_ZERO) continue;
+        if ((vx - RG_ZERO) * W.n[0] + (vy - RG_ZERO) * W.n[1] + (vz - RG_ZERO) * W.n[2] > RG_ZERO)
+          continue;
+        const double dv = (M.V[n1] - RG_ZERO) * W.n[0] + (M.V[n2] - RG_ZERO) * W.n[1] +
+                          (M.V[n3] - RG_ZERO) * W.n[2];
+        const double da = M.A[n1] * W.n[0] + M.A[n2] * W.n[1] + M.A[n3] * W.n[2];
+        M.A[n1] = M.A[n1] - da * W.n[0];
+        M.A[n2] = M.A[n2] - da * W.n[1];
+        M.A[n3] = M.A[n3] - da * W.n[2];
+        M.V[n1] = M.V[n1] - dv * W.n[0];
+        M.V[n2] = M.V[n2] - dv * W.n[1];
+        M.V[n3] = M.V[n3] - dv * W.n[2];
       }
     }
     // VELOCITY (velocity.F:59-75), DEPLA (displacement.F:68-100)
@@ -1136,5 +1149,9 @@ int or_energy(void *m, double *eint, double *ekin, double *ekinr,
 }
 
 int or_error(void *m) { return ((OrModelWrap *)m)->m.error; }
+
+int or_get_shell_state(void *m, int which, double *out) {
+  return rg_oracle_shell::get_state(((OrModelWrap *)m)->sh, which, out);
+}
 
 }  // extern "C"

@@ -72,6 +72,9 @@ int or_get_hexa_state(void *m, int group, int which, double *out);
 int or_energy(void *m, double *eint, double *ekin, double *ekinr,
               double *ehour);
 int or_error(void *m);
+/* Shell state: which = 0 FOR (5 x nc), 1 MOM (3 x nc), 2 THK, 3 EINT
+ * (2 x nc), 4 OFF, 5 SIG (5 x npt x nc), 6 PLA (npt x nc), 7 HOUR (5 x nc). */
+int or_get_shell_state(void *m, int which, double *out);
 
 #ifdef __cplusplus
 }
