@@ -35,13 +35,17 @@ sys.path.insert(0, ROOT)
 from openradioss_gb300 import model as M  # noqa: E402
 
 WORKLOADS = {
+    # square crash box of Belytschko-Tsay shells, 60x60 mm section, 300 mm
+    # long, 308 x 390 = 120,120 elements, t = 1.2 mm, NPT = 5, Johnson-Cook,
+    # seeded imperfection U[-0.1t, 0.1t], planar rigid wall hit at 15 m/s
+    "crash_box_120k_jc": lambda: M.crash_box(n_side=77, n_len=390),
     # JC hexa block, 128^3 one-point hexas (2,097,152 elements), seeded
     # velocity 20 m/s + N(0, 0.5): the largest single-GPU hexa configuration.
     "hexa_block_128_jc": lambda: M.large_block(n=128),
     # steel bar impact, 20^3 LAW1 (the CPU-runnable case)
     "bar_impact_20_law1": lambda: M.bar_impact(n=20),
 }
-DEFAULT_WORKLOAD = "hexa_block_128_jc"
+DEFAULT_WORKLOAD = "crash_box_120k_jc"
 
 
 def peaks():
@@ -99,31 +103,44 @@ class Clocks:
                 "samples": len(self.samples)}
 
 
-def hexa_bytes(model, prec, law):
-    """Algorithmic DRAM bytes per element of one hexa element-kernel launch
+def element_bytes(model, prec):
+    """Algorithmic DRAM bytes of one element-kernel launch over the model,
     and per node of one node-kernel launch, from the implemented arrays
-    (each node record read once per pass: ideal reuse)."""
-    ne, nn = model.numels, model.numnod
+    (each node record read once per pass: ideal reuse).  Returns
+    (bytes per element, bytes per node, kernel key)."""
+    nn = model.numnod
     er = 8 if prec == 0 else 4
     slot = 32 if prec == 0 else 16
-    # element kernel: reads NC, IADS (8 int32 each), OFF, SIG(6), QVIS (ER),
-    # EINT, RHO, VOL0, EHOU (FP64), [PLA, EPSD (ER)]; node X4, V4 (32 B each)
-    rd = 32 + 32 + er * (1 + 6 + 1) + 8 * 4 + (2 * er if law == 2 else 0) + 64.0 * nn / ne
-    # writes: SIG, QVIS (ER), EINT, RHO, EHOU (FP64), [PLA, EPSD], 8 slots
-    wr = er * (6 + 1) + 8 * 3 + (2 * er if law == 2 else 0) + 8 * slot
-    elem = rd + wr
-    # node kernel: ADSKY, its slots, X4/V4/D4 read + write
-    slots_per_node = 8.0 * ne / nn
-    node = 4 + slots_per_node * slot + 3 * 32 * 2
-    return elem, node
+    if model.hexa:
+        ne = model.numels
+        law = model.hexa[0].mat["mtn"]
+        # reads NC, IADS (8 int32 each), OFF, SIG(6), QVIS (ER), EINT, RHO,
+        # VOL0, EHOU (FP64), [PLA, EPSD]; node X4, V4 (32 B each)
+        rd = 32 + 32 + er * (1 + 6 + 1) + 8 * 4 + (2 * er if law == 2 else 0) + 64.0 * nn / ne
+        # writes SIG, QVIS, EINT, RHO, EHOU, [PLA, EPSD], 8 slots
+        wr = er * (6 + 1) + 8 * 3 + (2 * er if law == 2 else 0) + 8 * slot
+        spn = 8.0 * ne / nn
+        node = 4 + spn * slot + 3 * 32 * 2
+        return rd + wr, node, "hexa"
+    nc = model.numelc
+    npt = model.shells[0].npt
+    # reads IX, IADC (4 int32 each), DEGEN, OFF, THKE (ER), THK (FP64),
+    # FOR(5), MOM(3), HOUR(5), GSTR(8) (ER), EINT(2), EHOU (FP64),
+    # per point SIG(5), PLA, EPSD (ER); node X4, V4, VR4 (32 B each)
+    rd = 16 + 16 + 4 + 2 * er + 8 + 21 * er + 24 + npt * 7 * er + 96.0 * nn / nc
+    # writes GSTR(8), EPSDG, THK, EINT(2), FOR(5), MOM(3), HOUR(5), EHOU,
+    # per point SIG(5), PLA, EPSD; 4 slots of forces + 4 of moments
+    wr = 22 * er + 8 + 16 + 8 + npt * 7 * er + 4 * 2 * slot
+    spn = 4.0 * nc / nn
+    node = 4 + spn * 2 * slot + 4 * 32 * 2
+    return rd + wr, node, "shell"
 
 
 def run_ours(args, rank, world, local_rank):
     from openradioss_gb300.engine import Engine, RG_PREC_FP64, RG_PREC_MIXED
     wl = args.workload
     model = WORKLOADS[wl]()
-    ne = model.numels
-    law = model.hexa[0].mat["mtn"]
+    ne = model.numels + model.numelc
     hbm_peak, peak_kind = peaks()
     out = {}
     dist = world > 1
@@ -158,9 +175,9 @@ def run_ours(args, rank, world, local_rank):
         eng.cycle(max(3, min(args.steps, 20)))
         kt = eng.kernel_times()
         eng.set_timing(False)
-        eb, nb = hexa_bytes(model, prec, law)
+        eb, nb, kkey = element_bytes(model, prec)
         out[prec] = dict(ms=ms, clocks=clk.summary(), kt=kt, status=st,
-                         elem_bytes=eb, node_bytes=nb, eng=eng)
+                         elem_bytes=eb, node_bytes=nb, kkey=kkey, eng=eng)
     # e2e: FORINT-level call with pinned host buffers (headline form)
     eng = out[forms[0]]["eng"]
     nd = eng.nodes()
@@ -168,17 +185,24 @@ def run_ours(args, rank, world, local_rank):
     v = np.ascontiguousarray(nd["V"].T)
     f = np.empty((model.numnod, 3))
     stf = np.empty(model.numnod)
-    for a in (x, v, f, stf):
+    bufs = [x, v, f, stf]
+    vr = fr = stfr = None
+    if model.shells:
+        vr = np.ascontiguousarray(nd["VR"].T)
+        fr = np.empty((model.numnod, 3))
+        stfr = np.empty(model.numnod)
+        bufs += [vr, fr, stfr]
+    for a in bufs:
         eng.host_register(a)
     dt1 = eng.time()["dt2"]
     for _ in range(max(1, args.warmup)):
-        eng.forint_step(x, v, dt1, f=f, stifn=stf)
+        eng.forint_step(x, v, dt1, vr=vr, f=f, stifn=stf, fr=fr, stifr=stfr)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        eng.forint_step(x, v, dt1, f=f, stifn=stf)
+        eng.forint_step(x, v, dt1, vr=vr, f=f, stifn=stf, fr=fr, stifr=stfr)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    for a in (x, v, f, stf):
+    for a in bufs:
         eng.host_unregister(a)
 
     if args.forms != "both":
@@ -190,9 +214,10 @@ def run_ours(args, rank, world, local_rank):
     res64, res32 = out[RG_PREC_FP64], out[RG_PREC_MIXED]
     value = world * ne * args.steps / (res64["ms"] * 1e-3)
     value32 = world * ne * args.steps / (res32["ms"] * 1e-3)
-    k64 = res64["kt"]["hexa"]
+    kk = res64["kkey"]
+    k64 = res64["kt"][kk]
     ach = res64["elem_bytes"] * ne / (k64 * 1e-3) / 1e9
-    k32 = res32["kt"]["hexa"]
+    k32 = res32["kt"][kk]
     ach32 = res32["elem_bytes"] * ne / (k32 * 1e-3) / 1e9
     traffic = None
     tf = os.path.join(ROOT, "profiles", "hexa_traffic.json")
@@ -215,18 +240,22 @@ def run_ours(args, rank, world, local_rank):
         "dtype": "f64",
         "data": "synthetic (seeded mesh and velocity field of the named shape)",
         "config": {"workload": wl, "elements": ne, "nodes": model.numnod,
-                   "law": "LAW%d" % law, "formulation": "one-point hexa Isolid=1 Iframe=1 "
-                   "Ismstr=4, viscous hourglass, PARITH/ON",
+                   "law": "LAW2 Johnson-Cook" if (model.shells or model.hexa[0].mat["mtn"] == 2)
+                   else "LAW1",
+                   "formulation": ("one-point hexa Isolid=1 Iframe=1 Ismstr=4, viscous "
+                                   "hourglass" if model.hexa else
+                                   "Belytschko-Tsay shell Ishell=1 Ismstr=4 Ithick=1 NPT=5 "
+                                   "Iplas=1, planar sliding rigid wall") + ", PARITH/ON",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (model state %.2f GB)" %
                          (eng.info()["device_bytes"] / 1e9)},
         "e2e": {"value": world * ne * args.steps / e2e_s, "unit": "element-updates/s",
-                "h2d_bytes_per_step": 2 * 3 * 8 * model.numnod,
-                "d2h_bytes_per_step": 4 * 8 * model.numnod},
-        "gpu_launches": (len(model.hexa) + 2) * args.steps,
+                "h2d_bytes_per_step": (3 if model.shells else 2) * 3 * 8 * model.numnod,
+                "d2h_bytes_per_step": (8 if model.shells else 4) * 8 * model.numnod},
+        "gpu_launches": (len(model.hexa) + len(model.shells) + 2) * args.steps,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": ach / hbm_peak, "traffic": traffic,
-                     "kernel": "hexa_kernel<double,LAW%d>" % law,
+                     "kernel": "%s_kernel<double>" % kk,
                      "bytes_per_element": res64["elem_bytes"], "ms_per_launch": k64,
                      "peak_kind": peak_kind,
                      "note": "FP64 form is FP64-pipe bound on GB300; see fp64 key"},

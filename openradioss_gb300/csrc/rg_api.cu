@@ -163,25 +163,36 @@ node_kernel(NodeView N, const int *__restrict__ adsky,
     if (code & 2) a1 = 0.0;
     if (code & 4) a2 = 0.0;
   }
-  // rigid wall (sliding, infinite plane): remove the normal approach
-  // velocity of slave nodes lying on or behind the plane.
+  // RGWALL (constraints/general/rwall/rgwall.F:33), fixed infinite plane,
+  // sliding: a slave node whose predicted position X + (V + A*DT12)*DT2 is
+  // on or behind the plane and which does not move away from it loses the
+  // normal components of its acceleration and velocity.
   if (wall) {
     const int w = __ldg(wall + n);
     if (w >= 0) {
       const double *W = walls + 6 * w;
-      const double vx = __dadd_rn(v.x, __dmul_rn(dt12, a0));
-      const double vy = __dadd_rn(v.y, __dmul_rn(dt12, a1));
-      const double vz = __dadd_rn(v.z, __dmul_rn(dt12, a2));
+      const double vx = __dadd_rn(v.x, __dmul_rn(a0, dt12));
+      const double vy = __dadd_rn(v.y, __dmul_rn(a1, dt12));
+      const double vz = __dadd_rn(v.z, __dmul_rn(a2, dt12));
+      const double ux = __dadd_rn(x.x, __dmul_rn(vx, dt2));
+      const double uy = __dadd_rn(x.y, __dmul_rn(vy, dt2));
+      const double uz = __dadd_rn(x.z, __dmul_rn(vz, dt2));
+      const double dp = __dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(ux, -W[0]), W[3]),
+                                            __dmul_rn(__dadd_rn(uy, -W[1]), W[4])),
+                                  __dmul_rn(__dadd_rn(uz, -W[2]), W[5]));
       const double vn = __dadd_rn(__dadd_rn(__dmul_rn(vx, W[3]), __dmul_rn(vy, W[4])),
                                   __dmul_rn(vz, W[5]));
-      const double dd = __dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(x.x, -W[0]), W[3]),
-                                            __dmul_rn(__dadd_rn(x.y, -W[1]), W[4])),
-                                  __dmul_rn(__dadd_rn(x.z, -W[2]), W[5]));
-      if (dd <= 0.0 && vn < 0.0) {
-        const double an = __ddiv_rn(vn, dt12);
-        a0 = __dadd_rn(a0, -__dmul_rn(an, W[3]));
-        a1 = __dadd_rn(a1, -__dmul_rn(an, W[4]));
-        a2 = __dadd_rn(a2, -__dmul_rn(an, W[5]));
+      if (!(dp > 0.0) && !(vn > 0.0)) {
+        const double dv = __dadd_rn(__dadd_rn(__dmul_rn(v.x, W[3]), __dmul_rn(v.y, W[4])),
+                                    __dmul_rn(v.z, W[5]));
+        const double da = __dadd_rn(__dadd_rn(__dmul_rn(a0, W[3]), __dmul_rn(a1, W[4])),
+                                    __dmul_rn(a2, W[5]));
+        a0 = __dadd_rn(a0, -__dmul_rn(da, W[3]));
+        a1 = __dadd_rn(a1, -__dmul_rn(da, W[4]));
+        a2 = __dadd_rn(a2, -__dmul_rn(da, W[5]));
+        v.x = __dadd_rn(v.x, -__dmul_rn(dv, W[3]));
+        v.y = __dadd_rn(v.y, -__dmul_rn(dv, W[4]));
+        v.z = __dadd_rn(v.z, -__dmul_rn(dv, W[5]));
       }
     }
   }

@@ -1,41 +1,889 @@
-// Belytschko-Tsay 4-node shell module (CFORC3 chain): host bookkeeping and
-// launches.  Filled in with the element kernel; until then a model without
-// shells passes through these entry points unchanged.
+// Belytschko-Tsay 4-node shell element kernel (CFORC3 chain) and its host
+// bookkeeping.
+//
+// One thread per element, the NPT through-thickness points in registers.
+// The arithmetic follows, step by step and in the same expression order,
+// the reference routines (paths relative to the OpenRadioss source tree):
+//   CCOOR3 gather            elements/shell/coque/ccoor3.F:31
+//   CNVEC3 convected frame   elements/shell/coque/cnvec3.F:35 (ISHFRAM = 0)
+//   CDERI3 local geometry    elements/shell/coque/cderi3.F:30 (ISMSTR = 4)
+//   CCOEF3 coefficients      elements/shell/coque/ccoef3.F:30 (ITHK > 0)
+//   CDLEN3 length for dt     elements/shell/coque/cdlen3.F:30
+//   CDEFO3 membrane rates    elements/shell/coque/cdefo3.F:30 (IHBE <= 1)
+//   CCURV3 curvature rates   elements/shell/coque/ccurv3.F:30
+//   CSTRA3 increments, GSTR  elements/shell/coque/cstra3.F:30
+//   MULAWC + SIGEPS02C + M2CPLR  materials/mat_share/mulawc.F90:185,
+//                            materials/mat/mat002/sigeps02c.F:33, m2cplr.F:29
+//   CHVIS3 hourglass         elements/shell/coque/chvis3.F:32
+//   CDT3 element dt, STI     elements/shell/coque/cdt3.F:32
+//   CFINT3 nodal forces      elements/shell/coque/cfint3.F:30
+//   CUPDT3P slot writes      elements/shell/coque/cupdt3.F:967-1100
+// Through-thickness positions / weights: the COQINI tables
+// (elements/shell/coqini.F:46-123), default-real literals.
+#include "../../include/rg_api.h"
 #include "rg_shell.h"
 
-#include "../../include/rg_api.h"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#include <vector>
 
 namespace rg {
 
-struct ShellGroupHost {
-  int nel = 0;
+struct ShellParams {
+  int nft, nel, npt, ipla;
+  int part_off, pad;
+  double rho, young, nu, g, a11, ssp;
+  double h1, h2, h3, srh1, srh2, srh3, dm, ish, fsh;
+  double ca, cb, cn, ymax, cc, eps0, pm9;
+  int icc, vp, israte, pad2;
+  double dtfac;
 };
 
-int shell_group_add(ShellModelHost &, int, int, const int *, int,
-                    const double *, const double *, const double *,
-                    const int *, const double *, int, int,
-                    std::string &why) {
-  why = "shell groups are not available in this build";
-  return RG_E_UNSUP;
+template <typename ER>
+struct ShellArrays {
+  int nc;                 // shell count (SoA stride)
+  const int *ix;          // [4][nc] 0-based nodes
+  const int *iadc;        // [4][nc] 0-based slots
+  const int *degen;       // [nc] IXC(4) == IXC(5) (degenerate quad)
+  ER *offg, *thke;
+  double *thk;            // FP64 in both forms (slow accumulation)
+  ER *forc, *mom, *hour, *gstr, *epsdg;  // [5|3|5|8|1][nc]
+  double *eint;           // [2][nc]
+  ER *sig, *pla, *epsd;   // [npt][5][nc], [npt][nc], [npt][nc]
+  double *ehou;           // [nc]
+};
+
+struct ShellGroupHost {
+  ShellParams P{};
+};
+
+struct ShellDev {
+  ShellArrays<double> a64{};
+  ShellArrays<float> a32{};
+  int prec = 0;
+  int *ix = nullptr, *iadc = nullptr, *degen = nullptr;
+  double *epart = nullptr;  // energy partials
+};
+
+// COQINI tables (NPT = 1..5), single-precision DATA literals.
+__constant__ float c_z0[5][5] = {{0.f, 0.f, 0.f, 0.f, 0.f},
+                                 {-.5f, 0.5f, 0.f, 0.f, 0.f},
+                                 {-.5f, 0.f, 0.5f, 0.f, 0.f},
+                                 {-.5f, -.1666667f, 0.1666667f, 0.5f, 0.f},
+                                 {-.5f, -.25f, 0.f, 0.25f, 0.5f}};
+__constant__ float c_wf[5][5] = {{1.f, 0.f, 0.f, 0.f, 0.f},
+                                 {0.5f, 0.5f, 0.f, 0.f, 0.f},
+                                 {0.25f, 0.5f, 0.25f, 0.f, 0.f},
+                                 {0.1666667f, 0.3333333f, 0.3333333f, 0.1666667f, 0.f},
+                                 {0.125f, 0.25f, 0.25f, 0.25f, 0.125f}};
+__constant__ float c_wm[5][5] = {{0.f, 0.f, 0.f, 0.f, 0.f},
+                                 {-.0833333f, 0.0833333f, 0.f, 0.f, 0.f},
+                                 {-.0833333f, 0.f, 0.0833333f, 0.f, 0.f},
+                                 {-.0648148f, -.0555556f, 0.0555556f, 0.0648148f, 0.f},
+                                 {-.0520833f, -.0625f, 0.f, 0.0625f, 0.0520833f}};
+
+template <typename T>
+__device__ __forceinline__ T smax(T a, T b) {
+  return a > b ? a : b;
 }
+template <typename T>
+__device__ __forceinline__ T smin(T a, T b) {
+  return a < b ? a : b;
+}
+
+template <typename ER, int NPT, int NT>
+__global__ void __launch_bounds__(NT)
+shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
+             typename SlotT<ER>::type *__restrict__ fsky,
+             typename SlotT<ER>::type *__restrict__ fskyr, DtPartials dp,
+             const Time *__restrict__ T, int key0, int nc_total) {
+  typedef ER R;
+  constexpr bool F64 = std::is_same<ER, double>::value;
+  const int il = blockIdx.x * NT + threadIdx.x;
+  const int nc = S.nc;
+  double dtmine = RG_EP06;
+  int elmin = -1;
+  if (il < P.nel) {
+    const int e = P.nft + il;
+    const double DT1 = T->dt2;
+    const R dt1 = (R)DT1;
+    // ---- CCOOR3 ----
+    int nn[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) nn[k] = __ldg(S.ix + k * nc + e);
+    double xa[4], ya[4], za[4];
+    R vl[4][3], vrl[4][3];
+    const R offg = S.offg[e];
+    const R off = smin((R)RG_ONE, fabs(offg));
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const dbl4 x = ld4(N.X4 + nn[k]);
+      const dbl4 v = ld4(N.V4 + nn[k]);
+      const dbl4 w = ld4(N.VR4 + nn[k]);
+      xa[k] = x.x;
+      ya[k] = x.y;
+      za[k] = x.z;
+      const bool z0 = offg < (R)0;
+      vl[k][0] = z0 ? (R)0 : (R)v.x;
+      vl[k][1] = z0 ? (R)0 : (R)v.y;
+      vl[k][2] = z0 ? (R)0 : (R)v.z;
+      vrl[k][0] = z0 ? (R)0 : (R)w.x;
+      vrl[k][1] = z0 ? (R)0 : (R)w.y;
+      vrl[k][2] = z0 ? (R)0 : (R)w.z;
+    }
+    // coordinates: absolute (FP64) or relative to node 1 (mixed); every
+    // quantity below uses coordinate differences only.
+    R xg[4], yg[4], zg[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      xg[k] = F64 ? (R)xa[k] : (R)(xa[k] - xa[0]);
+      yg[k] = F64 ? (R)ya[k] : (R)(ya[k] - ya[0]);
+      zg[k] = F64 ? (R)za[k] : (R)(za[k] - za[0]);
+    }
+    R thk0 = S.thke[e];
+    // ---- CNVEC3 ----
+    R e1x, e1y, e1z, e2x, e2y, e2z, e3x, e3y, e3z;
+    {
+      const R x21 = xg[1] - xg[0], x32 = xg[2] - xg[1], x34 = xg[2] - xg[3], x41 = xg[3] - xg[0];
+      const R y21 = yg[1] - yg[0], y32 = yg[2] - yg[1], y34 = yg[2] - yg[3], y41 = yg[3] - yg[0];
+      const R z21 = zg[1] - zg[0], z32 = zg[2] - zg[1], z34 = zg[2] - zg[3], z41 = zg[3] - zg[0];
+      e1x = (x21 + x34);
+      e1y = (y21 + y34);
+      e1z = (z21 + z34);
+      e2x = (x32 + x41);
+      e2y = (y32 + y41);
+      e2z = (z32 + z41);
+      e3x = e1y * e2z - e1z * e2y;
+      e3y = e1z * e2x - e1x * e2z;
+      e3z = e1x * e2y - e1y * e2x;
+      R suma = e3x * e3x + e3y * e3y + e3z * e3z;
+      suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+      e3x = e3x * suma;
+      e3y = e3y * suma;
+      e3z = e3z * suma;
+      const R s1 = e1x * e1x + e1y * e1y + e1z * e1z;
+      const R s2 = e2x * e2x + e2y * e2y + e2z * e2z;
+      suma = sqrt(s1 / s2);
+      e1x = e1x + (e2y * e3z - e2z * e3y) * suma;
+      e1y = e1y + (e2z * e3x - e2x * e3z) * suma;
+      e1z = e1z + (e2x * e3y - e2y * e3x) * suma;
+      suma = e1x * e1x + e1y * e1y + e1z * e1z;
+      suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+      e1x = e1x * suma;
+      e1y = e1y * suma;
+      e1z = e1z * suma;
+      e2x = e3y * e1z - e3z * e1y;
+      e2y = e3z * e1x - e3x * e1z;
+      e2z = e3x * e1y - e3y * e1x;
+    }
+    // ---- CDERI3 ----
+    R x2, y2, x3, y3, x4, y4, px1, px2, py1, py2, area, vhx, vhy;
+    {
+      const R x21 = xg[1] - xg[0], y21 = yg[1] - yg[0], z21 = zg[1] - zg[0];
+      const R x31 = xg[2] - xg[0], y31 = yg[2] - yg[0], z31 = zg[2] - zg[0];
+      const R x41 = xg[3] - xg[0], y41 = yg[3] - yg[0], z41 = zg[3] - zg[0];
+      x2 = e1x * x21 + e1y * y21 + e1z * z21;
+      y2 = e2x * x21 + e2y * y21 + e2z * z21;
+      y3 = e2x * x31 + e2y * y31 + e2z * z31;
+      x3 = e1x * x31 + e1y * y31 + e1z * z31;
+      x4 = e1x * x41 + e1y * y41 + e1z * z41;
+      y4 = e2x * x41 + e2y * y41 + e2z * z41;
+      px1 = (R)RG_HALF * (y2 - y4);
+      py1 = (R)RG_HALF * (x4 - x2);
+      px2 = (R)RG_HALF * y3;
+      py2 = -(R)RG_HALF * x3;
+      area = smax((R)RG_TWO * (py2 * px1 - py1 * px2), (R)RG_EM20);
+      vhx = (-x2 + x3 - x4) / area;
+      vhy = (-y2 + y3 - y4) / area;
+    }
+    // ---- CCOEF3 (ITHK > 0) ----
+    const double thk_cur = S.thk[e];
+    thk0 = (R)thk_cur;
+    const R vol0 = thk0 * area;
+    const R thk02 = thk0 * thk0;
+    const R nu = (R)P.nu, ym = (R)P.young, gmod = (R)P.g, a11 = (R)P.a11, ssp = (R)P.ssp,
+            rho = (R)P.rho;
+    R shf;
+    if (NPT == 1) {
+      shf = (R)0;
+    } else {
+      const R fac1tmp = (R)2.0 * ((R)1.0 + nu) * thk02;
+      const R ish = (R)P.ish, fsh = (R)P.fsh;
+      shf = fsh * ((R)1.0 - ish + ish * fac1tmp / (fsh * area + fac1tmp));
+    }
+    const R gs = gmod * shf;
+    // ---- CDLEN3 (IHBE /= 0) ----
+    R aldt;
+    {
+      const R al1 = x2 * x2 + y2 * y2;
+      const R al2 = (x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2);
+      const R al6 = x3 * x3 + y3 * y3;
+      const R al3 = (x4 - x3) * (x4 - x3) + (y4 - y3) * (y4 - y3);
+      const R al4 = x4 * x4 + y4 * y4;
+      const R al5 = (x4 - x2) * (x4 - x2) + (y4 - y2) * (y4 - y2);
+      R almin = smin(smin(al1, al2), al4);
+      const R alquad = smin(smin(al3, al5), al6);
+      if (al3 != (R)0) almin = smin(almin, alquad);
+      const R dtdyn = area * area / smax(smax(al5, al6), (R)RG_EM20);
+      aldt = smax(dtdyn, almin);
+      const R dthour = (R)RG_HALF * (almin + aldt) / smax((R)P.h1, (R)P.h2);
+      if (dthour < aldt) aldt = dthour;
+      aldt = sqrt(aldt);
+    }
+    // ---- CDEFO3 (IHBE <= 1) ----
+    R vx[4], vy[4], vz[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      vx[k] = e1x * vl[k][0] + e1y * vl[k][1] + e1z * vl[k][2];
+      vy[k] = e2x * vl[k][0] + e2y * vl[k][1] + e2z * vl[k][2];
+      vz[k] = e3x * vl[k][0] + e3y * vl[k][1] + e3z * vl[k][2];
+    }
+    R exx, eyy, exy, exz, eyz;
+    {
+      const R vz13 = vz[0] - vz[2], vz24 = vz[1] - vz[3];
+      eyz = py1 * vz13 + py2 * vz24;
+      exz = px1 * vz13 + px2 * vz24;
+      const R dt1v4 = (R)RG_FOURTH * dt1;
+      const R tmp2a = py2 + py1;
+      const R tmp3a = copysign(smax(fabs(tmp2a), (R)RG_EM20), tmp2a);
+      const R tmp1a = dt1v4 * (vz13 - vz24) * (vz13 - vz24) / tmp3a;
+      R vx13 = vx[0] - vx[2], vx24 = vx[1] - vx[3];
+      vx13 = vx13 - tmp1a;
+      vx24 = vx24 + tmp1a;
+      exx = px1 * vx13 + px2 * vx24;
+      exy = py1 * vx13 + py2 * vx24;
+      const R tmp1b = px2 - px1;
+      const R tmp3b = copysign(smax(fabs(tmp1b), (R)RG_EM20), tmp1b);
+      const R tmp2b = dt1v4 * (vz13 + vz24) * (vz13 + vz24) / tmp3b;
+      R vy13 = vy[0] - vy[2], vy24 = vy[1] - vy[3];
+      vy13 = vy13 + tmp2b;
+      vy24 = vy24 + tmp2b;
+      exy = exy + px1 * vy13 + px2 * vy24;
+      eyy = py1 * vy13 + py2 * vy24;
+    }
+    // ---- CCURV3 ----
+    R rx[4], ry[4], kxx, kyy, kxy;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      rx[k] = e1x * vrl[k][0] + e1y * vrl[k][1] + e1z * vrl[k][2];
+      ry[k] = e2x * vrl[k][0] + e2y * vrl[k][1] + e2z * vrl[k][2];
+    }
+    {
+      const R rx13 = rx[0] - rx[2], rxav = rx[0] + rx[1] + rx[2] + rx[3], rx24 = rx[1] - rx[3];
+      kyy = -py1 * rx13 - py2 * rx24;
+      kxy = px1 * rx13 + px2 * rx24;
+      const R ry13 = ry[0] - ry[2], ryav = ry[0] + ry[1] + ry[2] + ry[3], ry24 = ry[1] - ry[3];
+      kxx = px1 * ry13 + px2 * ry24;
+      kxy = py1 * ry13 + py2 * ry24 - kxy;
+      exz = exz + ryav * ((R)0.25 * area);
+      eyz = eyz - rxav * ((R)0.25 * area);
+    }
+    // ---- CSTRA3 ----
+    {
+      const R fac1 = dt1 / area;
+      exx = exx * fac1;
+      eyy = eyy * fac1;
+      exy = exy * fac1;
+      eyz = eyz * fac1;
+      exz = exz * fac1;
+      kxx = kxx * fac1;
+      kyy = kyy * fac1;
+      kxy = kxy * fac1;
+      const R inc[8] = {exx, eyy, exy, eyz, exz, kxx, kyy, kxy};
+#pragma unroll
+      for (int c = 0; c < 8; c++) S.gstr[c * nc + e] = S.gstr[c * nc + e] + inc[c];
+    }
+    // element strain rate (ASRATE = 1)
+    R epsd_pg;
+    {
+      const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
+      const R th = thk0;
+      const R eps_k2 = (kxx * kxx + kyy * kyy + kxx * kyy + (R)RG_FOURTH * kxy * kxy) *
+                       (R)RG_ONE_OVER_9 * th * th;
+      const R eps_m2 =
+          (R)RG_FOUR_OVER_3 * (exx * exx + eyy * eyy + exx * eyy + (R)RG_FOURTH * exy * exy);
+      epsd_pg = sqrt(eps_k2 + eps_m2) * dtinv;
+      S.epsdg[e] = epsd_pg;
+    }
+    // ---- MULAWC: through-thickness loop (SIGEPS02C / M2CPLR) ----
+    R forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
+    R degmb = S.forc[0 * nc + e] * exx + S.forc[1 * nc + e] * eyy + S.forc[2 * nc + e] * exy +
+              S.forc[3 * nc + e] * eyz + S.forc[4 * nc + e] * exz;
+    R degfx = S.mom[0 * nc + e] * kxx + S.mom[1 * nc + e] * kyy + S.mom[2 * nc + e] * kxy;
+    double thkn = thk_cur;
+    const R asrate = P.israte > 0 ? smin((R)RG_ONE, (R)(P.pm9 * DT1)) : (R)RG_ONE;
+    const R a1 = ym / ((R)RG_ONE - nu * nu);
+    const R a2 = a1 * nu;
+    const R epdr = smax((R)P.eps0 * dt1, (R)RG_EM20);
+#pragma unroll
+    for (int it = 0; it < NPT; it++) {
+      const R thkly = (R)c_wf[NPT - 1][it];
+      const R thklyl = thkly * thk0;
+      const R wmc = (R)c_wm[NPT - 1][it];
+      const R zt = (R)c_z0[NPT - 1][it] * thk0;
+      const R depsxx = exx + zt * kxx;
+      const R depsyy = eyy + zt * kyy;
+      const R depsxy = exy + zt * kxy;
+      const int ip5 = (it * 5) * nc + e;
+      R sn[5];
+#pragma unroll
+      for (int c = 0; c < 5; c++) sn[c] = S.sig[ip5 + c * nc];
+      R ep = S.epsd[it * nc + e];
+      R epsdot;
+      if (P.vp == 2) {
+        ep = asrate * epsd_pg + ((R)RG_ONE - asrate) * ep;
+        S.epsd[it * nc + e] = ep;
+        epsdot = ep * dt1;
+      } else {
+        epsdot = ep * dt1;
+      }
+      R ezz = (R)0;
+      R ca = (R)P.ca, cb = (R)P.cb, ymax = (R)P.ymax;
+      sn[0] = sn[0] + a1 * depsxx + a2 * depsyy;
+      sn[1] = sn[1] + a2 * depsxx + a1 * depsyy;
+      sn[2] = sn[2] + gmod * depsxy;
+      sn[3] = sn[3] + gs * eyz;
+      sn[4] = sn[4] + gs * exz;
+      if (P.cc != 0.0) {
+        R epsp = epsdot;
+        if (P.israte == 0 && P.vp == 2)
+          epsp = smax(smax(fabs(depsxx), fabs(depsyy)), (R)RG_HALF * fabs(depsxy));
+        epsp = smax(epsp, epdr);
+        const R logep = log(epsp / epdr);
+        R q = ((R)RG_ONE + (R)P.cc * logep);
+        q = smax(q, (R)RG_EM20);
+        ca = ca * q;
+        cb = cb * q;
+        if (P.icc == 1) ymax = ymax * q;
+      }
+      R pla = S.pla[it * nc + e];
+      R yld = pla == (R)0 ? ca : ca + cb * exp((R)P.cn * log(pla));
+      yld = smin(yld, ymax);
+      if (P.ipla == 0) {
+        const R svm = sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2]);
+        const R r = smin((R)RG_ONE, yld / (svm + (R)RG_EM15));
+        if (r < (R)RG_ONE) {
+          sn[0] = sn[0] * r;
+          sn[1] = sn[1] * r;
+          sn[2] = sn[2] * r;
+          const R dpla = off * smax((R)0, (svm - yld) / ym);
+          const R s1 = (R)RG_HALF * (sn[0] + sn[1]);
+          ezz = dpla * s1 / yld;
+          pla = pla + dpla;
+        }
+      } else {
+        const R s1 = sn[0] + sn[1];
+        const R s2 = sn[0] - sn[1];
+        const R s3 = sn[2];
+        const R A = (R)RG_FOURTH * s1 * s1;
+        const R B = (R)RG_THREE_OVER_4 * s2 * s2 + (R)RG_THREE * s3 * s3;
+        const R svm = sqrt(A + B);
+        if (svm > yld && off == (R)RG_ONE) {
+          const R nu1 = (R)RG_ONE / ((R)RG_ONE - nu);
+          const R nu2 = (R)RG_ONE / ((R)RG_ONE + nu);
+          const R h = yld >= ymax ? (R)0 : (R)P.cn * cb * exp(((R)P.cn - (R)RG_ONE) * log(pla + (R)RG_EM07));
+          R dpla_j = (svm - yld) / ((R)RG_THREE * gmod + h);
+          const R anu1 = A * nu1;
+          const R bnu2 = (R)RG_THREE * B * nu2;
+          const R h2 = (R)RG_TWO * h;
+          R dpla_i = 0, Pp = 1, Qq = 1, dr = 0;
+#pragma unroll
+          for (int n = 0; n < 3; n++) {
+            dpla_i = dpla_j;
+            const R pla_i = pla + dpla_i;
+            const R yld_i = pla_i == (R)0 ? smin(ymax, ca) : smin(ymax, ca + cb * exp((R)P.cn * log(pla_i)));
+            dr = (R)RG_HALF * ym * dpla_i / yld_i;
+            Pp = (R)RG_ONE / ((R)RG_ONE + dr * nu1);
+            Qq = (R)RG_ONE / ((R)RG_ONE + (R)RG_THREE * dr * nu2);
+            const R p2 = Pp * Pp, q2 = Qq * Qq;
+            const R f = A * p2 + B * q2 - yld_i * yld_i;
+            const R df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) / yld_i - h2 * yld_i;
+            dpla_j = dpla_i > (R)0 ? smax((R)0, dpla_i - f / df) : (R)0;
+          }
+          pla = pla + dpla_i;
+          const R t1 = (sn[0] + sn[1]) * Pp;
+          const R t2 = (sn[0] - sn[1]) * Qq;
+          sn[0] = (R)RG_HALF * (t1 + t2);
+          sn[1] = (R)RG_HALF * (t1 - t2);
+          sn[2] = sn[2] * Qq;
+          ezz = dr * t1 / ym;
+        }
+      }
+      S.pla[it * nc + e] = pla;
+      ezz = -(depsxx + depsyy) * nu - ((R)RG_ONE - (R)RG_TWO * nu) * ezz;
+      ezz = ezz / ((R)RG_ONE - nu);
+      thkn = thkn + (double)(ezz * thklyl * off);
+#pragma unroll
+      for (int c = 0; c < 5; c++) {
+        S.sig[ip5 + c * nc] = sn[c];
+        forn[c] = forn[c] + thkly * sn[c];
+      }
+      momn[0] = momn[0] + wmc * sn[0];
+      momn[1] = momn[1] + wmc * sn[1];
+      momn[2] = momn[2] + wmc * sn[2];
+    }
+    S.thk[e] = thkn > RG_EM30 ? thkn : RG_EM30;
+    if (P.dm != 0.0) {
+      const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
+      const R visc = ((R)RG_ONEP414 * (R)P.dm) * ssp * sqrt(area) * dtinv * rho;
+      forn[0] = forn[0] + visc * (exx + (R)RG_HALF * eyy);
+      forn[1] = forn[1] + visc * (eyy + (R)RG_HALF * exx);
+      forn[2] = forn[2] + visc * exy * (R)RG_THIRD;
+    }
+#pragma unroll
+    for (int c = 0; c < 5; c++) forn[c] = forn[c] * off;
+#pragma unroll
+    for (int c = 0; c < 3; c++) momn[c] = momn[c] * off;
+    degmb = degmb + forn[0] * exx + forn[1] * eyy + forn[2] * exy + forn[3] * eyz + forn[4] * exz;
+    degfx = degfx + momn[0] * kxx + momn[1] * kyy + momn[2] * kxy;
+    {
+      const R vol2 = (R)RG_HALF * vol0;
+      S.eint[e] = S.eint[e] + (double)(degmb * vol2);
+      S.eint[nc + e] = S.eint[nc + e] + (double)(degfx * thk0 * vol2);
+    }
+#pragma unroll
+    for (int c = 0; c < 5; c++) S.forc[c * nc + e] = forn[c];
+#pragma unroll
+    for (int c = 0; c < 3; c++) S.mom[c * nc + e] = momn[c];
+    // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) ----
+    R h11, h12, h13, h21, h22, h23, h31, h32, h33, hr4, hr5;
+    {
+      const R px1v = px1 * vhx, px2v = px2 * vhx, py1v = py1 * vhy, py2v = py2 * vhy;
+      const R gama1 = off * ((R)RG_ONE - px1v - py1v);
+      const R gama3 = off * ((R)RG_ONE + px1v + py1v);
+      const R gama2 = off * (-(R)RG_ONE - px2v - py2v);
+      const R gama4 = off * (-(R)RG_ONE + px2v + py2v);
+      // HVLIN = 0: the linear viscous terms vanish; HVISC = HELAS = 1/2
+      const R shfpr3 = shf / ((R)RG_THREE * ((R)RG_ONE + nu));
+      const R r1 = (R)RG_FOURTH * rho * (R)RG_HUNDRED;
+      const R A1 = r1 * ((R)RG_HALF * (R)P.h1);
+      const R A3 = r1 * ((R)RG_HALF * (R)P.h2) * sqrt(shfpr3);
+      const R A5 = ((R)RG_HALF * (R)P.h3) * r1 * (R)RG_ZEP072169;
+      const R r0e = (R)RG_FOURTH * ym * (R)RG_HALF;
+      const R A7 = (R)P.h1 * r0e;
+      const R A8 = (R)P.h2 * r0e * shfpr3;
+      const R t2a = thk02 * area;
+      const R tsa = sqrt(t2a);
+      R h1q = A1 * tsa;
+      R h2q = A3 * thk02;
+      R h3q = A5 * t2a;
+      const R td = thk0 * dt1;
+      R hh1 = A7 * td;
+      const R b1 = px1 * px1 + py1 * py1, b2 = px2 * px2 + py2 * py2;
+      R hh2 = A8 * thk02 * td / (b1 + b2);
+      if (S.degen[e]) h1q = h2q = h3q = hh1 = hh2 = (R)0;
+      R hg1 = vx[0] * gama1 + vx[1] * gama2 + vx[2] * gama3 + vx[3] * gama4;
+      R hg2 = vy[0] * gama1 + vy[1] * gama2 + vy[2] * gama3 + vy[3] * gama4;
+      R hou0 = S.hour[0 * nc + e] + hg1 * hh1;
+      R hou1 = S.hour[1 * nc + e] + hg2 * hh1;
+      const R hour1a = hou0 + hg1 * ((R)0 + h1q * fabs(hg1));
+      h11 = hour1a * gama1;
+      h12 = hour1a * gama2;
+      h13 = hour1a * gama3;
+      const R hour2a = hou1 + hg2 * ((R)0 + h1q * fabs(hg2));
+      h21 = hour2a * gama1;
+      h22 = hour2a * gama2;
+      h23 = hour2a * gama3;
+      R ehou = hour1a * hg1 + hour2a * hg2;
+      hg1 = vz[0] * gama1 + vz[1] * gama2 + vz[2] * gama3 + vz[3] * gama4;
+      const R hou2 = S.hour[2 * nc + e] + hg1 * hh2;
+      const R hour3a = hou2 + hg1 * ((R)0 + h2q * fabs(hg1));
+      h31 = hour3a * gama1;
+      h32 = hour3a * gama2;
+      h33 = hour3a * gama3;
+      ehou = ehou + hour3a * hg1;
+      hg1 = rx[0] - rx[1] + rx[2] - rx[3];
+      hg2 = ry[0] - ry[1] + ry[2] - ry[3];
+      hr4 = hg1 * ((R)0 + h3q * fabs(hg1));
+      hr5 = hg2 * ((R)0 + h3q * fabs(hg2));
+      ehou = ehou + hr4 * hg1 + hr5 * hg2;
+      ehou = dt1 * ehou * off;
+      S.hour[0 * nc + e] = hou0;
+      S.hour[1 * nc + e] = hou1;
+      S.hour[2 * nc + e] = hou2;
+      S.hour[3 * nc + e] = hr4;
+      S.hour[4 * nc + e] = hr5;
+      S.ehou[e] = S.ehou[e] + (double)ehou;
+    }
+    // ---- CDT3 ----
+    R sti;
+    {
+      const R dt = (R)P.dtfac * aldt / ssp;
+      if (offg > (R)0 && off != (R)0) {
+        dtmine = (double)dt;
+        elmin = key0 + (nc_total - 1 - e);  // first element wins ties (strict <)
+      }
+      const R divm = smax(aldt * aldt, (R)RG_EM20);
+      sti = (R)RG_HALF * vol0 * ym / divm;
+      sti = (R)RG_ZEP81 * sti * off;
+    }
+    // ---- CFINT3 ----
+    R F[3][4], M[3][4];
+    {
+      const R f1a = forn[0] * thk0, f2a = forn[1] * thk0, f3a = forn[2] * thk0;
+      const R f4a = forn[3] * thk0, f5a = forn[4] * thk0;
+      R m4 = f4a * area, m5 = f5a * area;
+      const R f12 = f1a * px2 + f3a * py2;
+      const R f22 = f2a * py2 + f3a * px2;
+      const R f32 = f5a * px2 + f4a * py2;
+      const R f11 = f1a * px1 + f3a * py1;
+      const R f21 = f2a * py1 + f3a * px1;
+      const R f31 = f5a * px1 + f4a * py1;
+      const R g11 = f11 + h11, g13 = h13 - f11;
+      const R g21 = f21 + h21, g23 = h23 - f21;
+      const R g31 = f31 + h31, g33 = h33 - f31;
+      const R g12 = f12 + h12, g22 = f22 + h22, g32 = f32 + h32;
+      F[0][0] = e1x * g11 + e2x * g21 + e3x * g31;
+      F[0][1] = e1x * g12 + e2x * g22 + e3x * g32;
+      F[0][2] = e1x * g13 + e2x * g23 + e3x * g33;
+      F[1][0] = e1y * g11 + e2y * g21 + e3y * g31;
+      F[1][1] = e1y * g12 + e2y * g22 + e3y * g32;
+      F[1][2] = e1y * g13 + e2y * g23 + e3y * g33;
+      F[2][0] = e1z * g11 + e2z * g21 + e3z * g31;
+      F[2][1] = e1z * g12 + e2z * g22 + e3z * g32;
+      F[2][2] = e1z * g13 + e2z * g23 + e3z * g33;
+#pragma unroll
+      for (int c = 0; c < 3; c++) F[c][3] = -F[c][0] - F[c][1] - F[c][2];
+      const R m1a = momn[0] * thk02, m2a = momn[1] * thk02, m3a = momn[2] * thk02;
+      m4 = m4 * (R)RG_FOURTH;
+      m5 = m5 * (R)RG_FOURTH;
+      const R m11 = -m2a * py1 - m3a * px1;
+      const R m21 = m1a * px1 + m3a * py1;
+      const R m12 = -m2a * py2 - m3a * px2;
+      const R m22 = m1a * px2 + m3a * py2;
+      const R b1x[4] = {hr4 * off, -hr4 * off, hr4 * off, -hr4 * off};
+      const R b2x[4] = {hr5 * off, -hr5 * off, hr5 * off, -hr5 * off};
+      const R gg1[4] = {m11 - m4 + b1x[0], m12 - m4 + b1x[1], -m11 - m4 + b1x[2], -m12 - m4 + b1x[3]};
+      const R gg2[4] = {m21 + m5 + b2x[0], m22 + m5 + b2x[1], -m21 + m5 + b2x[2], -m22 + m5 + b2x[3]};
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        M[0][k] = e1x * gg1[k] + e2x * gg2[k];
+        M[1][k] = e1y * gg1[k] + e2y * gg2[k];
+        M[2][k] = e1z * gg1[k] + e2z * gg2[k];
+      }
+    }
+    // ---- CUPDT3P ----
+    R offg_new = offg;
+    if (off < (R)RG_ONE) {
+      offg_new = off;
+      S.offg[e] = off;
+    }
+    const bool zero = offg_new < (R)0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int K = __ldg(S.iadc + k * nc + e);
+      typename SlotT<ER>::type a, b;
+      a.x = zero ? (R)0 : -F[0][k];
+      a.y = zero ? (R)0 : -F[1][k];
+      a.z = zero ? (R)0 : -F[2][k];
+      a.w = zero ? (R)0 : sti;
+      b.x = zero ? (R)0 : -M[0][k];
+      b.y = zero ? (R)0 : -M[1][k];
+      b.z = zero ? (R)0 : -M[2][k];
+      b.w = (R)0;  // STIR = 0 (element time step)
+      fsky[K] = a;
+      fskyr[K] = b;
+    }
+  }
+  block_dt_min<NT>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
+}
+
+// Fixed-order shell energy partials: [0] internal (membrane + bending),
+// [1] hourglass.
+__global__ void shell_energy_kernel(int nc, const double *__restrict__ eint,
+                                    const double *__restrict__ ehou,
+                                    double *__restrict__ out) {
+  __shared__ double s0[256], s1[256];
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < nc; i += 256) {
+    a += eint[i] + eint[nc + i];
+    b += ehou[i];
+  }
+  s0[threadIdx.x] = a;
+  s1[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s0[threadIdx.x] += s0[threadIdx.x + o];
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = s0[0];
+    out[1] = s1[0];
+  }
+}
+
+constexpr int SHELL_NT = 128;
+int shell_blocks(int nel) { return (nel + SHELL_NT - 1) / SHELL_NT; }
+
+template <typename ER>
+static void launch_shell(const ShellParams &P, const ShellArrays<ER> &A, const NodeView &N,
+                         void *fsky, void *fskyr, DtPartials dp, const Time *T, int key0,
+                         int nct, cudaStream_t s) {
+  typedef typename SlotT<ER>::type ST;
+  const int nb = shell_blocks(P.nel);
+  ST *f = (ST *)fsky, *fr = (ST *)fskyr;
+  switch (P.npt) {
+    case 1: shell_kernel<ER, 1, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
+    case 2: shell_kernel<ER, 2, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
+    case 3: shell_kernel<ER, 3, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
+    case 4: shell_kernel<ER, 4, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
+    default: shell_kernel<ER, 5, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int shell_group_add(ShellModelHost &S, int numnod, int nel, const int *ixc, int npt,
+                    const double *pm, const double *geo, const double *uparam,
+                    const int *iparam, const double *thk0, int ismstr, int ithk,
+                    std::string &why) {
+  if (nel <= 0 || !ixc || !pm || !geo || !uparam || !iparam || !thk0) {
+    why = "rg_shell_group_add: bad arguments";
+    return RG_E_ARG;
+  }
+  if (npt < 1 || npt > 5) {
+    why = "shell: NPT must be 1..5";
+    return RG_E_UNSUP;
+  }
+  if (ismstr != 2 && ismstr != 4) {
+    why = "shell: supported ISMSTR is 4 (2 accepted, run without the small-strain switch)";
+    return RG_E_UNSUP;
+  }
+  if (ithk <= 0) {
+    why = "shell: supported formulation is ITHK > 0 (thickness update)";
+    return RG_E_UNSUP;
+  }
+  if (iparam[0] != 0 || uparam[7] != 0.0) {
+    why = "shell LAW2: Zerilli or kinematic hardening not supported";
+    return RG_E_UNSUP;
+  }
+  for (int e = 0; e < nel; e++) {
+    for (int k = 1; k <= 4; k++)
+      if (ixc[7 * e + k] < 1 || ixc[7 * e + k] > numnod) {
+        why = "IXC node number out of range";
+        return RG_E_ARG;
+      }
+    if (!(thk0[e] > 0.0)) {
+      why = "shell thickness must be > 0";
+      return RG_E_ARG;
+    }
+  }
+  auto *g = new ShellGroupHost();
+  ShellParams &P = g->P;
+  P.nft = S.numelc;
+  P.nel = nel;
+  P.npt = npt;
+  P.ipla = (int)geo[38];
+  if (P.ipla != 0 && P.ipla != 1) {
+    delete g;
+    why = "shell LAW2: Iplas 0 or 1 supported";
+    return RG_E_UNSUP;
+  }
+  P.rho = pm[0];
+  P.young = pm[19];
+  P.nu = pm[20];
+  P.g = pm[21];
+  P.a11 = pm[23];
+  P.ssp = pm[26];
+  P.h1 = geo[12];
+  P.h2 = geo[13];
+  P.h3 = geo[14];
+  P.dm = geo[15];
+  P.srh1 = geo[17];
+  P.srh2 = geo[18];
+  P.srh3 = geo[19];
+  P.ish = std::nearbyint(geo[36]);
+  P.fsh = geo[37];
+  P.icc = iparam[1];
+  P.vp = iparam[2];
+  P.israte = iparam[3];
+  P.ca = uparam[0];
+  P.cb = uparam[1];
+  P.cn = uparam[2];
+  P.ymax = uparam[4];
+  P.cc = uparam[5];
+  P.eps0 = uparam[6];
+  P.pm9 = uparam[8];
+  if (P.srh1 != 0.0 || P.srh2 != 0.0 || P.srh3 != 0.0) {
+    delete g;
+    why = "shell: linear hourglass viscosity (GEO(18..20)) not supported";
+    return RG_E_UNSUP;
+  }
+  S.groups.push_back(g);
+  S.ixc.insert(S.ixc.end(), ixc, ixc + 7 * (size_t)nel);
+  S.thk0.insert(S.thk0.end(), thk0, thk0 + nel);
+  S.numelc += nel;
+  return (int)S.groups.size() - 1;
+}
+
 int shell_numelc(const ShellModelHost &S) { return S.numelc; }
 const int *shell_ixc(const ShellModelHost &S) { return S.ixc.data(); }
 void shell_user_ids(const ShellModelHost &S, int *out) {
-  for (int e = 0; e < S.numelc; e++) out[e] = S.ixc[7 * e + 6];
+  // reversed: the dt kernel keeps the largest key on ties, CDT3 the first
+  for (int e = 0; e < S.numelc; e++) out[S.numelc - 1 - e] = S.ixc[7 * e + 6];
 }
-int shell_finalize(ShellModelHost &, int, const double *, const int *, int,
-                   double, int &, const DevAlloc &, std::string &) {
-  return RG_OK;
-}
-void shell_enqueue(ShellModelHost &, int, const NodeView &, void *, void *,
-                   DtPartials, const Time *, int *, cudaStream_t) {}
-int shell_energy_enqueue(ShellModelHost &, int, double *, cudaStream_t) {
+
+template <typename ER>
+static int alloc_arrays(ShellArrays<ER> &A, int nc, const DevAlloc &alloc) {
+  auto get = [&](void **p, size_t bytes) { return alloc(p, bytes); };
+  int r = 0;
+  A.nc = nc;
+  if ((r = get((void **)&A.offg, nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.thke, nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.thk, nc * sizeof(double)))) return r;
+  if ((r = get((void **)&A.forc, 5 * (size_t)nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.mom, 3 * (size_t)nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.hour, 5 * (size_t)nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.gstr, 8 * (size_t)nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.epsdg, nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.eint, 2 * (size_t)nc * sizeof(double)))) return r;
+  if ((r = get((void **)&A.sig, 25 * (size_t)nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.pla, 5 * (size_t)nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.epsd, 5 * (size_t)nc * sizeof(ER)))) return r;
+  if ((r = get((void **)&A.ehou, nc * sizeof(double)))) return r;
   return 0;
 }
-int shell_download(ShellModelHost &, int, int, double *, std::string &why) {
-  why = "no shell groups";
-  return RG_E_STATE;
+
+template <typename ER>
+static int init_arrays(ShellModelHost &S, ShellArrays<ER> &A) {
+  const int nc = S.numelc;
+  std::vector<ER> one(nc, (ER)1), zero(25 * (size_t)nc, (ER)0), th(nc);
+  std::vector<double> zd(2 * (size_t)nc, 0.0), thd(S.thk0.begin(), S.thk0.end());
+  for (int e = 0; e < nc; e++) th[e] = (ER)S.thk0[e];
+  auto cp = [](void *d, const void *h, size_t b) { return cudaMemcpy(d, h, b, cudaMemcpyHostToDevice); };
+  if (cp(A.offg, one.data(), nc * sizeof(ER)) || cp(A.thke, th.data(), nc * sizeof(ER)) ||
+      cp(A.thk, thd.data(), nc * sizeof(double)) ||
+      cp(A.forc, zero.data(), 5 * (size_t)nc * sizeof(ER)) ||
+      cp(A.mom, zero.data(), 3 * (size_t)nc * sizeof(ER)) ||
+      cp(A.hour, zero.data(), 5 * (size_t)nc * sizeof(ER)) ||
+      cp(A.gstr, zero.data(), 8 * (size_t)nc * sizeof(ER)) ||
+      cp(A.epsdg, zero.data(), nc * sizeof(ER)) ||
+      cp(A.eint, zd.data(), 2 * (size_t)nc * sizeof(double)) ||
+      cp(A.sig, zero.data(), 25 * (size_t)nc * sizeof(ER)) ||
+      cp(A.pla, zero.data(), 5 * (size_t)nc * sizeof(ER)) ||
+      cp(A.epsd, zero.data(), 5 * (size_t)nc * sizeof(ER)) ||
+      cp(A.ehou, zd.data(), nc * sizeof(double)))
+    return RG_E_CUDA;
+  return 0;
 }
-void shell_free(ShellModelHost &) {}
+
+int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc, int key0,
+                   double dtfac, int &part_off, const DevAlloc &alloc, std::string &why) {
+  (void)X;
+  const int nc = S.numelc;
+  if (nc == 0) return RG_OK;
+  auto *D = new ShellDev();
+  S.dev = D;
+  D->prec = prec;
+  std::vector<int> ix(4 * (size_t)nc), ia(4 * (size_t)nc), dg(nc);
+  for (int e = 0; e < nc; e++) {
+    for (int k = 0; k < 4; k++) {
+      ix[(size_t)k * nc + e] = S.ixc[7 * e + 1 + k] - 1;
+      ia[(size_t)k * nc + e] = iadc[4 * e + k] - 1;
+    }
+    dg[e] = S.ixc[7 * e + 3] == S.ixc[7 * e + 4] ? 1 : 0;
+  }
+  int r;
+  if ((r = alloc((void **)&D->ix, ix.size() * sizeof(int)))) return r;
+  if ((r = alloc((void **)&D->iadc, ia.size() * sizeof(int)))) return r;
+  if ((r = alloc((void **)&D->degen, dg.size() * sizeof(int)))) return r;
+  if ((r = alloc((void **)&D->epart, 8 * sizeof(double)))) return r;
+  if (cudaMemcpy(D->ix, ix.data(), ix.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(D->iadc, ia.data(), ia.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(D->degen, dg.data(), dg.size() * sizeof(int), cudaMemcpyHostToDevice)) {
+    why = "copy of shell tables failed";
+    return RG_E_CUDA;
+  }
+  if (prec == RG_PREC_FP64) {
+    if ((r = alloc_arrays(D->a64, nc, alloc))) return r;
+    D->a64.ix = D->ix;
+    D->a64.iadc = D->iadc;
+    D->a64.degen = D->degen;
+    if ((r = init_arrays(S, D->a64))) return r;
+  } else {
+    if ((r = alloc_arrays(D->a32, nc, alloc))) return r;
+    D->a32.ix = D->ix;
+    D->a32.iadc = D->iadc;
+    D->a32.degen = D->degen;
+    if ((r = init_arrays(S, D->a32))) return r;
+  }
+  S.key0 = key0;
+  for (auto *g : S.groups) {
+    g->P.part_off = part_off;
+    g->P.dtfac = dtfac;
+    part_off += shell_blocks(g->P.nel);
+  }
+  return RG_OK;
+}
+
+void shell_enqueue(ShellModelHost &S, int prec, const NodeView &N, void *fsky, void *fskyr,
+                   DtPartials dp, const Time *T, int *status, cudaStream_t s) {
+  (void)status;
+  if (S.numelc == 0 || !S.dev) return;
+  auto *D = (ShellDev *)S.dev;
+  for (auto *g : S.groups) {
+    if (prec == RG_PREC_FP64)
+      launch_shell<double>(g->P, D->a64, N, fsky, fskyr, dp, T, S.key0, S.numelc, s);
+    else
+      launch_shell<float>(g->P, D->a32, N, fsky, fskyr, dp, T, S.key0, S.numelc, s);
+  }
+}
+
+int shell_energy_enqueue(ShellModelHost &S, int prec, double *out2, cudaStream_t s) {
+  if (S.numelc == 0 || !S.dev) return 0;
+  auto *D = (ShellDev *)S.dev;
+  const double *ei = prec == RG_PREC_FP64 ? D->a64.eint : D->a32.eint;
+  const double *eh = prec == RG_PREC_FP64 ? D->a64.ehou : D->a32.ehou;
+  shell_energy_kernel<<<1, 256, 0, s>>>(S.numelc, ei, eh, out2);
+  return 2;
+}
+
+int shell_download(ShellModelHost &S, int prec, int which, double *out, std::string &why) {
+  if (S.numelc == 0 || !S.dev) {
+    why = "no shell groups";
+    return RG_E_STATE;
+  }
+  auto *D = (ShellDev *)S.dev;
+  const size_t n = S.numelc;
+  const int npt = S.groups.empty() ? 0 : S.groups[0]->P.npt;
+  auto fetch = [&](const void *src64, const void *src32, size_t cnt, bool isdouble) -> int {
+    if (prec == RG_PREC_FP64 || isdouble) {
+      return cudaMemcpy(out, prec == RG_PREC_FP64 ? src64 : src32, cnt * sizeof(double),
+                        cudaMemcpyDeviceToHost) == cudaSuccess ? 0 : RG_E_CUDA;
+    }
+    std::vector<float> t(cnt);
+    if (cudaMemcpy(t.data(), src32, cnt * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return RG_E_CUDA;
+    for (size_t i = 0; i < cnt; i++) out[i] = t[i];
+    return 0;
+  };
+  const ShellArrays<double> &a = D->a64;
+  const ShellArrays<float> &b = D->a32;
+  switch (which) {
+    case 0: return fetch(a.forc, b.forc, 5 * n, false);
+    case 1: return fetch(a.mom, b.mom, 3 * n, false);
+    case 2: return fetch(a.thk, b.thk, n, true);
+    case 3: return fetch(a.eint, b.eint, 2 * n, true);
+    case 4: return fetch(a.offg, b.offg, n, false);
+    case 5: return fetch(a.sig, b.sig, 5 * (size_t)npt * n, false);
+    case 6: return fetch(a.pla, b.pla, (size_t)npt * n, false);
+    case 7: return fetch(a.hour, b.hour, 5 * n, false);
+  }
+  why = "unknown shell state index";
+  return RG_E_ARG;
+}
+
+void shell_free(ShellModelHost &S) {
+  for (auto *g : S.groups) delete g;
+  S.groups.clear();
+  delete (ShellDev *)S.dev;
+  S.dev = nullptr;
+}
 
 }  // namespace rg

@@ -13,7 +13,9 @@ struct ShellGroupHost;
 struct ShellModelHost {
   int numelc = 0;
   std::vector<int> ixc;                 // 7 * numelc (reference layout)
+  std::vector<double> thk0;             // initial thickness per shell
   std::vector<ShellGroupHost *> groups;
+  int key0 = 0;                         // dt-order key of the first shell
   void *dev = nullptr;                  // device arrays (rg_shell.cu)
 };
 

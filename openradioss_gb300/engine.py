@@ -109,10 +109,10 @@ class Engine:
     def status(self):
         return self._chk(self.L.rg_status(self.h), "rg_status")
 
-    def forint_step(self, x, v, dt1, vr=None, f=None, stifn=None):
-        """FORINT-level call with host buffers: x, v as X(3,N) arrays
-        (numpy (N,3) row-major == Fortran (3,N)).  Returns (f, stifn, dt2t,
-        neltst)."""
+    def forint_step(self, x, v, dt1, vr=None, f=None, stifn=None, fr=None, stifr=None):
+        """FORINT-level call with host buffers: x, v (and vr for shells) as
+        X(3,N) arrays (numpy (N,3) row-major == Fortran (3,N)).  Returns
+        (f, stifn, dt2t, neltst); moments go to fr / stifr when given."""
         n = self.model.numnod
         if f is None:
             f = np.empty((n, 3))
@@ -121,8 +121,8 @@ class Engine:
         dt2t = C.c_double()
         el = C.c_int()
         self._chk(self.L.rg_forint_step(self.h, _p(x), _p(v), _p(vr), float(dt1), _p(f),
-                                        _p(stifn), None, None, C.byref(dt2t), C.byref(el)),
-                  "rg_forint_step")
+                                        _p(stifn), _p(fr), _p(stifr), C.byref(dt2t),
+                                        C.byref(el)), "rg_forint_step")
         return f, stifn, dt2t.value, el.value
 
     def host_register(self, a):

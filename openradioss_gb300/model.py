@@ -42,6 +42,16 @@ def _g_bulk(young, nu):
     return g, c1
 
 
+def _plane_stress(pm, young, nu, rho):
+    """PM(24) = E/(1-nu^2), PM(25) = nu*PM(24), PM(27) = sqrt(E/rho): the
+    plane-stress modulus and sound speed the shell path reads
+    (hm_read_mat02_jc.F90:151-160)."""
+    a11 = young / (1.0 - nu ** 2)
+    pm[23] = a11
+    pm[24] = nu * a11
+    pm[26] = math.sqrt(young / max(rho, 1e-20))
+
+
 def law1(rho, young, nu):
     """/MAT/ELAST (LAW1): PM(1)=rho, PM(20)=E, PM(21)=nu, PM(22)=G, PM(32)=C1."""
     pm = np.zeros(NPROPM)
@@ -51,6 +61,7 @@ def law1(rho, young, nu):
     pm[20] = nu
     pm[21] = g
     pm[31] = c1
+    _plane_stress(pm, young, nu, rho)
     pm[88] = rho  # PM(89) = RHO0
     return dict(mtn=1, pm=pm, uparam=np.zeros(NUPARAM), iparam=np.zeros(NIPARAM, np.int32))
 
@@ -85,6 +96,7 @@ def law2(rho, young, nu, a, b, n, c=0.0, eps0=1.0, epsmax=0.0, sigmax=0.0,
     pm[20] = nu
     pm[21] = g
     pm[31] = bulk
+    _plane_stress(pm, young, nu, rho)
     pm[37], pm[38], pm[39] = a, b, n
     pm[88] = rho
     up = np.zeros(NUPARAM)
@@ -102,14 +114,18 @@ def solid_prop(qa=1.1, qb=0.05, qh=0.1, dn1=0.0, dn2=0.0):
     return geo
 
 
-def shell_prop(thk, npt=5, hm=0.02, hf=0.02, hr=0.02, dm=0.0, ishell=3):
-    """/PROP/SHELL, Ishell=3 style BT with physical-stabilisation-free viscous
-    hourglass: GEO(1)=thickness, GEO(3)=ISMSTR, GEO(13..15)=hm,hf,hr,
-    GEO(16)=dm, NPT through-thickness points."""
+def shell_prop(thk, hm=0.01, hf=0.01, hr=0.01, dm=0.0, iplas=1):
+    """/PROP/SHELL, Ishell=1 (Belytschko-Tsay, viscous/elastic hourglass),
+    Ismstr=4, Ithick=1, with the reader's defaults
+    (starter/source/properties/shell/hm_read_prop01.F:200-330):
+    GEO(1)=thickness, GEO(13..15)=hm, hf, hr (default 0.01), GEO(16)=dm,
+    GEO(37)=Ishear=0, GEO(38)=shear factor 5/6, GEO(39)=Iplas."""
     geo = np.zeros(NPROPG)
     geo[0] = thk
     geo[12], geo[13], geo[14], geo[15] = hm, hf, hr, dm
-    geo[37] = 5.0 / 6.0  # shear factor
+    geo[36] = 0.0
+    geo[37] = 5.0 / 6.0
+    geo[38] = float(iplas)
     return geo
 
 
@@ -249,3 +265,76 @@ def large_block(n=128, h=0.005, vmean=20.0, vstd=0.5, seed=1, rho=7850.0,
     V[:, X[2] == 0.0] = 0.0
     return Model("large_block_%d" % n, X, V, ms, icodt,
                  hexa=[HexaGroupSpec(ixs, mat, solid_prop())])
+
+
+def shell_mass_inertia(X, ixc, thk, rho, ms=None, inr=None):
+    """Nodal mass and rotational inertia of 4-node shells
+    (starter/source/elements/shell/coque/cinmas.F): each node receives
+    EMS = rho*t*A/4 and EMS*(A/9 + t^2/12) (FAC = 9 for Ishell < 11)."""
+    numnod = X.shape[1]
+    ms = np.zeros(numnod) if ms is None else ms
+    inr = np.zeros(numnod) if inr is None else inr
+    n = ixc[1:5] - 1
+    p = [X[:, n[k]] for k in range(4)]
+    # area of the quadrilateral: half the norm of the diagonals' cross product
+    d13, d24 = p[2] - p[0], p[3] - p[1]
+    area = 0.5 * np.linalg.norm(np.cross(d13.T, d24.T), axis=1)
+    ems = rho * thk * area * 0.25
+    xi = ems * (area / 9.0 + thk * thk / 12.0)
+    for k in range(4):
+        np.add.at(ms, n[k], ems)
+        np.add.at(inr, n[k], xi)
+    return ms, inr
+
+
+def crash_box(n_side=77, n_len=390, side=0.060, length=0.300, thk=1.2e-3,
+              v0=15.0, seed=0, rho=7850.0, young=210e9, nu=0.3,
+              a=350e6, b=275e6, n=0.36, c=0.022, gap=1e-4, npt=5):
+    """Square crash box of Belytschko-Tsay shells: a tube of square section
+    (side x side) and the given length along z, n_side elements per face
+    across and n_len along (4*n_side*n_len shells), thickness thk, NPT
+    through-thickness points, Johnson-Cook LAW2.  Nodes get a seeded
+    imperfection U[-0.1 t, 0.1 t] along their face normal; the box moves at
+    v0 towards a fixed planar rigid wall just below its lower end."""
+    per = 4 * n_side
+    s = np.linspace(0.0, 4.0 * side, per + 1)[:-1]
+    face = (s // side).astype(int)
+    u = s - face * side
+    h = side / 2.0
+    xs = np.where(face == 0, -h + u, np.where(face == 1, h, np.where(face == 2, h - u, -h)))
+    ys = np.where(face == 0, -h, np.where(face == 1, -h + u, np.where(face == 2, h, h - u)))
+    nxn = np.where(face == 0, 0.0, np.where(face == 1, 1.0, np.where(face == 2, 0.0, -1.0)))
+    nyn = np.where(face == 0, -1.0, np.where(face == 1, 0.0, np.where(face == 2, 1.0, 0.0)))
+    corner = (u == 0.0)
+    zs = np.linspace(0.0, length, n_len + 1)
+    numnod = per * (n_len + 1)
+    X = np.zeros((3, numnod))
+    X[0] = np.tile(xs, n_len + 1)
+    X[1] = np.tile(ys, n_len + 1)
+    X[2] = np.repeat(zs, per)
+    rng = np.random.default_rng(seed)
+    amp = rng.uniform(-0.1 * thk, 0.1 * thk, size=numnod)
+    cn = np.tile(corner, n_len + 1)
+    amp[cn] = 0.0
+    X[0] += amp * np.tile(nxn, n_len + 1)
+    X[1] += amp * np.tile(nyn, n_len + 1)
+    nid = lambda i, j: j * per + (i % per)
+    ii, jj = np.meshgrid(np.arange(per), np.arange(n_len), indexing="xy")
+    ii, jj = ii.ravel(), jj.ravel()
+    conn = np.stack([nid(ii, jj), nid(ii + 1, jj), nid(ii + 1, jj + 1), nid(ii, jj + 1)])
+    nel = conn.shape[1]
+    ixc = np.zeros((7, nel), np.int32)
+    ixc[0] = 1
+    ixc[1:5] = conn + 1
+    ixc[5] = 1
+    ixc[6] = np.arange(1, nel + 1, dtype=np.int32)
+    t = np.full(nel, thk)
+    mat = law2(rho, young, nu, a, b, n, c=c, eps0=1.0)
+    ms, inr = shell_mass_inertia(X, ixc, t, rho)
+    V = np.zeros_like(X)
+    V[2] = -v0
+    icodt = np.zeros(numnod, np.int32)
+    m = Model("crash_box_%d" % nel, X, V, ms, icodt,
+              shells=[ShellGroupSpec(ixc, mat, shell_prop(thk), t, npt)], IN=inr)
+    m.rwalls = [((0.0, 0.0, -gap), (0.0, 0.0, 1.0), 2.0 * length)]
+    return m

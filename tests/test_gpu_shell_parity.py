@@ -1,0 +1,97 @@
+"""GPU parity of the Belytschko-Tsay shell path (CFORC3 chain, LAW2,
+PARITH/ON with rotational slots, sliding rigid wall) against the CPU oracle.
+Tolerances as for the hexa path: forces of a cycle 1e-12, trajectories over
+N cycles 1e-10 (relative to the max magnitude)."""
+import numpy as np
+import pytest
+
+from openradioss_gb300 import model as M
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    s = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / (s if s > 0 else 1.0))
+
+
+@pytest.fixture(scope="module")
+def Engine():
+    from openradioss_gb300.engine import Engine
+    return Engine
+
+
+def test_shell_skyline_matches_oracle(Engine, oracle_lib):
+    m = M.crash_box(n_side=4, n_len=6)
+    e = Engine(m)
+    o = oracle_lib.OracleModel(m, nthreads=2)
+    a1, _, c1, l1 = e.skyline()
+    a2, _, c2, l2 = o.skyline()
+    assert l1 == l2 == 4 * m.numelc
+    assert np.array_equal(a1, a2) and np.array_equal(c1, c2)
+
+
+@pytest.mark.parametrize("iplas", [1, 0])
+def test_crash_box_first_cycles(Engine, oracle_lib, iplas):
+    m = M.crash_box(n_side=5, n_len=12, v0=40.0)
+    m.shells[0].geo[38] = iplas
+    e = Engine(m)
+    o = oracle_lib.OracleModel(m, nthreads=2)
+    for _ in range(3):
+        e.cycle(1)
+        o.cycle(1)
+        fg, fo = e.forces(), o.nodes()
+        assert rel(fg["F"], fo["F"]) < 1e-12
+        assert rel(fg["FR"], fo["FR"]) < 1e-12
+        assert rel(fg["STIFN"], fo["STIFN"]) < 1e-12
+    tg, to = e.time(), o.time()
+    assert abs(tg["dt2"] - to["dt2"]) <= 1e-12 * to["dt2"]
+    assert tg["neltst"] == to["neltst"]
+
+
+def test_crash_box_trajectory(Engine, oracle_lib):
+    """Small crash box against the rigid wall, 400 cycles: plastic hinges
+    form at the impacted end; trajectories, rotations, thickness, plastic
+    strain and energies within 1e-10 / 1e-9."""
+    m = M.crash_box(n_side=6, n_len=16, v0=15.0)
+    e = Engine(m)
+    o = oracle_lib.OracleModel(m, nthreads=2)
+    for k in range(4):
+        e.cycle(100)
+        o.cycle(100)
+        ng, no = e.nodes(), o.nodes()
+        assert rel(ng["X"] - m.X, no["X"] - m.X) < 1e-10, k
+        assert rel(ng["V"], no["V"]) < 1e-10, k
+        assert rel(ng["VR"], no["VR"]) < 1e-9, k
+    nc = m.numelc
+    assert rel(e.shell_state(2, nc), o.shell_state(2, nc)) < 1e-10
+    pg, po = e.shell_state(6, 5 * nc), o.shell_state(6, 5 * nc)
+    assert po.max() > 0.0
+    assert rel(pg, po) < 1e-8
+    eg, eo = e.energy(), o.energy()
+    for key in ("eint", "ekin", "ekinr", "ehour"):
+        assert abs(eg[key] - eo[key]) <= 1e-9 * max(abs(eo[key]), 1e-12), key
+    assert e.status() == 0
+
+
+def test_shell_mixed_vs_fp64(Engine):
+    """Mixed form on the crash box: displacement, peak force and internal
+    energy within 1e-4 of the FP64 GPU path."""
+    m = M.crash_box(n_side=8, n_len=24, v0=15.0)
+    res = {}
+    for prec in (0, 1):
+        e = Engine(m, precision=prec)
+        peak, eint = 0.0, []
+        for _ in range(8):
+            e.cycle(100)
+            f = e.forces()["F"]
+            peak = max(peak, float(np.max(np.linalg.norm(f, axis=0))))
+            eint.append(e.energy()["eint"])
+        res[prec] = (e.nodes()["D"], peak, np.array(eint))
+    d64, p64, e64 = res[0]
+    d32, p32, e32 = res[1]
+    err_d = np.max(np.abs(d32 - d64)) / np.max(np.abs(d64))
+    err_p = abs(p32 - p64) / p64
+    err_e = np.max(np.abs(e32 - e64)) / np.max(np.abs(e64))
+    print("shell mixed: displacement %.2e peak force %.2e internal energy %.2e" % (err_d, err_p, err_e))
+    assert err_d < 1e-4 and err_p < 1e-4 and err_e < 1e-4

@@ -142,3 +142,60 @@ def test_energy_bounded_elastic(oracle_lib):
         e = o.energy()
         tot = e["eint"] + e["ekin"] + e["ehour"]
         assert abs(tot - e0) <= 0.08 * e0
+
+
+def flat_plate(n=3, h=0.01, thk=1e-3, V=None, VR=None):
+    """n x n flat plate of shells in the z=0 plane, no boundary conditions."""
+    ix = np.arange(n + 1)
+    gy, gx = np.meshgrid(ix, ix, indexing="ij")
+    X = np.stack([h * gx.ravel(), h * gy.ravel(), np.zeros((n + 1) ** 2)])
+    nid = lambda i, j: j * (n + 1) + i
+    ey, ex = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    ex, ey = ex.ravel(), ey.ravel()
+    conn = np.stack([nid(ex, ey), nid(ex + 1, ey), nid(ex + 1, ey + 1), nid(ex, ey + 1)])
+    ixc = np.zeros((7, conn.shape[1]), np.int32)
+    ixc[0] = 1
+    ixc[1:5] = conn + 1
+    ixc[5] = 1
+    ixc[6] = np.arange(1, conn.shape[1] + 1)
+    t = np.full(conn.shape[1], thk)
+    mat = M.law2(7850.0, 210e9, 0.3, 350e6, 275e6, 0.36, c=0.022, eps0=1.0)
+    ms, inr = M.shell_mass_inertia(X, ixc, t, 7850.0)
+    m = M.Model("plate", X, np.zeros_like(X) if V is None else V, ms,
+                np.zeros(X.shape[1], np.int32),
+                shells=[M.ShellGroupSpec(ixc, mat, M.shell_prop(thk), t, 5)], IN=inr)
+    return m
+
+
+def test_shell_rigid_translation(oracle_lib):
+    m = flat_plate()
+    m.V[0] = 2.0
+    m.V[2] = -1.0
+    o = oracle_lib.OracleModel(m, nthreads=1)
+    o.cycle(3)
+    nd = o.nodes()
+    assert np.max(np.abs(nd["F"])) < 1e-9
+    assert np.max(np.abs(nd["FR"])) < 1e-12
+
+
+def test_shell_membrane_patch(oracle_lib):
+    """Uniform in-plane velocity gradient on a flat plate: after the first
+    stressed cycle every integration point holds the plane-stress elastic
+    increment A11*dexx + A12*deyy, A12*dexx + A11*deyy, G*dexy."""
+    m = flat_plate()
+    L = np.array([[2.0, 0.5], [0.5, -1.0]])
+    m.V[:2] = L @ m.X[:2]
+    o = oracle_lib.OracleModel(m, nthreads=1)
+    o.cycle(1)
+    dt1 = o.time()["dt2"]
+    o.cycle(1)
+    nc = m.numelc
+    sig = o.shell_state(5, 5 * 5 * nc).reshape(5, 5, nc)
+    E, nu = 210e9, 0.3
+    a11 = E / (1 - nu * nu)
+    a12 = nu * a11
+    G = E / (2 * (1 + nu))
+    dexx, deyy, dexy = L[0, 0] * dt1, L[1, 1] * dt1, 2 * L[0, 1] * dt1
+    exp = [a11 * dexx + a12 * deyy, a12 * dexx + a11 * deyy, G * dexy]
+    for c in range(3):
+        assert np.allclose(sig[:, c, :], exp[c], rtol=1e-3), c
