@@ -273,19 +273,23 @@ def run_ours(args, rank, world, local_rank):
     return line
 
 
-def cpu_baseline(wl, sample_cycles, threads=None, steps=None):
+def cpu_baseline(wl, sample_s, threads=None):
     """Time the CPU restatement (oracle/) on the host cores: a bounded
     sample of the same workload."""
     from oracle.oracle import OracleModel
     model = WORKLOADS[wl]()
     nt = threads or os.cpu_count() or 1
     o = OracleModel(model, nthreads=nt)
+    t0 = time.perf_counter()
     o.cycle(1)
-    n = sample_cycles
+    t1 = time.perf_counter() - t0
+    # bounded sample: about sample_s seconds of CPU work
+    n = max(3, min(5000, int(sample_s / max(t1, 1e-6))))
     t0 = time.perf_counter()
     o.cycle(n)
     dt = time.perf_counter() - t0
-    return {"value": model.numels * n / dt, "unit": "element-updates/s", "cores": nt,
+    ne = model.numels + model.numelc
+    return {"value": ne * n / dt, "unit": "element-updates/s", "cores": nt,
             "kind": "port", "sample": "%s, %d cycles after 1 warm-up cycle (%.1f s)" % (wl, n, dt)}
 
 
@@ -304,12 +308,13 @@ def run_reference(args, rank, world):
     t0 = time.perf_counter()
     o.cycle(args.steps)
     dt = time.perf_counter() - t0
-    v = model.numels * args.steps / dt
+    v = (model.numels + model.numelc) * args.steps / dt
     return {"metric": "element-updates/s", "value": v, "unit": "element-updates/s",
             "impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl, "elements": model.numels, "nodes": model.numnod},
+            "config": {"workload": wl, "elements": model.numels + model.numelc,
+                       "nodes": model.numnod},
             "cpu_baseline": {"value": v, "unit": "element-updates/s", "cores": nt, "kind": "port",
                              "sample": "%s, %d cycles" % (wl, args.steps)},
             "e2e": {"value": v, "unit": "element-updates/s", "h2d_bytes_per_step": 0,
@@ -326,7 +331,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-sample", type=int, default=20)
+    ap.add_argument("--cpu-sample", type=float, default=15.0,
+                    help="seconds of CPU work in the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="both", choices=["both", "f64", "mixed"],
                     help="arithmetic forms to run (profiling runs pick one)")

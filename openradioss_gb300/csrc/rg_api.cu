@@ -120,43 +120,80 @@ int dalloc(rg_ctx *c, T **p, size_t n) {
 // multiply-add is fused and each node's result does not depend on the
 // launch configuration.
 // ---------------------------------------------------------------------------
-template <typename ST, bool ROT>
+__device__ __forceinline__ F8 split_hilo(double x, double y, double z) {
+  F8 c;
+  c.hx = __double2float_rn(x);
+  c.hy = __double2float_rn(y);
+  c.hz = __double2float_rn(z);
+  c.lx = __double2float_rn(x - (double)c.hx);
+  c.ly = __double2float_rn(y - (double)c.hy);
+  c.lz = __double2float_rn(z - (double)c.hz);
+  c.pad0 = c.pad1 = 0.f;
+  return c;
+}
+
+template <bool F64, bool ROT>
 __global__ void __launch_bounds__(NODE_NT)
-node_kernel(NodeView N, const int *__restrict__ adsky,
-            const ST *__restrict__ fsky, const ST *__restrict__ fskyr,
-            const Time *__restrict__ T, const int *__restrict__ wall,
-            const double *__restrict__ walls, int *__restrict__ status) {
+node_kernel(NodeView N, const int *__restrict__ adsky, const void *__restrict__ fsky_,
+            const void *__restrict__ fskyr_, const Time *__restrict__ T,
+            const int *__restrict__ wall, const double *__restrict__ walls,
+            int *__restrict__ status) {
   const int n = blockIdx.x * NODE_NT + threadIdx.x;
   if (n >= N.numnod) return;
   const int k0 = __ldg(adsky + n), k1 = __ldg(adsky + n + 1);
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  double r0 = 0.0, r1 = 0.0, r2 = 0.0;
-  for (int k = k0; k < k1; k++) {
-    const ST f = fsky[k];
-    a0 = __dadd_rn(a0, (double)f.x);
-    a1 = __dadd_rn(a1, (double)f.y);
-    a2 = __dadd_rn(a2, (double)f.z);
-    if (ROT) {
-      const ST g = fskyr[k];
-      r0 = __dadd_rn(r0, (double)g.x);
-      r1 = __dadd_rn(r1, (double)g.y);
-      r2 = __dadd_rn(r2, (double)g.z);
+  double a0, a1, a2, r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  if constexpr (F64) {
+    // ASSPAR4: A = 0 + sum of the node's slots in PARITH/ON order, FP64
+    const dbl4 *fsky = (const dbl4 *)fsky_;
+    const dbl4 *fskyr = (const dbl4 *)fskyr_;
+    a0 = a1 = a2 = 0.0;
+    for (int k = k0; k < k1; k++) {
+      const dbl4 f = fsky[k];
+      a0 = __dadd_rn(a0, f.x);
+      a1 = __dadd_rn(a1, f.y);
+      a2 = __dadd_rn(a2, f.z);
+      if (ROT) {
+        const dbl4 g = fskyr[k];
+        r0 = __dadd_rn(r0, g.x);
+        r1 = __dadd_rn(r1, g.y);
+        r2 = __dadd_rn(r2, g.z);
+      }
     }
+    if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicOr(status, RG_ST_NAN);
+  } else {
+    // mixed form: FP32 element forces summed in the same fixed order in
+    // FP32 (explicit round-to-nearest adds: no reassociation), then FP64
+    const float4 *fsky = (const float4 *)fsky_;
+    const float4 *fskyr = (const float4 *)fskyr_;
+    float b0 = 0.f, b1 = 0.f, b2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    for (int k = k0; k < k1; k++) {
+      const float4 f = __ldg(fsky + k);
+      b0 = __fadd_rn(b0, f.x);
+      b1 = __fadd_rn(b1, f.y);
+      b2 = __fadd_rn(b2, f.z);
+      if (ROT) {
+        const float4 g = __ldg(fskyr + k);
+        c0 = __fadd_rn(c0, g.x);
+        c1 = __fadd_rn(c1, g.y);
+        c2 = __fadd_rn(c2, g.z);
+      }
+    }
+    if (!(isfinite(b0) && isfinite(b1) && isfinite(b2))) atomicOr(status, RG_ST_NAN);
+    a0 = b0;
+    a1 = b1;
+    a2 = b2;
+    r0 = c0;
+    r1 = c1;
+    r2 = c2;
   }
   dbl4 x = ld4(N.X4 + n);
   dbl4 v = ld4(N.V4 + n);
   dbl4 d = ld4(N.D4 + n);
   const double dt12 = T->dt12, dt2 = T->dt2;
-  // ACCELE
-  if (x.w > 0.0) {
-    const double rt = __ddiv_rn(1.0, x.w);
-    a0 = __dmul_rn(a0, rt);
-    a1 = __dmul_rn(a1, rt);
-    a2 = __dmul_rn(a2, rt);
-  } else {
-    a0 = a1 = a2 = 0.0;
-  }
-  if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicOr(status, RG_ST_NAN);
+  // ACCELE: A = A * (1/MS); X4.w holds 1/MS (0 when MS <= 0, giving A = 0)
+  a0 = __dmul_rn(a0, x.w);
+  a1 = __dmul_rn(a1, x.w);
+  a2 = __dmul_rn(a2, x.w);
   const int code = (int)v.w;
   if (code) {
     if (code & 1) a0 = 0.0;
@@ -196,31 +233,41 @@ node_kernel(NodeView N, const int *__restrict__ adsky,
       }
     }
   }
-  // VELOCITY + DEPLA
-  v.x = __dadd_rn(v.x, __dmul_rn(dt12, a0));
-  v.y = __dadd_rn(v.y, __dmul_rn(dt12, a1));
-  v.z = __dadd_rn(v.z, __dmul_rn(dt12, a2));
-  const double vdx = __dmul_rn(dt2, v.x), vdy = __dmul_rn(dt2, v.y),
-               vdz = __dmul_rn(dt2, v.z);
-  d.x = __dadd_rn(d.x, vdx);
-  d.y = __dadd_rn(d.y, vdy);
-  d.z = __dadd_rn(d.z, vdz);
-  x.x = __dadd_rn(x.x, vdx);
-  x.y = __dadd_rn(x.y, vdy);
-  x.z = __dadd_rn(x.z, vdz);
+  // VELOCITY + DEPLA (FP64 in both forms; FP64 form without fused
+  // multiply-add, as the reference)
+  if constexpr (F64) {
+    v.x = __dadd_rn(v.x, __dmul_rn(dt12, a0));
+    v.y = __dadd_rn(v.y, __dmul_rn(dt12, a1));
+    v.z = __dadd_rn(v.z, __dmul_rn(dt12, a2));
+    const double vdx = __dmul_rn(dt2, v.x), vdy = __dmul_rn(dt2, v.y), vdz = __dmul_rn(dt2, v.z);
+    d.x = __dadd_rn(d.x, vdx);
+    d.y = __dadd_rn(d.y, vdy);
+    d.z = __dadd_rn(d.z, vdz);
+    x.x = __dadd_rn(x.x, vdx);
+    x.y = __dadd_rn(x.y, vdy);
+    x.z = __dadd_rn(x.z, vdz);
+  } else {
+    v.x = fma(dt12, a0, v.x);
+    v.y = fma(dt12, a1, v.y);
+    v.z = fma(dt12, a2, v.z);
+    d.x = fma(dt2, v.x, d.x);
+    d.y = fma(dt2, v.y, d.y);
+    d.z = fma(dt2, v.z, d.z);
+    x.x = fma(dt2, v.x, x.x);
+    x.y = fma(dt2, v.y, x.y);
+    x.z = fma(dt2, v.z, x.z);
+    N.XF[n] = split_hilo(x.x, x.y, x.z);
+    N.VF[n] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y),
+                          __double2float_rn(v.z), 0.f);
+  }
   st4(N.X4 + n, x);
   st4(N.V4 + n, v);
   st4(N.D4 + n, d);
   if (ROT) {
     dbl4 vr = ld4(N.VR4 + n);
-    if (vr.w > 0.0) {
-      const double rt = __ddiv_rn(1.0, vr.w);
-      r0 = __dmul_rn(r0, rt);
-      r1 = __dmul_rn(r1, rt);
-      r2 = __dmul_rn(r2, rt);
-    } else {
-      r0 = r1 = r2 = 0.0;
-    }
+    r0 = __dmul_rn(r0, vr.w);
+    r1 = __dmul_rn(r1, vr.w);
+    r2 = __dmul_rn(r2, vr.w);
     if (code) {
       if (code & 8) r0 = 0.0;
       if (code & 16) r1 = 0.0;
@@ -230,6 +277,23 @@ node_kernel(NodeView N, const int *__restrict__ adsky,
     vr.y = __dadd_rn(vr.y, __dmul_rn(dt12, r1));
     vr.z = __dadd_rn(vr.z, __dmul_rn(dt12, r2));
     st4(N.VR4 + n, vr);
+    if constexpr (!F64)
+      N.VRF[n] = make_float4(__double2float_rn(vr.x), __double2float_rn(vr.y),
+                             __double2float_rn(vr.z), 0.f);
+  }
+}
+
+// Mixed form: refresh the FP32 copies from the FP64 node records (after a
+// host upload).
+__global__ void refresh_copies_kernel(NodeView N, int rot) {
+  const int n = blockIdx.x * NODE_NT + threadIdx.x;
+  if (n >= N.numnod) return;
+  const dbl4 x = N.X4[n], v = N.V4[n];
+  N.XF[n] = split_hilo(x.x, x.y, x.z);
+  N.VF[n] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y), __double2float_rn(v.z), 0.f);
+  if (rot) {
+    const dbl4 w = N.VR4[n];
+    N.VRF[n] = make_float4(__double2float_rn(w.x), __double2float_rn(w.y), __double2float_rn(w.z), 0.f);
   }
 }
 
@@ -322,11 +386,11 @@ energy_kernel(int ne, const double *__restrict__ eint,
     s[1] += ehou[i];
   }
   for (int i = blockIdx.x * EN_NT + threadIdx.x; i < N.numnod; i += stride) {
-    const dbl4 x = N.X4[i], v = N.V4[i];
-    s[2] += 0.5 * x.w * (v.x * v.x + v.y * v.y + v.z * v.z);
+    const dbl4 m = N.D4[i], v = N.V4[i];
+    s[2] += 0.5 * m.w * (v.x * v.x + v.y * v.y + v.z * v.z);
     if (rot) {
-      const dbl4 w = N.VR4[i];
-      s[3] += 0.5 * w.w * (w.x * w.x + w.y * w.y + w.z * w.z);
+      const dbl4 w = N.VR4[i], in = N.DR4[i];
+      s[3] += 0.5 * in.w * (w.x * w.x + w.y * w.y + w.z * w.z);
     }
   }
   __shared__ double sh[4][EN_NT];
@@ -534,22 +598,18 @@ int enqueue_nodes(rg_ctx *c) {
   const int nb = (c->numnod + NODE_NT - 1) / NODE_NT;
   if (c->prec == RG_PREC_FP64) {
     if (c->rot)
-      node_kernel<dbl4, true><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, (const dbl4 *)c->d_fsky, (const dbl4 *)c->d_fskyr,
-          c->d_time, c->d_wall, c->d_walls, c->d_status);
+      node_kernel<true, true><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, c->d_fsky, c->d_fskyr, c->d_time, c->d_wall, c->d_walls, c->d_status);
     else
-      node_kernel<dbl4, false><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, (const dbl4 *)c->d_fsky, nullptr, c->d_time, c->d_wall,
-          c->d_walls, c->d_status);
+      node_kernel<true, false><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, c->d_fsky, nullptr, c->d_time, c->d_wall, c->d_walls, c->d_status);
   } else {
     if (c->rot)
-      node_kernel<float4, true><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, (const float4 *)c->d_fsky, (const float4 *)c->d_fskyr,
-          c->d_time, c->d_wall, c->d_walls, c->d_status);
+      node_kernel<false, true><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, c->d_fsky, c->d_fskyr, c->d_time, c->d_wall, c->d_walls, c->d_status);
     else
-      node_kernel<float4, false><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, (const float4 *)c->d_fsky, nullptr, c->d_time, c->d_wall,
-          c->d_walls, c->d_status);
+      node_kernel<false, false><<<nb, NODE_NT, 0, c->stream>>>(
+          c->nv, c->d_adsky, c->d_fsky, nullptr, c->d_time, c->d_wall, c->d_walls, c->d_status);
   }
   return RG_OK;
 }
@@ -777,12 +837,17 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     return fail(c, RG_E_ARG, "skyline: " + why);
   int r;
   // nodes
+  // X4.w = 1/MS and VR4.w = 1/IN: ACCELE's RTMP = ONE/MS(N) evaluated once
+  // (the same IEEE quotient), D4.w = MS and DR4.w = IN for the energies.
   std::vector<dbl4> x4(numnod), v4(numnod), z4(numnod, mk4(0, 0, 0, 0)),
-      vr4(numnod, mk4(0, 0, 0, 0));
+      vr4(numnod, mk4(0, 0, 0, 0)), dr4(numnod, mk4(0, 0, 0, 0));
   for (int n = 0; n < numnod; n++) {
-    x4[n] = mk4(c->X[3 * n], c->X[3 * n + 1], c->X[3 * n + 2], c->MS[n]);
+    const double ms = c->MS[n], in = c->IN[n];
+    x4[n] = mk4(c->X[3 * n], c->X[3 * n + 1], c->X[3 * n + 2], ms > 0.0 ? 1.0 / ms : 0.0);
     v4[n] = mk4(c->V[3 * n], c->V[3 * n + 1], c->V[3 * n + 2], (double)c->icodt[n]);
-    vr4[n].w = c->IN[n];
+    z4[n] = mk4(0, 0, 0, ms);
+    vr4[n].w = in > 0.0 ? 1.0 / in : 0.0;
+    dr4[n].w = in;
   }
   if ((r = dalloc(c, &c->nv.X4, numnod))) return r;
   if ((r = dalloc(c, &c->nv.V4, numnod))) return r;
@@ -793,7 +858,17 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   RG_CUDA(c, cudaMemcpy(c->nv.D4, z4.data(), numnod * sizeof(dbl4), cudaMemcpyHostToDevice));
   if (c->rot) {
     if ((r = dalloc(c, &c->nv.VR4, numnod))) return r;
+    if ((r = dalloc(c, &c->nv.DR4, numnod))) return r;
     RG_CUDA(c, cudaMemcpy(c->nv.VR4, vr4.data(), numnod * sizeof(dbl4), cudaMemcpyHostToDevice));
+    RG_CUDA(c, cudaMemcpy(c->nv.DR4, dr4.data(), numnod * sizeof(dbl4), cudaMemcpyHostToDevice));
+  }
+  if (c->prec == RG_PREC_MIXED) {
+    if ((r = dalloc(c, &c->nv.XF, numnod))) return r;
+    if ((r = dalloc(c, &c->nv.VF, numnod))) return r;
+    if (c->rot && (r = dalloc(c, &c->nv.VRF, numnod))) return r;
+    refresh_copies_kernel<<<(numnod + NODE_NT - 1) / NODE_NT, NODE_NT, 0, c->stream>>>(
+        c->nv, c->rot ? 1 : 0);
+    RG_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   // skyline (0-based on the device)
   std::vector<int> ad0(numnod + 1);
@@ -998,9 +1073,13 @@ int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr
                                cudaMemcpyHostToDevice, c->stream));
     pack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, st + 6 * (size_t)n, c->nv.VR4);
   }
+  if (c->prec == RG_PREC_MIXED)
+    refresh_copies_kernel<<<nb, NODE_NT, 0, c->stream>>>(c->nv, (vr && c->rot) ? 1 : 0);
   // DT1 for this call: the element kernels read it from Time::dt2
   RG_CUDA(c, cudaMemcpyAsync(&c->d_time->dt2, &dt1, sizeof(double), cudaMemcpyHostToDevice,
                              c->stream));
+  if (c->prec == RG_PREC_MIXED && c->numels > 0)
+    launch_hexa_prev_volume(c->h32, c->nv, c->d_time, c->stream);
   enqueue_elements(c);
   dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time, c->d_status, 0);
   enqueue_assemble(c, st);

@@ -40,12 +40,22 @@ struct Time {
   int ncycle, neltst, status, pad;
 };
 
+// FP32 copy of a node position as an unevaluated sum hi + lo of two floats
+// (mixed form): the difference of two nodes' copies keeps FP32 relative
+// precision however far the nodes are from the origin.
+struct __align__(32) F8 {
+  float hx, hy, hz, pad0, lx, ly, lz, pad1;
+};
+
 struct NodeView {
-  dbl4 *X4;   // x y z MS
+  dbl4 *X4;   // x y z 1/MS      (1/MS = 0 when MS <= 0)
   dbl4 *V4;   // vx vy vz code(as double)
-  dbl4 *D4;   // dx dy dz -
-  dbl4 *VR4;  // vrx vry vrz IN (shell models only)
-  dbl4 *DR4;  // unused slot, kept for alignment of the record set
+  dbl4 *D4;   // dx dy dz MS
+  dbl4 *VR4;  // vrx vry vrz 1/IN (shell models only)
+  dbl4 *DR4;  // - - - IN          (shell models only)
+  F8 *XF;     // mixed form: FP32 hi/lo position copies
+  float4 *VF;   // mixed form: FP32 velocity copies
+  float4 *VRF;  // mixed form: FP32 rotational velocity copies (shells)
   int numnod;
 };
 
@@ -57,6 +67,8 @@ struct DtPartials {
 
 __device__ __forceinline__ dbl4 ld4(const dbl4 *__restrict__ p) { return *p; }
 __device__ __forceinline__ void st4(dbl4 *__restrict__ p, dbl4 v) { *p = v; }
+__device__ __forceinline__ F8 ldF8(const F8 *__restrict__ p) { return *p; }
+__device__ __forceinline__ float4 ldf4(const float4 *__restrict__ p) { return __ldg(p); }
 
 // Block-level (min dt, element) reduction; ties keep the larger element
 // order key (the last element attaining the minimum in sequential order).
@@ -68,15 +80,25 @@ __device__ __forceinline__ void dt_pair_min(double &d, int &k, double d2,
   }
 }
 
-template <int NT>
-__device__ __forceinline__ void block_dt_min(double d, int k, double *out_d,
+template <typename T>
+__device__ __forceinline__ void dt_pair_min_t(T &d, int &k, T d2, int k2) {
+  if (d2 < d || (d2 == d && k2 > k)) {
+    d = d2;
+    k = k2;
+  }
+}
+
+// Block minimum of (dt, key) in the element arithmetic type T; the block's
+// result is stored as FP64.
+template <int NT, typename T = double>
+__device__ __forceinline__ void block_dt_min(T d, int k, double *out_d,
                                              int *out_k) {
-  __shared__ double sd[NT / 32];
+  __shared__ T sd[NT / 32];
   __shared__ int sk[NT / 32];
   for (int o = 16; o > 0; o >>= 1) {
-    double d2 = __shfl_down_sync(0xffffffffu, d, o);
+    T d2 = __shfl_down_sync(0xffffffffu, d, o);
     int k2 = __shfl_down_sync(0xffffffffu, k, o);
-    dt_pair_min(d, k, d2, k2);
+    dt_pair_min_t(d, k, d2, k2);
   }
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) {
@@ -85,15 +107,15 @@ __device__ __forceinline__ void block_dt_min(double d, int k, double *out_d,
   }
   __syncthreads();
   if (w == 0) {
-    d = l < NT / 32 ? sd[l] : RG_EP30;
+    d = l < NT / 32 ? sd[l] : (T)RG_EP30;
     k = l < NT / 32 ? sk[l] : -1;
     for (int o = 16; o > 0; o >>= 1) {
-      double d2 = __shfl_down_sync(0xffffffffu, d, o);
+      T d2 = __shfl_down_sync(0xffffffffu, d, o);
       int k2 = __shfl_down_sync(0xffffffffu, k, o);
-      dt_pair_min(d, k, d2, k2);
+      dt_pair_min_t(d, k, d2, k2);
     }
     if (l == 0) {
-      *out_d = d;
+      *out_d = (double)d;
       *out_k = k;
     }
   }

@@ -32,15 +32,6 @@
 
 namespace rg {
 
-template <typename T>
-__device__ __forceinline__ T rmax(T a, T b) {
-  return a > b ? a : (b != b ? b : a);
-}
-template <typename T>
-__device__ __forceinline__ T rmin(T a, T b) {
-  return a < b ? a : (b != b ? b : a);
-}
-
 // Fortran MAX/MIN with the argument order of the source: MAX(a,b) returns
 // a if a>b, else b (NaN propagation is not relied on).
 template <typename T>
@@ -61,7 +52,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
   constexpr bool F64 = std::is_same<ER, double>::value;
   const int il = blockIdx.x * NT + threadIdx.x;
   const int ne = A.ne;
-  double dtmine = RG_EP06;
+  R dtmine = (R)RG_EP06;
   int elmin = -1;
 
   if (il < P.nel) {
@@ -76,41 +67,48 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     const R offg0 = A.off[e];
     R offg = offg0;
     R off = fabs(offg0);
-    double xa[8], ya[8], za[8];
-    R vx[8], vy[8], vz[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      const dbl4 x = ld4(N.X4 + nc[k]);
-      const dbl4 v = ld4(N.V4 + nc[k]);
-      xa[k] = x.x;
-      ya[k] = x.y;
-      za[k] = x.z;
-      if (offg0 < (R)0) {
-        vx[k] = vy[k] = vz[k] = (R)0;
-      } else {
-        vx[k] = (R)v.x;
-        vy[k] = (R)v.y;
-        vz[k] = (R)v.z;
-      }
-    }
-    // geometry in the element type: absolute (FP64) or relative to node 1
     R x[8], y[8], z[8];
+    R vx[8], vy[8], vz[8];
+    if constexpr (F64) {
+      // FP64 form: absolute FP64 coordinates, as the reference
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      if (F64) {
-        x[k] = (R)xa[k];
-        y[k] = (R)ya[k];
-        z[k] = (R)za[k];
-      } else {
-        x[k] = (R)(xa[k] - xa[0]);
-        y[k] = (R)(ya[k] - ya[0]);
-        z[k] = (R)(za[k] - za[0]);
+      for (int k = 0; k < 8; k++) {
+        const dbl4 xk = ld4(N.X4 + nc[k]);
+        const dbl4 vk = ld4(N.V4 + nc[k]);
+        x[k] = xk.x;
+        y[k] = xk.y;
+        z[k] = xk.z;
+        const bool z0 = offg0 < (R)0;
+        vx[k] = z0 ? (R)0 : (R)vk.x;
+        vy[k] = z0 ? (R)0 : (R)vk.y;
+        vz[k] = z0 ? (R)0 : (R)vk.z;
+      }
+    } else {
+      // mixed form: FP32 copies kept by the node kernel -- coordinates as a
+      // hi + lo pair of floats, so that differences between the nodes of an
+      // element keep FP32 relative precision at any distance from the origin
+      F8 c[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        c[k] = ldF8(N.XF + nc[k]);
+        const float4 vk = ldf4(N.VF + nc[k]);
+        const bool z0 = offg0 < (R)0;
+        vx[k] = z0 ? 0.f : vk.x;
+        vy[k] = z0 ? 0.f : vk.y;
+        vz[k] = z0 ? 0.f : vk.z;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        x[k] = (c[k].hx - c[0].hx) + (c[k].lx - c[0].lx);
+        y[k] = (c[k].hy - c[0].hy) + (c[k].ly - c[0].ly);
+        z[k] = (c[k].hz - c[0].hz) + (c[k].lz - c[0].lz);
       }
     }
 
     // ---- SDERI3 ------------------------------------------------------------
     R px[4], py[4], pz[4], ph[4][3];
-    double voln;  // VOLDP: FP64 in both forms
+    double voln;  // element volume (VOLDP)
+    double vold_mixed = 0.0;
     {
       const R x17 = x[6] - x[0], x28 = x[7] - x[1], x35 = x[4] - x[2], x46 = x[5] - x[3];
       const R y17 = y[6] - y[0], y28 = y[7] - y[1], y35 = y[4] - y[2], y46 = y[5] - y[3];
@@ -126,36 +124,61 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
       const R j5968 = jac5 * jac9 - jac6 * jac8;
       const R j6749 = jac6 * jac7 - jac4 * jac9;
       const R j4857 = jac4 * jac8 - jac5 * jac7;
-      double det;
-      if (F64) {
-        det = RG_ONE_OVER_64 * ((double)jac1 * (double)j5968 + (double)jac2 * (double)j6749 +
-                                (double)jac3 * (double)j4857);
-      } else {
-        // FP64 determinant from FP64 relative coordinates (VOLDP)
-        const double X17 = xa[6] - xa[0], X28 = xa[7] - xa[1], X35 = xa[4] - xa[2], X46 = xa[5] - xa[3];
-        const double Y17 = ya[6] - ya[0], Y28 = ya[7] - ya[1], Y35 = ya[4] - ya[2], Y46 = ya[5] - ya[3];
-        const double Z17 = za[6] - za[0], Z28 = za[7] - za[1], Z35 = za[4] - za[2], Z46 = za[5] - za[3];
-        const double J1 = X17 + X28 - X35 - X46, J2 = Y17 + Y28 - Y35 - Y46, J3 = Z17 + Z28 - Z35 - Z46;
-        const double J4 = (X17 + X46) + (X28 + X35), J5 = (Y17 + Y46) + (Y28 + Y35),
-                     J6 = (Z17 + Z46) + (Z28 + Z35);
-        const double J7 = (X17 + X46) - (X28 + X35), J8 = (Y17 + Y46) - (Y28 + Y35),
-                     J9 = (Z17 + Z46) - (Z28 + Z35);
-        det = RG_ONE_OVER_64 * (J1 * (J5 * J9 - J6 * J8) + J2 * (J6 * J7 - J4 * J9) +
-                                J3 * (J4 * J8 - J5 * J7));
-      }
+      R det = (R)RG_ONE_OVER_64 * (jac1 * j5968 + jac2 * j6749 + jac3 * j4857);
       // SCHKJABT3: a live element with a non-positive volume is switched
       // off and the run is flagged (INEG_V = 0 stops the run).
+      bool live = true;
       if (off == (R)0) {
-        det = RG_ONE;
-      } else if (det <= RG_ZERO) {
-        det = RG_ONE;
+        det = (R)RG_ONE;
+        live = false;
+      } else if (det <= (R)0) {
+        det = (R)RG_ONE;
         off = (R)0;
         offg = (R)0;
         A.off[e] = (R)0;
         atomicOr(status, 1);
+        live = false;
       }
-      voln = det;
-      const R dett = (R)(RG_ONE_OVER_64 / det);
+      if constexpr (F64) {
+        voln = det;
+      } else {
+        // Volume change over the last step, V(X) - V(X - DT1*V), as the
+        // exact trilinear expansion of the determinant in the rows
+        // a=(J1,J2,J3), b=(J4,J5,J6), c=(J7,J8,J9) and their velocity
+        // increments: every term is computed in FP32 at its own scale (no
+        // cancellation), and the volume is accumulated in FP64.
+        vold_mixed = A.rho[e];
+        if (live) {
+          const R u17 = vx[6] - vx[0], u28 = vx[7] - vx[1], u35 = vx[4] - vx[2], u46 = vx[5] - vx[3];
+          const R v17 = vy[6] - vy[0], v28 = vy[7] - vy[1], v35 = vy[4] - vy[2], v46 = vy[5] - vy[3];
+          const R w17 = vz[6] - vz[0], w28 = vz[7] - vz[1], w35 = vz[4] - vz[2], w46 = vz[5] - vz[3];
+          const R da1 = dt1 * (u17 + u28 - u35 - u46), da2 = dt1 * (v17 + v28 - v35 - v46),
+                  da3 = dt1 * (w17 + w28 - w35 - w46);
+          const R db1 = dt1 * ((u17 + u46) + (u28 + u35)), db2 = dt1 * ((v17 + v46) + (v28 + v35)),
+                  db3 = dt1 * ((w17 + w46) + (w28 + w35));
+          const R dc1 = dt1 * ((u17 + u46) - (u28 + u35)), dc2 = dt1 * ((v17 + v46) - (v28 + v35)),
+                  dc3 = dt1 * ((w17 + w46) - (w28 + w35));
+          // c x a, a x b
+          const R ca1 = jac8 * jac3 - jac9 * jac2, ca2 = jac9 * jac1 - jac7 * jac3,
+                  ca3 = jac7 * jac2 - jac8 * jac1;
+          const R ab1 = jac2 * jac6 - jac3 * jac5, ab2 = jac3 * jac4 - jac1 * jac6,
+                  ab3 = jac1 * jac5 - jac2 * jac4;
+          const R t1 = (da1 * j5968 + da2 * j6749 + da3 * j4857) +
+                       (db1 * ca1 + db2 * ca2 + db3 * ca3) + (dc1 * ab1 + dc2 * ab2 + dc3 * ab3);
+          // db x c + b x dc, db x dc
+          const R m1 = (db2 * jac9 - db3 * jac8) + (jac5 * dc3 - jac6 * dc2);
+          const R m2 = (db3 * jac7 - db1 * jac9) + (jac6 * dc1 - jac4 * dc3);
+          const R m3 = (db1 * jac8 - db2 * jac7) + (jac4 * dc2 - jac5 * dc1);
+          const R q1 = db2 * dc3 - db3 * dc2, q2 = db3 * dc1 - db1 * dc3, q3 = db1 * dc2 - db2 * dc1;
+          const R t2 = (da1 * m1 + da2 * m2 + da3 * m3) + (jac1 * q1 + jac2 * q2 + jac3 * q3);
+          const R t3 = da1 * q1 + da2 * q2 + da3 * q3;
+          const R dv = (R)RG_ONE_OVER_64 * ((t1 - t2) + t3);
+          voln = vold_mixed + (double)dv;
+        } else {
+          voln = vold_mixed;
+        }
+      }
+      const R dett = (R)RG_ONE_OVER_64 / det;
       const R jaci1 = dett * j5968;
       const R jaci4 = dett * j6749;
       const R jaci7 = dett * j4857;
@@ -250,29 +273,26 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
 
     // ---- SRHO3 (Lagrangian) -------------------------------------------------
     // FP64 form: RHO state, DVOL = VOLN - (RHO0/RHO)*VOL0, RHO = RHO0*VOL0/VOLN.
-    // Mixed form: the FP64 state array holds the volume of the last cycle
-    // instead of the density (same information, RHO = RHO0*VOL0/VOL), so
-    // DVOL is one FP64 subtraction and no FP64 division is needed.
+    // Mixed form: the FP64 state array holds the element volume of the last
+    // cycle instead of the density (RHO = RHO0*VOL0/VOL), DVOL is the
+    // FP32 volume change computed above.
     const double vol0 = A.vol0[e];
     if (offg == (R)0 && voln == RG_ONE) voln = vol0;
-    double dvol_d, rho_new;
     R rho_r, amu, dvol_r;
-    if (F64) {
+    double dvol_d = 0.0;
+    if constexpr (F64) {
       const double rho_old = A.rho[e];
       dvol_d = voln - (P.rho0 / rho_old) * vol0;
-      rho_new = P.rho0 * (vol0 / voln);
+      const double rho_new = P.rho0 * (vol0 / voln);
       A.rho[e] = rho_new;
       rho_r = (R)rho_new;
       amu = (R)(rho_new / P.rho0 - RG_ONE);
       dvol_r = (R)dvol_d;
     } else {
-      const double vold = A.rho[e];
-      dvol_d = voln - vold;
       A.rho[e] = voln;
-      rho_new = 0.0;
+      dvol_r = (R)(voln - vold_mixed);
       rho_r = (R)P.rho0 * ((R)vol0 / volr);
       amu = (R)(vol0 - voln) / volr;  // RHO/RHO0 - 1 = VOL0/VOLN - 1
-      dvol_r = (R)dvol_d;
     }
 
     // ---- SROTA3 --------------------------------------------------------------
@@ -413,7 +433,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
         const R tidt = (R)RG_ONE / dtx;
         sti = (rhoe * tidt) * (volr * tidt);
       }
-      const double dtxd = F64 ? P.dtfac * (double)dtx : (double)((R)P.dtfac * dtx);
+      const R dtxd = (R)P.dtfac * dtx;
       if (voln > RG_ZERO && (off != (R)0 && offg >= (R)0)) {
         dtmine = dtxd;
         elmin = e;  // element order key; mapped to the user id by the dt kernel
@@ -583,8 +603,8 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
   }
 
   // per-block time-step candidate
-  block_dt_min<NT>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x,
-                   dp.el + P.part_off + blockIdx.x);
+  block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x,
+                      dp.el + P.part_off + blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -599,6 +619,44 @@ static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
 }
 
 int hexa_blocks(int nel) { return (nel + 127) / 128; }
+
+// Mixed form, FORINT-level call: the host supplies X and V for the cycle, so
+// the FP64 volume that the element kernel advances by its FP32 increment
+// V(X) - V(X - DT1*V) is re-anchored to the previous configuration
+// X - DT1*V, in FP64 with the SDERI3 determinant.
+__global__ void hexa_prev_volume_kernel(const HexaArrays<float> A, const NodeView N,
+                                        const Time *__restrict__ T) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= A.ne) return;
+  const double dt1 = T->dt2;
+  double x[8], y[8], z[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int n = __ldg(A.nc + k * A.ne + e);
+    const dbl4 xk = ld4(N.X4 + n), vk = ld4(N.V4 + n);
+    x[k] = xk.x - dt1 * vk.x;
+    y[k] = xk.y - dt1 * vk.y;
+    z[k] = xk.z - dt1 * vk.z;
+  }
+  const double x17 = x[6] - x[0], x28 = x[7] - x[1], x35 = x[4] - x[2], x46 = x[5] - x[3];
+  const double y17 = y[6] - y[0], y28 = y[7] - y[1], y35 = y[4] - y[2], y46 = y[5] - y[3];
+  const double z17 = z[6] - z[0], z28 = z[7] - z[1], z35 = z[4] - z[2], z46 = z[5] - z[3];
+  const double jac1 = x17 + x28 - x35 - x46, jac2 = y17 + y28 - y35 - y46,
+               jac3 = z17 + z28 - z35 - z46;
+  const double jac4 = (x17 + x46) + (x28 + x35), jac5 = (y17 + y46) + (y28 + y35),
+               jac6 = (z17 + z46) + (z28 + z35);
+  const double jac7 = (x17 + x46) - (x28 + x35), jac8 = (y17 + y46) - (y28 + y35),
+               jac9 = (z17 + z46) - (z28 + z35);
+  const double det = RG_ONE_OVER_64 * (jac1 * (jac5 * jac9 - jac6 * jac8) +
+                                       jac2 * (jac6 * jac7 - jac4 * jac9) +
+                                       jac3 * (jac4 * jac8 - jac5 * jac7));
+  if (A.off[e] != 0.f) A.rho[e] = det;
+}
+
+void launch_hexa_prev_volume(const HexaArrays<float> &A, const NodeView &N, const Time *T,
+                             cudaStream_t s) {
+  if (A.ne > 0) hexa_prev_volume_kernel<<<(A.ne + 255) / 256, 256, 0, s>>>(A, N, T);
+}
 
 void launch_hexa_f64(const HexaParams &P, const HexaArrays<double> &A,
                      const NodeView &N, dbl4 *fsky, DtPartials dp,

@@ -11,6 +11,8 @@ void launch_hexa_f64(const HexaParams &P, const HexaArrays<double> &A,
 void launch_hexa_f32(const HexaParams &P, const HexaArrays<float> &A,
                      const NodeView &N, float4 *fsky, DtPartials dp,
                      const Time *T, int *status, cudaStream_t s);
+void launch_hexa_prev_volume(const HexaArrays<float> &A, const NodeView &N, const Time *T,
+                             cudaStream_t s);
 
 // Belytschko-Tsay shells (rg_shell.cu)
 struct ShellParams;

@@ -103,7 +103,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
   constexpr bool F64 = std::is_same<ER, double>::value;
   const int il = blockIdx.x * NT + threadIdx.x;
   const int nc = S.nc;
-  double dtmine = RG_EP06;
+  R dtmine = (R)RG_EP06;
   int elmin = -1;
   if (il < P.nel) {
     const int e = P.nft + il;
@@ -113,34 +113,49 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     int nn[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) nn[k] = __ldg(S.ix + k * nc + e);
-    double xa[4], ya[4], za[4];
     R vl[4][3], vrl[4][3];
     const R offg = S.offg[e];
     const R off = smin((R)RG_ONE, fabs(offg));
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const dbl4 x = ld4(N.X4 + nn[k]);
-      const dbl4 v = ld4(N.V4 + nn[k]);
-      const dbl4 w = ld4(N.VR4 + nn[k]);
-      xa[k] = x.x;
-      ya[k] = x.y;
-      za[k] = x.z;
-      const bool z0 = offg < (R)0;
-      vl[k][0] = z0 ? (R)0 : (R)v.x;
-      vl[k][1] = z0 ? (R)0 : (R)v.y;
-      vl[k][2] = z0 ? (R)0 : (R)v.z;
-      vrl[k][0] = z0 ? (R)0 : (R)w.x;
-      vrl[k][1] = z0 ? (R)0 : (R)w.y;
-      vrl[k][2] = z0 ? (R)0 : (R)w.z;
-    }
-    // coordinates: absolute (FP64) or relative to node 1 (mixed); every
-    // quantity below uses coordinate differences only.
+    const bool z0 = offg < (R)0;
+    // coordinates: absolute (FP64) or node-1-relative from the FP32 hi/lo
+    // copies (mixed); every quantity below uses coordinate differences only.
     R xg[4], yg[4], zg[4];
+    if constexpr (F64) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      xg[k] = F64 ? (R)xa[k] : (R)(xa[k] - xa[0]);
-      yg[k] = F64 ? (R)ya[k] : (R)(ya[k] - ya[0]);
-      zg[k] = F64 ? (R)za[k] : (R)(za[k] - za[0]);
+      for (int k = 0; k < 4; k++) {
+        const dbl4 x = ld4(N.X4 + nn[k]);
+        const dbl4 v = ld4(N.V4 + nn[k]);
+        const dbl4 w = ld4(N.VR4 + nn[k]);
+        xg[k] = x.x;
+        yg[k] = x.y;
+        zg[k] = x.z;
+        vl[k][0] = z0 ? (R)0 : v.x;
+        vl[k][1] = z0 ? (R)0 : v.y;
+        vl[k][2] = z0 ? (R)0 : v.z;
+        vrl[k][0] = z0 ? (R)0 : w.x;
+        vrl[k][1] = z0 ? (R)0 : w.y;
+        vrl[k][2] = z0 ? (R)0 : w.z;
+      }
+    } else {
+      F8 c[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        c[k] = ldF8(N.XF + nn[k]);
+        const float4 v = ldf4(N.VF + nn[k]);
+        const float4 w = ldf4(N.VRF + nn[k]);
+        vl[k][0] = z0 ? 0.f : v.x;
+        vl[k][1] = z0 ? 0.f : v.y;
+        vl[k][2] = z0 ? 0.f : v.z;
+        vrl[k][0] = z0 ? 0.f : w.x;
+        vrl[k][1] = z0 ? 0.f : w.y;
+        vrl[k][2] = z0 ? 0.f : w.z;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        xg[k] = (c[k].hx - c[0].hx) + (c[k].lx - c[0].lx);
+        yg[k] = (c[k].hy - c[0].hy) + (c[k].ly - c[0].ly);
+        zg[k] = (c[k].hz - c[0].hz) + (c[k].lz - c[0].lz);
+      }
     }
     R thk0 = S.thke[e];
     // ---- CNVEC3 ----
@@ -512,7 +527,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     {
       const R dt = (R)P.dtfac * aldt / ssp;
       if (offg > (R)0 && off != (R)0) {
-        dtmine = (double)dt;
+        dtmine = dt;
         elmin = key0 + (nc_total - 1 - e);  // first element wins ties (strict <)
       }
       const R divm = smax(aldt * aldt, (R)RG_EM20);
@@ -587,7 +602,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
       fskyr[K] = b;
     }
   }
-  block_dt_min<NT>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
+  block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
 }
 
 // Fixed-order shell energy partials: [0] internal (membrane + bending),

@@ -289,13 +289,15 @@ def shell_mass_inertia(X, ixc, thk, rho, ms=None, inr=None):
 
 def crash_box(n_side=77, n_len=390, side=0.060, length=0.300, thk=1.2e-3,
               v0=15.0, seed=0, rho=7850.0, young=210e9, nu=0.3,
-              a=350e6, b=275e6, n=0.36, c=0.022, gap=1e-4, npt=5):
+              a=350e6, b=275e6, n=0.36, c=0.022, gap=1e-4, npt=5, vpert=0.0):
     """Square crash box of Belytschko-Tsay shells: a tube of square section
     (side x side) and the given length along z, n_side elements per face
     across and n_len along (4*n_side*n_len shells), thickness thk, NPT
     through-thickness points, Johnson-Cook LAW2.  Nodes get a seeded
     imperfection U[-0.1 t, 0.1 t] along their face normal; the box moves at
-    v0 towards a fixed planar rigid wall just below its lower end."""
+    v0 towards a fixed planar rigid wall just below its lower end.  vpert > 0
+    adds a seeded N(0, vpert) velocity to every node (deformation from the
+    first cycle on)."""
     per = 4 * n_side
     s = np.linspace(0.0, 4.0 * side, per + 1)[:-1]
     face = (s // side).astype(int)
@@ -333,6 +335,8 @@ def crash_box(n_side=77, n_len=390, side=0.060, length=0.300, thk=1.2e-3,
     ms, inr = shell_mass_inertia(X, ixc, t, rho)
     V = np.zeros_like(X)
     V[2] = -v0
+    if vpert > 0.0:
+        V += rng.normal(0.0, vpert, size=V.shape)
     icodt = np.zeros(numnod, np.int32)
     m = Model("crash_box_%d" % nel, X, V, ms, icodt,
               shells=[ShellGroupSpec(ixc, mat, shell_prop(thk), t, npt)], IN=inr)

@@ -42,3 +42,26 @@ def test_mixed_vs_fp64(wl):
     assert err_p < TOL
     assert err_e < TOL
     assert e32.status() == 0 and e64.status() == 0
+
+
+def test_mixed_forint_step_tracks_cycle():
+    """FORINT-level call in the mixed form: fed, call after call, the X, V
+    and DT1 of a device-resident mixed run, it returns that run's assembled
+    forces within the mixed tolerance (the element volume is re-anchored to
+    the host coordinates on every call)."""
+    from openradioss_gb300.engine import Engine
+    m = M.large_block(n=10, seed=3)
+    e1 = Engine(m, precision=1)
+    e2 = Engine(m, precision=1)
+    e1.cycle(20)
+    e2.cycle(20)
+    for _ in range(3):
+        nd = e1.nodes()
+        t = e1.time()
+        e1.cycle(1)
+        f_ref = e1.forces()["F"]
+        x = np.ascontiguousarray(nd["X"].T)
+        v = np.ascontiguousarray(nd["V"].T)
+        f, st, dt2t, el = e2.forint_step(x, v, t["dt2"])
+        err = np.max(np.abs(f.T - f_ref)) / np.max(np.abs(f_ref))
+        assert err < TOL, err

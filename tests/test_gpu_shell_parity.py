@@ -33,7 +33,9 @@ def test_shell_skyline_matches_oracle(Engine, oracle_lib):
 
 @pytest.mark.parametrize("iplas", [1, 0])
 def test_crash_box_first_cycles(Engine, oracle_lib, iplas):
-    m = M.crash_box(n_side=5, n_len=12, v0=40.0)
+    # seeded velocity perturbation: the shells deform from the first cycle
+    # (a rigid translation would leave only round-off forces to compare)
+    m = M.crash_box(n_side=5, n_len=12, v0=40.0, vpert=2.0)
     m.shells[0].geo[38] = iplas
     e = Engine(m)
     o = oracle_lib.OracleModel(m, nthreads=2)
