@@ -920,6 +920,7 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   for (auto &g : c->hg) {
     g.P.part_off = c->nparts;
     g.P.dtfac = dtfac_solid;
+    hexa_params_mirror(g.P);
     c->nparts += hexa_blocks(g.nel);
   }
   {

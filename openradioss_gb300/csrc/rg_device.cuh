@@ -135,7 +135,47 @@ struct HexaParams {
   // LAW2 Johnson-Cook (mat_param%uparam / iparam)
   double ca, cb, cn, epmx, sigm0, cc, epdr, asrate, z3;
   int icc, vp, israte, pad;
+  // FP32 copies of the coefficients above (the same round-to-nearest
+  // conversion, done once on the host) for the mixed form, and the two
+  // branch flags CC /= 0, N == 1 evaluated on the FP64 values
+  struct {
+    float rho0, g, c1, qh, qa, qb, vns1, vns2, dtfac, ssp1;
+    float ca, cb, cn, epmx, sigm0, cc, epdr, asrate;
+    int cc_nz, cn_one;
+  } f;
 };
+
+inline void hexa_params_mirror(HexaParams &P) {
+  P.f.rho0 = (float)P.rho0;
+  P.f.g = (float)P.g;
+  P.f.c1 = (float)P.c1;
+  P.f.qh = (float)P.qh;
+  P.f.qa = (float)P.qa;
+  P.f.qb = (float)P.qb;
+  P.f.vns1 = (float)P.vns1;
+  P.f.vns2 = (float)P.vns2;
+  P.f.dtfac = (float)P.dtfac;
+  P.f.ssp1 = (float)P.ssp1;
+  P.f.ca = (float)P.ca;
+  P.f.cb = (float)P.cb;
+  P.f.cn = (float)P.cn;
+  P.f.epmx = (float)P.epmx;
+  P.f.sigm0 = (float)P.sigm0;
+  P.f.cc = (float)P.cc;
+  P.f.epdr = (float)P.epdr;
+  P.f.asrate = (float)P.asrate;
+  P.f.cc_nz = P.cc != 0.0;
+  P.f.cn_one = P.cn == 1.0;
+}
+
+// coefficient in the element type: the FP64 value or its FP32 copy
+template <typename R>
+__device__ __forceinline__ R pcoef(double d, float f) {
+  if constexpr (sizeof(R) == 8)
+    return d;
+  else
+    return f;
+}
 
 template <typename ER>
 struct HexaArrays {

@@ -32,6 +32,8 @@
 
 namespace rg {
 
+#define PC(name) pcoef<R>(P.name, P.f.name)
+
 // Fortran MAX/MIN with the argument order of the source: MAX(a,b) returns
 // a if a>b, else b (NaN propagation is not relied on).
 template <typename T>
@@ -43,8 +45,8 @@ __device__ __forceinline__ T fmin_(T a, T b) {
   return a < b ? a : b;
 }
 
-template <typename ER, int LAW, int NT>
-__global__ void __launch_bounds__(NT)
+template <typename ER, int LAW, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
             typename SlotT<ER>::type *__restrict__ fsky, DtPartials dp,
             const Time *__restrict__ T, int *__restrict__ status) {
@@ -109,6 +111,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     R px[4], py[4], pz[4], ph[4][3];
     double voln;  // element volume (VOLDP)
     double vold_mixed = 0.0;
+    R dv_mixed = (R)0;  // mixed form: FP32 volume change of the cycle
     {
       const R x17 = x[6] - x[0], x28 = x[7] - x[1], x35 = x[4] - x[2], x46 = x[5] - x[3];
       const R y17 = y[6] - y[0], y28 = y[7] - y[1], y35 = y[4] - y[2], y46 = y[5] - y[3];
@@ -174,6 +177,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
           const R t3 = da1 * q1 + da2 * q2 + da3 * q3;
           const R dv = (R)RG_ONE_OVER_64 * ((t1 - t2) + t3);
           voln = vold_mixed + (double)dv;
+          dv_mixed = dv;
         } else {
           voln = vold_mixed;
         }
@@ -277,7 +281,9 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     // cycle instead of the density (RHO = RHO0*VOL0/VOL), DVOL is the
     // FP32 volume change computed above.
     const double vol0 = A.vol0[e];
-    if (offg == (R)0 && voln == RG_ONE) voln = vol0;
+    if constexpr (F64) {
+      if (offg == (R)0 && voln == RG_ONE) voln = vol0;
+    }
     R rho_r, amu, dvol_r;
     double dvol_d = 0.0;
     if constexpr (F64) {
@@ -290,8 +296,8 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
       dvol_r = (R)dvol_d;
     } else {
       A.rho[e] = voln;
-      dvol_r = (R)(voln - vold_mixed);
-      rho_r = (R)P.rho0 * ((R)vol0 / volr);
+      dvol_r = dv_mixed;
+      rho_r = PC(rho0) * ((R)vol0 / volr);
       amu = (R)(vol0 - voln) / volr;  // RHO/RHO0 - 1 = VOL0/VOLN - 1
     }
 
@@ -315,10 +321,10 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     const R vol_avg_r = volr - (R)RG_HALF * dvol_r;
 
     // ---- material law ----------------------------------------------------------
-    const R gg = (R)P.g * off;
+    const R gg = PC(g) * off;
     // sound speed: per-group constant for live elements (OFF = 1)
-    const R ssp = off == (R)RG_ONE ? (R)P.ssp1
-                                   : sqrt(((R)RG_ONEP333 * gg + (R)P.c1) / (R)P.rho0);
+    const R ssp = off == (R)RG_ONE ? PC(ssp1)
+                                   : sqrt(((R)RG_ONEP333 * gg + PC(c1)) / PC(rho0));
     {
       const R g1 = dt1 * gg, g2 = (R)RG_TWO * g1;
       const R p = -(R)RG_THIRD * (sg[0] + sg[1] + sg[2]);
@@ -350,41 +356,45 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
           const R epsp = (R)RG_HALF * (e1 * e1 + e2 * e2 + e3 * e3) + e4 * e4 + e5 * e5 + e6 * e6;
           epsdot = sqrt((R)RG_THREE * epsp) / (R)RG_THREE_HALF;
         }
-        const R asrate = (R)fmin_(RG_ONE, P.asrate * DT1);
+        R asrate;
+        if constexpr (F64)
+          asrate = fmin_(RG_ONE, P.asrate * DT1);
+        else
+          asrate = fmin_(1.f, P.f.asrate * dt1);
         if (P.israte == 0)
           epsd = epsdot;
         else
           epsd = asrate * epsdot + ((R)RG_ONE - asrate) * epsd;
         A.epsd[e] = epsd;
       }
-      R epd = (R)RG_ONE, sigmx = (R)P.sigm0;
-      if (P.cc != RG_ZERO) {
+      R epd = (R)RG_ONE, sigmx = PC(sigm0);
+      if (P.f.cc_nz) {
         if (P.vp == 1) {
-          epd = fmax_(epsd, (R)P.epdr);
-          epd = log(epd / (R)P.epdr);
+          epd = fmax_(epsd, PC(epdr));
+          epd = log(epd / PC(epdr));
         } else {
           epd = fmax_(epsd, (R)RG_EM15);
-          epd = log(epd / (R)P.epdr);
+          epd = log(epd / PC(epdr));
         }
         epd = fmax_((R)RG_ZERO, epd);
-        epd = ((R)RG_ONE + (R)P.cc * epd);  // (1 - T*^m) = 1 without heating
-        if (P.icc == 1) sigmx = (R)P.sigm0 * epd;
+        epd = ((R)RG_ONE + PC(cc) * epd);  // (1 - T*^m) = 1 without heating
+        if (P.icc == 1) sigmx = PC(sigm0) * epd;
       } else {
         epd = (R)RG_ONE;
-        if (P.icc == 1) sigmx = (R)P.sigm0 * epd;
+        if (P.icc == 1) sigmx = PC(sigm0) * epd;
       }
       const R epxe = A.pla[e];
       R ak, qh;
-      if (P.cn == RG_ONE) {
-        ak = (R)P.ca + (R)P.cb * epxe;
-        qh = (R)P.cb * epd;
+      if (P.f.cn_one) {
+        ak = PC(ca) + PC(cb) * epxe;
+        qh = PC(cb) * epd;
       } else if (epxe > (R)0) {
         // EPXE**(N-1) = EPXE**N / EPXE: one power evaluation
-        const R pn = pow(epxe, (R)P.cn);
-        ak = (R)P.ca + (R)P.cb * pn;
-        qh = ((R)P.cb * (R)P.cn * (pn / epxe)) * epd;
+        const R pn = pow(epxe, PC(cn));
+        ak = PC(ca) + PC(cb) * pn;
+        qh = (PC(cb) * PC(cn) * (pn / epxe)) * epd;
       } else {
-        ak = (R)P.ca;
+        ak = PC(ca);
         qh = (R)0;
       }
       ak = ak * epd;
@@ -392,7 +402,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
         ak = sigmx;
         qh = (R)0;
       }
-      if (epxe > (R)P.epmx) {
+      if (epxe > PC(epmx)) {
         ak = (R)0;
         qh = (R)0;
       }
@@ -412,17 +422,17 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
       const R dd = -dxx - dyy - dzz;
       R al = (R)0, ad = (R)0;
       if (off == (R)RG_ONE) {
-        al = voln > RG_ZERO ? cbv : (R)0;
+        al = (F64 ? voln > RG_ZERO : volr > (R)0) ? cbv : (R)0;
         ad = fmax_((R)0, dd);
       }
       const R rhoe = rho_r;
-      const R qa = (R)P.qa, qb = (R)P.qb;
+      const R qa = PC(qa), qb = PC(qb);
       const R qaa = qa * qa * ad;
       R qx = qb * ssp + al * qaa;
       if (P.has_cns) {
-        const R nrho = sqrt(rhoe * (R)P.rho0);
-        const R cns1 = (R)P.vns1 * al * nrho * ssp * off;
-        const R cns2 = (R)P.vns2 * al * nrho * ssp * off;
+        const R nrho = sqrt(rhoe * PC(rho0));
+        const R cns1 = PC(vns1) * al * nrho * ssp * off;
+        const R cns2 = PC(vns2) * al * nrho * ssp * off;
         qx = qx + (cns1 + cns2) / fmax_((R)RG_EM20, rhoe * deltax);
       }
       qnew = rhoe * ad * al * (qaa * al + qb * ssp);
@@ -433,8 +443,8 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
         const R tidt = (R)RG_ONE / dtx;
         sti = (rhoe * tidt) * (volr * tidt);
       }
-      const R dtxd = (R)P.dtfac * dtx;
-      if (voln > RG_ZERO && (off != (R)0 && offg >= (R)0)) {
+      const R dtxd = PC(dtfac) * dtx;
+      if ((F64 ? voln > RG_ZERO : volr > (R)0) && (off != (R)0 && offg >= (R)0)) {
         dtmine = dtxd;
         elmin = e;  // element order key; mapped to the user id by the dt kernel
       }
@@ -442,7 +452,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
 
     // ---- law epilogue: pressure, energy, QOLD ----------------------------------
     {
-      const R pnew = (R)P.c1 * amu;
+      const R pnew = PC(c1) * amu;
       sg[0] = (sg[0] - pnew) * off;
       sg[1] = (sg[1] - pnew) * off;
       sg[2] = (sg[2] - pnew) * off;
@@ -499,7 +509,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
     // ---- SHVIS3 (JHBE >= 1) ----------------------------------------------------
     R f[3][8];
     {
-      const R caq = (R)RG_FOURTH * off * (R)P.qh;
+      const R caq = (R)RG_FOURTH * off * PC(qh);
       R fcl = caq * rho_r * (cbv * cbv);  // VOL**(2/3) = (VOL**(1/3))**2
       const R fcq = fcl * caq * (R)RG_HUNDRED;
       fcl = fcl * ssp;
@@ -614,8 +624,11 @@ static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
                        DtPartials dp, const Time *T, int *status,
                        cudaStream_t s) {
   constexpr int NT = 128;
+  // mixed form: 5 resident blocks per SM fit in 96 registers without
+  // spilling; the FP64 form needs its ~200 registers
+  constexpr int MINB = std::is_same<ER, float>::value ? 5 : 1;
   const int nb = (P.nel + NT - 1) / NT;
-  hexa_kernel<ER, LAW, NT><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status);
+  hexa_kernel<ER, LAW, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status);
 }
 
 int hexa_blocks(int nel) { return (nel + 127) / 128; }

@@ -39,7 +39,41 @@ struct ShellParams {
   double ca, cb, cn, ymax, cc, eps0, pm9;
   int icc, vp, israte, pad2;
   double dtfac;
+  // FP32 copies for the mixed form (converted once on the host) and the
+  // branch flags CC /= 0, DM /= 0 evaluated on the FP64 values
+  struct {
+    float rho, young, nu, g, a11, ssp, h1, h2, h3, dm, ish, fsh;
+    float ca, cb, cn, ymax, cc, eps0, pm9, dtfac;
+    int cc_nz, dm_nz;
+  } f;
 };
+
+static void shell_params_mirror(ShellParams &P) {
+  P.f.rho = (float)P.rho;
+  P.f.young = (float)P.young;
+  P.f.nu = (float)P.nu;
+  P.f.g = (float)P.g;
+  P.f.a11 = (float)P.a11;
+  P.f.ssp = (float)P.ssp;
+  P.f.h1 = (float)P.h1;
+  P.f.h2 = (float)P.h2;
+  P.f.h3 = (float)P.h3;
+  P.f.dm = (float)P.dm;
+  P.f.ish = (float)P.ish;
+  P.f.fsh = (float)P.fsh;
+  P.f.ca = (float)P.ca;
+  P.f.cb = (float)P.cb;
+  P.f.cn = (float)P.cn;
+  P.f.ymax = (float)P.ymax;
+  P.f.cc = (float)P.cc;
+  P.f.eps0 = (float)P.eps0;
+  P.f.pm9 = (float)P.pm9;
+  P.f.dtfac = (float)P.dtfac;
+  P.f.cc_nz = P.cc != 0.0;
+  P.f.dm_nz = P.dm != 0.0;
+}
+
+#define PC(name) pcoef<R>(P.name, P.f.name)
 
 template <typename ER>
 struct ShellArrays {
@@ -218,14 +252,14 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     thk0 = (R)thk_cur;
     const R vol0 = thk0 * area;
     const R thk02 = thk0 * thk0;
-    const R nu = (R)P.nu, ym = (R)P.young, gmod = (R)P.g, a11 = (R)P.a11, ssp = (R)P.ssp,
-            rho = (R)P.rho;
+    const R nu = PC(nu), ym = PC(young), gmod = PC(g), a11 = PC(a11), ssp = PC(ssp),
+            rho = PC(rho);
     R shf;
     if (NPT == 1) {
       shf = (R)0;
     } else {
       const R fac1tmp = (R)2.0 * ((R)1.0 + nu) * thk02;
-      const R ish = (R)P.ish, fsh = (R)P.fsh;
+      const R ish = PC(ish), fsh = PC(fsh);
       shf = fsh * ((R)1.0 - ish + ish * fac1tmp / (fsh * area + fac1tmp));
     }
     const R gs = gmod * shf;
@@ -243,7 +277,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
       if (al3 != (R)0) almin = smin(almin, alquad);
       const R dtdyn = area * area / smax(smax(al5, al6), (R)RG_EM20);
       aldt = smax(dtdyn, almin);
-      const R dthour = (R)RG_HALF * (almin + aldt) / smax((R)P.h1, (R)P.h2);
+      const R dthour = (R)RG_HALF * (almin + aldt) / smax(PC(h1), PC(h2));
       if (dthour < aldt) aldt = dthour;
       aldt = sqrt(aldt);
     }
@@ -328,10 +362,16 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
               S.forc[3 * nc + e] * eyz + S.forc[4 * nc + e] * exz;
     R degfx = S.mom[0 * nc + e] * kxx + S.mom[1 * nc + e] * kyy + S.mom[2 * nc + e] * kxy;
     double thkn = thk_cur;
-    const R asrate = P.israte > 0 ? smin((R)RG_ONE, (R)(P.pm9 * DT1)) : (R)RG_ONE;
+    R asrate = (R)RG_ONE;
+    if (P.israte > 0) {
+      if constexpr (F64)
+        asrate = smin((R)RG_ONE, (R)(P.pm9 * DT1));
+      else
+        asrate = smin(1.f, P.f.pm9 * dt1);
+    }
     const R a1 = ym / ((R)RG_ONE - nu * nu);
     const R a2 = a1 * nu;
-    const R epdr = smax((R)P.eps0 * dt1, (R)RG_EM20);
+    const R epdr = smax(PC(eps0) * dt1, (R)RG_EM20);
 #pragma unroll
     for (int it = 0; it < NPT; it++) {
       const R thkly = (R)c_wf[NPT - 1][it];
@@ -355,26 +395,26 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
         epsdot = ep * dt1;
       }
       R ezz = (R)0;
-      R ca = (R)P.ca, cb = (R)P.cb, ymax = (R)P.ymax;
+      R ca = PC(ca), cb = PC(cb), ymax = PC(ymax);
       sn[0] = sn[0] + a1 * depsxx + a2 * depsyy;
       sn[1] = sn[1] + a2 * depsxx + a1 * depsyy;
       sn[2] = sn[2] + gmod * depsxy;
       sn[3] = sn[3] + gs * eyz;
       sn[4] = sn[4] + gs * exz;
-      if (P.cc != 0.0) {
+      if (P.f.cc_nz) {
         R epsp = epsdot;
         if (P.israte == 0 && P.vp == 2)
           epsp = smax(smax(fabs(depsxx), fabs(depsyy)), (R)RG_HALF * fabs(depsxy));
         epsp = smax(epsp, epdr);
         const R logep = log(epsp / epdr);
-        R q = ((R)RG_ONE + (R)P.cc * logep);
+        R q = ((R)RG_ONE + PC(cc) * logep);
         q = smax(q, (R)RG_EM20);
         ca = ca * q;
         cb = cb * q;
         if (P.icc == 1) ymax = ymax * q;
       }
       R pla = S.pla[it * nc + e];
-      R yld = pla == (R)0 ? ca : ca + cb * exp((R)P.cn * log(pla));
+      R yld = pla == (R)0 ? ca : ca + cb * exp(PC(cn) * log(pla));
       yld = smin(yld, ymax);
       if (P.ipla == 0) {
         const R svm = sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2]);
@@ -398,7 +438,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
         if (svm > yld && off == (R)RG_ONE) {
           const R nu1 = (R)RG_ONE / ((R)RG_ONE - nu);
           const R nu2 = (R)RG_ONE / ((R)RG_ONE + nu);
-          const R h = yld >= ymax ? (R)0 : (R)P.cn * cb * exp(((R)P.cn - (R)RG_ONE) * log(pla + (R)RG_EM07));
+          const R h = yld >= ymax ? (R)0 : PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
           R dpla_j = (svm - yld) / ((R)RG_THREE * gmod + h);
           const R anu1 = A * nu1;
           const R bnu2 = (R)RG_THREE * B * nu2;
@@ -408,7 +448,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
           for (int n = 0; n < 3; n++) {
             dpla_i = dpla_j;
             const R pla_i = pla + dpla_i;
-            const R yld_i = pla_i == (R)0 ? smin(ymax, ca) : smin(ymax, ca + cb * exp((R)P.cn * log(pla_i)));
+            const R yld_i = pla_i == (R)0 ? smin(ymax, ca) : smin(ymax, ca + cb * exp(PC(cn) * log(pla_i)));
             dr = (R)RG_HALF * ym * dpla_i / yld_i;
             Pp = (R)RG_ONE / ((R)RG_ONE + dr * nu1);
             Qq = (R)RG_ONE / ((R)RG_ONE + (R)RG_THREE * dr * nu2);
@@ -440,9 +480,9 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
       momn[2] = momn[2] + wmc * sn[2];
     }
     S.thk[e] = thkn > RG_EM30 ? thkn : RG_EM30;
-    if (P.dm != 0.0) {
+    if (P.f.dm_nz) {
       const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
-      const R visc = ((R)RG_ONEP414 * (R)P.dm) * ssp * sqrt(area) * dtinv * rho;
+      const R visc = ((R)RG_ONEP414 * PC(dm)) * ssp * sqrt(area) * dtinv * rho;
       forn[0] = forn[0] + visc * (exx + (R)RG_HALF * eyy);
       forn[1] = forn[1] + visc * (eyy + (R)RG_HALF * exx);
       forn[2] = forn[2] + visc * exy * (R)RG_THIRD;
@@ -473,12 +513,12 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
       // HVLIN = 0: the linear viscous terms vanish; HVISC = HELAS = 1/2
       const R shfpr3 = shf / ((R)RG_THREE * ((R)RG_ONE + nu));
       const R r1 = (R)RG_FOURTH * rho * (R)RG_HUNDRED;
-      const R A1 = r1 * ((R)RG_HALF * (R)P.h1);
-      const R A3 = r1 * ((R)RG_HALF * (R)P.h2) * sqrt(shfpr3);
-      const R A5 = ((R)RG_HALF * (R)P.h3) * r1 * (R)RG_ZEP072169;
+      const R A1 = r1 * ((R)RG_HALF * PC(h1));
+      const R A3 = r1 * ((R)RG_HALF * PC(h2)) * sqrt(shfpr3);
+      const R A5 = ((R)RG_HALF * PC(h3)) * r1 * (R)RG_ZEP072169;
       const R r0e = (R)RG_FOURTH * ym * (R)RG_HALF;
-      const R A7 = (R)P.h1 * r0e;
-      const R A8 = (R)P.h2 * r0e * shfpr3;
+      const R A7 = PC(h1) * r0e;
+      const R A8 = PC(h2) * r0e * shfpr3;
       const R t2a = thk02 * area;
       const R tsa = sqrt(t2a);
       R h1q = A1 * tsa;
@@ -525,7 +565,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     // ---- CDT3 ----
     R sti;
     {
-      const R dt = (R)P.dtfac * aldt / ssp;
+      const R dt = PC(dtfac) * aldt / ssp;
       if (offg > (R)0 && off != (R)0) {
         dtmine = dt;
         elmin = key0 + (nc_total - 1 - e);  // first element wins ties (strict <)
@@ -832,6 +872,7 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
   for (auto *g : S.groups) {
     g->P.part_off = part_off;
     g->P.dtfac = dtfac;
+    shell_params_mirror(g->P);
     part_off += shell_blocks(g->P.nel);
   }
   return RG_OK;
