@@ -48,6 +48,7 @@ extern "C" {
 #define RG_ST_NAN 2        /* non-finite nodal acceleration */
 #define RG_ST_SLOT 4       /* skyline slot index out of range */
 #define RG_ST_DTMIN 8      /* time step below the configured minimum */
+#define RG_ST_BARRIER 16   /* batched kernel: grid barrier wait gave up */
 
 /* precision modes (rg_set_precision) */
 #define RG_PREC_FP64 0     /* plain form: everything in FP64 */
@@ -167,6 +168,45 @@ int rg_kernel_times(rg_ctx *ctx, double *ms4);
 /* Advance ncycle cycles (graph launches) bracketed by CUDA events recorded
  * on the context's stream; *ms = device time of the whole span. */
 int rg_time_cycles(rg_ctx *ctx, int ncycle, double *ms);
+
+/* ---- Batched jobs -------------------------------------------------------
+ * A batch advances many finalized contexts (independent models, "jobs") of
+ * the same arithmetic form together: one persistent cooperative kernel per
+ * cycle (element tiles of every job -> grid barrier -> per-job time step ->
+ * grid barrier -> node tiles of every job), captured in a CUDA graph.  Each
+ * job keeps its own state, time step and cycle target; a job's results are
+ * bitwise those of rg_cycle on it alone.  While a context is in a batch,
+ * only the batch advances it; read its results with the rg_download_* calls
+ * after rg_batch_synchronize.  No counterpart in the reference (its engine
+ * runs one model per process); the per-job cycle is the RESOL loop body. */
+typedef struct rg_batch rg_batch;
+int rg_batch_create(int device, rg_batch **out);
+int rg_batch_destroy(rg_batch *b);
+const char *rg_batch_last_error(rg_batch *b);
+/* Add a job; it advances until its Time::ncycle reaches target_ncycle
+ * (< 0: no target).  Returns the slot (>= 0) or an error. */
+int rg_batch_add(rg_batch *b, rg_ctx *job, int target_ncycle);
+int rg_batch_remove(rg_batch *b, int slot);
+int rg_batch_set_target(rg_batch *b, int slot, int target_ncycle);
+/* Launch configuration: elements per tile = 128*ktile, nodes per tile =
+ * 128*knode, resident blocks per SM (0 = occupancy maximum), schedule 0 =
+ * one persistent cooperative launch per cycle, 1 = three launches. */
+int rg_batch_set_config(rg_batch *b, int ktile, int knode, int blocks_per_sm,
+                        int schedule);
+/* cfg5 = {ktile, knode, blocks_per_sm, schedule, max blocks per SM}. */
+int rg_batch_get_config(rg_batch *b, int *cfg5);
+int rg_batch_cycle(rg_batch *b, int ncycle);
+int rg_batch_synchronize(rg_batch *b);
+int rg_batch_time_cycles(rg_batch *b, int ncycle, double *ms);
+/* ncycle[slot] = the job's cycle count after the last batched cycle (-1 for
+ * a free slot); bstatus = batch status (RG_ST_BARRIER), cleared. */
+int rg_batch_progress(rg_batch *b, int *ncycle, int nslots, int *bstatus);
+/* Autotuner: times each candidate configuration ({ktile, knode,
+ * blocks_per_sm, schedule} rows; NULL = built-in list) for trial_cycles on
+ * the batch's jobs with their state saved and restored, keeps the fastest.
+ * best5 = {ktile, knode, blocks_per_sm, schedule, microseconds per cycle}. */
+int rg_batch_autotune(rg_batch *b, int trial_cycles, const int *cand,
+                      int ncand, int *best5);
 
 #ifdef __cplusplus
 }

@@ -45,6 +45,19 @@ SIGNATURES = [
     ("rg_set_timing", _ip, [_vp, _ip]),
     ("rg_kernel_times", _ip, [_vp, _vp]),
     ("rg_time_cycles", _ip, [_vp, _ip, _vp]),
+    ("rg_batch_create", _ip, [_ip, C.POINTER(C.c_void_p)]),
+    ("rg_batch_destroy", _ip, [_vp]),
+    ("rg_batch_last_error", C.c_char_p, [_vp]),
+    ("rg_batch_add", _ip, [_vp, _vp, _ip]),
+    ("rg_batch_remove", _ip, [_vp, _ip]),
+    ("rg_batch_set_target", _ip, [_vp, _ip, _ip]),
+    ("rg_batch_set_config", _ip, [_vp, _ip, _ip, _ip, _ip]),
+    ("rg_batch_get_config", _ip, [_vp, _vp]),
+    ("rg_batch_cycle", _ip, [_vp, _ip]),
+    ("rg_batch_synchronize", _ip, [_vp]),
+    ("rg_batch_time_cycles", _ip, [_vp, _ip, _vp]),
+    ("rg_batch_progress", _ip, [_vp, _vp, _ip, _vp]),
+    ("rg_batch_autotune", _ip, [_vp, _ip, _vp, _ip, _vp]),
 ]
 
 

@@ -5,7 +5,9 @@
 #include "../../include/rg_api.h"
 #include "rg_device.cuh"
 #include "rg_kernels.h"
+#include "rg_node.cuh"
 #include "rg_shell.h"
+#include "rg_ctx.h"
 
 #include <algorithm>
 #include <cmath>
@@ -25,66 +27,7 @@ constexpr int DT_NT = 1024;
 constexpr int EN_BLOCKS = 304;  // 2 x 152 SMs, fixed: reductions are order-fixed
 constexpr int EN_NT = 256;
 
-struct HexaGroupHost {
-  HexaParams P;
-  int nel;
-};
-
-struct WallHost {
-  double p0[3], n[3], dsearch;
-};
-
 }  // namespace
-
-struct rg_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  int prec = RG_PREC_FP64;
-  bool finalized = false;
-  bool timing = false;
-  double ktime[4] = {0, 0, 0, 0};
-
-  // ---- host-side model (until finalize) ----
-  int numnod = 0;
-  std::vector<double> X, V, MS, IN;
-  std::vector<int> icodt;
-  int numels = 0;
-  std::vector<int> ixs;  // 11 * numels
-  std::vector<HexaGroupHost> hg;
-  ShellModelHost shells;  // rg_shell.h
-  std::vector<WallHost> walls;
-  std::vector<int> adsky, iads, iadc;  // 1-based as given / built
-  bool skyline_given = false;
-  int lsky = 0;
-  double dtfac_solid = RG_ZEP9, dtfac_shell = RG_ZEP9, dtmx = RG_EP30,
-         dt2old = RG_EP30;
-
-  // ---- device ----
-  NodeView nv{};
-  int *d_adsky = nullptr;
-  void *d_fsky = nullptr;   // dbl4 or float4 [lsky]
-  void *d_fskyr = nullptr;  // rotational slots (shell models)
-  HexaArrays<double> h64{};
-  HexaArrays<float> h32{};
-  int *d_nc = nullptr, *d_iads = nullptr, *d_ngl_all = nullptr;
-  Time *d_time = nullptr;
-  int *d_status = nullptr;
-  DtPartials dp{};
-  int nparts = 0;
-  int *d_wall = nullptr;       // per node: wall index or -1
-  double *d_walls = nullptr;   // 6 doubles per wall (p0, n)
-  int nwalls = 0;
-  bool rot = false;
-  // staging for forint_step / downloads
-  double *d_stage = nullptr;   // 12 * numnod doubles
-  double *d_epart = nullptr;   // energy partials
-  std::vector<void *> allocs;
-  unsigned long long dev_bytes = 0;
-  cudaGraphExec_t gexec = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaEvent_t ev[8] = {};
-};
 
 namespace {
 
@@ -108,30 +51,12 @@ int dalloc(rg_ctx *c, T **p, size_t n) {
   if (e != cudaSuccess)
     return fail(c, RG_E_MEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   c->allocs.push_back((void *)*p);
+  c->alloc_bytes.push_back(bytes);
   c->dev_bytes += bytes;
   return RG_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Node kernel: ASSPAR4 (asspar4.F:165-180) fixed-order slot sums, ACCELE
-// (accele.F:66-78), BCS10/BCS1V (bcs10.F:31), planar rigid wall, VELOCITY
-// (velocity.F:59-75), DEPLA (displacement.F:68-100).  The update arithmetic
-// is written with explicit round-to-nearest multiply / add so that no
-// multiply-add is fused and each node's result does not depend on the
-// launch configuration.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ F8 split_hilo(double x, double y, double z) {
-  F8 c;
-  c.hx = __double2float_rn(x);
-  c.hy = __double2float_rn(y);
-  c.hz = __double2float_rn(z);
-  c.lx = __double2float_rn(x - (double)c.hx);
-  c.ly = __double2float_rn(y - (double)c.hy);
-  c.lz = __double2float_rn(z - (double)c.hz);
-  c.pad0 = c.pad1 = 0.f;
-  return c;
-}
-
+// Node kernel: one thread per node (node_update in rg_node.cuh).
 template <bool F64, bool ROT>
 __global__ void __launch_bounds__(NODE_NT)
 node_kernel(NodeView N, const int *__restrict__ adsky, const void *__restrict__ fsky_,
@@ -140,147 +65,7 @@ node_kernel(NodeView N, const int *__restrict__ adsky, const void *__restrict__ 
             int *__restrict__ status) {
   const int n = blockIdx.x * NODE_NT + threadIdx.x;
   if (n >= N.numnod) return;
-  const int k0 = __ldg(adsky + n), k1 = __ldg(adsky + n + 1);
-  double a0, a1, a2, r0 = 0.0, r1 = 0.0, r2 = 0.0;
-  if constexpr (F64) {
-    // ASSPAR4: A = 0 + sum of the node's slots in PARITH/ON order, FP64
-    const dbl4 *fsky = (const dbl4 *)fsky_;
-    const dbl4 *fskyr = (const dbl4 *)fskyr_;
-    a0 = a1 = a2 = 0.0;
-    for (int k = k0; k < k1; k++) {
-      const dbl4 f = fsky[k];
-      a0 = __dadd_rn(a0, f.x);
-      a1 = __dadd_rn(a1, f.y);
-      a2 = __dadd_rn(a2, f.z);
-      if (ROT) {
-        const dbl4 g = fskyr[k];
-        r0 = __dadd_rn(r0, g.x);
-        r1 = __dadd_rn(r1, g.y);
-        r2 = __dadd_rn(r2, g.z);
-      }
-    }
-    if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicOr(status, RG_ST_NAN);
-  } else {
-    // mixed form: FP32 element forces summed in the same fixed order in
-    // FP32 (explicit round-to-nearest adds: no reassociation), then FP64
-    const float4 *fsky = (const float4 *)fsky_;
-    const float4 *fskyr = (const float4 *)fskyr_;
-    float b0 = 0.f, b1 = 0.f, b2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
-    for (int k = k0; k < k1; k++) {
-      const float4 f = __ldg(fsky + k);
-      b0 = __fadd_rn(b0, f.x);
-      b1 = __fadd_rn(b1, f.y);
-      b2 = __fadd_rn(b2, f.z);
-      if (ROT) {
-        const float4 g = __ldg(fskyr + k);
-        c0 = __fadd_rn(c0, g.x);
-        c1 = __fadd_rn(c1, g.y);
-        c2 = __fadd_rn(c2, g.z);
-      }
-    }
-    if (!(isfinite(b0) && isfinite(b1) && isfinite(b2))) atomicOr(status, RG_ST_NAN);
-    a0 = b0;
-    a1 = b1;
-    a2 = b2;
-    r0 = c0;
-    r1 = c1;
-    r2 = c2;
-  }
-  dbl4 x = ld4(N.X4 + n);
-  dbl4 v = ld4(N.V4 + n);
-  dbl4 d = ld4(N.D4 + n);
-  const double dt12 = T->dt12, dt2 = T->dt2;
-  // ACCELE: A = A * (1/MS); X4.w holds 1/MS (0 when MS <= 0, giving A = 0)
-  a0 = __dmul_rn(a0, x.w);
-  a1 = __dmul_rn(a1, x.w);
-  a2 = __dmul_rn(a2, x.w);
-  const int code = (int)v.w;
-  if (code) {
-    if (code & 1) a0 = 0.0;
-    if (code & 2) a1 = 0.0;
-    if (code & 4) a2 = 0.0;
-  }
-  // RGWALL (constraints/general/rwall/rgwall.F:33), fixed infinite plane,
-  // sliding: a slave node whose predicted position X + (V + A*DT12)*DT2 is
-  // on or behind the plane and which does not move away from it loses the
-  // normal components of its acceleration and velocity.
-  if (wall) {
-    const int w = __ldg(wall + n);
-    if (w >= 0) {
-      const double *W = walls + 6 * w;
-      const double vx = __dadd_rn(v.x, __dmul_rn(a0, dt12));
-      const double vy = __dadd_rn(v.y, __dmul_rn(a1, dt12));
-      const double vz = __dadd_rn(v.z, __dmul_rn(a2, dt12));
-      const double ux = __dadd_rn(x.x, __dmul_rn(vx, dt2));
-      const double uy = __dadd_rn(x.y, __dmul_rn(vy, dt2));
-      const double uz = __dadd_rn(x.z, __dmul_rn(vz, dt2));
-      const double dp = __dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(ux, -W[0]), W[3]),
-                                            __dmul_rn(__dadd_rn(uy, -W[1]), W[4])),
-                                  __dmul_rn(__dadd_rn(uz, -W[2]), W[5]));
-      const double vn = __dadd_rn(__dadd_rn(__dmul_rn(vx, W[3]), __dmul_rn(vy, W[4])),
-                                  __dmul_rn(vz, W[5]));
-      if (!(dp > 0.0) && !(vn > 0.0)) {
-        const double dv = __dadd_rn(__dadd_rn(__dmul_rn(v.x, W[3]), __dmul_rn(v.y, W[4])),
-                                    __dmul_rn(v.z, W[5]));
-        const double da = __dadd_rn(__dadd_rn(__dmul_rn(a0, W[3]), __dmul_rn(a1, W[4])),
-                                    __dmul_rn(a2, W[5]));
-        a0 = __dadd_rn(a0, -__dmul_rn(da, W[3]));
-        a1 = __dadd_rn(a1, -__dmul_rn(da, W[4]));
-        a2 = __dadd_rn(a2, -__dmul_rn(da, W[5]));
-        v.x = __dadd_rn(v.x, -__dmul_rn(dv, W[3]));
-        v.y = __dadd_rn(v.y, -__dmul_rn(dv, W[4]));
-        v.z = __dadd_rn(v.z, -__dmul_rn(dv, W[5]));
-      }
-    }
-  }
-  // VELOCITY + DEPLA (FP64 in both forms; FP64 form without fused
-  // multiply-add, as the reference)
-  if constexpr (F64) {
-    v.x = __dadd_rn(v.x, __dmul_rn(dt12, a0));
-    v.y = __dadd_rn(v.y, __dmul_rn(dt12, a1));
-    v.z = __dadd_rn(v.z, __dmul_rn(dt12, a2));
-    const double vdx = __dmul_rn(dt2, v.x), vdy = __dmul_rn(dt2, v.y), vdz = __dmul_rn(dt2, v.z);
-    d.x = __dadd_rn(d.x, vdx);
-    d.y = __dadd_rn(d.y, vdy);
-    d.z = __dadd_rn(d.z, vdz);
-    x.x = __dadd_rn(x.x, vdx);
-    x.y = __dadd_rn(x.y, vdy);
-    x.z = __dadd_rn(x.z, vdz);
-  } else {
-    v.x = fma(dt12, a0, v.x);
-    v.y = fma(dt12, a1, v.y);
-    v.z = fma(dt12, a2, v.z);
-    d.x = fma(dt2, v.x, d.x);
-    d.y = fma(dt2, v.y, d.y);
-    d.z = fma(dt2, v.z, d.z);
-    x.x = fma(dt2, v.x, x.x);
-    x.y = fma(dt2, v.y, x.y);
-    x.z = fma(dt2, v.z, x.z);
-    N.XF[n] = split_hilo(x.x, x.y, x.z);
-    N.VF[n] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y),
-                          __double2float_rn(v.z), 0.f);
-  }
-  st4(N.X4 + n, x);
-  st4(N.V4 + n, v);
-  st4(N.D4 + n, d);
-  if (ROT) {
-    dbl4 vr = ld4(N.VR4 + n);
-    r0 = __dmul_rn(r0, vr.w);
-    r1 = __dmul_rn(r1, vr.w);
-    r2 = __dmul_rn(r2, vr.w);
-    if (code) {
-      if (code & 8) r0 = 0.0;
-      if (code & 16) r1 = 0.0;
-      if (code & 32) r2 = 0.0;
-    }
-    vr.x = __dadd_rn(vr.x, __dmul_rn(dt12, r0));
-    vr.y = __dadd_rn(vr.y, __dmul_rn(dt12, r1));
-    vr.z = __dadd_rn(vr.z, __dmul_rn(dt12, r2));
-    st4(N.VR4 + n, vr);
-    if constexpr (!F64)
-      N.VRF[n] = make_float4(__double2float_rn(vr.x), __double2float_rn(vr.y),
-                             __double2float_rn(vr.z), 0.f);
-  }
+  node_update<F64, ROT>(N, adsky, fsky_, fskyr_, T, wall, walls, status, n);
 }
 
 // Mixed form: refresh the FP32 copies from the FP64 node records (after a
@@ -332,9 +117,8 @@ __global__ void assemble_kernel(int numnod, const int *__restrict__ adsky,
   out[7 * numnod + n] = sr;
 }
 
-// RESOL time-step logic (resol.F:2721-2722, 6123-6127, 6352, 6494-6497):
-// fixed-order reduction of the per-block element minima, then
-// DT2 = min(DT2T, 1.1*DT2OLD, DTMX) (1.1 is a REAL*4 literal), DT12, TT.
+// Time-step kernel: fixed-order reduction of the per-block element minima
+// by one block, then the RESOL logic (dt_apply in rg_node.cuh).
 __global__ void __launch_bounds__(DT_NT)
 dt_kernel(DtPartials dp, int nparts, const int *__restrict__ ngl,
           Time *__restrict__ T, int *__restrict__ status, int advance) {
@@ -348,28 +132,7 @@ dt_kernel(DtPartials dp, int nparts, const int *__restrict__ ngl,
   __shared__ int ok;
   block_dt_min<DT_NT>(d, k, &od, &ok);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const double dt2t = od;
-    T->dt2t = dt2t;
-    if (!advance) {
-      T->neltst = ok >= 0 ? ngl[ok] : 0;
-      return;
-    }
-    const double dt1 = T->dt2;
-    double dt2 = RG_EP06;
-    if (dt2t < dt2) {
-      dt2 = dt2t;
-      T->neltst = ok >= 0 ? ngl[ok] : 0;
-    }
-    dt2 = fmin(fmin(dt2, __dmul_rn(RG_SP_1P1, T->dt2old)), T->dtmx);
-    T->dt1 = dt1;
-    T->dt2 = dt2;
-    T->dt2old = dt2;
-    T->dt12 = __dmul_rn(RG_HALF, __dadd_rn(dt1, dt2));
-    T->tt = __dadd_rn(T->tt, dt2);
-    T->ncycle += 1;
-    if (T->dtmin > 0.0 && dt2 < T->dtmin) atomicOr(status, RG_ST_DTMIN);
-  }
+  if (threadIdx.x == 0) dt_apply(T, od, ok, ngl, status, advance);
 }
 
 // Fixed-order energy partials: [0] element internal (EINT * VOL0),
@@ -928,6 +691,7 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
       cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
       if (e != cudaSuccess) return fail(c, RG_E_MEM, cudaGetErrorString(e));
       c->allocs.push_back(*p);
+      c->alloc_bytes.push_back(std::max<size_t>(bytes, 16));
       c->dev_bytes += bytes;
       return RG_OK;
     };

@@ -1,0 +1,85 @@
+#pragma once
+// Internal definition of the C-ABI context (rg_ctx): shared by the
+// translation units of librg that work on a context's device arrays
+// (rg_api.cu, rg_batch.cu).  Not part of the public interface.
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rg_api.h"
+#include "rg_device.cuh"
+#include "rg_shell.h"
+
+namespace rg {
+
+struct HexaGroupHost {
+  HexaParams P;
+  int nel;
+};
+
+struct WallHost {
+  double p0[3], n[3], dsearch;
+};
+
+}  // namespace rg
+
+struct rg_ctx {
+  typedef rg::HexaGroupHost HexaGroupHost;
+  typedef rg::WallHost WallHost;
+  typedef rg::ShellModelHost ShellModelHost;
+  typedef rg::NodeView NodeView;
+  typedef rg::Time Time;
+  typedef rg::DtPartials DtPartials;
+  template <typename T>
+  using HexaArrays = rg::HexaArrays<T>;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int prec = RG_PREC_FP64;
+  bool finalized = false;
+  bool timing = false;
+  double ktime[4] = {0, 0, 0, 0};
+
+  // ---- host-side model (until finalize) ----
+  int numnod = 0;
+  std::vector<double> X, V, MS, IN;
+  std::vector<int> icodt;
+  int numels = 0;
+  std::vector<int> ixs;  // 11 * numels
+  std::vector<HexaGroupHost> hg;
+  ShellModelHost shells;  // rg_shell.h
+  std::vector<WallHost> walls;
+  std::vector<int> adsky, iads, iadc;  // 1-based as given / built
+  bool skyline_given = false;
+  int lsky = 0;
+  double dtfac_solid = RG_ZEP9, dtfac_shell = RG_ZEP9, dtmx = RG_EP30,
+         dt2old = RG_EP30;
+
+  // ---- device ----
+  NodeView nv{};
+  int *d_adsky = nullptr;
+  void *d_fsky = nullptr;   // dbl4 or float4 [lsky]
+  void *d_fskyr = nullptr;  // rotational slots (shell models)
+  HexaArrays<double> h64{};
+  HexaArrays<float> h32{};
+  int *d_nc = nullptr, *d_iads = nullptr, *d_ngl_all = nullptr;
+  Time *d_time = nullptr;
+  int *d_status = nullptr;
+  DtPartials dp{};
+  int nparts = 0;
+  int *d_wall = nullptr;       // per node: wall index or -1
+  double *d_walls = nullptr;   // 6 doubles per wall (p0, n)
+  int nwalls = 0;
+  bool rot = false;
+  // staging for forint_step / downloads
+  double *d_stage = nullptr;   // 12 * numnod doubles
+  double *d_epart = nullptr;   // energy partials
+  std::vector<void *> allocs;
+  std::vector<size_t> alloc_bytes;  // size of each allocation (snapshots)
+  unsigned long long dev_bytes = 0;
+  cudaGraphExec_t gexec = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaEvent_t ev[8] = {};
+};
+

@@ -176,6 +176,7 @@ __device__ __forceinline__ R pcoef(double d, float f) {
   else
     return f;
 }
+#define PC(name) pcoef<R>(P.name, P.f.name)
 
 template <typename ER>
 struct HexaArrays {

@@ -1,0 +1,220 @@
+#pragma once
+// Nodal phase of the explicit cycle and the RESOL time-step logic as device
+// functions, shared by the single-model kernels (rg_api.cu) and the batched
+// persistent kernel (rg_batch.cu).
+#include "../../include/rg_api.h"
+#include "rg_device.cuh"
+
+namespace rg {
+
+// ---------------------------------------------------------------------------
+// Node update: ASSPAR4 (asspar4.F:165-180) fixed-order slot sums, ACCELE
+// (accele.F:66-78), BCS10/BCS1V (bcs10.F:31), planar rigid wall, VELOCITY
+// (velocity.F:59-75), DEPLA (displacement.F:68-100).  The update arithmetic
+// is written with explicit round-to-nearest multiply / add so that no
+// multiply-add is fused and each node's result does not depend on the
+// launch configuration.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ F8 split_hilo(double x, double y, double z) {
+  F8 c;
+  c.hx = __double2float_rn(x);
+  c.hy = __double2float_rn(y);
+  c.hz = __double2float_rn(z);
+  c.lx = __double2float_rn(x - (double)c.hx);
+  c.ly = __double2float_rn(y - (double)c.hy);
+  c.lz = __double2float_rn(z - (double)c.hz);
+  c.pad0 = c.pad1 = 0.f;
+  return c;
+}
+
+// L2-coherent loads (ld.global.cg): used where the data was written by other
+// blocks earlier in the same launch (batched persistent kernel).
+__device__ __forceinline__ dbl4 ldcg4(const dbl4 *p) {
+  const double2 a = __ldcg((const double2 *)p), b = __ldcg((const double2 *)p + 1);
+  return mk4(a.x, a.y, b.x, b.y);
+}
+
+// COH = true: the slots and the time-step scalars were written earlier in
+// the same launch by other blocks, so they are read through L2.
+template <bool F64, bool ROT, bool COH = false>
+__device__ __forceinline__ void node_update(const NodeView &N, const int *__restrict__ adsky,
+                                            const void *__restrict__ fsky_,
+                                            const void *__restrict__ fskyr_,
+                                            const Time *__restrict__ T,
+                                            const int *__restrict__ wall,
+                                            const double *__restrict__ walls,
+                                            int *__restrict__ status, const int n) {
+  const int k0 = __ldg(adsky + n), k1 = __ldg(adsky + n + 1);
+  double a0, a1, a2, r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  if constexpr (F64) {
+    // ASSPAR4: A = 0 + sum of the node's slots in PARITH/ON order, FP64
+    const dbl4 *fsky = (const dbl4 *)fsky_;
+    const dbl4 *fskyr = (const dbl4 *)fskyr_;
+    a0 = a1 = a2 = 0.0;
+    for (int k = k0; k < k1; k++) {
+      const dbl4 f = COH ? ldcg4(fsky + k) : fsky[k];
+      a0 = __dadd_rn(a0, f.x);
+      a1 = __dadd_rn(a1, f.y);
+      a2 = __dadd_rn(a2, f.z);
+      if (ROT) {
+        const dbl4 g = COH ? ldcg4(fskyr + k) : fskyr[k];
+        r0 = __dadd_rn(r0, g.x);
+        r1 = __dadd_rn(r1, g.y);
+        r2 = __dadd_rn(r2, g.z);
+      }
+    }
+    if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicOr(status, RG_ST_NAN);
+  } else {
+    // mixed form: FP32 element forces summed in the same fixed order in
+    // FP32 (explicit round-to-nearest adds: no reassociation), then FP64
+    const float4 *fsky = (const float4 *)fsky_;
+    const float4 *fskyr = (const float4 *)fskyr_;
+    float b0 = 0.f, b1 = 0.f, b2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    for (int k = k0; k < k1; k++) {
+      const float4 f = COH ? __ldcg(fsky + k) : __ldg(fsky + k);
+      b0 = __fadd_rn(b0, f.x);
+      b1 = __fadd_rn(b1, f.y);
+      b2 = __fadd_rn(b2, f.z);
+      if (ROT) {
+        const float4 g = COH ? __ldcg(fskyr + k) : __ldg(fskyr + k);
+        c0 = __fadd_rn(c0, g.x);
+        c1 = __fadd_rn(c1, g.y);
+        c2 = __fadd_rn(c2, g.z);
+      }
+    }
+    if (!(isfinite(b0) && isfinite(b1) && isfinite(b2))) atomicOr(status, RG_ST_NAN);
+    a0 = b0;
+    a1 = b1;
+    a2 = b2;
+    r0 = c0;
+    r1 = c1;
+    r2 = c2;
+  }
+  dbl4 x = ld4(N.X4 + n);
+  dbl4 v = ld4(N.V4 + n);
+  dbl4 d = ld4(N.D4 + n);
+  const double dt12 = COH ? __ldcg(&T->dt12) : T->dt12;
+  const double dt2 = COH ? __ldcg(&T->dt2) : T->dt2;
+  // ACCELE: A = A * (1/MS); X4.w holds 1/MS (0 when MS <= 0, giving A = 0)
+  a0 = __dmul_rn(a0, x.w);
+  a1 = __dmul_rn(a1, x.w);
+  a2 = __dmul_rn(a2, x.w);
+  const int code = (int)v.w;
+  if (code) {
+    if (code & 1) a0 = 0.0;
+    if (code & 2) a1 = 0.0;
+    if (code & 4) a2 = 0.0;
+  }
+  // RGWALL (constraints/general/rwall/rgwall.F:33), fixed infinite plane,
+  // sliding: a slave node whose predicted position X + (V + A*DT12)*DT2 is
+  // on or behind the plane and which does not move away from it loses the
+  // normal components of its acceleration and velocity.
+  if (wall) {
+    const int w = __ldg(wall + n);
+    if (w >= 0) {
+      const double *W = walls + 6 * w;
+      const double vx = __dadd_rn(v.x, __dmul_rn(a0, dt12));
+      const double vy = __dadd_rn(v.y, __dmul_rn(a1, dt12));
+      const double vz = __dadd_rn(v.z, __dmul_rn(a2, dt12));
+      const double ux = __dadd_rn(x.x, __dmul_rn(vx, dt2));
+      const double uy = __dadd_rn(x.y, __dmul_rn(vy, dt2));
+      const double uz = __dadd_rn(x.z, __dmul_rn(vz, dt2));
+      const double dp = __dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(ux, -W[0]), W[3]),
+                                            __dmul_rn(__dadd_rn(uy, -W[1]), W[4])),
+                                  __dmul_rn(__dadd_rn(uz, -W[2]), W[5]));
+      const double vn = __dadd_rn(__dadd_rn(__dmul_rn(vx, W[3]), __dmul_rn(vy, W[4])),
+                                  __dmul_rn(vz, W[5]));
+      if (!(dp > 0.0) && !(vn > 0.0)) {
+        const double dv = __dadd_rn(__dadd_rn(__dmul_rn(v.x, W[3]), __dmul_rn(v.y, W[4])),
+                                    __dmul_rn(v.z, W[5]));
+        const double da = __dadd_rn(__dadd_rn(__dmul_rn(a0, W[3]), __dmul_rn(a1, W[4])),
+                                    __dmul_rn(a2, W[5]));
+        a0 = __dadd_rn(a0, -__dmul_rn(da, W[3]));
+        a1 = __dadd_rn(a1, -__dmul_rn(da, W[4]));
+        a2 = __dadd_rn(a2, -__dmul_rn(da, W[5]));
+        v.x = __dadd_rn(v.x, -__dmul_rn(dv, W[3]));
+        v.y = __dadd_rn(v.y, -__dmul_rn(dv, W[4]));
+        v.z = __dadd_rn(v.z, -__dmul_rn(dv, W[5]));
+      }
+    }
+  }
+  // VELOCITY + DEPLA (FP64 in both forms; FP64 form without fused
+  // multiply-add, as the reference)
+  if constexpr (F64) {
+    v.x = __dadd_rn(v.x, __dmul_rn(dt12, a0));
+    v.y = __dadd_rn(v.y, __dmul_rn(dt12, a1));
+    v.z = __dadd_rn(v.z, __dmul_rn(dt12, a2));
+    const double vdx = __dmul_rn(dt2, v.x), vdy = __dmul_rn(dt2, v.y), vdz = __dmul_rn(dt2, v.z);
+    d.x = __dadd_rn(d.x, vdx);
+    d.y = __dadd_rn(d.y, vdy);
+    d.z = __dadd_rn(d.z, vdz);
+    x.x = __dadd_rn(x.x, vdx);
+    x.y = __dadd_rn(x.y, vdy);
+    x.z = __dadd_rn(x.z, vdz);
+  } else {
+    v.x = fma(dt12, a0, v.x);
+    v.y = fma(dt12, a1, v.y);
+    v.z = fma(dt12, a2, v.z);
+    d.x = fma(dt2, v.x, d.x);
+    d.y = fma(dt2, v.y, d.y);
+    d.z = fma(dt2, v.z, d.z);
+    x.x = fma(dt2, v.x, x.x);
+    x.y = fma(dt2, v.y, x.y);
+    x.z = fma(dt2, v.z, x.z);
+    N.XF[n] = split_hilo(x.x, x.y, x.z);
+    N.VF[n] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y),
+                          __double2float_rn(v.z), 0.f);
+  }
+  st4(N.X4 + n, x);
+  st4(N.V4 + n, v);
+  st4(N.D4 + n, d);
+  if (ROT) {
+    dbl4 vr = ld4(N.VR4 + n);
+    r0 = __dmul_rn(r0, vr.w);
+    r1 = __dmul_rn(r1, vr.w);
+    r2 = __dmul_rn(r2, vr.w);
+    if (code) {
+      if (code & 8) r0 = 0.0;
+      if (code & 16) r1 = 0.0;
+      if (code & 32) r2 = 0.0;
+    }
+    vr.x = __dadd_rn(vr.x, __dmul_rn(dt12, r0));
+    vr.y = __dadd_rn(vr.y, __dmul_rn(dt12, r1));
+    vr.z = __dadd_rn(vr.z, __dmul_rn(dt12, r2));
+    st4(N.VR4 + n, vr);
+    if constexpr (!F64)
+      N.VRF[n] = make_float4(__double2float_rn(vr.x), __double2float_rn(vr.y),
+                             __double2float_rn(vr.z), 0.f);
+  }
+}
+
+
+// RESOL time-step logic (resol.F:2721-2722, 6123-6127, 6352, 6494-6497),
+// applied by one thread to the reduced element minimum (dt2t, key ok):
+// DT2 = min(DT2T, 1.1*DT2OLD, DTMX) (1.1 is a REAL*4 literal), DT12, TT.
+// advance = 0 only records DT2T / NELTST (FORINT-level call).
+__device__ __forceinline__ void dt_apply(Time *__restrict__ T, const double dt2t, const int ok,
+                                         const int *__restrict__ ngl, int *__restrict__ status,
+                                         const int advance) {
+  T->dt2t = dt2t;
+  if (!advance) {
+    T->neltst = ok >= 0 ? ngl[ok] : 0;
+    return;
+  }
+  const double dt1 = T->dt2;
+  double dt2 = RG_EP06;
+  if (dt2t < dt2) {
+    dt2 = dt2t;
+    T->neltst = ok >= 0 ? ngl[ok] : 0;
+  }
+  dt2 = fmin(fmin(dt2, __dmul_rn(RG_SP_1P1, T->dt2old)), T->dtmx);
+  T->dt1 = dt1;
+  T->dt2 = dt2;
+  T->dt2old = dt2;
+  T->dt12 = __dmul_rn(RG_HALF, __dadd_rn(dt1, dt2));
+  T->tt = __dadd_rn(T->tt, dt2);
+  T->ncycle += 1;
+  if (T->dtmin > 0.0 && dt2 < T->dtmin) atomicOr(status, RG_ST_DTMIN);
+}
+
+}  // namespace rg

@@ -1,27 +1,9 @@
-// Belytschko-Tsay 4-node shell element kernel (CFORC3 chain) and its host
-// bookkeeping.
-//
-// One thread per element, the NPT through-thickness points in registers.
-// The arithmetic follows, step by step and in the same expression order,
-// the reference routines (paths relative to the OpenRadioss source tree):
-//   CCOOR3 gather            elements/shell/coque/ccoor3.F:31
-//   CNVEC3 convected frame   elements/shell/coque/cnvec3.F:35 (ISHFRAM = 0)
-//   CDERI3 local geometry    elements/shell/coque/cderi3.F:30 (ISMSTR = 4)
-//   CCOEF3 coefficients      elements/shell/coque/ccoef3.F:30 (ITHK > 0)
-//   CDLEN3 length for dt     elements/shell/coque/cdlen3.F:30
-//   CDEFO3 membrane rates    elements/shell/coque/cdefo3.F:30 (IHBE <= 1)
-//   CCURV3 curvature rates   elements/shell/coque/ccurv3.F:30
-//   CSTRA3 increments, GSTR  elements/shell/coque/cstra3.F:30
-//   MULAWC + SIGEPS02C + M2CPLR  materials/mat_share/mulawc.F90:185,
-//                            materials/mat/mat002/sigeps02c.F:33, m2cplr.F:29
-//   CHVIS3 hourglass         elements/shell/coque/chvis3.F:32
-//   CDT3 element dt, STI     elements/shell/coque/cdt3.F:32
-//   CFINT3 nodal forces      elements/shell/coque/cfint3.F:30
-//   CUPDT3P slot writes      elements/shell/coque/cupdt3.F:967-1100
-// Through-thickness positions / weights: the COQINI tables
-// (elements/shell/coqini.F:46-123), default-real literals.
+// Belytschko-Tsay shell element kernel (single model) and the host-side
+// bookkeeping of the shell groups; the element arithmetic is
+// shell_element() in rg_shell_elem.cuh.
 #include "../../include/rg_api.h"
 #include "rg_shell.h"
+#include "rg_shell_elem.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -30,64 +12,6 @@
 #include <vector>
 
 namespace rg {
-
-struct ShellParams {
-  int nft, nel, npt, ipla;
-  int part_off, pad;
-  double rho, young, nu, g, a11, ssp;
-  double h1, h2, h3, srh1, srh2, srh3, dm, ish, fsh;
-  double ca, cb, cn, ymax, cc, eps0, pm9;
-  int icc, vp, israte, pad2;
-  double dtfac;
-  // FP32 copies for the mixed form (converted once on the host) and the
-  // branch flags CC /= 0, DM /= 0 evaluated on the FP64 values
-  struct {
-    float rho, young, nu, g, a11, ssp, h1, h2, h3, dm, ish, fsh;
-    float ca, cb, cn, ymax, cc, eps0, pm9, dtfac;
-    int cc_nz, dm_nz;
-  } f;
-};
-
-static void shell_params_mirror(ShellParams &P) {
-  P.f.rho = (float)P.rho;
-  P.f.young = (float)P.young;
-  P.f.nu = (float)P.nu;
-  P.f.g = (float)P.g;
-  P.f.a11 = (float)P.a11;
-  P.f.ssp = (float)P.ssp;
-  P.f.h1 = (float)P.h1;
-  P.f.h2 = (float)P.h2;
-  P.f.h3 = (float)P.h3;
-  P.f.dm = (float)P.dm;
-  P.f.ish = (float)P.ish;
-  P.f.fsh = (float)P.fsh;
-  P.f.ca = (float)P.ca;
-  P.f.cb = (float)P.cb;
-  P.f.cn = (float)P.cn;
-  P.f.ymax = (float)P.ymax;
-  P.f.cc = (float)P.cc;
-  P.f.eps0 = (float)P.eps0;
-  P.f.pm9 = (float)P.pm9;
-  P.f.dtfac = (float)P.dtfac;
-  P.f.cc_nz = P.cc != 0.0;
-  P.f.dm_nz = P.dm != 0.0;
-}
-
-#define PC(name) pcoef<R>(P.name, P.f.name)
-
-template <typename ER>
-struct ShellArrays {
-  int nc;                 // shell count (SoA stride)
-  const int *ix;          // [4][nc] 0-based nodes
-  const int *iadc;        // [4][nc] 0-based slots
-  const int *degen;       // [nc] IXC(4) == IXC(5) (degenerate quad)
-  ER *offg, *thke;
-  double *thk;            // FP64 in both forms (slow accumulation)
-  ER *forc, *mom, *hour, *gstr, *epsdg;  // [5|3|5|8|1][nc]
-  double *eint;           // [2][nc]
-  ER *sig, *pla, *epsd;   // [npt][5][nc], [npt][nc], [npt][nc]
-  double *ehou;           // [nc]
-};
 
 struct ShellGroupHost {
   ShellParams P{};
@@ -101,32 +25,6 @@ struct ShellDev {
   double *epart = nullptr;  // energy partials
 };
 
-// COQINI tables (NPT = 1..5), single-precision DATA literals.
-__constant__ float c_z0[5][5] = {{0.f, 0.f, 0.f, 0.f, 0.f},
-                                 {-.5f, 0.5f, 0.f, 0.f, 0.f},
-                                 {-.5f, 0.f, 0.5f, 0.f, 0.f},
-                                 {-.5f, -.1666667f, 0.1666667f, 0.5f, 0.f},
-                                 {-.5f, -.25f, 0.f, 0.25f, 0.5f}};
-__constant__ float c_wf[5][5] = {{1.f, 0.f, 0.f, 0.f, 0.f},
-                                 {0.5f, 0.5f, 0.f, 0.f, 0.f},
-                                 {0.25f, 0.5f, 0.25f, 0.f, 0.f},
-                                 {0.1666667f, 0.3333333f, 0.3333333f, 0.1666667f, 0.f},
-                                 {0.125f, 0.25f, 0.25f, 0.25f, 0.125f}};
-__constant__ float c_wm[5][5] = {{0.f, 0.f, 0.f, 0.f, 0.f},
-                                 {-.0833333f, 0.0833333f, 0.f, 0.f, 0.f},
-                                 {-.0833333f, 0.f, 0.0833333f, 0.f, 0.f},
-                                 {-.0648148f, -.0555556f, 0.0555556f, 0.0648148f, 0.f},
-                                 {-.0520833f, -.0625f, 0.f, 0.0625f, 0.0520833f}};
-
-template <typename T>
-__device__ __forceinline__ T smax(T a, T b) {
-  return a > b ? a : b;
-}
-template <typename T>
-__device__ __forceinline__ T smin(T a, T b) {
-  return a < b ? a : b;
-}
-
 template <typename ER, int NPT, int NT>
 __global__ void __launch_bounds__(NT)
 shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
@@ -134,514 +32,11 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              typename SlotT<ER>::type *__restrict__ fskyr, DtPartials dp,
              const Time *__restrict__ T, int key0, int nc_total) {
   typedef ER R;
-  constexpr bool F64 = std::is_same<ER, double>::value;
   const int il = blockIdx.x * NT + threadIdx.x;
-  const int nc = S.nc;
   R dtmine = (R)RG_EP06;
   int elmin = -1;
-  if (il < P.nel) {
-    const int e = P.nft + il;
-    const double DT1 = T->dt2;
-    const R dt1 = (R)DT1;
-    // ---- CCOOR3 ----
-    int nn[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) nn[k] = __ldg(S.ix + k * nc + e);
-    R vl[4][3], vrl[4][3];
-    const R offg = S.offg[e];
-    const R off = smin((R)RG_ONE, fabs(offg));
-    const bool z0 = offg < (R)0;
-    // coordinates: absolute (FP64) or node-1-relative from the FP32 hi/lo
-    // copies (mixed); every quantity below uses coordinate differences only.
-    R xg[4], yg[4], zg[4];
-    if constexpr (F64) {
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const dbl4 x = ld4(N.X4 + nn[k]);
-        const dbl4 v = ld4(N.V4 + nn[k]);
-        const dbl4 w = ld4(N.VR4 + nn[k]);
-        xg[k] = x.x;
-        yg[k] = x.y;
-        zg[k] = x.z;
-        vl[k][0] = z0 ? (R)0 : v.x;
-        vl[k][1] = z0 ? (R)0 : v.y;
-        vl[k][2] = z0 ? (R)0 : v.z;
-        vrl[k][0] = z0 ? (R)0 : w.x;
-        vrl[k][1] = z0 ? (R)0 : w.y;
-        vrl[k][2] = z0 ? (R)0 : w.z;
-      }
-    } else {
-      F8 c[4];
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        c[k] = ldF8(N.XF + nn[k]);
-        const float4 v = ldf4(N.VF + nn[k]);
-        const float4 w = ldf4(N.VRF + nn[k]);
-        vl[k][0] = z0 ? 0.f : v.x;
-        vl[k][1] = z0 ? 0.f : v.y;
-        vl[k][2] = z0 ? 0.f : v.z;
-        vrl[k][0] = z0 ? 0.f : w.x;
-        vrl[k][1] = z0 ? 0.f : w.y;
-        vrl[k][2] = z0 ? 0.f : w.z;
-      }
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        xg[k] = (c[k].hx - c[0].hx) + (c[k].lx - c[0].lx);
-        yg[k] = (c[k].hy - c[0].hy) + (c[k].ly - c[0].ly);
-        zg[k] = (c[k].hz - c[0].hz) + (c[k].lz - c[0].lz);
-      }
-    }
-    R thk0 = S.thke[e];
-    // ---- CNVEC3 ----
-    R e1x, e1y, e1z, e2x, e2y, e2z, e3x, e3y, e3z;
-    {
-      const R x21 = xg[1] - xg[0], x32 = xg[2] - xg[1], x34 = xg[2] - xg[3], x41 = xg[3] - xg[0];
-      const R y21 = yg[1] - yg[0], y32 = yg[2] - yg[1], y34 = yg[2] - yg[3], y41 = yg[3] - yg[0];
-      const R z21 = zg[1] - zg[0], z32 = zg[2] - zg[1], z34 = zg[2] - zg[3], z41 = zg[3] - zg[0];
-      e1x = (x21 + x34);
-      e1y = (y21 + y34);
-      e1z = (z21 + z34);
-      e2x = (x32 + x41);
-      e2y = (y32 + y41);
-      e2z = (z32 + z41);
-      e3x = e1y * e2z - e1z * e2y;
-      e3y = e1z * e2x - e1x * e2z;
-      e3z = e1x * e2y - e1y * e2x;
-      R suma = e3x * e3x + e3y * e3y + e3z * e3z;
-      suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
-      e3x = e3x * suma;
-      e3y = e3y * suma;
-      e3z = e3z * suma;
-      const R s1 = e1x * e1x + e1y * e1y + e1z * e1z;
-      const R s2 = e2x * e2x + e2y * e2y + e2z * e2z;
-      suma = sqrt(s1 / s2);
-      e1x = e1x + (e2y * e3z - e2z * e3y) * suma;
-      e1y = e1y + (e2z * e3x - e2x * e3z) * suma;
-      e1z = e1z + (e2x * e3y - e2y * e3x) * suma;
-      suma = e1x * e1x + e1y * e1y + e1z * e1z;
-      suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
-      e1x = e1x * suma;
-      e1y = e1y * suma;
-      e1z = e1z * suma;
-      e2x = e3y * e1z - e3z * e1y;
-      e2y = e3z * e1x - e3x * e1z;
-      e2z = e3x * e1y - e3y * e1x;
-    }
-    // ---- CDERI3 ----
-    R x2, y2, x3, y3, x4, y4, px1, px2, py1, py2, area, vhx, vhy;
-    {
-      const R x21 = xg[1] - xg[0], y21 = yg[1] - yg[0], z21 = zg[1] - zg[0];
-      const R x31 = xg[2] - xg[0], y31 = yg[2] - yg[0], z31 = zg[2] - zg[0];
-      const R x41 = xg[3] - xg[0], y41 = yg[3] - yg[0], z41 = zg[3] - zg[0];
-      x2 = e1x * x21 + e1y * y21 + e1z * z21;
-      y2 = e2x * x21 + e2y * y21 + e2z * z21;
-      y3 = e2x * x31 + e2y * y31 + e2z * z31;
-      x3 = e1x * x31 + e1y * y31 + e1z * z31;
-      x4 = e1x * x41 + e1y * y41 + e1z * z41;
-      y4 = e2x * x41 + e2y * y41 + e2z * z41;
-      px1 = (R)RG_HALF * (y2 - y4);
-      py1 = (R)RG_HALF * (x4 - x2);
-      px2 = (R)RG_HALF * y3;
-      py2 = -(R)RG_HALF * x3;
-      area = smax((R)RG_TWO * (py2 * px1 - py1 * px2), (R)RG_EM20);
-      vhx = (-x2 + x3 - x4) / area;
-      vhy = (-y2 + y3 - y4) / area;
-    }
-    // ---- CCOEF3 (ITHK > 0) ----
-    const double thk_cur = S.thk[e];
-    thk0 = (R)thk_cur;
-    const R vol0 = thk0 * area;
-    const R thk02 = thk0 * thk0;
-    const R nu = PC(nu), ym = PC(young), gmod = PC(g), a11 = PC(a11), ssp = PC(ssp),
-            rho = PC(rho);
-    R shf;
-    if (NPT == 1) {
-      shf = (R)0;
-    } else {
-      const R fac1tmp = (R)2.0 * ((R)1.0 + nu) * thk02;
-      const R ish = PC(ish), fsh = PC(fsh);
-      shf = fsh * ((R)1.0 - ish + ish * fac1tmp / (fsh * area + fac1tmp));
-    }
-    const R gs = gmod * shf;
-    // ---- CDLEN3 (IHBE /= 0) ----
-    R aldt;
-    {
-      const R al1 = x2 * x2 + y2 * y2;
-      const R al2 = (x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2);
-      const R al6 = x3 * x3 + y3 * y3;
-      const R al3 = (x4 - x3) * (x4 - x3) + (y4 - y3) * (y4 - y3);
-      const R al4 = x4 * x4 + y4 * y4;
-      const R al5 = (x4 - x2) * (x4 - x2) + (y4 - y2) * (y4 - y2);
-      R almin = smin(smin(al1, al2), al4);
-      const R alquad = smin(smin(al3, al5), al6);
-      if (al3 != (R)0) almin = smin(almin, alquad);
-      const R dtdyn = area * area / smax(smax(al5, al6), (R)RG_EM20);
-      aldt = smax(dtdyn, almin);
-      const R dthour = (R)RG_HALF * (almin + aldt) / smax(PC(h1), PC(h2));
-      if (dthour < aldt) aldt = dthour;
-      aldt = sqrt(aldt);
-    }
-    // ---- CDEFO3 (IHBE <= 1) ----
-    R vx[4], vy[4], vz[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      vx[k] = e1x * vl[k][0] + e1y * vl[k][1] + e1z * vl[k][2];
-      vy[k] = e2x * vl[k][0] + e2y * vl[k][1] + e2z * vl[k][2];
-      vz[k] = e3x * vl[k][0] + e3y * vl[k][1] + e3z * vl[k][2];
-    }
-    R exx, eyy, exy, exz, eyz;
-    {
-      const R vz13 = vz[0] - vz[2], vz24 = vz[1] - vz[3];
-      eyz = py1 * vz13 + py2 * vz24;
-      exz = px1 * vz13 + px2 * vz24;
-      const R dt1v4 = (R)RG_FOURTH * dt1;
-      const R tmp2a = py2 + py1;
-      const R tmp3a = copysign(smax(fabs(tmp2a), (R)RG_EM20), tmp2a);
-      const R tmp1a = dt1v4 * (vz13 - vz24) * (vz13 - vz24) / tmp3a;
-      R vx13 = vx[0] - vx[2], vx24 = vx[1] - vx[3];
-      vx13 = vx13 - tmp1a;
-      vx24 = vx24 + tmp1a;
-      exx = px1 * vx13 + px2 * vx24;
-      exy = py1 * vx13 + py2 * vx24;
-      const R tmp1b = px2 - px1;
-      const R tmp3b = copysign(smax(fabs(tmp1b), (R)RG_EM20), tmp1b);
-      const R tmp2b = dt1v4 * (vz13 + vz24) * (vz13 + vz24) / tmp3b;
-      R vy13 = vy[0] - vy[2], vy24 = vy[1] - vy[3];
-      vy13 = vy13 + tmp2b;
-      vy24 = vy24 + tmp2b;
-      exy = exy + px1 * vy13 + px2 * vy24;
-      eyy = py1 * vy13 + py2 * vy24;
-    }
-    // ---- CCURV3 ----
-    R rx[4], ry[4], kxx, kyy, kxy;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      rx[k] = e1x * vrl[k][0] + e1y * vrl[k][1] + e1z * vrl[k][2];
-      ry[k] = e2x * vrl[k][0] + e2y * vrl[k][1] + e2z * vrl[k][2];
-    }
-    {
-      const R rx13 = rx[0] - rx[2], rxav = rx[0] + rx[1] + rx[2] + rx[3], rx24 = rx[1] - rx[3];
-      kyy = -py1 * rx13 - py2 * rx24;
-      kxy = px1 * rx13 + px2 * rx24;
-      const R ry13 = ry[0] - ry[2], ryav = ry[0] + ry[1] + ry[2] + ry[3], ry24 = ry[1] - ry[3];
-      kxx = px1 * ry13 + px2 * ry24;
-      kxy = py1 * ry13 + py2 * ry24 - kxy;
-      exz = exz + ryav * ((R)0.25 * area);
-      eyz = eyz - rxav * ((R)0.25 * area);
-    }
-    // ---- CSTRA3 ----
-    {
-      const R fac1 = dt1 / area;
-      exx = exx * fac1;
-      eyy = eyy * fac1;
-      exy = exy * fac1;
-      eyz = eyz * fac1;
-      exz = exz * fac1;
-      kxx = kxx * fac1;
-      kyy = kyy * fac1;
-      kxy = kxy * fac1;
-      const R inc[8] = {exx, eyy, exy, eyz, exz, kxx, kyy, kxy};
-#pragma unroll
-      for (int c = 0; c < 8; c++) S.gstr[c * nc + e] = S.gstr[c * nc + e] + inc[c];
-    }
-    // element strain rate (ASRATE = 1)
-    R epsd_pg;
-    {
-      const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
-      const R th = thk0;
-      const R eps_k2 = (kxx * kxx + kyy * kyy + kxx * kyy + (R)RG_FOURTH * kxy * kxy) *
-                       (R)RG_ONE_OVER_9 * th * th;
-      const R eps_m2 =
-          (R)RG_FOUR_OVER_3 * (exx * exx + eyy * eyy + exx * eyy + (R)RG_FOURTH * exy * exy);
-      epsd_pg = sqrt(eps_k2 + eps_m2) * dtinv;
-      S.epsdg[e] = epsd_pg;
-    }
-    // ---- MULAWC: through-thickness loop (SIGEPS02C / M2CPLR) ----
-    R forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
-    R degmb = S.forc[0 * nc + e] * exx + S.forc[1 * nc + e] * eyy + S.forc[2 * nc + e] * exy +
-              S.forc[3 * nc + e] * eyz + S.forc[4 * nc + e] * exz;
-    R degfx = S.mom[0 * nc + e] * kxx + S.mom[1 * nc + e] * kyy + S.mom[2 * nc + e] * kxy;
-    double thkn = thk_cur;
-    R asrate = (R)RG_ONE;
-    if (P.israte > 0) {
-      if constexpr (F64)
-        asrate = smin((R)RG_ONE, (R)(P.pm9 * DT1));
-      else
-        asrate = smin(1.f, P.f.pm9 * dt1);
-    }
-    const R a1 = ym / ((R)RG_ONE - nu * nu);
-    const R a2 = a1 * nu;
-    const R epdr = smax(PC(eps0) * dt1, (R)RG_EM20);
-#pragma unroll
-    for (int it = 0; it < NPT; it++) {
-      const R thkly = (R)c_wf[NPT - 1][it];
-      const R thklyl = thkly * thk0;
-      const R wmc = (R)c_wm[NPT - 1][it];
-      const R zt = (R)c_z0[NPT - 1][it] * thk0;
-      const R depsxx = exx + zt * kxx;
-      const R depsyy = eyy + zt * kyy;
-      const R depsxy = exy + zt * kxy;
-      const int ip5 = (it * 5) * nc + e;
-      R sn[5];
-#pragma unroll
-      for (int c = 0; c < 5; c++) sn[c] = S.sig[ip5 + c * nc];
-      R ep = S.epsd[it * nc + e];
-      R epsdot;
-      if (P.vp == 2) {
-        ep = asrate * epsd_pg + ((R)RG_ONE - asrate) * ep;
-        S.epsd[it * nc + e] = ep;
-        epsdot = ep * dt1;
-      } else {
-        epsdot = ep * dt1;
-      }
-      R ezz = (R)0;
-      R ca = PC(ca), cb = PC(cb), ymax = PC(ymax);
-      sn[0] = sn[0] + a1 * depsxx + a2 * depsyy;
-      sn[1] = sn[1] + a2 * depsxx + a1 * depsyy;
-      sn[2] = sn[2] + gmod * depsxy;
-      sn[3] = sn[3] + gs * eyz;
-      sn[4] = sn[4] + gs * exz;
-      if (P.f.cc_nz) {
-        R epsp = epsdot;
-        if (P.israte == 0 && P.vp == 2)
-          epsp = smax(smax(fabs(depsxx), fabs(depsyy)), (R)RG_HALF * fabs(depsxy));
-        epsp = smax(epsp, epdr);
-        const R logep = log(epsp / epdr);
-        R q = ((R)RG_ONE + PC(cc) * logep);
-        q = smax(q, (R)RG_EM20);
-        ca = ca * q;
-        cb = cb * q;
-        if (P.icc == 1) ymax = ymax * q;
-      }
-      R pla = S.pla[it * nc + e];
-      R yld = pla == (R)0 ? ca : ca + cb * exp(PC(cn) * log(pla));
-      yld = smin(yld, ymax);
-      if (P.ipla == 0) {
-        const R svm = sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2]);
-        const R r = smin((R)RG_ONE, yld / (svm + (R)RG_EM15));
-        if (r < (R)RG_ONE) {
-          sn[0] = sn[0] * r;
-          sn[1] = sn[1] * r;
-          sn[2] = sn[2] * r;
-          const R dpla = off * smax((R)0, (svm - yld) / ym);
-          const R s1 = (R)RG_HALF * (sn[0] + sn[1]);
-          ezz = dpla * s1 / yld;
-          pla = pla + dpla;
-        }
-      } else {
-        const R s1 = sn[0] + sn[1];
-        const R s2 = sn[0] - sn[1];
-        const R s3 = sn[2];
-        const R A = (R)RG_FOURTH * s1 * s1;
-        const R B = (R)RG_THREE_OVER_4 * s2 * s2 + (R)RG_THREE * s3 * s3;
-        const R svm = sqrt(A + B);
-        if (svm > yld && off == (R)RG_ONE) {
-          const R nu1 = (R)RG_ONE / ((R)RG_ONE - nu);
-          const R nu2 = (R)RG_ONE / ((R)RG_ONE + nu);
-          const R h = yld >= ymax ? (R)0 : PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
-          R dpla_j = (svm - yld) / ((R)RG_THREE * gmod + h);
-          const R anu1 = A * nu1;
-          const R bnu2 = (R)RG_THREE * B * nu2;
-          const R h2 = (R)RG_TWO * h;
-          R dpla_i = 0, Pp = 1, Qq = 1, dr = 0;
-#pragma unroll
-          for (int n = 0; n < 3; n++) {
-            dpla_i = dpla_j;
-            const R pla_i = pla + dpla_i;
-            const R yld_i = pla_i == (R)0 ? smin(ymax, ca) : smin(ymax, ca + cb * exp(PC(cn) * log(pla_i)));
-            dr = (R)RG_HALF * ym * dpla_i / yld_i;
-            Pp = (R)RG_ONE / ((R)RG_ONE + dr * nu1);
-            Qq = (R)RG_ONE / ((R)RG_ONE + (R)RG_THREE * dr * nu2);
-            const R p2 = Pp * Pp, q2 = Qq * Qq;
-            const R f = A * p2 + B * q2 - yld_i * yld_i;
-            const R df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) / yld_i - h2 * yld_i;
-            dpla_j = dpla_i > (R)0 ? smax((R)0, dpla_i - f / df) : (R)0;
-          }
-          pla = pla + dpla_i;
-          const R t1 = (sn[0] + sn[1]) * Pp;
-          const R t2 = (sn[0] - sn[1]) * Qq;
-          sn[0] = (R)RG_HALF * (t1 + t2);
-          sn[1] = (R)RG_HALF * (t1 - t2);
-          sn[2] = sn[2] * Qq;
-          ezz = dr * t1 / ym;
-        }
-      }
-      S.pla[it * nc + e] = pla;
-      ezz = -(depsxx + depsyy) * nu - ((R)RG_ONE - (R)RG_TWO * nu) * ezz;
-      ezz = ezz / ((R)RG_ONE - nu);
-      thkn = thkn + (double)(ezz * thklyl * off);
-#pragma unroll
-      for (int c = 0; c < 5; c++) {
-        S.sig[ip5 + c * nc] = sn[c];
-        forn[c] = forn[c] + thkly * sn[c];
-      }
-      momn[0] = momn[0] + wmc * sn[0];
-      momn[1] = momn[1] + wmc * sn[1];
-      momn[2] = momn[2] + wmc * sn[2];
-    }
-    S.thk[e] = thkn > RG_EM30 ? thkn : RG_EM30;
-    if (P.f.dm_nz) {
-      const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
-      const R visc = ((R)RG_ONEP414 * PC(dm)) * ssp * sqrt(area) * dtinv * rho;
-      forn[0] = forn[0] + visc * (exx + (R)RG_HALF * eyy);
-      forn[1] = forn[1] + visc * (eyy + (R)RG_HALF * exx);
-      forn[2] = forn[2] + visc * exy * (R)RG_THIRD;
-    }
-#pragma unroll
-    for (int c = 0; c < 5; c++) forn[c] = forn[c] * off;
-#pragma unroll
-    for (int c = 0; c < 3; c++) momn[c] = momn[c] * off;
-    degmb = degmb + forn[0] * exx + forn[1] * eyy + forn[2] * exy + forn[3] * eyz + forn[4] * exz;
-    degfx = degfx + momn[0] * kxx + momn[1] * kyy + momn[2] * kxy;
-    {
-      const R vol2 = (R)RG_HALF * vol0;
-      S.eint[e] = S.eint[e] + (double)(degmb * vol2);
-      S.eint[nc + e] = S.eint[nc + e] + (double)(degfx * thk0 * vol2);
-    }
-#pragma unroll
-    for (int c = 0; c < 5; c++) S.forc[c * nc + e] = forn[c];
-#pragma unroll
-    for (int c = 0; c < 3; c++) S.mom[c * nc + e] = momn[c];
-    // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) ----
-    R h11, h12, h13, h21, h22, h23, h31, h32, h33, hr4, hr5;
-    {
-      const R px1v = px1 * vhx, px2v = px2 * vhx, py1v = py1 * vhy, py2v = py2 * vhy;
-      const R gama1 = off * ((R)RG_ONE - px1v - py1v);
-      const R gama3 = off * ((R)RG_ONE + px1v + py1v);
-      const R gama2 = off * (-(R)RG_ONE - px2v - py2v);
-      const R gama4 = off * (-(R)RG_ONE + px2v + py2v);
-      // HVLIN = 0: the linear viscous terms vanish; HVISC = HELAS = 1/2
-      const R shfpr3 = shf / ((R)RG_THREE * ((R)RG_ONE + nu));
-      const R r1 = (R)RG_FOURTH * rho * (R)RG_HUNDRED;
-      const R A1 = r1 * ((R)RG_HALF * PC(h1));
-      const R A3 = r1 * ((R)RG_HALF * PC(h2)) * sqrt(shfpr3);
-      const R A5 = ((R)RG_HALF * PC(h3)) * r1 * (R)RG_ZEP072169;
-      const R r0e = (R)RG_FOURTH * ym * (R)RG_HALF;
-      const R A7 = PC(h1) * r0e;
-      const R A8 = PC(h2) * r0e * shfpr3;
-      const R t2a = thk02 * area;
-      const R tsa = sqrt(t2a);
-      R h1q = A1 * tsa;
-      R h2q = A3 * thk02;
-      R h3q = A5 * t2a;
-      const R td = thk0 * dt1;
-      R hh1 = A7 * td;
-      const R b1 = px1 * px1 + py1 * py1, b2 = px2 * px2 + py2 * py2;
-      R hh2 = A8 * thk02 * td / (b1 + b2);
-      if (S.degen[e]) h1q = h2q = h3q = hh1 = hh2 = (R)0;
-      R hg1 = vx[0] * gama1 + vx[1] * gama2 + vx[2] * gama3 + vx[3] * gama4;
-      R hg2 = vy[0] * gama1 + vy[1] * gama2 + vy[2] * gama3 + vy[3] * gama4;
-      R hou0 = S.hour[0 * nc + e] + hg1 * hh1;
-      R hou1 = S.hour[1 * nc + e] + hg2 * hh1;
-      const R hour1a = hou0 + hg1 * ((R)0 + h1q * fabs(hg1));
-      h11 = hour1a * gama1;
-      h12 = hour1a * gama2;
-      h13 = hour1a * gama3;
-      const R hour2a = hou1 + hg2 * ((R)0 + h1q * fabs(hg2));
-      h21 = hour2a * gama1;
-      h22 = hour2a * gama2;
-      h23 = hour2a * gama3;
-      R ehou = hour1a * hg1 + hour2a * hg2;
-      hg1 = vz[0] * gama1 + vz[1] * gama2 + vz[2] * gama3 + vz[3] * gama4;
-      const R hou2 = S.hour[2 * nc + e] + hg1 * hh2;
-      const R hour3a = hou2 + hg1 * ((R)0 + h2q * fabs(hg1));
-      h31 = hour3a * gama1;
-      h32 = hour3a * gama2;
-      h33 = hour3a * gama3;
-      ehou = ehou + hour3a * hg1;
-      hg1 = rx[0] - rx[1] + rx[2] - rx[3];
-      hg2 = ry[0] - ry[1] + ry[2] - ry[3];
-      hr4 = hg1 * ((R)0 + h3q * fabs(hg1));
-      hr5 = hg2 * ((R)0 + h3q * fabs(hg2));
-      ehou = ehou + hr4 * hg1 + hr5 * hg2;
-      ehou = dt1 * ehou * off;
-      S.hour[0 * nc + e] = hou0;
-      S.hour[1 * nc + e] = hou1;
-      S.hour[2 * nc + e] = hou2;
-      S.hour[3 * nc + e] = hr4;
-      S.hour[4 * nc + e] = hr5;
-      S.ehou[e] = S.ehou[e] + (double)ehou;
-    }
-    // ---- CDT3 ----
-    R sti;
-    {
-      const R dt = PC(dtfac) * aldt / ssp;
-      if (offg > (R)0 && off != (R)0) {
-        dtmine = dt;
-        elmin = key0 + (nc_total - 1 - e);  // first element wins ties (strict <)
-      }
-      const R divm = smax(aldt * aldt, (R)RG_EM20);
-      sti = (R)RG_HALF * vol0 * ym / divm;
-      sti = (R)RG_ZEP81 * sti * off;
-    }
-    // ---- CFINT3 ----
-    R F[3][4], M[3][4];
-    {
-      const R f1a = forn[0] * thk0, f2a = forn[1] * thk0, f3a = forn[2] * thk0;
-      const R f4a = forn[3] * thk0, f5a = forn[4] * thk0;
-      R m4 = f4a * area, m5 = f5a * area;
-      const R f12 = f1a * px2 + f3a * py2;
-      const R f22 = f2a * py2 + f3a * px2;
-      const R f32 = f5a * px2 + f4a * py2;
-      const R f11 = f1a * px1 + f3a * py1;
-      const R f21 = f2a * py1 + f3a * px1;
-      const R f31 = f5a * px1 + f4a * py1;
-      const R g11 = f11 + h11, g13 = h13 - f11;
-      const R g21 = f21 + h21, g23 = h23 - f21;
-      const R g31 = f31 + h31, g33 = h33 - f31;
-      const R g12 = f12 + h12, g22 = f22 + h22, g32 = f32 + h32;
-      F[0][0] = e1x * g11 + e2x * g21 + e3x * g31;
-      F[0][1] = e1x * g12 + e2x * g22 + e3x * g32;
-      F[0][2] = e1x * g13 + e2x * g23 + e3x * g33;
-      F[1][0] = e1y * g11 + e2y * g21 + e3y * g31;
-      F[1][1] = e1y * g12 + e2y * g22 + e3y * g32;
-      F[1][2] = e1y * g13 + e2y * g23 + e3y * g33;
-      F[2][0] = e1z * g11 + e2z * g21 + e3z * g31;
-      F[2][1] = e1z * g12 + e2z * g22 + e3z * g32;
-      F[2][2] = e1z * g13 + e2z * g23 + e3z * g33;
-#pragma unroll
-      for (int c = 0; c < 3; c++) F[c][3] = -F[c][0] - F[c][1] - F[c][2];
-      const R m1a = momn[0] * thk02, m2a = momn[1] * thk02, m3a = momn[2] * thk02;
-      m4 = m4 * (R)RG_FOURTH;
-      m5 = m5 * (R)RG_FOURTH;
-      const R m11 = -m2a * py1 - m3a * px1;
-      const R m21 = m1a * px1 + m3a * py1;
-      const R m12 = -m2a * py2 - m3a * px2;
-      const R m22 = m1a * px2 + m3a * py2;
-      const R b1x[4] = {hr4 * off, -hr4 * off, hr4 * off, -hr4 * off};
-      const R b2x[4] = {hr5 * off, -hr5 * off, hr5 * off, -hr5 * off};
-      const R gg1[4] = {m11 - m4 + b1x[0], m12 - m4 + b1x[1], -m11 - m4 + b1x[2], -m12 - m4 + b1x[3]};
-      const R gg2[4] = {m21 + m5 + b2x[0], m22 + m5 + b2x[1], -m21 + m5 + b2x[2], -m22 + m5 + b2x[3]};
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        M[0][k] = e1x * gg1[k] + e2x * gg2[k];
-        M[1][k] = e1y * gg1[k] + e2y * gg2[k];
-        M[2][k] = e1z * gg1[k] + e2z * gg2[k];
-      }
-    }
-    // ---- CUPDT3P ----
-    R offg_new = offg;
-    if (off < (R)RG_ONE) {
-      offg_new = off;
-      S.offg[e] = off;
-    }
-    const bool zero = offg_new < (R)0;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int K = __ldg(S.iadc + k * nc + e);
-      typename SlotT<ER>::type a, b;
-      a.x = zero ? (R)0 : -F[0][k];
-      a.y = zero ? (R)0 : -F[1][k];
-      a.z = zero ? (R)0 : -F[2][k];
-      a.w = zero ? (R)0 : sti;
-      b.x = zero ? (R)0 : -M[0][k];
-      b.y = zero ? (R)0 : -M[1][k];
-      b.z = zero ? (R)0 : -M[2][k];
-      b.w = (R)0;  // STIR = 0 (element time step)
-      fsky[K] = a;
-      fskyr[K] = b;
-    }
-  }
+  if (il < P.nel)
+    shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin);
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
 }
 
@@ -778,6 +173,16 @@ int shell_group_add(ShellModelHost &S, int numnod, int nel, const int *ixc, int 
 }
 
 int shell_numelc(const ShellModelHost &S) { return S.numelc; }
+
+const void *shell_device_arrays(const ShellModelHost &S, int prec) {
+  if (!S.dev) return nullptr;
+  const auto *D = (const ShellDev *)S.dev;
+  return prec == RG_PREC_FP64 ? (const void *)&D->a64 : (const void *)&D->a32;
+}
+int shell_group_count(const ShellModelHost &S) { return (int)S.groups.size(); }
+const ShellParams *shell_group_params(const ShellModelHost &S, int g) {
+  return &S.groups[g]->P;
+}
 const int *shell_ixc(const ShellModelHost &S) { return S.ixc.data(); }
 void shell_user_ids(const ShellModelHost &S, int *out) {
   // reversed: the dt kernel keeps the largest key on ties, CDT3 the first

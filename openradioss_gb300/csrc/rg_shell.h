@@ -44,4 +44,12 @@ int shell_download(ShellModelHost &S, int prec, int which, double *out,
                    std::string &why);
 void shell_free(ShellModelHost &S);
 
+// Views for the batched kernel (rg_batch.cu): the model's device arrays
+// (a ShellArrays<double> or ShellArrays<float> by prec, nullptr before
+// finalize) and the parameters of group g.
+struct ShellParams;
+const void *shell_device_arrays(const ShellModelHost &S, int prec);
+int shell_group_count(const ShellModelHost &S);
+const ShellParams *shell_group_params(const ShellModelHost &S, int g);
+
 }  // namespace rg

@@ -342,3 +342,79 @@ def crash_box(n_side=77, n_len=390, side=0.060, length=0.300, thk=1.2e-3,
               shells=[ShellGroupSpec(ixc, mat, shell_prop(thk), t, npt)], IN=inr)
     m.rwalls = [((0.0, 0.0, -gap), (0.0, 0.0, 1.0), 2.0 * length)]
     return m
+
+
+def crash_box_variant(i, seed0=100):
+    """Variant i of the batched crash-box sweep: element count U[5k, 60k],
+    section U[40, 80] mm, length U[200, 400] mm, thickness U[0.8, 2.0] mm,
+    Johnson-Cook A U[250, 450] MPa, impact speed U[8, 20] m/s, all drawn from
+    the seeded generator of seed seed0 + i (which also seeds the
+    imperfections).  The element edge follows from the element count."""
+    rng = np.random.default_rng(seed0 + i)
+    nel = rng.uniform(5e3, 6e4)
+    side = rng.uniform(40.0, 80.0) * 1e-3
+    length = rng.uniform(200.0, 400.0) * 1e-3
+    thk = rng.uniform(0.8, 2.0) * 1e-3
+    a = rng.uniform(250.0, 450.0) * 1e6
+    v0 = rng.uniform(8.0, 20.0)
+    h = np.sqrt(4.0 * side * length / nel)
+    ns = max(2, int(round(side / h)))
+    nl = max(2, int(round(length / h)))
+    m = crash_box(n_side=ns, n_len=nl, side=side, length=length, thk=thk, v0=v0,
+                  seed=seed0 + i, a=a)
+    m.name = "crash_box_variant_%d" % i
+    return m
+
+
+def crash_box_sweep(n=64, seed0=100):
+    """The batched sweep: n crash-box variants (seeds seed0 .. seed0+n-1)."""
+    return [crash_box_variant(i, seed0) for i in range(n)]
+
+
+def hexa_impact_block(nel, h=0.005, v0=10.0, vstd=0.5, seed=0, law="law2", a=350e6):
+    """Hexa impact block of about nel one-point hexas: a bar of square
+    section (nx = ny, nz = 2 nx) with its z=0 face fixed and a seeded velocity
+    field v0 + N(0, vstd) towards that face."""
+    nx = max(2, int(round((nel / 2.0) ** (1.0 / 3.0))))
+    nz = max(2, int(round(nel / (nx * nx))))
+    X, ixs = hexa_block(nx, nx, nz, h)
+    mat = law2(7850.0, 210e9, 0.3, a, 275e6, 0.36, c=0.022, eps0=1.0) \
+        if law == "law2" else law1(7850.0, 210e9, 0.3)
+    ms = lumped_mass_hexa(X, ixs, 7850.0)
+    rng = np.random.default_rng(seed)
+    V = rng.normal(0.0, vstd, size=X.shape)
+    V[2] += -v0
+    icodt = np.zeros(X.shape[1], np.int32)
+    fixed = X[2] == 0.0
+    icodt[fixed] = 7
+    V[:, fixed] = 0.0
+    return Model("hexa_impact_%d" % ixs.shape[1], X, V, ms, icodt,
+                 hexa=[HexaGroupSpec(ixs, mat, solid_prop())])
+
+
+def serving_job(k, seed=7):
+    """Job k of the serving stream (seeded): a 50/50 draw between a shell
+    crash box of U[2k, 150k] elements and a hexa impact block of U[2k, 200k]
+    elements, U[2000, 20000] cycles, LAW1 or LAW2 (hexa blocks) / LAW2
+    (shells) with A U[250, 450] MPa and speeds U[8, 20] m/s.  Returns
+    (model, ncycles)."""
+    rng = np.random.default_rng([seed, k])
+    shell = rng.uniform() < 0.5
+    ncyc = int(rng.integers(2000, 20001))
+    a = rng.uniform(250.0, 450.0) * 1e6
+    v0 = rng.uniform(8.0, 20.0)
+    if shell:
+        nel = rng.uniform(2e3, 1.5e5)
+        side = rng.uniform(40.0, 80.0) * 1e-3
+        length = rng.uniform(200.0, 400.0) * 1e-3
+        thk = rng.uniform(0.8, 2.0) * 1e-3
+        h = np.sqrt(4.0 * side * length / nel)
+        m = crash_box(n_side=max(2, int(round(side / h))),
+                      n_len=max(2, int(round(length / h))), side=side, length=length,
+                      thk=thk, v0=v0, seed=1000 + k, a=a)
+    else:
+        nel = rng.uniform(2e3, 2e5)
+        law = "law1" if rng.uniform() < 0.5 else "law2"
+        m = hexa_impact_block(nel, v0=v0, seed=1000 + k, law=law, a=a)
+    m.name = "job_%d" % k
+    return m, ncyc
