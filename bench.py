@@ -273,6 +273,146 @@ def run_ours(args, rank, world, local_rank):
     return line
 
 
+SWEEP_JOBS = 64
+SWEEP_CYCLES_PER_JOB = 2000
+
+
+def run_sweep(args, njobs=SWEEP_JOBS, timed_cycles=None, device=0):
+    """Batched crash-box sweep: njobs seeded variants (5k-60k shells each)
+    stepped together in one persistent kernel per cycle (autotuned launch
+    shape), against the same jobs run one after another, alone, in the plain
+    FP64 form.  A job is SWEEP_CYCLES_PER_JOB cycles; the timed region is
+    timed_cycles cycles of every job and jobs/h is scaled from it."""
+    from openradioss_gb300.batch import Batch
+    from openradioss_gb300.engine import Engine
+    models = M.crash_box_sweep(njobs)
+    K = timed_cycles or args.steps
+    ne = sum(m.numels + m.numelc for m in models)
+    hbm_peak, peak_kind = peaks()
+    seq = {}
+    for prec in (0, 1):
+        tot = 0.0
+        for m in models:
+            e = Engine(m, device=device, precision=prec)
+            e.cycle(args.warmup)
+            tot += e.time_cycles(K)
+            e.close()
+        seq[prec] = tot
+    bat = {}
+    for prec in (0, 1):
+        es = [Engine(m, device=device, precision=prec) for m in models]
+        b = Batch(device)
+        for e in es:
+            b.add(e)
+        b.cycle(args.warmup)
+        b.sync()
+        cfg = b.autotune(trial_cycles=3)
+        b.cycle(args.warmup)
+        with Clocks(device) as clk:
+            ms = b.time_cycles(K)
+        prog, st = b.progress()
+        bat[prec] = dict(ms=ms, cfg=cfg, status=st, clocks=clk.summary(),
+                         status_jobs=sum(e.status() for e in es))
+        b.close()
+        for e in es:
+            e.close()
+
+    def jobs_h(ms):
+        return njobs * 3600.0 / (ms * 1e-3 * SWEEP_CYCLES_PER_JOB / K)
+
+    eb32 = sum(element_bytes(m, 1)[0] * m.numelc for m in models)
+    ach = eb32 / (bat[1]["ms"] * 1e-3 / K) / 1e9
+    return {
+        "metric": "jobs/h",
+        "value": jobs_h(bat[1]["ms"]),
+        "unit": "jobs/h",
+        "n_gpus": 1,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": bat[1]["ms"] / K,
+        "higher_is_better": True,
+        "dtype": "f32 element / f64 nodal",
+        "data": "synthetic (64 seeded crash-box variants)",
+        "config": {"workload": "crash_box_sweep_64", "jobs": njobs, "elements": ne,
+                   "elements_per_job": [min(m.numelc for m in models),
+                                        max(m.numelc for m in models)],
+                   "cycles_per_job": SWEEP_CYCLES_PER_JOB,
+                   "note": "jobs/h scaled from %d timed cycles of every job" % K},
+        "batched_mixed": {"jobs_h": jobs_h(bat[1]["ms"]),
+                          "element_updates_s": ne * K / (bat[1]["ms"] * 1e-3),
+                          "autotuned": bat[1]["cfg"]},
+        "batched_fp64": {"jobs_h": jobs_h(bat[0]["ms"]),
+                         "element_updates_s": ne * K / (bat[0]["ms"] * 1e-3),
+                         "autotuned": bat[0]["cfg"]},
+        "sequential_fp64": {"jobs_h": jobs_h(seq[0]),
+                            "element_updates_s": ne * K / (seq[0] * 1e-3)},
+        "sequential_mixed": {"jobs_h": jobs_h(seq[1]),
+                             "element_updates_s": ne * K / (seq[1] * 1e-3)},
+        "speedup_vs_sequential_plain": seq[0] / bat[1]["ms"],
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": ach / hbm_peak, "peak_kind": peak_kind,
+                     "note": "batched mixed cycle: shell element-phase algorithmic bytes "
+                             "over the whole cycle time"},
+        "clocks": bat[1]["clocks"],
+        "device_status": [bat[0]["status"], bat[1]["status"], bat[0]["status_jobs"],
+                          bat[1]["status_jobs"]],
+    }
+
+
+SERVE_JOBS = 32
+SERVE_RATE = 4.0          # Poisson arrivals, jobs/s
+SERVE_BUDGET = 48 << 30   # HBM budget of the serving loop (bytes)
+
+
+def run_serving(args, njobs=SERVE_JOBS, device=0):
+    """Serving stream: njobs seeded requests (50/50 shell crash boxes of
+    2k-150k elements and hexa impact blocks of 2k-200k elements, 2,000-20,000
+    cycles each) arriving as a Poisson process of SERVE_RATE jobs/s, admitted
+    by HBM budget into a continuously batched mixed-form run.  Beside it, the
+    same jobs as sequential plain FP64 runs alone (GPU time of each job from a
+    timed 50-cycle sample scaled to its cycle count)."""
+    from openradioss_gb300.engine import Engine
+    from openradioss_gb300.serving import Server, poisson_arrivals
+    jobs = [M.serving_job(k) for k in range(njobs)]
+    arr = poisson_arrivals(njobs, SERVE_RATE, seed=7)
+    seq = 0.0
+    for m, n in jobs:
+        e = Engine(m, device=device, precision=0)
+        e.cycle(3)
+        seq += e.time_cycles(50) * 1e-3 * n / 50.0
+        e.close()
+    srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device)
+    with Clocks(device) as clk:
+        st = srv.run([(k, m, n, float(a)) for k, ((m, n), a) in enumerate(zip(jobs, arr))])
+    bad = sum(1 for r in srv.done if r.result.get("status", 0))
+    srv.close()
+    seq_jobs_h = 3600.0 * njobs / seq
+    ne = [m.numels + m.numelc for m, _ in jobs]
+    return {
+        "metric": "jobs/h",
+        "value": st["jobs_per_h"],
+        "unit": "jobs/h",
+        "n_gpus": 1,
+        "higher_is_better": True,
+        "dtype": "f32 element / f64 nodal",
+        "data": "synthetic (seeded serving stream)",
+        "config": {"workload": "serving_mix", "jobs": njobs, "arrival_rate_per_s": SERVE_RATE,
+                   "elements_per_job": [min(ne), max(ne)],
+                   "cycles_per_job": [min(n for _, n in jobs), max(n for _, n in jobs)],
+                   "hbm_budget_gb": SERVE_BUDGET / 2 ** 30, "step_cycles": 100},
+        "p50_latency_s": st["p50_latency_s"],
+        "p99_latency_s": st["p99_latency_s"],
+        "mean_latency_s": st["mean_latency_s"],
+        "makespan_s": st["makespan_s"],
+        "element_updates_s": st["element_updates"] / st["makespan_s"],
+        "max_used_gb": st["max_used_bytes"] / 2 ** 30,
+        "sequential_fp64_jobs_h": seq_jobs_h,
+        "speedup_vs_sequential_plain": st["jobs_per_h"] / seq_jobs_h,
+        "jobs_with_device_status": bad,
+        "clocks": clk.summary(),
+    }
+
+
 def cpu_baseline(wl, sample_s, threads=None):
     """Time the CPU restatement (oracle/) on the host cores: a bounded
     sample of the same workload."""
@@ -330,7 +470,10 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
+                    choices=sorted(WORKLOADS) + ["crash_box_sweep_64", "serving_mix"])
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the batched-sweep and serving summaries of the default run")
     ap.add_argument("--cpu-sample", type=float, default=15.0,
                     help="seconds of CPU work in the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -352,7 +495,24 @@ def main():
         import torch.distributed as tdist
         torch.cuda.set_device(local_rank)
         tdist.init_process_group("nccl")
+    if args.workload in ("crash_box_sweep_64", "serving_mix"):
+        line = (run_sweep(args, device=local_rank) if args.workload == "crash_box_sweep_64"
+                else run_serving(args, device=local_rank))
+        line["n_gpus"] = world
+        if rank == 0:
+            print(json.dumps(line, default=float), flush=True)
+        return
     line = run_ours(args, rank, world, local_rank)
+    if rank == 0 and world == 1 and not args.no_sweep:
+        sw = run_sweep(args, timed_cycles=20)
+        line["batched_sweep"] = {k: sw[k] for k in (
+            "batched_mixed", "batched_fp64", "sequential_fp64", "sequential_mixed",
+            "speedup_vs_sequential_plain", "config", "device_status")}
+        sv = run_serving(args)
+        line["serving"] = {k: sv[k] for k in (
+            "value", "unit", "p50_latency_s", "p99_latency_s", "sequential_fp64_jobs_h",
+            "speedup_vs_sequential_plain", "element_updates_s", "config",
+            "jobs_with_device_status")}
     if rank == 0:
         print(json.dumps(line, default=float), flush=True)
     if world > 1:

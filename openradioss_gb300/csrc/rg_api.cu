@@ -629,6 +629,9 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     if ((r = dalloc(c, &c->nv.XF, numnod))) return r;
     if ((r = dalloc(c, &c->nv.VF, numnod))) return r;
     if (c->rot && (r = dalloc(c, &c->nv.VRF, numnod))) return r;
+    // the synchronous uploads above ran on the legacy stream, which the
+    // context's non-blocking stream does not wait for: fence them first
+    RG_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));
     refresh_copies_kernel<<<(numnod + NODE_NT - 1) / NODE_NT, NODE_NT, 0, c->stream>>>(
         c->nv, c->rot ? 1 : 0);
     RG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -739,7 +742,8 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   }
   if ((r = dalloc(c, &c->d_stage, 12 * (size_t)numnod + 16))) return r;
   if ((r = dalloc(c, &c->d_epart, 4 * EN_BLOCKS + 8))) return r;
-  RG_CUDA(c, cudaDeviceSynchronize());
+  RG_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));  // uploads complete
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
   // capture one cycle as a graph
   RG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   enqueue_cycle(c);
@@ -915,6 +919,7 @@ int rg_download_forces(rg_ctx *c, double *f, double *stifn, double *fr) {
 int rg_download_hexa_state(rg_ctx *c, int which, double *out) {
   if (!c || !out) return RG_E_ARG;
   if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));  // results of enqueued cycles
   const int ne = c->numels;
   if (ne == 0) return RG_OK;
   RG_CUDA(c, cudaSetDevice(c->device));
@@ -958,6 +963,7 @@ int rg_download_hexa_state(rg_ctx *c, int which, double *out) {
 int rg_download_shell_state(rg_ctx *c, int which, double *out) {
   if (!c || !out) return RG_E_ARG;
   if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));  // results of enqueued cycles
   RG_CUDA(c, cudaSetDevice(c->device));
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
   std::string why;

@@ -1,0 +1,204 @@
+"""Serving loop: simulation jobs admitted by HBM budget and advanced together
+(continuous batching) on one GPU.
+
+Requests (a model plus a cycle count) arrive over time.  The loop keeps a
+:class:`~openradioss_gb300.batch.Batch` running; between two batched steps
+of ``step_cycles`` cycles it
+
+* admits waiting requests, in arrival order, while a job slot is free and
+  the job's estimated device bytes fit the remaining HBM budget -- the job's
+  model is uploaded to the device (its state then stays there) and it joins
+  the running batch with its own cycle target;
+* retires the jobs whose cycle count reached their target: their results are
+  read back, their device memory is released, and the freed slot and bytes go
+  to the next waiting requests.
+
+While the GPU runs a step, the host prepares the next admissions (upload
+and set-up), so requests that arrive while others are on the GPU overlap
+with them.  Each job's results are bitwise those of the same job run alone
+(the batched kernel computes every element and node exactly as the
+single-model path does), which the tests check.
+
+The latency of a job is its completion time minus its arrival time; the
+loop reports jobs/h and the p50 / p99 latencies.
+"""
+from __future__ import annotations
+
+import heapq
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .batch import Batch
+from .engine import Engine, RG_PREC_MIXED
+
+
+def estimate_device_bytes(model, precision=RG_PREC_MIXED):
+    """Upper estimate of the device bytes an Engine of this model holds
+    (element state, connectivity, skyline slots, node records, staging).
+    Admission uses it before the job is uploaded."""
+    er = 8 if precision == 0 else 4
+    slot = 32 if precision == 0 else 16
+    nn = model.numnod
+    b = 0
+    if model.numels:
+        ne = model.numels
+        # SIG 6, QVIS, OFF, PLA, EPSD (ER); EINT, RHO, VOL0, EHOU (FP64);
+        # NC, IADS (8 int32 each), user id, slots, dt partials
+        b += ne * (er * 10 + 8 * 4 + 64 + 4 + 8 * slot + 4) + (ne // 128 + 1) * 12
+    if model.numelc:
+        nc = model.numelc
+        npt = model.shells[0].npt
+        # FOR 5, MOM 3, HOUR 5, GSTR 8, OFF, THKE, EPSDG (ER), THK, EINT 2,
+        # EHOU (FP64), per point SIG 5, PLA, EPSD; IX, IADC, DEGEN; 2x4 slots
+        b += nc * (er * (24 + 7 * npt) + 8 * 4 + 36 + 8 * slot + 4) + (nc // 128 + 1) * 12
+    rot = model.numelc > 0
+    # X4 V4 D4 (+VR4 DR4), FP32 copies, ADSKY, wall index, staging 12 doubles
+    b += nn * (96 + (64 if rot else 0) + (48 + (16 if rot else 0) if precision else 0)
+               + 4 + 4 + 96)
+    return int(1.15 * b) + (1 << 20)
+
+
+@dataclass(order=True)
+class Request:
+    arrival: float
+    key: int
+    model: object = field(compare=False)
+    ncycles: int = field(compare=False)
+
+
+@dataclass
+class JobRecord:
+    key: int
+    arrival: float
+    admitted: float = 0.0
+    finished: float = 0.0
+    ncycles: int = 0
+    elements: int = 0
+    device_bytes: int = 0
+    result: dict = field(default_factory=dict)
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+class Server:
+    """Continuous-batching server of explicit simulation jobs on one GPU."""
+
+    def __init__(self, hbm_budget_bytes, max_jobs=64, precision=RG_PREC_MIXED,
+                 step_cycles=100, device=0, config=None, keep_results=False,
+                 result_fn=None):
+        self.budget = int(hbm_budget_bytes)
+        self.max_jobs = max_jobs
+        self.precision = precision
+        self.step_cycles = step_cycles
+        self.device = device
+        self.batch = Batch(device)
+        if config:
+            self.batch.set_config(**config)
+        self.keep_results = keep_results
+        self.result_fn = result_fn
+        self.used = 0
+        self.running = {}     # slot -> (Engine, JobRecord, reserved bytes)
+        self.waiting = []     # heap of Request (arrival order)
+        self.done = []
+        self.max_used = 0
+
+    def submit(self, key, model, ncycles, arrival):
+        heapq.heappush(self.waiting, Request(arrival, key, model, ncycles))
+
+    def _admit(self, now):
+        n = 0
+        while self.waiting and self.waiting[0].arrival <= now and \
+                len(self.running) < self.max_jobs:
+            req = self.waiting[0]
+            need = estimate_device_bytes(req.model, self.precision)
+            if self.used + need > self.budget:
+                if not self.running:
+                    raise RuntimeError("job %d needs %d bytes, more than the whole budget %d"
+                                       % (req.key, need, self.budget))
+                break
+            heapq.heappop(self.waiting)
+            e = Engine(req.model, device=self.device, precision=self.precision)
+            rec = JobRecord(req.key, req.arrival, admitted=self._clock(), ncycles=req.ncycles,
+                            elements=req.model.numels + req.model.numelc,
+                            device_bytes=e.info()["device_bytes"])
+            slot = self.batch.add(e, req.ncycles)
+            self.running[slot] = (e, rec, need)
+            self.used += need
+            self.max_used = max(self.max_used, self.used)
+            n += 1
+        return n
+
+    def _retire(self, prog):
+        fin = [s for s, (e, rec, need) in self.running.items() if prog.get(s, -1) >= rec.ncycles]
+        if not fin:
+            return 0
+        self.batch.sync()
+        now = self._clock()
+        for s in fin:
+            e, rec, need = self.running.pop(s)
+            self.batch.remove(s)
+            rec.finished = now
+            if self.result_fn is not None:
+                rec.result = self.result_fn(e)
+            elif self.keep_results:
+                nd = e.nodes()
+                rec.result = dict(X=nd["X"], V=nd["V"], time=e.time(), energy=e.energy(),
+                                  status=e.status())
+            else:
+                rec.result = dict(time=e.time(), energy=e.energy(), status=e.status())
+            e.close()
+            self.used -= need
+            self.done.append(rec)
+        return len(fin)
+
+    def _clock(self):
+        return time.perf_counter() - self.t0
+
+    def run(self, requests):
+        """Serve ``requests`` -- (key, model, ncycles, arrival seconds) --
+        arriving on the wall clock from now; returns the statistics."""
+        for (k, m, n, a) in requests:
+            self.submit(k, m, n, a)
+        total = len(self.waiting)
+        self.t0 = time.perf_counter()
+        steps = 0
+        while len(self.done) < total:
+            now = self._clock()
+            if self.running:
+                # launch a step; admissions prepared meanwhile overlap with it
+                self.batch.cycle(self.step_cycles)
+                steps += 1
+                self._admit(self._clock())
+                prog, st = self.batch.progress()
+                if st:
+                    raise RuntimeError("batched kernel status %d" % st)
+                self._retire(prog)
+            else:
+                if self.waiting and self.waiting[0].arrival > now:
+                    time.sleep(min(0.05, self.waiting[0].arrival - now))
+                self._admit(self._clock())
+        makespan = self._clock()
+        lat = np.array([r.latency for r in self.done])
+        return dict(jobs=total, makespan_s=makespan, jobs_per_h=3600.0 * total / makespan,
+                    p50_latency_s=float(np.percentile(lat, 50)),
+                    p99_latency_s=float(np.percentile(lat, 99)),
+                    mean_latency_s=float(lat.mean()), steps=steps,
+                    max_used_bytes=self.max_used, budget_bytes=self.budget,
+                    element_updates=float(sum(r.elements * r.ncycles for r in self.done)))
+
+    def close(self):
+        for s, (e, rec, need) in list(self.running.items()):
+            self.batch.remove(s)
+            e.close()
+        self.running.clear()
+        self.batch.close()
+
+
+def poisson_arrivals(n, rate, seed=7):
+    """n arrival times of a Poisson process of the given rate (1/s)."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
