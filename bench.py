@@ -120,7 +120,8 @@ def element_bytes(model, prec):
         # writes SIG, QVIS, EINT, RHO, EHOU, [PLA, EPSD], 8 slots
         wr = er * (6 + 1) + 8 * 3 + (2 * er if law == 2 else 0) + 8 * slot
         spn = 8.0 * ne / nn
-        node = 4 + spn * slot + 3 * 32 * 2
+        # ADSKY, slots, X4 V4 D4 read + written, FP32 copies XF VF written
+        node = 4 + spn * slot + 3 * 32 * 2 + (48 if prec else 0)
         return rd + wr, node, "hexa"
     nc = model.numelc
     npt = model.shells[0].npt
@@ -132,7 +133,9 @@ def element_bytes(model, prec):
     # per point SIG(5), PLA, EPSD; 4 slots of forces + 4 of moments
     wr = 22 * er + 8 + 16 + 8 + npt * 7 * er + 4 * 2 * slot
     spn = 4.0 * nc / nn
-    node = 4 + spn * 2 * slot + 4 * 32 * 2
+    # ADSKY, force + moment slots, X4 V4 D4 VR4 read + written, DR4 unread;
+    # FP32 copies XF VF VRF written
+    node = 4 + spn * 2 * slot + 4 * 32 * 2 + (64 if prec else 0)
     return rd + wr, node, "shell"
 
 
