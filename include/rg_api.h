@@ -42,6 +42,7 @@ extern "C" {
 #define RG_E_UNSUP (-4)    /* formulation not supported by this build */
 #define RG_E_DEVICE (-5)   /* device-side status raised (see rg_status) */
 #define RG_E_MEM (-6)      /* device memory budget exceeded */
+#define RG_E_SIZE (-7)     /* size above a fixed no-allocation scratch */
 
 /* device status bits (rg_status) */
 #define RG_ST_NEGVOL 1     /* non-positive hexa volume (SCHKJABT3) */
@@ -168,6 +169,27 @@ int rg_kernel_times(rg_ctx *ctx, double *ms4);
 /* Advance ncycle cycles (graph launches) bracketed by CUDA events recorded
  * on the context's stream; *ms = device time of the whole span. */
 int rg_time_cycles(rg_ctx *ctx, int ncycle, double *ms);
+
+/* Kinetic energy 0.5*sum(MS*|V|^2) of caller-owned DEVICE arrays V(3,numnod)
+ * and MS(numnod) on CUDA device `device`, without allocating device memory:
+ * the per-block partial sums live in a fixed file-scope device scratch of
+ * RG_NOALLOC_MAX_BLOCKS doubles, each block covering
+ * RG_NOALLOC_NODES_PER_BLOCK nodes, so numnod may be at most
+ * RG_NOALLOC_MAX_BLOCKS * RG_NOALLOC_NODES_PER_BLOCK (67,108,864); larger
+ * sizes are refused with RG_E_SIZE before any device work.  For callers that
+ * must not allocate at that moment (a serving loop whose HBM budget is fully
+ * reserved; an engine that accounts its own device memory).  Synchronous, on
+ * the legacy default stream: the arrays must be complete when it is called.
+ * Nothing in the scratch needs to start at zero (each call overwrites the
+ * partials it reads); the scratch is shared per device, so calls that
+ * overlap in time on one device race and must be serialised by the caller.
+ * The first call on a device looks the scratch address up
+ * (cudaGetSymbolAddress); make it before starting any stream capture on that
+ * device.  No counterpart in the reference (its energy sums are host loops). */
+#define RG_NOALLOC_NODES_PER_BLOCK 1024
+#define RG_NOALLOC_MAX_BLOCKS 65536
+int rg_kinetic_energy_noalloc(int device, int numnod, const double *d_v,
+                              const double *d_ms, double *ekin);
 
 /* ---- Batched jobs -------------------------------------------------------
  * A batch advances many finalized contexts (independent models, "jobs") of
