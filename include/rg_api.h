@@ -163,12 +163,18 @@ int rg_info(rg_ctx *ctx, int *numnod, int *numels, int *numelc, int *lsky,
             unsigned long long *device_bytes);
 /* Mean device time per launch (ms) of each kernel class over the last
  * rg_cycle call when timing is enabled: [0] hexa, [1] shell, [2] dt,
- * [3] node.  rg_set_timing(ctx, 1) enables event timing (no graph). */
+ * [3] node.  rg_set_timing(ctx, 1) enables event timing (no graph); once
+ * rg_time_cycles_cold has run, each timed cycle starts from cold L2. */
 int rg_set_timing(rg_ctx *ctx, int on);
 int rg_kernel_times(rg_ctx *ctx, double *ms4);
 /* Advance ncycle cycles (graph launches) bracketed by CUDA events recorded
  * on the context's stream; *ms = device time of the whole span. */
 int rg_time_cycles(rg_ctx *ctx, int ncycle, double *ms);
+/* Same, each cycle preceded by a write of flush_bytes (> L2) to a buffer of
+ * the context, outside the timed spans: *ms = sum of the per-cycle device
+ * times, every cycle starting from cold L2. */
+int rg_time_cycles_cold(rg_ctx *ctx, int ncycle, unsigned long long flush_bytes,
+                        double *ms);
 
 /* Kinetic energy 0.5*sum(MS*|V|^2) of caller-owned DEVICE arrays V(3,numnod)
  * and MS(numnod) on CUDA device `device`, without allocating device memory:

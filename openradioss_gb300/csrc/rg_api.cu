@@ -438,6 +438,7 @@ int rg_ctx_destroy(rg_ctx *c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   shell_free(c->shells);
   for (void *p : c->allocs) cudaFree(p);
+  if (c->d_flush) cudaFree(c->d_flush);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
@@ -776,6 +777,8 @@ int rg_cycle(rg_ctx *c, int ncycle) {
   // timed path: the same launches, bracketed by events per kernel class
   double acc[4] = {0, 0, 0, 0};
   for (int i = 0; i < ncycle; i++) {
+    // after rg_time_cycles_cold: each timed cycle starts from cold L2 too
+    if (c->d_flush) cudaMemsetAsync(c->d_flush, i & 0xff, c->flush_bytes, c->stream);
     cudaEventRecord(c->ev[0], c->stream);
     const DtPartials dp = c->dp;
     for (auto &g : c->hg) {
@@ -1053,6 +1056,34 @@ int rg_time_cycles(rg_ctx *c, int ncycle, double *ms) {
   float f = 0;
   RG_CUDA(c, cudaEventElapsedTime(&f, c->ev[5], c->ev[6]));
   *ms = f;
+  return RG_OK;
+}
+
+int rg_time_cycles_cold(rg_ctx *c, int ncycle, unsigned long long flush_bytes, double *ms) {
+  if (!c || !ms || ncycle < 0) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  if (flush_bytes > c->flush_bytes) {
+    if (c->d_flush) RG_CUDA(c, cudaFree(c->d_flush));
+    c->d_flush = nullptr;
+    c->flush_bytes = 0;
+    RG_CUDA(c, cudaMalloc(&c->d_flush, flush_bytes));
+    c->flush_bytes = flush_bytes;
+  }
+  double tot = 0.0;
+  for (int i = 0; i < ncycle; i++) {
+    // overwrite a buffer larger than L2 so the cycle starts from cold L2
+    if (flush_bytes)
+      RG_CUDA(c, cudaMemsetAsync(c->d_flush, i & 0xff, flush_bytes, c->stream));
+    RG_CUDA(c, cudaEventRecord(c->ev[5], c->stream));
+    RG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+    RG_CUDA(c, cudaEventRecord(c->ev[6], c->stream));
+    RG_CUDA(c, cudaEventSynchronize(c->ev[6]));
+    float f = 0;
+    RG_CUDA(c, cudaEventElapsedTime(&f, c->ev[5], c->ev[6]));
+    tot += f;
+  }
+  *ms = tot;
   return RG_OK;
 }
 

@@ -81,5 +81,7 @@ struct rg_ctx {
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
   cudaEvent_t ev[8] = {};
+  void *d_flush = nullptr;     // L2 flush buffer of rg_time_cycles_cold
+  size_t flush_bytes = 0;
 };
 

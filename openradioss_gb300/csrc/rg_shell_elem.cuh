@@ -360,6 +360,9 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     const R a1 = ym / ((R)RG_ONE - nu * nu);
     const R a2 = a1 * nu;
     const R epdr = smax(PC(eps0) * dt1, (R)RG_EM20);
+    // LOG(EPSP/EPDR) of the previous point: the points usually share one
+    // strain rate (ASRATE = 1), and an equal argument gives the same value
+    R memo_epsp = (R)-1, memo_log = (R)0;
 #pragma unroll
     for (int it = 0; it < NPT; it++) {
       const R thkly = (R)c_wf[NPT - 1][it];
@@ -394,7 +397,14 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         if (P.israte == 0 && P.vp == 2)
           epsp = smax(smax(fabs(depsxx), fabs(depsyy)), (R)RG_HALF * fabs(depsxy));
         epsp = smax(epsp, epdr);
-        const R logep = log(epsp / epdr);
+        R logep;
+        if (epsp == memo_epsp) {
+          logep = memo_log;
+        } else {
+          logep = log(epsp / epdr);
+          memo_epsp = epsp;
+          memo_log = logep;
+        }
         R q = ((R)RG_ONE + PC(cc) * logep);
         q = smax(q, (R)RG_EM20);
         ca = ca * q;

@@ -188,6 +188,14 @@ class Engine:
     def set_timing(self, on):
         self._chk(self.L.rg_set_timing(self.h, 1 if on else 0), "rg_set_timing")
 
+    def time_cycles_cold(self, n, flush_bytes=256 << 20):
+        """Run n cycles, each after overwriting flush_bytes (more than the L2)
+        outside the timed span; returns the summed device time in ms."""
+        ms = C.c_double()
+        self._chk(self.L.rg_time_cycles_cold(self.h, int(n), int(flush_bytes), C.byref(ms)),
+                  "rg_time_cycles_cold")
+        return ms.value
+
     def time_cycles(self, n):
         """Run n cycles between two CUDA events on the context stream and
         return the device time in ms."""
