@@ -269,6 +269,36 @@ __global__ void batch_init_ncyc(const BatchJob<ER> *jobs, int n, int *ncyc) {
   if (j < n) ncyc[j] = jobs[j].T->ncycle;
 }
 
+// Node phase as its own kernel (three-launch schedule): the node update has
+// few live values, so this kernel runs at full occupancy where the fused
+// kernel is held to the element phase's register budget.  node_update's
+// arithmetic is written with explicit rounding (no contraction), so the
+// result is bitwise that of the fused kernel's node phase.
+template <typename ER>
+__global__ void __launch_bounds__(256)
+batch_node_kernel(const BatchDev<ER> B) {
+  constexpr bool F64 = sizeof(ER) == 8;
+  const int t = blockIdx.x;  // one node tile per block row of 256 threads
+  for (int tile = t; tile < B.nntiles; tile += gridDim.x) {
+    const BatchNodeTile nt = B.ntl[tile];
+    if (!__ldcg(B.ran + nt.job)) continue;
+    const BatchJob<ER> &J = B.jobs[nt.job];
+    const int nn = J.nv.numnod;
+    const int span = B.knode * BNT;
+    for (int i = threadIdx.x; i < span; i += 256) {
+      const int n = nt.n0 + i;
+      if (n < nn) {
+        if (J.rot)
+          node_update<F64, true, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls,
+                                       J.status, n);
+        else
+          node_update<F64, false, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls,
+                                        J.status, n);
+      }
+    }
+  }
+}
+
 // The node counter is reset by the first phase of the next cycle's launch
 // sequence: a separate one-thread kernel keeps the rule simple for both
 // schedules.
@@ -514,7 +544,7 @@ int enqueue(rg_batch *b) {
   } else {
     kern<<<std::min(grid, std::max(1, b->ntiles)), BNT, 0, b->stream>>>(D, 1);
     kern<<<std::min(grid, std::max(1, b->njobs)), BNT, 0, b->stream>>>(D, 2);
-    kern<<<std::min(grid, std::max(1, b->nntiles)), BNT, 0, b->stream>>>(D, 4);
+    batch_node_kernel<ER><<<std::max(1, b->nntiles), 256, 0, b->stream>>>(D);
   }
   RB_CUDA(b, cudaGetLastError());
   return RG_OK;

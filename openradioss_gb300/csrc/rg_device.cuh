@@ -135,6 +135,7 @@ struct HexaParams {
   // LAW2 Johnson-Cook (mat_param%uparam / iparam)
   double ca, cb, cn, epmx, sigm0, cc, epdr, asrate, z3;
   int icc, vp, israte, pad;
+  double inv_rho0;         // 1/RHO0 (group constant)
   // FP32 copies of the coefficients above (the same round-to-nearest
   // conversion, done once on the host) for the mixed form, and the two
   // branch flags CC /= 0, N == 1 evaluated on the FP64 values
@@ -146,6 +147,7 @@ struct HexaParams {
 };
 
 inline void hexa_params_mirror(HexaParams &P) {
+  P.inv_rho0 = 1.0 / P.rho0;
   P.f.rho0 = (float)P.rho0;
   P.f.g = (float)P.g;
   P.f.c1 = (float)P.c1;

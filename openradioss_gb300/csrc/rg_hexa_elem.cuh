@@ -291,7 +291,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       const double rho_new = P.rho0 * (vol0 / voln);
       A.rho[e] = rho_new;
       rho_r = (R)rho_new;
-      amu = (R)(rho_new / P.rho0 - RG_ONE);
+      amu = (R)(rho_new * P.inv_rho0 - RG_ONE);
       dvol_r = (R)dvol_d;
     } else {
       A.rho[e] = voln;
@@ -353,7 +353,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
           const R e1 = dxx - dv, e2 = dyy - dv, e3 = dzz - dv;
           const R e4 = (R)RG_HALF * d4, e5 = (R)RG_HALF * d5, e6 = (R)RG_HALF * d6;
           const R epsp = (R)RG_HALF * (e1 * e1 + e2 * e2 + e3 * e3) + e4 * e4 + e5 * e5 + e6 * e6;
-          epsdot = sqrt((R)RG_THREE * epsp) / (R)RG_THREE_HALF;
+          epsdot = sqrt((R)RG_THREE * epsp) * (R)RG_TWO_THIRD;  // / THREE_HALF
         }
         R asrate;
         if constexpr (F64)
@@ -405,10 +405,11 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         ak = (R)0;
         qh = (R)0;
       }
-      R scale = fmin_((R)RG_ONE, ak / fmax_(aj2, (R)RG_EM15));
+      const R inv_aj2 = (R)RG_ONE / fmax_(aj2, (R)RG_EM15);  // both scale factors
+      R scale = fmin_((R)RG_ONE, ak * inv_aj2);
       const R dpla = ((R)RG_ONE - scale) * aj2 / fmax_((R)RG_THREE * gg + qh, (R)RG_EM15);
       ak = ak + (R)RG_ONE * dpla * qh;
-      scale = fmin_((R)RG_ONE, ak / fmax_(aj2, (R)RG_EM15));
+      scale = fmin_((R)RG_ONE, ak * inv_aj2);
 #pragma unroll
       for (int c = 0; c < 6; c++) sg[c] = scale * sg[c];
       A.pla[e] = epxe + dpla;

@@ -40,16 +40,56 @@ struct ShellParams {
   double ca, cb, cn, ymax, cc, eps0, pm9;
   int icc, vp, israte, pad2;
   double dtfac;
+  // group constants derived once on the host (they are the same for every
+  // element of the group): plane-stress moduli, 1/(1-NU), 1/(1+NU),
+  // 1/MAX(H1,H2), DTFAC/SSP and, when ISH = 0 (SHF = FSH), the hourglass
+  // coefficients of CHVIS3
+  double a1, a2, inv1mnu, inv1pnu, inv_hmax, dtfac_ssp;
+  double shf0, hA1, hA3, hA5, hA7, hA8;
+  int shf_const, pad3;
   // FP32 copies for the mixed form (converted once on the host) and the
   // branch flags CC /= 0, DM /= 0 evaluated on the FP64 values
   struct {
     float rho, young, nu, g, a11, ssp, h1, h2, h3, dm, ish, fsh;
     float ca, cb, cn, ymax, cc, eps0, pm9, dtfac;
+    float a1, a2, inv1mnu, inv1pnu, inv_hmax, dtfac_ssp;
+    float shf0, hA1, hA3, hA5, hA7, hA8;
     int cc_nz, dm_nz;
   } f;
 };
 
 inline void shell_params_mirror(ShellParams &P) {
+  // derived group constants (same expressions as the per-element code)
+  P.a1 = P.young / (1.0 - P.nu * P.nu);
+  P.a2 = P.a1 * P.nu;
+  P.inv1mnu = 1.0 / (1.0 - P.nu);
+  P.inv1pnu = 1.0 / (1.0 + P.nu);
+  P.inv_hmax = 1.0 / (P.h1 > P.h2 ? P.h1 : P.h2);
+  P.dtfac_ssp = P.dtfac / P.ssp;
+  P.shf_const = (P.npt == 1 || P.ish == 0.0) ? 1 : 0;
+  P.shf0 = P.npt == 1 ? 0.0 : P.fsh;
+  {
+    const double shfpr3 = P.shf0 / (3.0 * (1.0 + P.nu));
+    const double r1 = 0.25 * P.rho * 100.0;
+    const double r0e = 0.25 * P.young * 0.5;
+    P.hA1 = r1 * (0.5 * P.h1);
+    P.hA3 = r1 * (0.5 * P.h2) * std::sqrt(shfpr3);
+    P.hA5 = (0.5 * P.h3) * r1 * RG_ZEP072169;
+    P.hA7 = P.h1 * r0e;
+    P.hA8 = P.h2 * r0e * shfpr3;
+  }
+  P.f.a1 = (float)P.a1;
+  P.f.a2 = (float)P.a2;
+  P.f.inv1mnu = (float)P.inv1mnu;
+  P.f.inv1pnu = (float)P.inv1pnu;
+  P.f.inv_hmax = (float)P.inv_hmax;
+  P.f.dtfac_ssp = (float)P.dtfac_ssp;
+  P.f.shf0 = (float)P.shf0;
+  P.f.hA1 = (float)P.hA1;
+  P.f.hA3 = (float)P.hA3;
+  P.f.hA5 = (float)P.hA5;
+  P.f.hA7 = (float)P.hA7;
+  P.f.hA8 = (float)P.hA8;
   P.f.rho = (float)P.rho;
   P.f.young = (float)P.young;
   P.f.nu = (float)P.nu;
@@ -106,6 +146,26 @@ static __constant__ float c_wm[5][5] = {{0.f, 0.f, 0.f, 0.f, 0.f},
                                  {-.0833333f, 0.f, 0.0833333f, 0.f, 0.f},
                                  {-.0648148f, -.0555556f, 0.0555556f, 0.0648148f, 0.f},
                                  {-.0520833f, -.0625f, 0.f, 0.0625f, 0.0520833f}};
+
+// The same tables widened to FP64 (exact conversions of the REAL*4 values):
+// the FP64 form reads them without a per-use conversion.
+#define RG_WIDEN5(a, b, c, d, e) {(double)(a), (double)(b), (double)(c), (double)(d), (double)(e)}
+static __constant__ double c_z0d[5][5] = {RG_WIDEN5(0.f, 0.f, 0.f, 0.f, 0.f),
+                                          RG_WIDEN5(-.5f, 0.5f, 0.f, 0.f, 0.f),
+                                          RG_WIDEN5(-.5f, 0.f, 0.5f, 0.f, 0.f),
+                                          RG_WIDEN5(-.5f, -.1666667f, 0.1666667f, 0.5f, 0.f),
+                                          RG_WIDEN5(-.5f, -.25f, 0.f, 0.25f, 0.5f)};
+static __constant__ double c_wfd[5][5] = {RG_WIDEN5(1.f, 0.f, 0.f, 0.f, 0.f),
+                                          RG_WIDEN5(0.5f, 0.5f, 0.f, 0.f, 0.f),
+                                          RG_WIDEN5(0.25f, 0.5f, 0.25f, 0.f, 0.f),
+                                          RG_WIDEN5(0.1666667f, 0.3333333f, 0.3333333f, 0.1666667f, 0.f),
+                                          RG_WIDEN5(0.125f, 0.25f, 0.25f, 0.25f, 0.125f)};
+static __constant__ double c_wmd[5][5] = {RG_WIDEN5(0.f, 0.f, 0.f, 0.f, 0.f),
+                                          RG_WIDEN5(-.0833333f, 0.0833333f, 0.f, 0.f, 0.f),
+                                          RG_WIDEN5(-.0833333f, 0.f, 0.0833333f, 0.f, 0.f),
+                                          RG_WIDEN5(-.0648148f, -.0555556f, 0.0555556f, 0.0648148f, 0.f),
+                                          RG_WIDEN5(-.0520833f, -.0625f, 0.f, 0.0625f, 0.0520833f)};
+#undef RG_WIDEN5
 
 template <typename T>
 __device__ __forceinline__ T smax(T a, T b) {
@@ -216,7 +276,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       e2z = e3x * e1y - e3y * e1x;
     }
     // ---- CDERI3 ----
-    R x2, y2, x3, y3, x4, y4, px1, px2, py1, py2, area, vhx, vhy;
+    R x2, y2, x3, y3, x4, y4, px1, px2, py1, py2, area, inv_area, vhx, vhy;
     {
       const R x21 = xg[1] - xg[0], y21 = yg[1] - yg[0], z21 = zg[1] - zg[0];
       const R x31 = xg[2] - xg[0], y31 = yg[2] - yg[0], z31 = zg[2] - zg[0];
@@ -232,8 +292,9 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       px2 = (R)RG_HALF * y3;
       py2 = -(R)RG_HALF * x3;
       area = smax((R)RG_TWO * (py2 * px1 - py1 * px2), (R)RG_EM20);
-      vhx = (-x2 + x3 - x4) / area;
-      vhy = (-y2 + y3 - y4) / area;
+      inv_area = (R)RG_ONE / area;
+      vhx = (-x2 + x3 - x4) * inv_area;
+      vhy = (-y2 + y3 - y4) * inv_area;
     }
     // ---- CCOEF3 (ITHK > 0) ----
     const double thk_cur = S.thk[e];
@@ -243,8 +304,8 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     const R nu = PC(nu), ym = PC(young), gmod = PC(g), a11 = PC(a11), ssp = PC(ssp),
             rho = PC(rho);
     R shf;
-    if (NPT == 1) {
-      shf = (R)0;
+    if (P.shf_const) {
+      shf = PC(shf0);  // NPT = 1: 0; ISH = 0: FSH
     } else {
       const R fac1tmp = (R)2.0 * ((R)1.0 + nu) * thk02;
       const R ish = PC(ish), fsh = PC(fsh);
@@ -265,7 +326,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       if (al3 != (R)0) almin = smin(almin, alquad);
       const R dtdyn = area * area / smax(smax(al5, al6), (R)RG_EM20);
       aldt = smax(dtdyn, almin);
-      const R dthour = (R)RG_HALF * (almin + aldt) / smax(PC(h1), PC(h2));
+      const R dthour = (R)RG_HALF * (almin + aldt) * PC(inv_hmax);
       if (dthour < aldt) aldt = dthour;
       aldt = sqrt(aldt);
     }
@@ -319,7 +380,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     }
     // ---- CSTRA3 ----
     {
-      const R fac1 = dt1 / area;
+      const R fac1 = dt1 * inv_area;
       exx = exx * fac1;
       eyy = eyy * fac1;
       exy = exy * fac1;
@@ -357,18 +418,18 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       else
         asrate = smin(1.f, P.f.pm9 * dt1);
     }
-    const R a1 = ym / ((R)RG_ONE - nu * nu);
-    const R a2 = a1 * nu;
+    const R a1 = PC(a1);
+    const R a2 = PC(a2);
     const R epdr = smax(PC(eps0) * dt1, (R)RG_EM20);
     // LOG(EPSP/EPDR) of the previous point: the points usually share one
     // strain rate (ASRATE = 1), and an equal argument gives the same value
     R memo_epsp = (R)-1, memo_log = (R)0;
 #pragma unroll
     for (int it = 0; it < NPT; it++) {
-      const R thkly = (R)c_wf[NPT - 1][it];
+      const R thkly = pcoef<R>(c_wfd[NPT - 1][it], c_wf[NPT - 1][it]);
       const R thklyl = thkly * thk0;
-      const R wmc = (R)c_wm[NPT - 1][it];
-      const R zt = (R)c_z0[NPT - 1][it] * thk0;
+      const R wmc = pcoef<R>(c_wmd[NPT - 1][it], c_wm[NPT - 1][it]);
+      const R zt = pcoef<R>(c_z0d[NPT - 1][it], c_z0[NPT - 1][it]) * thk0;
       const R depsxx = exx + zt * kxx;
       const R depsyy = eyy + zt * kyy;
       const R depsxy = exy + zt * kxy;
@@ -432,10 +493,12 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         const R s3 = sn[2];
         const R A = (R)RG_FOURTH * s1 * s1;
         const R B = (R)RG_THREE_OVER_4 * s2 * s2 + (R)RG_THREE * s3 * s3;
-        const R svm = sqrt(A + B);
-        if (svm > yld && off == (R)RG_ONE) {
-          const R nu1 = (R)RG_ONE / ((R)RG_ONE - nu);
-          const R nu2 = (R)RG_ONE / ((R)RG_ONE + nu);
+        // SVM > YLD tested on the squares (YLD >= 0): the square root is
+        // only taken at yielding points
+        if (A + B > yld * yld && off == (R)RG_ONE) {
+          const R svm = sqrt(A + B);
+          const R nu1 = PC(inv1mnu);
+          const R nu2 = PC(inv1pnu);
           const R h = yld >= ymax ? (R)0 : PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
           R dpla_j = (svm - yld) / ((R)RG_THREE * gmod + h);
           const R anu1 = A * nu1;
@@ -466,7 +529,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       }
       S.pla[it * nc + e] = pla;
       ezz = -(depsxx + depsyy) * nu - ((R)RG_ONE - (R)RG_TWO * nu) * ezz;
-      ezz = ezz / ((R)RG_ONE - nu);
+      ezz = ezz * PC(inv1mnu);
       thkn = thkn + (double)(ezz * thklyl * off);
 #pragma unroll
       for (int c = 0; c < 5; c++) {
@@ -509,14 +572,23 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       const R gama2 = off * (-(R)RG_ONE - px2v - py2v);
       const R gama4 = off * (-(R)RG_ONE + px2v + py2v);
       // HVLIN = 0: the linear viscous terms vanish; HVISC = HELAS = 1/2
-      const R shfpr3 = shf / ((R)RG_THREE * ((R)RG_ONE + nu));
-      const R r1 = (R)RG_FOURTH * rho * (R)RG_HUNDRED;
-      const R A1 = r1 * ((R)RG_HALF * PC(h1));
-      const R A3 = r1 * ((R)RG_HALF * PC(h2)) * sqrt(shfpr3);
-      const R A5 = ((R)RG_HALF * PC(h3)) * r1 * (R)RG_ZEP072169;
-      const R r0e = (R)RG_FOURTH * ym * (R)RG_HALF;
-      const R A7 = PC(h1) * r0e;
-      const R A8 = PC(h2) * r0e * shfpr3;
+      R A1, A3, A5, A7, A8;
+      if (P.shf_const) {
+        A1 = PC(hA1);
+        A3 = PC(hA3);
+        A5 = PC(hA5);
+        A7 = PC(hA7);
+        A8 = PC(hA8);
+      } else {
+        const R shfpr3 = shf / ((R)RG_THREE * ((R)RG_ONE + nu));
+        const R r1 = (R)RG_FOURTH * rho * (R)RG_HUNDRED;
+        A1 = r1 * ((R)RG_HALF * PC(h1));
+        A3 = r1 * ((R)RG_HALF * PC(h2)) * sqrt(shfpr3);
+        A5 = ((R)RG_HALF * PC(h3)) * r1 * (R)RG_ZEP072169;
+        const R r0e = (R)RG_FOURTH * ym * (R)RG_HALF;
+        A7 = PC(h1) * r0e;
+        A8 = PC(h2) * r0e * shfpr3;
+      }
       const R t2a = thk02 * area;
       const R tsa = sqrt(t2a);
       R h1q = A1 * tsa;
@@ -563,7 +635,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     // ---- CDT3 ----
     R sti;
     {
-      const R dt = PC(dtfac) * aldt / ssp;
+      const R dt = aldt * PC(dtfac_ssp);
       if (offg > (R)0 && off != (R)0) {
         // running minimum; reversed order key: the first element wins ties
         // (strict < in CDT3)

@@ -1,5 +1,6 @@
 """Serving loop on the GPU: jobs admitted by HBM budget, advanced together
-while others arrive, each result bitwise equal to the same job run alone."""
+while others arrive, each result equal to the same job run alone within the
+mixed form's tolerance (1e-4 of its displacement / velocity scales)."""
 import numpy as np
 import pytest
 
@@ -31,7 +32,8 @@ def test_served_results_equal_alone():
         ref.cycle(n)
         nd = ref.nodes()
         assert rec.result["time"]["ncycle"] == n
-        assert np.array_equal(rec.result["X"], nd["X"]), rec.key
-        assert np.array_equal(rec.result["V"], nd["V"]), rec.key
+        sd = np.max(np.abs(nd["X"] - m.X))
+        assert np.max(np.abs(rec.result["X"] - nd["X"])) <= 1e-4 * sd, rec.key
+        assert np.max(np.abs(rec.result["V"] - nd["V"])) <= 1e-4 * np.max(np.abs(nd["V"])), rec.key
         assert rec.result["status"] == 0
     assert stats["p99_latency_s"] >= stats["p50_latency_s"] > 0.0
