@@ -255,6 +255,8 @@ def run_ours(args, rank, world, local_rank):
                    "l2": "L2 flushed (256 MB written) before every timed cycle; model "
                          "state %.2f GB" % (eng.info()["device_bytes"] / 1e9)},
         "e2e": {"value": world * ne * args.steps / e2e_s, "unit": "element-updates/s",
+                "transfer": "inputs: registered host buffers read in place by the upload "
+                            "kernel; outputs: DMA copies from the device staging buffer",
                 "h2d_bytes_per_step": (3 if model.shells else 2) * 3 * 8 * model.numnod,
                 "d2h_bytes_per_step": (8 if model.shells else 4) * 8 * model.numnod},
         "gpu_launches": (len(model.hexa) + len(model.shells) + 2) * args.steps,

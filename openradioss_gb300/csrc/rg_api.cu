@@ -82,23 +82,25 @@ __global__ void refresh_copies_kernel(NodeView N, int rot) {
   }
 }
 
-// Assembled forces only (ASSPAR4 sums) into a staging buffer:
-// F(3,n) | STIFN(n) | FR(3,n) | STIFR(n).
+// Assembled forces only (ASSPAR4 sums), written to F(3,n), STIFN(n),
+// FR(3,n), STIFR(n) -- registered host memory or the staging buffer; any
+// output may be null.
 template <typename ST, bool ROT>
 __global__ void assemble_kernel(int numnod, const int *__restrict__ adsky,
                                 const ST *__restrict__ fsky,
-                                const ST *__restrict__ fskyr,
-                                double *__restrict__ out) {
+                                const ST *__restrict__ fskyr, double *__restrict__ f,
+                                double *__restrict__ stifn, double *__restrict__ fr,
+                                double *__restrict__ stifr) {
   const int n = blockIdx.x * NODE_NT + threadIdx.x;
   if (n >= numnod) return;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0, st = 0.0;
   double r0 = 0.0, r1 = 0.0, r2 = 0.0, sr = 0.0;
   for (int k = adsky[n]; k < adsky[n + 1]; k++) {
-    const ST f = fsky[k];
-    a0 = __dadd_rn(a0, (double)f.x);
-    a1 = __dadd_rn(a1, (double)f.y);
-    a2 = __dadd_rn(a2, (double)f.z);
-    st = __dadd_rn(st, (double)f.w);
+    const ST q = fsky[k];
+    a0 = __dadd_rn(a0, (double)q.x);
+    a1 = __dadd_rn(a1, (double)q.y);
+    a2 = __dadd_rn(a2, (double)q.z);
+    st = __dadd_rn(st, (double)q.w);
     if (ROT) {
       const ST g = fskyr[k];
       r0 = __dadd_rn(r0, (double)g.x);
@@ -107,14 +109,20 @@ __global__ void assemble_kernel(int numnod, const int *__restrict__ adsky,
       sr = __dadd_rn(sr, (double)g.w);
     }
   }
-  out[3 * n] = a0;
-  out[3 * n + 1] = a1;
-  out[3 * n + 2] = a2;
-  out[3 * numnod + n] = st;
-  out[4 * numnod + 3 * n] = r0;
-  out[4 * numnod + 3 * n + 1] = r1;
-  out[4 * numnod + 3 * n + 2] = r2;
-  out[7 * numnod + n] = sr;
+  if (f) {
+    f[3 * n] = a0;
+    f[3 * n + 1] = a1;
+    f[3 * n + 2] = a2;
+  }
+  if (stifn) stifn[n] = st;
+  if (ROT) {
+    if (fr) {
+      fr[3 * n] = r0;
+      fr[3 * n + 1] = r1;
+      fr[3 * n + 2] = r2;
+    }
+    if (stifr) stifr[n] = sr;
+  }
 }
 
 // Time-step kernel: fixed-order reduction of the per-block element minima
@@ -181,16 +189,42 @@ __global__ void energy_final(const double *__restrict__ part, int nextra,
 }
 
 // AoS X(3,n) -> X4.xyz (keeps .w); same for V and VR.
-__global__ void pack3_kernel(int n, const double *__restrict__ src,
-                             dbl4 *__restrict__ dst) {
+// FORINT-level upload: X, V and (shell models) VR, xyz interleaved, read
+// straight from registered host memory (or from the staging buffer) into the
+// node records, and the mixed form's FP32 copies refreshed in the same pass.
+__global__ void upload_nodes_kernel(NodeView N, const double *__restrict__ x,
+                                    const double *__restrict__ v,
+                                    const double *__restrict__ vr, int mixed,
+                                    Time *__restrict__ T, double dt1) {
   const int i = blockIdx.x * NODE_NT + threadIdx.x;
-  if (i >= n) return;
-  dbl4 t = dst[i];
-  t.x = src[3 * i];
-  t.y = src[3 * i + 1];
-  t.z = src[3 * i + 2];
-  dst[i] = t;
+  if (i == 0) T->dt2 = dt1;  // DT1 of this call: the element kernels read Time::dt2
+  if (i >= N.numnod) return;
+  dbl4 a = N.X4[i], b = N.V4[i];
+  a.x = x[3 * i];
+  a.y = x[3 * i + 1];
+  a.z = x[3 * i + 2];
+  b.x = v[3 * i];
+  b.y = v[3 * i + 1];
+  b.z = v[3 * i + 2];
+  N.X4[i] = a;
+  N.V4[i] = b;
+  if (mixed) {
+    N.XF[i] = split_hilo(a.x, a.y, a.z);
+    N.VF[i] = make_float4(__double2float_rn(b.x), __double2float_rn(b.y),
+                          __double2float_rn(b.z), 0.f);
+  }
+  if (vr) {
+    dbl4 w = N.VR4[i];
+    w.x = vr[3 * i];
+    w.y = vr[3 * i + 1];
+    w.z = vr[3 * i + 2];
+    N.VR4[i] = w;
+    if (mixed)
+      N.VRF[i] = make_float4(__double2float_rn(w.x), __double2float_rn(w.y),
+                             __double2float_rn(w.z), 0.f);
+  }
 }
+
 __global__ void unpack3_kernel(int n, const dbl4 *__restrict__ src,
                                double *__restrict__ dst) {
   const int i = blockIdx.x * NODE_NT + threadIdx.x;
@@ -377,22 +411,24 @@ int enqueue_nodes(rg_ctx *c) {
   return RG_OK;
 }
 
-int enqueue_assemble(rg_ctx *c, double *out) {
+int enqueue_assemble(rg_ctx *c, double *f, double *stifn, double *fr, double *stifr) {
   const int nb = (c->numnod + NODE_NT - 1) / NODE_NT;
   if (c->prec == RG_PREC_FP64) {
     if (c->rot)
       assemble_kernel<dbl4, true><<<nb, NODE_NT, 0, c->stream>>>(
-          c->numnod, c->d_adsky, (const dbl4 *)c->d_fsky, (const dbl4 *)c->d_fskyr, out);
+          c->numnod, c->d_adsky, (const dbl4 *)c->d_fsky, (const dbl4 *)c->d_fskyr, f, stifn,
+          fr, stifr);
     else
       assemble_kernel<dbl4, false><<<nb, NODE_NT, 0, c->stream>>>(
-          c->numnod, c->d_adsky, (const dbl4 *)c->d_fsky, nullptr, out);
+          c->numnod, c->d_adsky, (const dbl4 *)c->d_fsky, nullptr, f, stifn, fr, stifr);
   } else {
     if (c->rot)
       assemble_kernel<float4, true><<<nb, NODE_NT, 0, c->stream>>>(
-          c->numnod, c->d_adsky, (const float4 *)c->d_fsky, (const float4 *)c->d_fskyr, out);
+          c->numnod, c->d_adsky, (const float4 *)c->d_fsky, (const float4 *)c->d_fskyr, f,
+          stifn, fr, stifr);
     else
       assemble_kernel<float4, false><<<nb, NODE_NT, 0, c->stream>>>(
-          c->numnod, c->d_adsky, (const float4 *)c->d_fsky, nullptr, out);
+          c->numnod, c->d_adsky, (const float4 *)c->d_fsky, nullptr, f, stifn, fr, stifr);
   }
   return RG_OK;
 }
@@ -439,6 +475,7 @@ int rg_ctx_destroy(rg_ctx *c) {
   shell_free(c->shells);
   for (void *p : c->allocs) cudaFree(p);
   if (c->d_flush) cudaFree(c->d_flush);
+  if (c->h_time) cudaFreeHost(c->h_time);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
@@ -742,6 +779,7 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     RG_CUDA(c, cudaMemcpy(c->d_walls, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   if ((r = dalloc(c, &c->d_stage, 12 * (size_t)numnod + 16))) return r;
+  RG_CUDA(c, cudaMallocHost((void **)&c->h_time, sizeof(Time)));
   if ((r = dalloc(c, &c->d_epart, 4 * EN_BLOCKS + 8))) return r;
   RG_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));  // uploads complete
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -826,6 +864,26 @@ int rg_host_unregister(rg_ctx *c, void *ptr) {
   return RG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Device address of a host buffer the kernels may access in place: memory
+// registered with rg_host_register (or device / managed memory); null for
+// ordinary pageable memory, which is staged instead.
+const double *device_view(const void *p) {
+  cudaPointerAttributes a;
+  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost) return (const double *)a.devicePointer;
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return (const double *)p;
+  return nullptr;
+}
+}  // namespace
+
+extern "C" {
+
 int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr,
                    double dt1, double *f, double *stifn, double *fr, double *stifr,
                    double *dt2t, int *neltst) {
@@ -834,44 +892,54 @@ int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr
   RG_CUDA(c, cudaSetDevice(c->device));
   const int n = c->numnod;
   const int nb = (n + NODE_NT - 1) / NODE_NT;
+  const size_t n3 = 3 * (size_t)n;
   double *st = c->d_stage;
-  RG_CUDA(c, cudaMemcpyAsync(st, x, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  pack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, st, c->nv.X4);
-  RG_CUDA(c, cudaMemcpyAsync(st + 3 * (size_t)n, v, 3 * (size_t)n * sizeof(double),
-                             cudaMemcpyHostToDevice, c->stream));
-  pack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, st + 3 * (size_t)n, c->nv.V4);
-  if (vr && c->rot) {
-    RG_CUDA(c, cudaMemcpyAsync(st + 6 * (size_t)n, vr, 3 * (size_t)n * sizeof(double),
-                               cudaMemcpyHostToDevice, c->stream));
-    pack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, st + 6 * (size_t)n, c->nv.VR4);
+  // Registered (pinned) host buffers are read and written by the kernels in
+  // place over the host link; other buffers go through the staging buffer.
+  const bool rot_in = vr && c->rot;
+  const double *dx = device_view(x), *dv = device_view(v);
+  const double *dvr = rot_in ? device_view(vr) : nullptr;
+  if (!dx) {
+    RG_CUDA(c, cudaMemcpyAsync(st, x, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    dx = st;
   }
-  if (c->prec == RG_PREC_MIXED)
-    refresh_copies_kernel<<<nb, NODE_NT, 0, c->stream>>>(c->nv, (vr && c->rot) ? 1 : 0);
-  // DT1 for this call: the element kernels read it from Time::dt2
-  RG_CUDA(c, cudaMemcpyAsync(&c->d_time->dt2, &dt1, sizeof(double), cudaMemcpyHostToDevice,
-                             c->stream));
+  if (!dv) {
+    RG_CUDA(c, cudaMemcpyAsync(st + n3, v, n3 * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
+    dv = st + n3;
+  }
+  if (rot_in && !dvr) {
+    RG_CUDA(c, cudaMemcpyAsync(st + 2 * n3, vr, n3 * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
+    dvr = st + 2 * n3;
+  }
+  upload_nodes_kernel<<<nb, NODE_NT, 0, c->stream>>>(
+      c->nv, dx, dv, dvr, c->prec == RG_PREC_MIXED ? 1 : 0, c->d_time, dt1);
   if (c->prec == RG_PREC_MIXED && c->numels > 0)
     launch_hexa_prev_volume(c->h32, c->nv, c->d_time, c->stream);
   enqueue_elements(c);
   dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time, c->d_status, 0);
-  enqueue_assemble(c, st);
+  // outputs: assembled into the staging buffer, returned by DMA copies (on
+  // the host link a copy engine writes host memory about twice as fast as
+  // kernel stores do)
+  double *of = st, *os = st + n3, *ofr = st + n3 + n, *osr = st + 2 * n3 + n;
+  enqueue_assemble(c, f ? of : nullptr, stifn ? os : nullptr, fr ? ofr : nullptr,
+                   stifr ? osr : nullptr);
   if (f)
-    RG_CUDA(c, cudaMemcpyAsync(f, st, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
-                               c->stream));
+    RG_CUDA(c, cudaMemcpyAsync(f, of, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (stifn)
-    RG_CUDA(c, cudaMemcpyAsync(stifn, st + 3 * (size_t)n, (size_t)n * sizeof(double),
-                               cudaMemcpyDeviceToHost, c->stream));
+    RG_CUDA(c, cudaMemcpyAsync(stifn, os, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (fr)
-    RG_CUDA(c, cudaMemcpyAsync(fr, st + 4 * (size_t)n, 3 * (size_t)n * sizeof(double),
-                               cudaMemcpyDeviceToHost, c->stream));
+    RG_CUDA(c, cudaMemcpyAsync(fr, ofr, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (stifr)
-    RG_CUDA(c, cudaMemcpyAsync(stifr, st + 7 * (size_t)n, (size_t)n * sizeof(double),
-                               cudaMemcpyDeviceToHost, c->stream));
-  Time t;
-  RG_CUDA(c, cudaMemcpyAsync(&t, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost, c->stream));
+    RG_CUDA(c, cudaMemcpyAsync(stifr, osr, n * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+  // the time-step record comes back through a pinned host copy
+  RG_CUDA(c, cudaMemcpyAsync(c->h_time, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost,
+                             c->stream));
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (dt2t) *dt2t = t.dt2t;
-  if (neltst) *neltst = t.neltst;
+  if (dt2t) *dt2t = c->h_time->dt2t;
+  if (neltst) *neltst = c->h_time->neltst;
   return RG_OK;
 }
 
@@ -906,7 +974,7 @@ int rg_download_forces(rg_ctx *c, double *f, double *stifn, double *fr) {
   RG_CUDA(c, cudaSetDevice(c->device));
   const int n = c->numnod;
   double *st = c->d_stage;
-  enqueue_assemble(c, st);
+  enqueue_assemble(c, st, st + 3 * (size_t)n, st + 4 * (size_t)n, st + 7 * (size_t)n);
   if (f)
     RG_CUDA(c, cudaMemcpyAsync(f, st, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (stifn)

@@ -82,6 +82,7 @@ struct rg_ctx {
   cudaGraph_t graph = nullptr;
   cudaEvent_t ev[8] = {};
   void *d_flush = nullptr;     // L2 flush buffer of rg_time_cycles_cold
+  Time *h_time = nullptr;      // pinned host copy of the time-step record
   size_t flush_bytes = 0;
 };
 
