@@ -103,6 +103,22 @@ class Clocks:
                 "samples": len(self.samples)}
 
 
+def reduce_max(x, device):
+    """Max of a per-rank scalar over the process group (replica timing: the
+    slowest rank sets the step time)."""
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, world, seconds):
+    """Whole-job throughput of N replicas: every rank processed
+    units_per_rank units in the (max over ranks) time."""
+    return world * units_per_rank / seconds
+
+
 def element_bytes(model, prec):
     """Algorithmic DRAM bytes of one element-kernel launch over the model,
     and per node of one node-kernel launch, from the implemented arrays
@@ -156,11 +172,7 @@ def run_ours(args, rank, world, local_rank):
             tdist.barrier()
 
     def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda:%d" % local_rank)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, "cuda:%d" % local_rank) if dist else x
 
     forms = [RG_PREC_FP64, RG_PREC_MIXED] if args.forms == "both" else (
         [RG_PREC_FP64] if args.forms == "f64" else [RG_PREC_MIXED])
@@ -217,8 +229,8 @@ def run_ours(args, rank, world, local_rank):
                 "kernel_ms": res["kt"], "e2e_s": e2e_s}
         return line
     res64, res32 = out[RG_PREC_FP64], out[RG_PREC_MIXED]
-    value = world * ne * args.steps / (res64["ms"] * 1e-3)
-    value32 = world * ne * args.steps / (res32["ms"] * 1e-3)
+    value = replica_value(ne * args.steps, world, res64["ms"] * 1e-3)
+    value32 = replica_value(ne * args.steps, world, res32["ms"] * 1e-3)
     kk = res64["kkey"]
     k64 = res64["kt"][kk]
     ach = res64["elem_bytes"] * ne / (k64 * 1e-3) / 1e9
