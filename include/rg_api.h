@@ -162,8 +162,8 @@ int rg_status(rg_ctx *ctx);
 int rg_info(rg_ctx *ctx, int *numnod, int *numels, int *numelc, int *lsky,
             unsigned long long *device_bytes);
 /* Mean device time per launch (ms) of each kernel class over the last
- * rg_cycle call when timing is enabled: [0] hexa, [1] shell, [2] dt,
- * [3] node.  rg_set_timing(ctx, 1) enables event timing (no graph); once
+ * rg_cycle call when timing is enabled: [0] hexa, [1] shell, [2] dt (0
+ * when the time-step reduction runs inside the element kernels), [3] node.  rg_set_timing(ctx, 1) enables event timing (no graph); once
  * rg_time_cycles_cold has run, each timed cycle starts from cold L2. */
 int rg_set_timing(rg_ctx *ctx, int on);
 int rg_kernel_times(rg_ctx *ctx, double *ms4);

@@ -375,19 +375,32 @@ int init_hexa_state(rg_ctx *c, HexaArrays<ER> &A) {
   return RG_OK;
 }
 
-// Enqueue the element phase (all groups) on the stream.
-int enqueue_elements(rg_ctx *c) {
+// Enqueue the element phase (all groups) on the stream, with the time-step
+// reduction fused into its last block (advance = 0: DT2T / NELTST only).  A
+// model without elements gets the stand-alone time-step kernel.
+int enqueue_elements(rg_ctx *c, int advance) {
   const DtPartials dp = c->dp;
+  if (c->nparts == 0) {
+    dt_kernel<<<1, DT_NT, 0, c->stream>>>(dp, 0, c->d_ngl_all, c->d_time, c->d_status, advance);
+    return RG_OK;
+  }
+  DtFinish F;
+  F.ctr = c->d_dtctr;
+  F.gdt = c->d_gdt;
+  F.gel = c->d_gel;
+  F.nparts = c->nparts;
+  F.advance = advance;
+  F.ngl = c->d_ngl_all;
   for (auto &g : c->hg) {
     if (c->prec == RG_PREC_FP64)
       launch_hexa_f64(g.P, c->h64, c->nv, (dbl4 *)c->d_fsky, dp, c->d_time,
-                      c->d_status, c->stream);
+                      c->d_status, F, c->stream);
     else
       launch_hexa_f32(g.P, c->h32, c->nv, (float4 *)c->d_fsky, dp, c->d_time,
-                      c->d_status, c->stream);
+                      c->d_status, F, c->stream);
   }
   shell_enqueue(c->shells, c->prec, c->nv, c->d_fsky, c->d_fskyr, dp, c->d_time,
-                c->d_status, c->stream);
+                c->d_status, F, c->stream);
   return RG_OK;
 }
 
@@ -434,9 +447,7 @@ int enqueue_assemble(rg_ctx *c, double *f, double *stifn, double *fr, double *st
 }
 
 int enqueue_cycle(rg_ctx *c) {
-  enqueue_elements(c);
-  dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time,
-                                        c->d_status, 1);
+  enqueue_elements(c, 1);
   enqueue_nodes(c);
   return RG_OK;
 }
@@ -778,6 +789,13 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     RG_CUDA(c, cudaMemcpy(c->d_wall, wn.data(), numnod * sizeof(int), cudaMemcpyHostToDevice));
     RG_CUDA(c, cudaMemcpy(c->d_walls, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
+  {
+    const int ng = (c->nparts + DT_GROUP - 1) / DT_GROUP;
+    if ((r = dalloc(c, &c->d_dtctr, ng + 1))) return r;
+    if ((r = dalloc(c, &c->d_gdt, std::max(ng, 1)))) return r;
+    if ((r = dalloc(c, &c->d_gel, std::max(ng, 1)))) return r;
+    RG_CUDA(c, cudaMemset(c->d_dtctr, 0, (ng + 1) * sizeof(unsigned)));
+  }
   if ((r = dalloc(c, &c->d_stage, 12 * (size_t)numnod + 16))) return r;
   RG_CUDA(c, cudaMallocHost((void **)&c->h_time, sizeof(Time)));
   if ((r = dalloc(c, &c->d_epart, 4 * EN_BLOCKS + 8))) return r;
@@ -819,20 +837,28 @@ int rg_cycle(rg_ctx *c, int ncycle) {
     if (c->d_flush) cudaMemsetAsync(c->d_flush, i & 0xff, c->flush_bytes, c->stream);
     cudaEventRecord(c->ev[0], c->stream);
     const DtPartials dp = c->dp;
+    DtFinish F;
+    F.ctr = c->d_dtctr;
+    F.gdt = c->d_gdt;
+    F.gel = c->d_gel;
+    F.nparts = c->nparts;
+    F.advance = 1;
+    F.ngl = c->d_ngl_all;
     for (auto &g : c->hg) {
       if (c->prec == RG_PREC_FP64)
-        launch_hexa_f64(g.P, c->h64, c->nv, (dbl4 *)c->d_fsky, dp, c->d_time, c->d_status,
+        launch_hexa_f64(g.P, c->h64, c->nv, (dbl4 *)c->d_fsky, dp, c->d_time, c->d_status, F,
                         c->stream);
       else
-        launch_hexa_f32(g.P, c->h32, c->nv, (float4 *)c->d_fsky, dp, c->d_time, c->d_status,
+        launch_hexa_f32(g.P, c->h32, c->nv, (float4 *)c->d_fsky, dp, c->d_time, c->d_status, F,
                         c->stream);
     }
     cudaEventRecord(c->ev[1], c->stream);
     shell_enqueue(c->shells, c->prec, c->nv, c->d_fsky, c->d_fskyr, dp, c->d_time, c->d_status,
-                  c->stream);
+                  F, c->stream);
     cudaEventRecord(c->ev[2], c->stream);
-    dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time,
-                                          c->d_status, 1);
+    // the time-step reduction runs inside the last element block
+    if (c->nparts == 0)
+      dt_kernel<<<1, DT_NT, 0, c->stream>>>(dp, 0, c->d_ngl_all, c->d_time, c->d_status, 1);
     cudaEventRecord(c->ev[3], c->stream);
     enqueue_nodes(c);
     cudaEventRecord(c->ev[4], c->stream);
@@ -917,8 +943,7 @@ int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr
       c->nv, dx, dv, dvr, c->prec == RG_PREC_MIXED ? 1 : 0, c->d_time, dt1);
   if (c->prec == RG_PREC_MIXED && c->numels > 0)
     launch_hexa_prev_volume(c->h32, c->nv, c->d_time, c->stream);
-  enqueue_elements(c);
-  dt_kernel<<<1, DT_NT, 0, c->stream>>>(c->dp, c->nparts, c->d_ngl_all, c->d_time, c->d_status, 0);
+  enqueue_elements(c, 0);
   // outputs: assembled into the staging buffer, returned by DMA copies (on
   // the host link a copy engine writes host memory about twice as fast as
   // kernel stores do)

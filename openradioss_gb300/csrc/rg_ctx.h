@@ -68,6 +68,9 @@ struct rg_ctx {
   int *d_status = nullptr;
   DtPartials dp{};
   int nparts = 0;
+  unsigned *d_dtctr = nullptr;  // fused dt: [1 + groups] completion counters
+  double *d_gdt = nullptr;      // fused dt: group minima
+  int *d_gel = nullptr;
   int *d_wall = nullptr;       // per node: wall index or -1
   double *d_walls = nullptr;   // 6 doubles per wall (p0, n)
   int nwalls = 0;

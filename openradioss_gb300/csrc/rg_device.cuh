@@ -65,6 +65,20 @@ struct DtPartials {
   int *el;  // user id of the element attaining it (-1 none)
 };
 
+// Time-step reduction fused into the element kernels, in two levels: the
+// block completing the last partial of a group of DT_GROUP partials reduces
+// that group; the block completing the last group (counted across all element
+// launches of the cycle) reduces the group minima and applies the RESOL logic.
+struct DtFinish {
+  unsigned *ctr;     // [1 + ngroups]: groups done, blocks done per group
+  double *gdt;       // [ngroups] group minima (64 partials per group)
+  int *gel;
+  int nparts;        // partials of the whole cycle
+  int advance;       // 0: record DT2T / NELTST only (FORINT-level call)
+  const int *ngl;    // element order key -> user id
+};
+constexpr int DT_GROUP = 64;  // partials per first-level group
+
 __device__ __forceinline__ dbl4 ld4(const dbl4 *__restrict__ p) { return *p; }
 __device__ __forceinline__ void st4(dbl4 *__restrict__ p, dbl4 v) { *p = v; }
 __device__ __forceinline__ F8 ldF8(const F8 *__restrict__ p) { return *p; }

@@ -2,6 +2,7 @@
 // element arithmetic is hexa_element() in rg_hexa_elem.cuh.
 #include "rg_hexa_elem.cuh"
 #include "rg_kernels.h"
+#include "rg_node.cuh"
 
 #include <type_traits>
 
@@ -11,7 +12,7 @@ template <typename ER, int LAW, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
             typename SlotT<ER>::type *__restrict__ fsky, DtPartials dp,
-            const Time *__restrict__ T, int *__restrict__ status) {
+            Time *__restrict__ T, int *__restrict__ status, const DtFinish F) {
   typedef ER R;
   const int il = blockIdx.x * NT + threadIdx.x;
   R dtmine = (R)RG_EP06;
@@ -20,20 +21,21 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
   // per-block time-step candidate
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x,
                       dp.el + P.part_off + blockIdx.x);
+  if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
 }
 
 // ---------------------------------------------------------------------------
 template <typename ER, int LAW>
 static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
                        const NodeView &N, typename SlotT<ER>::type *fsky,
-                       DtPartials dp, const Time *T, int *status,
+                       DtPartials dp, Time *T, int *status, const DtFinish &F,
                        cudaStream_t s) {
   constexpr int NT = 128;
   // mixed form: 5 resident blocks per SM fit in 96 registers without
   // spilling; the FP64 form needs its ~200 registers
   constexpr int MINB = std::is_same<ER, float>::value ? 5 : 1;
   const int nb = (P.nel + NT - 1) / NT;
-  hexa_kernel<ER, LAW, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status);
+  hexa_kernel<ER, LAW, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);
 }
 
 int hexa_blocks(int nel) { return (nel + 127) / 128; }
@@ -78,20 +80,20 @@ void launch_hexa_prev_volume(const HexaArrays<float> &A, const NodeView &N, cons
 
 void launch_hexa_f64(const HexaParams &P, const HexaArrays<double> &A,
                      const NodeView &N, dbl4 *fsky, DtPartials dp,
-                     const Time *T, int *status, cudaStream_t s) {
+                     Time *T, int *status, const DtFinish &F, cudaStream_t s) {
   if (P.mtn == 1)
-    launch_one<double, 1>(P, A, N, fsky, dp, T, status, s);
+    launch_one<double, 1>(P, A, N, fsky, dp, T, status, F, s);
   else
-    launch_one<double, 2>(P, A, N, fsky, dp, T, status, s);
+    launch_one<double, 2>(P, A, N, fsky, dp, T, status, F, s);
 }
 
 void launch_hexa_f32(const HexaParams &P, const HexaArrays<float> &A,
                      const NodeView &N, float4 *fsky, DtPartials dp,
-                     const Time *T, int *status, cudaStream_t s) {
+                     Time *T, int *status, const DtFinish &F, cudaStream_t s) {
   if (P.mtn == 1)
-    launch_one<float, 1>(P, A, N, fsky, dp, T, status, s);
+    launch_one<float, 1>(P, A, N, fsky, dp, T, status, F, s);
   else
-    launch_one<float, 2>(P, A, N, fsky, dp, T, status, s);
+    launch_one<float, 2>(P, A, N, fsky, dp, T, status, F, s);
 }
 
 }  // namespace rg

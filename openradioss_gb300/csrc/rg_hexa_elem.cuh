@@ -68,6 +68,23 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
     const R offg0 = A.off[e];
     R offg = offg0;
     R off = fabs(offg0);
+    R off_stored = offg0;  // OFFG as last written by this element
+    // The element state is read up front: as far as the compiler knows the
+    // state arrays may alias, so a load placed after a store could not be
+    // issued early; here all loads overlap the node gathers.
+    const double st_rho = A.rho[e];
+    const double st_vol0 = A.vol0[e];
+    R st_sig[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) st_sig[c] = A.sig[c * ne + e];
+    const R st_qvis = A.qvis[e];
+    const double st_eint = A.eint[e];
+    const double st_ehou = A.ehou[e];
+    R st_epsd = (R)0, st_pla = (R)0;
+    if (LAW == 2) {
+      st_epsd = A.epsd[e];
+      st_pla = A.pla[e];
+    }
     R x[8], y[8], z[8];
     R vx[8], vy[8], vz[8];
     if constexpr (F64) {
@@ -138,6 +155,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         off = (R)0;
         offg = (R)0;
         A.off[e] = (R)0;
+        off_stored = (R)0;
         atomicOr(status, 1);
         live = false;
       }
@@ -149,7 +167,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         // a=(J1,J2,J3), b=(J4,J5,J6), c=(J7,J8,J9) and their velocity
         // increments: every term is computed in FP32 at its own scale (no
         // cancellation), and the volume is accumulated in FP64.
-        vold_mixed = A.rho[e];
+        vold_mixed = st_rho;
         if (live) {
           const R u17 = vx[6] - vx[0], u28 = vx[7] - vx[1], u35 = vx[4] - vx[2], u46 = vx[5] - vx[3];
           const R v17 = vy[6] - vy[0], v28 = vy[7] - vy[1], v35 = vy[4] - vy[2], v46 = vy[5] - vy[3];
@@ -279,14 +297,14 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
     // Mixed form: the FP64 state array holds the element volume of the last
     // cycle instead of the density (RHO = RHO0*VOL0/VOL), DVOL is the
     // FP32 volume change computed above.
-    const double vol0 = A.vol0[e];
+    const double vol0 = st_vol0;
     if constexpr (F64) {
       if (offg == (R)0 && voln == RG_ONE) voln = vol0;
     }
     R rho_r, amu, dvol_r;
     double dvol_d = 0.0;
     if constexpr (F64) {
-      const double rho_old = A.rho[e];
+      const double rho_old = st_rho;
       dvol_d = voln - (P.rho0 / rho_old) * vol0;
       const double rho_new = P.rho0 * (vol0 / voln);
       A.rho[e] = rho_new;
@@ -303,7 +321,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
     // ---- SROTA3 --------------------------------------------------------------
     R s[6], sg[6];
 #pragma unroll
-    for (int c = 0; c < 6; c++) s[c] = A.sig[c * ne + e];
+    for (int c = 0; c < 6; c++) s[c] = st_sig[c];
     {
       const R q1 = (R)RG_TWO * s[3] * wzz;
       const R q2 = (R)RG_TWO * s[5] * wyy;
@@ -341,7 +359,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
               sg[3] * sg[3] + sg[4] * sg[4] + sg[5] * sg[5];
       aj2 = sqrt((R)RG_THREE * aj2);
       // MSTRAIN_RATE (materials/mat_share/mstrain_rate.F)
-      R epsd = A.epsd[e];
+      R epsd = st_epsd;
       if (P.israte >= 0) {
         R epsdot;
         if (P.vp - 2 == 0) {
@@ -382,7 +400,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         epd = (R)RG_ONE;
         if (P.icc == 1) sigmx = PC(sigm0) * epd;
       }
-      const R epxe = A.pla[e];
+      const R epxe = st_pla;
       R ak, qh;
       if (P.f.cn_one) {
         ak = PC(ca) + PC(cb) * epxe;
@@ -460,7 +478,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       sg[3] = sg[3] * off;
       sg[4] = sg[4] * off;
       sg[5] = sg[5] * off;
-      const R qold = A.qvis[e];
+      const R qold = st_qvis;
       const R dta = (R)RG_HALF * dt1;
       R ework, qwork;
       if (LAW == 1) {
@@ -486,12 +504,12 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       if (F64) {
         const double einc = (double)vol_avg_r * (double)ework * (double)dta -
                             RG_HALF * dvol_d * (double)qwork;
-        const double eint = A.eint[e] * vol0;
+        const double eint = st_eint * vol0;
         A.eint[e] = (eint + einc * (double)off) / fmax_(RG_ZERO + RG_EM15, vol0);
       } else {
         // EINT += EINC / VOL0: increment in FP32, accumulation in FP64
         const R einc = vol_avg_r * ework * dta - (R)RG_HALF * dvol_r * qwork;
-        A.eint[e] = A.eint[e] + (double)(einc * off / (R)vol0);
+        A.eint[e] = st_eint + (double)(einc * off / (R)vol0);
       }
       A.qvis[e] = qnew;
 #pragma unroll
@@ -499,11 +517,12 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       // SMALLB3
       if (off < (R)RG_ONE) {
         if (off == (R)0)
-          A.off[e] = (R)0;
+          off_stored = (R)0;
         else if (offg > (R)RG_ONE)
-          A.off[e] = (R)RG_ONE + off;
+          off_stored = (R)RG_ONE + off;
         else
-          A.off[e] = off;
+          off_stored = off;
+        A.off[e] = off_stored;
       }
     }
 
@@ -569,7 +588,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       const R ehou = dt1 * (hz[0] * hgz[0] + hz[1] * hgz[1] + hz[2] * hgz[2] + hz[3] * hgz[3] +
                             hx[0] * hgx[0] + hx[1] * hgx[1] + hx[2] * hgx[2] + hx[3] * hgx[3] +
                             hy[0] * hgy[0] + hy[1] * hgy[1] + hy[2] * hgy[2] + hy[3] * hgy[3]);
-      A.ehou[e] = A.ehou[e] + (double)ehou;
+      A.ehou[e] = st_ehou + (double)ehou;
     }
 
     // ---- SFINT3 ------------------------------------------------------------------
@@ -597,7 +616,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
 
     // ---- SCUMU3P -------------------------------------------------------------------
     {
-      const R offg_new = A.off[e];
+      const R offg_new = off_stored;
       const bool zero = offg_new < (R)0;
       const R st = (R)RG_FOURTH * sti;
 #pragma unroll

@@ -7,10 +7,10 @@ namespace rg {
 int hexa_blocks(int nel);
 void launch_hexa_f64(const HexaParams &P, const HexaArrays<double> &A,
                      const NodeView &N, dbl4 *fsky, DtPartials dp,
-                     const Time *T, int *status, cudaStream_t s);
+                     Time *T, int *status, const DtFinish &F, cudaStream_t s);
 void launch_hexa_f32(const HexaParams &P, const HexaArrays<float> &A,
                      const NodeView &N, float4 *fsky, DtPartials dp,
-                     const Time *T, int *status, cudaStream_t s);
+                     Time *T, int *status, const DtFinish &F, cudaStream_t s);
 void launch_hexa_prev_volume(const HexaArrays<float> &A, const NodeView &N, const Time *T,
                              cudaStream_t s);
 

@@ -217,4 +217,64 @@ __device__ __forceinline__ void dt_apply(Time *__restrict__ T, const double dt2t
   if (T->dtmin > 0.0 && dt2 < T->dtmin) atomicOr(status, RG_ST_DTMIN);
 }
 
+// Last-block time-step reduction (DtFinish), called by every element block
+// after thread 0 wrote its partial number p.  Thread 0 publishes (fence) and
+// takes a ticket of the partial's group; the block with the group's last
+// ticket reduces the group's partials through L2 and takes a ticket of the
+// cycle; the block with the cycle's last ticket reduces the group minima,
+// applies dt_apply and re-arms the counters.  No block waits on another.
+template <int NT>
+__device__ __forceinline__ void dt_finish_block(const DtPartials dp, const DtFinish F, int p,
+                                                Time *__restrict__ T,
+                                                int *__restrict__ status) {
+  static_assert(NT >= DT_GROUP, "one thread per partial of a group");
+  __shared__ int s_last;
+  __shared__ double od;
+  __shared__ int ok;
+  const int g = p / DT_GROUP;
+  const int ngroups = (F.nparts + DT_GROUP - 1) / DT_GROUP;
+  const int gsize = min(DT_GROUP, F.nparts - g * DT_GROUP);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(F.ctr + 1 + g, 1u) == (unsigned)(gsize - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  {
+    double d = RG_EP06;
+    int k = -1;
+    if (threadIdx.x < gsize) {
+      const int i = g * DT_GROUP + threadIdx.x;
+      const int ki = __ldcg(dp.el + i);
+      if (ki >= 0) {
+        d = __ldcg(dp.dt + i);
+        k = ki;
+      }
+    }
+    block_dt_min<NT>(d, k, F.gdt + g, F.gel + g);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    F.ctr[1 + g] = 0u;
+    __threadfence();
+    s_last = atomicAdd(F.ctr, 1u) == (unsigned)(ngroups - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double d = RG_EP06;
+  int k = -1;
+  for (int i = threadIdx.x; i < ngroups; i += NT) {
+    const int ki = __ldcg(F.gel + i);
+    if (ki >= 0) dt_pair_min(d, k, __ldcg(F.gdt + i), ki);
+  }
+  block_dt_min<NT>(d, k, &od, &ok);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    dt_apply(T, od, ok, F.ngl, status, F.advance);
+    F.ctr[0] = 0u;
+  }
+}
+
 }  // namespace rg

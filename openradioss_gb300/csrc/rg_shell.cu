@@ -4,6 +4,7 @@
 #include "../../include/rg_api.h"
 #include "rg_shell.h"
 #include "rg_shell_elem.cuh"
+#include "rg_node.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -25,12 +26,15 @@ struct ShellDev {
   double *epart = nullptr;  // energy partials
 };
 
+// mixed form: 4 resident blocks per SM (128 registers); FP64: as many as
+// its ~250 registers allow
 template <typename ER, int NPT, int NT>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, sizeof(ER) == 4 ? 4 : 1)
 shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              typename SlotT<ER>::type *__restrict__ fsky,
              typename SlotT<ER>::type *__restrict__ fskyr, DtPartials dp,
-             const Time *__restrict__ T, int key0, int nc_total) {
+             Time *__restrict__ T, int key0, int nc_total, int *__restrict__ status,
+             const DtFinish F) {
   typedef ER R;
   const int il = blockIdx.x * NT + threadIdx.x;
   R dtmine = (R)RG_EP06;
@@ -38,6 +42,7 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
   if (il < P.nel)
     shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin);
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
+  if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
 }
 
 // Fixed-order shell energy partials: [0] internal (membrane + bending),
@@ -72,17 +77,17 @@ int shell_blocks(int nel) { return (nel + SHELL_NT - 1) / SHELL_NT; }
 
 template <typename ER>
 static void launch_shell(const ShellParams &P, const ShellArrays<ER> &A, const NodeView &N,
-                         void *fsky, void *fskyr, DtPartials dp, const Time *T, int key0,
-                         int nct, cudaStream_t s) {
+                         void *fsky, void *fskyr, DtPartials dp, Time *T, int key0,
+                         int nct, int *status, const DtFinish &F, cudaStream_t s) {
   typedef typename SlotT<ER>::type ST;
   const int nb = shell_blocks(P.nel);
   ST *f = (ST *)fsky, *fr = (ST *)fskyr;
   switch (P.npt) {
-    case 1: shell_kernel<ER, 1, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
-    case 2: shell_kernel<ER, 2, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
-    case 3: shell_kernel<ER, 3, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
-    case 4: shell_kernel<ER, 4, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
-    default: shell_kernel<ER, 5, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct); break;
+    case 1: shell_kernel<ER, 1, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+    case 2: shell_kernel<ER, 2, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+    case 3: shell_kernel<ER, 3, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+    case 4: shell_kernel<ER, 4, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+    default: shell_kernel<ER, 5, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
   }
 }
 
@@ -284,15 +289,14 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
 }
 
 void shell_enqueue(ShellModelHost &S, int prec, const NodeView &N, void *fsky, void *fskyr,
-                   DtPartials dp, const Time *T, int *status, cudaStream_t s) {
-  (void)status;
+                   DtPartials dp, Time *T, int *status, const DtFinish &F, cudaStream_t s) {
   if (S.numelc == 0 || !S.dev) return;
   auto *D = (ShellDev *)S.dev;
   for (auto *g : S.groups) {
     if (prec == RG_PREC_FP64)
-      launch_shell<double>(g->P, D->a64, N, fsky, fskyr, dp, T, S.key0, S.numelc, s);
+      launch_shell<double>(g->P, D->a64, N, fsky, fskyr, dp, T, S.key0, S.numelc, status, F, s);
     else
-      launch_shell<float>(g->P, D->a32, N, fsky, fskyr, dp, T, S.key0, S.numelc, s);
+      launch_shell<float>(g->P, D->a32, N, fsky, fskyr, dp, T, S.key0, S.numelc, status, F, s);
   }
 }
 

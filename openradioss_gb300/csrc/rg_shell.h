@@ -36,8 +36,8 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X,
                    const int *iadc, int key0, double dtfac, int &part_off,
                    const DevAlloc &alloc, std::string &why);
 void shell_enqueue(ShellModelHost &S, int prec, const NodeView &N, void *fsky,
-                   void *fskyr, DtPartials dp, const Time *T, int *status,
-                   cudaStream_t s);
+                   void *fskyr, DtPartials dp, Time *T, int *status,
+                   const DtFinish &F, cudaStream_t s);
 int shell_energy_enqueue(ShellModelHost &S, int prec, double *out2,
                          cudaStream_t s);
 int shell_download(ShellModelHost &S, int prec, int which, double *out,

@@ -240,6 +240,16 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       }
     }
     R thk0 = S.thke[e];
+    // Element state read up front, ahead of the first store (the compiler
+    // must assume the state arrays may alias): the loads overlap the gathers.
+    R st_forc[5], st_mom[3], st_hour[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) st_forc[c] = S.forc[c * nc + e];
+#pragma unroll
+    for (int c = 0; c < 3; c++) st_mom[c] = S.mom[c * nc + e];
+#pragma unroll
+    for (int c = 0; c < 5; c++) st_hour[c] = S.hour[c * nc + e];
+    const double st_eint0 = S.eint[e], st_eint1 = S.eint[nc + e], st_ehou = S.ehou[e];
     // ---- CNVEC3 ----
     R e1x, e1y, e1z, e2x, e2y, e2z, e3x, e3y, e3z;
     {
@@ -407,9 +417,9 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     }
     // ---- MULAWC: through-thickness loop (SIGEPS02C / M2CPLR) ----
     R forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
-    R degmb = S.forc[0 * nc + e] * exx + S.forc[1 * nc + e] * eyy + S.forc[2 * nc + e] * exy +
-              S.forc[3 * nc + e] * eyz + S.forc[4 * nc + e] * exz;
-    R degfx = S.mom[0 * nc + e] * kxx + S.mom[1 * nc + e] * kyy + S.mom[2 * nc + e] * kxy;
+    R degmb = st_forc[0] * exx + st_forc[1] * eyy + st_forc[2] * exy + st_forc[3] * eyz +
+              st_forc[4] * exz;
+    R degfx = st_mom[0] * kxx + st_mom[1] * kyy + st_mom[2] * kxy;
     double thkn = thk_cur;
     R asrate = (R)RG_ONE;
     if (P.israte > 0) {
@@ -424,8 +434,26 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     // LOG(EPSP/EPDR) of the previous point: the points usually share one
     // strain rate (ASRATE = 1), and an equal argument gives the same value
     R memo_epsp = (R)-1, memo_log = (R)0;
+    // point state: point it+1 is loaded while point it is computed
+    R nx_sig[5], nx_ep, nx_pla;
+#pragma unroll
+    for (int c = 0; c < 5; c++) nx_sig[c] = S.sig[(c)*nc + e];
+    nx_ep = S.epsd[e];
+    nx_pla = S.pla[e];
 #pragma unroll
     for (int it = 0; it < NPT; it++) {
+      R sn[5];
+#pragma unroll
+      for (int c = 0; c < 5; c++) sn[c] = nx_sig[c];
+      R ep = nx_ep;
+      const R pla_in = nx_pla;
+      if (it + 1 < NPT) {
+        const int q5 = ((it + 1) * 5) * nc + e;
+#pragma unroll
+        for (int c = 0; c < 5; c++) nx_sig[c] = S.sig[q5 + c * nc];
+        nx_ep = S.epsd[(it + 1) * nc + e];
+        nx_pla = S.pla[(it + 1) * nc + e];
+      }
       const R thkly = pcoef<R>(c_wfd[NPT - 1][it], c_wf[NPT - 1][it]);
       const R thklyl = thkly * thk0;
       const R wmc = pcoef<R>(c_wmd[NPT - 1][it], c_wm[NPT - 1][it]);
@@ -434,10 +462,6 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       const R depsyy = eyy + zt * kyy;
       const R depsxy = exy + zt * kxy;
       const int ip5 = (it * 5) * nc + e;
-      R sn[5];
-#pragma unroll
-      for (int c = 0; c < 5; c++) sn[c] = S.sig[ip5 + c * nc];
-      R ep = S.epsd[it * nc + e];
       R epsdot;
       if (P.vp == 2) {
         ep = asrate * epsd_pg + ((R)RG_ONE - asrate) * ep;
@@ -472,7 +496,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         cb = cb * q;
         if (P.icc == 1) ymax = ymax * q;
       }
-      R pla = S.pla[it * nc + e];
+      R pla = pla_in;
       R yld = pla == (R)0 ? ca : ca + cb * exp(PC(cn) * log(pla));
       yld = smin(yld, ymax);
       if (P.ipla == 0) {
@@ -556,8 +580,8 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     degfx = degfx + momn[0] * kxx + momn[1] * kyy + momn[2] * kxy;
     {
       const R vol2 = (R)RG_HALF * vol0;
-      S.eint[e] = S.eint[e] + (double)(degmb * vol2);
-      S.eint[nc + e] = S.eint[nc + e] + (double)(degfx * thk0 * vol2);
+      S.eint[e] = st_eint0 + (double)(degmb * vol2);
+      S.eint[nc + e] = st_eint1 + (double)(degfx * thk0 * vol2);
     }
 #pragma unroll
     for (int c = 0; c < 5; c++) S.forc[c * nc + e] = forn[c];
@@ -601,8 +625,8 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       if (S.degen[e]) h1q = h2q = h3q = hh1 = hh2 = (R)0;
       R hg1 = vx[0] * gama1 + vx[1] * gama2 + vx[2] * gama3 + vx[3] * gama4;
       R hg2 = vy[0] * gama1 + vy[1] * gama2 + vy[2] * gama3 + vy[3] * gama4;
-      R hou0 = S.hour[0 * nc + e] + hg1 * hh1;
-      R hou1 = S.hour[1 * nc + e] + hg2 * hh1;
+      R hou0 = st_hour[0] + hg1 * hh1;
+      R hou1 = st_hour[1] + hg2 * hh1;
       const R hour1a = hou0 + hg1 * ((R)0 + h1q * fabs(hg1));
       h11 = hour1a * gama1;
       h12 = hour1a * gama2;
@@ -613,7 +637,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       h23 = hour2a * gama3;
       R ehou = hour1a * hg1 + hour2a * hg2;
       hg1 = vz[0] * gama1 + vz[1] * gama2 + vz[2] * gama3 + vz[3] * gama4;
-      const R hou2 = S.hour[2 * nc + e] + hg1 * hh2;
+      const R hou2 = st_hour[2] + hg1 * hh2;
       const R hour3a = hou2 + hg1 * ((R)0 + h2q * fabs(hg1));
       h31 = hour3a * gama1;
       h32 = hour3a * gama2;
@@ -630,7 +654,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       S.hour[2 * nc + e] = hou2;
       S.hour[3 * nc + e] = hr4;
       S.hour[4 * nc + e] = hr5;
-      S.ehou[e] = S.ehou[e] + (double)ehou;
+      S.ehou[e] = st_ehou + (double)ehou;
     }
     // ---- CDT3 ----
     R sti;
