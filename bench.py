@@ -136,8 +136,9 @@ def element_bytes(model, prec):
         # writes SIG, QVIS, EINT, RHO, EHOU, [PLA, EPSD], 8 slots
         wr = er * (6 + 1) + 8 * 3 + (2 * er if law == 2 else 0) + 8 * slot
         spn = 8.0 * ne / nn
-        # ADSKY, slots, X4 V4 D4 read + written, FP32 copies XF VF written
-        node = 4 + spn * slot + 3 * 32 * 2 + (48 if prec else 0)
+        # ADSKY, slots, X4 V4 (+ D4 in FP64) read + written; mixed: FP32
+        # position copy XF read + written, velocity copy VF written
+        node = 4 + spn * slot + (3 * 32 * 2 if prec == 0 else 2 * 32 * 2 + 64 + 16)
         return rd + wr, node, "hexa"
     nc = model.numelc
     npt = model.shells[0].npt
@@ -149,9 +150,9 @@ def element_bytes(model, prec):
     # per point SIG(5), PLA, EPSD; 4 slots of forces + 4 of moments
     wr = 22 * er + 8 + 16 + 8 + npt * 7 * er + 4 * 2 * slot
     spn = 4.0 * nc / nn
-    # ADSKY, force + moment slots, X4 V4 D4 VR4 read + written, DR4 unread;
-    # FP32 copies XF VF VRF written
-    node = 4 + spn * 2 * slot + 4 * 32 * 2 + (64 if prec else 0)
+    # ADSKY, force + moment slots, X4 V4 VR4 (+ D4 in FP64) read + written;
+    # mixed: XF read + written, VF VRF written
+    node = 4 + spn * 2 * slot + (4 * 32 * 2 if prec == 0 else 3 * 32 * 2 + 64 + 32)
     return rd + wr, node, "shell"
 
 

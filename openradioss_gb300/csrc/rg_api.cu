@@ -225,6 +225,17 @@ __global__ void upload_nodes_kernel(NodeView N, const double *__restrict__ x,
   }
 }
 
+// Mixed form: D = X - X0 (D4 holds the initial position).
+__global__ void unpack_disp_kernel(int n, const dbl4 *__restrict__ x4,
+                                   const dbl4 *__restrict__ x0, double *__restrict__ dst) {
+  const int i = blockIdx.x * NODE_NT + threadIdx.x;
+  if (i >= n) return;
+  const dbl4 a = x4[i], b = x0[i];
+  dst[3 * i] = a.x - b.x;
+  dst[3 * i + 1] = a.y - b.y;
+  dst[3 * i + 2] = a.z - b.z;
+}
+
 __global__ void unpack3_kernel(int n, const dbl4 *__restrict__ src,
                                double *__restrict__ dst) {
   const int i = blockIdx.x * NODE_NT + threadIdx.x;
@@ -657,7 +668,10 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     const double ms = c->MS[n], in = c->IN[n];
     x4[n] = mk4(c->X[3 * n], c->X[3 * n + 1], c->X[3 * n + 2], ms > 0.0 ? 1.0 / ms : 0.0);
     v4[n] = mk4(c->V[3 * n], c->V[3 * n + 1], c->V[3 * n + 2], (double)c->icodt[n]);
-    z4[n] = mk4(0, 0, 0, ms);
+    // D4: displacement (FP64 form) or initial position (mixed form), MS
+    z4[n] = c->prec == RG_PREC_MIXED
+                ? mk4(c->X[3 * n], c->X[3 * n + 1], c->X[3 * n + 2], ms)
+                : mk4(0, 0, 0, ms);
     vr4[n].w = in > 0.0 ? 1.0 / in : 0.0;
     dr4[n].w = in;
   }
@@ -985,7 +999,10 @@ int rg_download_nodes(rg_ctx *c, double *x, double *v, double *d, double *vr) {
       std::fill(it.dst, it.dst + 3 * (size_t)n, 0.0);
       continue;
     }
-    unpack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, it.src, st);
+    if (it.src == c->nv.D4 && c->prec == RG_PREC_MIXED)
+      unpack_disp_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, c->nv.X4, c->nv.D4, st);
+    else
+      unpack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, it.src, st);
     RG_CUDA(c, cudaMemcpyAsync(it.dst, st, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
                                c->stream));
     RG_CUDA(c, cudaStreamSynchronize(c->stream));

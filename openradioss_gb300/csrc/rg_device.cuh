@@ -50,7 +50,7 @@ struct __align__(32) F8 {
 struct NodeView {
   dbl4 *X4;   // x y z 1/MS      (1/MS = 0 when MS <= 0)
   dbl4 *V4;   // vx vy vz code(as double)
-  dbl4 *D4;   // dx dy dz MS
+  dbl4 *D4;   // dx dy dz MS (mixed form: x0 y0 z0 MS, D = X - X0)
   dbl4 *VR4;  // vrx vry vrz 1/IN (shell models only)
   dbl4 *DR4;  // - - - IN          (shell models only)
   F8 *XF;     // mixed form: FP32 hi/lo position copies

@@ -27,6 +27,18 @@ __device__ __forceinline__ F8 split_hilo(double x, double y, double z) {
   return c;
 }
 
+// (hi, lo) += d in FP32, exact two-sum then renormalisation (Knuth's
+// TwoSum, Dekker's fast renormalisation): hi + lo keeps about 48 bits.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, const float d) {
+  const float s = __fadd_rn(hi, d);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+  const float l = __fadd_rn(lo, err);
+  const float h2 = __fadd_rn(s, l);
+  lo = __fsub_rn(l, __fsub_rn(h2, s));
+  hi = h2;
+}
+
 // L2-coherent loads (ld.global.cg): used where the data was written by other
 // blocks earlier in the same launch (batched persistent kernel).
 __device__ __forceinline__ dbl4 ldcg4(const dbl4 *p) {
@@ -92,7 +104,10 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
   }
   dbl4 x = ld4(N.X4 + n);
   dbl4 v = ld4(N.V4 + n);
-  dbl4 d = ld4(N.D4 + n);
+  // FP64 form: D4 = displacement, MS.  Mixed form: D4 holds the initial
+  // position and MS (D = X - X0 on download), so it is not touched here.
+  dbl4 d;
+  if constexpr (F64) d = ld4(N.D4 + n);
   const double dt12 = COH ? __ldcg(&T->dt12) : T->dt12;
   const double dt2 = COH ? __ldcg(&T->dt2) : T->dt2;
   // ACCELE: A = A * (1/MS); X4.w holds 1/MS (0 when MS <= 0, giving A = 0)
@@ -155,19 +170,22 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     v.x = fma(dt12, a0, v.x);
     v.y = fma(dt12, a1, v.y);
     v.z = fma(dt12, a2, v.z);
-    d.x = fma(dt2, v.x, d.x);
-    d.y = fma(dt2, v.y, d.y);
-    d.z = fma(dt2, v.z, d.z);
     x.x = fma(dt2, v.x, x.x);
     x.y = fma(dt2, v.y, x.y);
     x.z = fma(dt2, v.z, x.z);
-    N.XF[n] = split_hilo(x.x, x.y, x.z);
+    // the FP32 hi/lo copy advances by the FP32-rounded increment with an
+    // exact two-sum (no FP64 split of the new position)
+    F8 c = N.XF[n];
+    ff_add(c.hx, c.lx, __double2float_rn(__dmul_rn(dt2, v.x)));
+    ff_add(c.hy, c.ly, __double2float_rn(__dmul_rn(dt2, v.y)));
+    ff_add(c.hz, c.lz, __double2float_rn(__dmul_rn(dt2, v.z)));
+    N.XF[n] = c;
     N.VF[n] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y),
                           __double2float_rn(v.z), 0.f);
   }
   st4(N.X4 + n, x);
   st4(N.V4 + n, v);
-  st4(N.D4 + n, d);
+  if constexpr (F64) st4(N.D4 + n, d);
   if (ROT) {
     dbl4 vr = ld4(N.VR4 + n);
     r0 = __dmul_rn(r0, vr.w);
