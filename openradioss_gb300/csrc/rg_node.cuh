@@ -128,17 +128,15 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     const int w = __ldg(wall + n);
     if (w >= 0) {
       const double *W = walls + 6 * w;
-      const double vx = __dadd_rn(v.x, __dmul_rn(a0, dt12));
-      const double vy = __dadd_rn(v.y, __dmul_rn(a1, dt12));
-      const double vz = __dadd_rn(v.z, __dmul_rn(a2, dt12));
-      const double ux = __dadd_rn(x.x, __dmul_rn(vx, dt2));
-      const double uy = __dadd_rn(x.y, __dmul_rn(vy, dt2));
-      const double uz = __dadd_rn(x.z, __dmul_rn(vz, dt2));
-      const double dp = __dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(ux, -W[0]), W[3]),
-                                            __dmul_rn(__dadd_rn(uy, -W[1]), W[4])),
-                                  __dmul_rn(__dadd_rn(uz, -W[2]), W[5]));
-      const double vn = __dadd_rn(__dadd_rn(__dmul_rn(vx, W[3]), __dmul_rn(vy, W[4])),
-                                  __dmul_rn(vz, W[5]));
+      // predicted normal velocity VN = (V + A*DT12).n and distance
+      // DP = (X + (V + A*DT12)*DT2 - P0).n = (X - P0).n + DT2*VN, in fused
+      // multiply-adds written out (the same bits in every kernel)
+      const double vx = fma(a0, dt12, v.x);
+      const double vy = fma(a1, dt12, v.y);
+      const double vz = fma(a2, dt12, v.z);
+      const double vn = fma(vz, W[5], fma(vy, W[4], vx * W[3]));
+      const double dp0 = fma(x.z - W[2], W[5], fma(x.y - W[1], W[4], (x.x - W[0]) * W[3]));
+      const double dp = fma(dt2, vn, dp0);
       if (!(dp > 0.0) && !(vn > 0.0)) {
         const double dv = __dadd_rn(__dadd_rn(__dmul_rn(v.x, W[3]), __dmul_rn(v.y, W[4])),
                                     __dmul_rn(v.z, W[5]));
