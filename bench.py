@@ -46,6 +46,8 @@ WORKLOADS = {
     "bar_impact_20_law1": lambda: M.bar_impact(n=20),
 }
 DEFAULT_WORKLOAD = "crash_box_120k_jc"
+# full run length of each configuration (the "job")
+JOB_CYCLES = {"crash_box_120k_jc": 20000, "hexa_block_128_jc": 2000, "bar_impact_20_law1": 1000}
 
 
 def peaks():
@@ -177,27 +179,40 @@ def run_ours(args, rank, world, local_rank):
 
     forms = [RG_PREC_FP64, RG_PREC_MIXED] if args.forms == "both" else (
         [RG_PREC_FP64] if args.forms == "f64" else [RG_PREC_MIXED])
+    def fresh(prec):
+        # every measurement starts from the same state: W cycles after set-up
+        e = Engine(model, device=local_rank, precision=prec)
+        e.cycle(args.warmup)
+        e.sync()
+        return e
+
     for prec in forms:
-        eng = Engine(model, device=local_rank, precision=prec)
-        eng.cycle(args.warmup)
-        eng.sync()
+        eng = fresh(prec)
         barrier()
         with Clocks(local_rank) as clk:
             # every timed cycle starts from cold L2 (256 MB written before it)
             ms = eng.time_cycles_cold(args.steps, L2_FLUSH_BYTES)
-            ms_warm = eng.time_cycles(args.steps)
         ms = max_over_ranks(ms)
         st = eng.status()
-        # per-kernel times (event-bracketed launches, same stream)
+        eng.close()
+        eng = fresh(prec)
+        ms_warm = eng.time_cycles(args.steps)
+        eng.close()
+        # per-kernel times (event-bracketed launches, same stream, cold L2)
+        eng = fresh(prec)
+        eng.time_cycles_cold(0, L2_FLUSH_BYTES)
         eng.set_timing(True)
         eng.cycle(max(3, min(args.steps, 20)))
         kt = eng.kernel_times()
         eng.set_timing(False)
+        st |= eng.status()
+        eng.close()
         eb, nb, kkey = element_bytes(model, prec)
         out[prec] = dict(ms=ms, ms_warm=ms_warm, clocks=clk.summary(), kt=kt, status=st,
-                         elem_bytes=eb, node_bytes=nb, kkey=kkey, eng=eng)
-    # e2e: FORINT-level call with pinned host buffers (headline form)
-    eng = out[forms[0]]["eng"]
+                         elem_bytes=eb, node_bytes=nb, kkey=kkey)
+    # e2e: FORINT-level call with pinned host buffers (headline form), from
+    # the same state
+    eng = fresh(forms[0])
     nd = eng.nodes()
     x = np.ascontiguousarray(nd["X"].T)
     v = np.ascontiguousarray(nd["V"].T)
@@ -222,6 +237,19 @@ def run_ours(args, rank, world, local_rank):
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     for a in bufs:
         eng.host_unregister(a)
+    dev_bytes = eng.info()["device_bytes"]
+    eng.close()
+    # the whole job of the configuration (its full cycle count, back to back
+    # graph launches, state evolving: contact, plasticity)
+    jobs = {}
+    if not args.no_job and args.forms == "both" and JOB_CYCLES.get(wl):
+        for prec in forms:
+            e = Engine(model, device=local_rank, precision=prec)
+            jms = e.time_cycles(JOB_CYCLES[wl])
+            jobs[prec] = dict(cycles=JOB_CYCLES[wl], seconds=jms * 1e-3,
+                              element_updates_s=ne * JOB_CYCLES[wl] / (jms * 1e-3),
+                              status=e.status())
+            e.close()
 
     if args.forms != "both":
         res = out[forms[0]]
@@ -266,7 +294,8 @@ def run_ours(args, rank, world, local_rank):
                                    "Iplas=1, planar sliding rigid wall") + ", PARITH/ON",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "L2 flushed (256 MB written) before every timed cycle; model "
-                         "state %.2f GB" % (eng.info()["device_bytes"] / 1e9)},
+                         "state %.2f GB" % (dev_bytes / 1e9),
+                   "state": "every measurement starts %d cycles after set-up" % args.warmup},
         "e2e": {"value": world * ne * args.steps / e2e_s, "unit": "element-updates/s",
                 "transfer": "inputs: registered host buffers read in place by the upload "
                             "kernel; outputs: DMA copies from the device staging buffer",
@@ -290,6 +319,10 @@ def run_ours(args, rank, world, local_rank):
         "clocks": res64["clocks"],
         "device_status": [res64["status"], res32["status"]],
     }
+    if jobs:
+        line["job"] = {("f64" if p == RG_PREC_FP64 else "mixed"): j for p, j in jobs.items()}
+        if len(jobs) == 2:
+            line["job"]["mixed_speedup"] = jobs[RG_PREC_FP64]["seconds"] / jobs[RG_PREC_MIXED]["seconds"]
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(wl, args.cpu_sample)
     return line
@@ -496,6 +529,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD,
                     choices=sorted(WORKLOADS) + ["crash_box_sweep_64", "serving_mix"])
+    ap.add_argument("--no-job", action="store_true",
+                    help="skip the full-length job runs of the configuration")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the batched-sweep and serving summaries of the default run")
     ap.add_argument("--cpu-sample", type=float, default=15.0,
