@@ -158,6 +158,19 @@ def element_bytes(model, prec):
     return rd + wr, node, "shell"
 
 
+def fp64_roofline(kkey, ne, ms, device):
+    """The plain form's element kernel against the FP64 pipe: FP64
+    instructions per launch over its time, against the measured FMA rate."""
+    pk = fp64_peak(device)
+    n = FP64_INSTR_PER_ELEMENT.get(kkey)
+    if not pk or not n:
+        return None
+    ach = n * ne / (ms * 1e-3)
+    return {"bound": "fp64 pipe", "achieved": ach, "peak": pk, "unit": "FP64 thread instr/s",
+            "frac": ach / pk, "instr_per_element": n,
+            "peak_kind": "measured (rg_fp64_peak: dependent FMA chains, all SMs)"}
+
+
 def run_ours(args, rank, world, local_rank):
     from openradioss_gb300.engine import Engine, RG_PREC_FP64, RG_PREC_MIXED
     wl = args.workload
@@ -307,7 +320,8 @@ def run_ours(args, rank, world, local_rank):
                      "kernel": "%s_kernel<double>" % kk,
                      "bytes_per_element": res64["elem_bytes"], "ms_per_launch": k64,
                      "peak_kind": peak_kind,
-                     "note": "FP64 form is FP64-pipe bound on GB300; see fp64 key"},
+                     "note": "FP64 form is FP64-pipe bound on GB300; see fp64_roofline"},
+        "fp64_roofline": fp64_roofline(kk, ne, k64, local_rank),
         "kernel_ms": res64["kt"],
         "l2_warm_back_to_back": {"f64": world * ne * args.steps / (res64["ms_warm"] * 1e-3),
                                  "mixed": world * ne * args.steps / (res32["ms_warm"] * 1e-3)},
@@ -329,6 +343,20 @@ def run_ours(args, rank, world, local_rank):
 
 
 L2_FLUSH_BYTES = 256 << 20  # twice the GB300 L2
+
+# FP64 thread instructions per element of the plain form's element kernels at
+# the benchmark's state (5 cycles after set-up), counted with ncu
+# (smsp__sass_thread_inst_executed_op_fp64_pred_on / elements per launch).
+FP64_INSTR_PER_ELEMENT = {"shell": 967.0, "hexa": 1030.0}
+
+
+def fp64_peak(device=0):
+    """Measured FP64 fused multiply-add rate of the device (thread instr/s)."""
+    import ctypes as C
+    from openradioss_gb300 import _lib
+    v = C.c_double()
+    r = _lib.lib().rg_fp64_peak(device, C.byref(v))
+    return v.value if r == 0 else None
 
 SWEEP_JOBS = 64
 SWEEP_CYCLES_PER_JOB = 2000

@@ -197,6 +197,12 @@ int rg_time_cycles_cold(rg_ctx *ctx, int ncycle, unsigned long long flush_bytes,
 int rg_kinetic_energy_noalloc(int device, int numnod, const double *d_v,
                               const double *d_ms, double *ekin);
 
+/* Measured FP64 fused multiply-add rate of device `device` (thread
+ * instructions per second, ~0.1 s of a dedicated kernel): the ceiling of the
+ * FP64-pipe roofline of the plain form.  Benchmarking aid; no counterpart in
+ * the reference. */
+int rg_fp64_peak(int device, double *fma_per_s);
+
 /* ---- Batched jobs -------------------------------------------------------
  * A batch advances many finalized contexts (independent models, "jobs") of
  * the same arithmetic form together: one persistent cooperative kernel per

@@ -47,6 +47,7 @@ SIGNATURES = [
     ("rg_time_cycles", _ip, [_vp, _ip, _vp]),
     ("rg_time_cycles_cold", _ip, [_vp, _ip, C.c_ulonglong, _vp]),
     ("rg_kinetic_energy_noalloc", _ip, [_ip, _ip, _vp, _vp, _vp]),
+    ("rg_fp64_peak", _ip, [_ip, _vp]),
     ("rg_batch_create", _ip, [_ip, C.POINTER(C.c_void_p)]),
     ("rg_batch_destroy", _ip, [_vp]),
     ("rg_batch_last_error", C.c_char_p, [_vp]),

@@ -103,3 +103,56 @@ extern "C" int rg_kinetic_energy_noalloc(int device, int numnod, const double *d
   if (prev != device) cudaSetDevice(prev);
   return r;
 }
+
+// ---------------------------------------------------------------------------
+// FP64 pipe ceiling of the device, measured: every thread runs 8 independent
+// chains of dependent FP64 fused multiply-adds.  Used as the denominator of
+// the FP64-pipe roofline of the plain form's kernels (bench).
+namespace {
+constexpr int PK_CHAINS = 8;
+constexpr int PK_ITERS = 4096;
+
+__global__ void __launch_bounds__(256) fp64_fma_kernel(double *out, double a, double b) {
+  double c[PK_CHAINS];
+#pragma unroll
+  for (int k = 0; k < PK_CHAINS; k++) c[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < PK_ITERS; i++) {
+#pragma unroll
+    for (int k = 0; k < PK_CHAINS; k++) c[k] = fma(c[k], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < PK_CHAINS; k++) s += c[k];
+  if (s == 12345.678) out[blockIdx.x] = s;  // keeps the chains live
+}
+}  // namespace
+
+extern "C" int rg_fp64_peak(int device, double *fma_per_s) {
+  if (!fma_per_s || device < 0) return RG_E_ARG;
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) return RG_E_CUDA;
+  if (prev != device && cudaSetDevice(device) != cudaSuccess) return RG_E_CUDA;
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  const int blocks = nsm * 8;
+  double *scr = nullptr;
+  int r = scratch_for(device, &scr);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (r == RG_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+    r = RG_E_CUDA;
+  if (r == RG_OK) {
+    fp64_fma_kernel<<<blocks, 256>>>(scr, 0.999999, 1e-9);  // warm-up
+    cudaEventRecord(e0);
+    fp64_fma_kernel<<<blocks, 256>>>(scr, 0.999999, 1e-9);
+    cudaEventRecord(e1);
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      r = RG_E_CUDA;
+    else
+      *fma_per_s = (double)blocks * 256 * PK_CHAINS * PK_ITERS / (ms * 1e-3);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (prev != device) cudaSetDevice(prev);
+  return r;
+}
