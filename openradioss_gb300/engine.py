@@ -75,7 +75,7 @@ class Engine:
             thk = np.ascontiguousarray(g.thk, np.float64)
             self._chk(L.rg_shell_group_add(self.h, g.ixc.shape[1], _p(ixc), g.npt,
                                            _p(g.mat["pm"]), _p(g.geo), _p(g.mat["uparam"]),
-                                           _p(g.mat["iparam"]), _p(thk), 2, 1),
+                                           _p(g.mat["iparam"]), _p(thk), g.ismstr, g.ithk),
                       "rg_shell_group_add")
         for (p0, nrm, ds) in m.rwalls:
             self._chk(L.rg_rwall_add(self.h, _p(np.asarray(p0, np.float64)),

@@ -160,6 +160,8 @@ class ShellGroupSpec:
     geo: np.ndarray
     thk: np.ndarray            # (nel,)
     npt: int = 5
+    ithk: int = 1              # 1: current thickness, 0: initial thickness
+    ismstr: int = 2
 
 
 @dataclass
@@ -174,6 +176,10 @@ class Model:
     shells: list = field(default_factory=list)
     IN: np.ndarray | None = None
     rwalls: list = field(default_factory=list)  # (p0[3], n[3], dsearch)
+    # rigid links (engine /VEL/TRA|ROT): (1-based nodes, ic, icr), direction
+    # bits 4 = x, 2 = y, 1 = z
+    rlinks: list = field(default_factory=list)
+    ishfram: int = 0           # local shell frame: 0 symmetric, 2 /SHFRA/V4
     dtfac_solid: float = 0.9
     dtfac_shell: float = 0.9
     dtmx: float = 1e30
@@ -418,3 +424,85 @@ def serving_job(k, seed=7):
         m = hexa_impact_block(nel, v0=v0, seed=1000 + k, law=law, a=a)
     m.name = "job_%d" % k
     return m, ncyc
+
+
+# --------------------------------------------------------------------------
+# decks read into arrays
+# --------------------------------------------------------------------------
+def _code_bits(digits, base):
+    """'101' (x, y, z flags of a /BCS card) -> bits base*{1, 2, 4}."""
+    return sum(base * (1 << k) for k in range(3) if digits[k] == "1")
+
+
+def model_from_deck(d, name="deck", with_links=True):
+    """Model of a shell deck held as arrays (the layout written by
+    tests/golden/make_cra2.py: nodes, /SHELL parts, /MAT/PLAS_JOHNS,
+    /PROP/SHELL, /DEF_SHELL, /SHFRA/V4, /BCS, /INIVEL/TRA, /ADMAS/0, engine
+    /VEL/TRA/XYZ links), with the starter's decisions for it:
+
+    * properties: Ishell 0 -> the /DEF_SHELL value, else 1; Ismstr 0 -> 2;
+      Ithick / Iplas 0 -> the /DEF_SHELL value; shear factor 0 -> 5/6; N = 0
+      with LAW2 -> 3 integration points
+      (starter/source/properties/shell/hm_read_prop01.F:177-273,
+      starter/source/elements/shell/coque/cgrtails.F:800-811);
+    * masses: cinmas lumping of every shell plus the /ADMAS masses;
+    * /SHFRA/V4 -> ISHFRAM = 2 (starter/source/starter/contrl.F:495-498).
+
+    Node and element ids must run 1..n (they do in the decks used here).
+    """
+    node_id = np.asarray(d["node_id"])
+    if not np.array_equal(node_id, np.arange(1, len(node_id) + 1)):
+        raise ValueError("node ids must be 1..numnod")
+    X = np.ascontiguousarray(np.asarray(d["X"], np.float64).T)
+    numnod = X.shape[1]
+    mcols = [str(c) for c in d["mat_columns"]]
+    pcols = [str(c) for c in d["prop_columns"]]
+    mats = {int(r[0]): dict(zip(mcols, r)) for r in np.asarray(d["mat"])}
+    props = {int(r[0]): dict(zip(pcols, r)) for r in np.asarray(d["prop"])}
+    ds = [int(v) for v in d["def_shell"]]  # ISHELL ISMSTR ITHICK IPLAS ISTRAIN ISH3N IDRIL
+    ms = np.zeros(numnod)
+    inr = np.zeros(numnod)
+    shells = []
+    sid = np.asarray(d["shell_id"])
+    spart = np.asarray(d["shell_part"])
+    snodes = np.asarray(d["shell_nodes"])
+    for p, mid, pid in zip(d["part_id"], d["part_mat"], d["part_prop"]):
+        sel = np.nonzero(spart == p)[0]
+        mt, pr = mats[int(mid)], props[int(pid)]
+        ihbe = int(pr["Ishell"]) or ds[0] or 1
+        if ihbe != 1:
+            raise ValueError("only Ishell = 1 shells are supported")
+        ismstr = int(pr["Ismstr"]) or ds[1] or 2
+        ithk = int(pr["Ithick"]) or ds[2]
+        ipla = int(pr["Iplas"]) or ds[3]
+        npt = int(pr["N"]) or 3
+        thick = float(pr["Thick"])
+        mat = law2(mt["rho"], mt["E"], mt["nu"], mt["a"], mt["b"], mt["n"], c=mt["c"],
+                   eps0=mt["eps0"], epsmax=mt["epsmax"], sigmax=mt["sigmax"], m_exp=mt["m"],
+                   icc=int(mt["ICC"]), fcut=mt["Fcut"])
+        geo = shell_prop(thick, hm=pr["hm"] or 0.01, hf=pr["hf"] or 0.01, hr=pr["hr"] or 0.01,
+                         dm=pr["dm"], iplas=ipla)
+        if pr["Ashear"]:
+            geo[37] = pr["Ashear"]
+        ixc = np.zeros((7, len(sel)), np.int32)
+        ixc[0] = int(mid)
+        ixc[1:5] = snodes[sel].T
+        ixc[5] = int(pid)
+        ixc[6] = sid[sel]
+        t = np.full(len(sel), thick)
+        shell_mass_inertia(X, ixc, t, mt["rho"], ms, inr)
+        shells.append(ShellGroupSpec(ixc, mat, geo, t, npt, ithk=ithk, ismstr=ismstr))
+    ms[np.asarray(d["admas_nodes"]) - 1] += float(d["admas"])
+    icodt = np.zeros(numnod, np.int32)
+    off = np.asarray(d["bcs_offsets"])
+    bn = np.asarray(d["bcs_nodes"])
+    for k, (tra, rot) in enumerate(zip(d["bcs_tra"], d["bcs_rot"])):
+        code = _code_bits(str(tra), 1) | _code_bits(str(rot), 8)
+        icodt[bn[off[k]:off[k + 1]] - 1] |= code
+    V = np.zeros_like(X)
+    V[:, np.asarray(d["inivel_nodes"]) - 1] = np.asarray(d["inivel"], np.float64)[:, None]
+    m = Model(name, X, V, ms, icodt, shells=shells, IN=inr)
+    if with_links and len(d["rlink_nodes"]):
+        m.rlinks = [(np.asarray(d["rlink_nodes"], np.int32), 7, 0)]
+    m.ishfram = 2 if int(d["shfra_v4"]) else 0
+    return m

@@ -3,8 +3,8 @@
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` use this module, and only as a checker / reported baseline;
 the product never imports it.  See rg_oracle.cpp for what it restates and
-its parity status (pinned by analytic known-answer tests; unpinned against
-outputs of the reference engine itself).
+its parity status (shell path pinned against the reference engine's own
+outputs for its QA deck CRA2V44; hexa path by analytic known-answer tests).
 """
 from __future__ import annotations
 
@@ -53,6 +53,11 @@ def lib():
         L.or_energy.argtypes = [vp] + [C.c_void_p] * 4
         L.or_error.argtypes = [vp]
         L.or_get_shell_state.argtypes = [vp, C.c_int, _dp]
+        L.or_shell_frame.argtypes = [vp, C.c_int]
+        L.or_rlink_add.argtypes = [vp, C.c_int, _ip, C.c_int, C.c_int]
+        L.or_rlink_clear.argtypes = [vp]
+        L.or_set_record.argtypes = [vp, C.c_int]
+        L.or_get_record.argtypes = [vp, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -84,13 +89,19 @@ class OracleModel:
                                      np.ascontiguousarray(g.ixc.T.reshape(-1), np.int32),
                                      g.npt, g.mat["pm"], g.geo, g.mat["uparam"],
                                      g.mat["iparam"], np.ascontiguousarray(g.thk, np.float64),
-                                     2, 1)
+                                     g.ismstr, g.ithk)
             if r < 0:
                 raise RuntimeError("or_shell_group_add failed %d" % r)
         if model.IN is not None:
             L.or_set_inertia(self.h, np.ascontiguousarray(model.IN, np.float64))
         for (p0, nrm, ds) in model.rwalls:
             L.or_rwall_add(self.h, np.asarray(p0, np.float64), np.asarray(nrm, np.float64), ds)
+        for (nodes, ic, icr) in model.rlinks:
+            nodes = np.ascontiguousarray(nodes, np.int32)
+            if L.or_rlink_add(self.h, len(nodes), nodes, ic, icr) < 0:
+                raise RuntimeError("or_rlink_add failed")
+        if L.or_shell_frame(self.h, model.ishfram) != 0:
+            raise RuntimeError("or_shell_frame: unsupported ISHFRAM %d" % model.ishfram)
         nt = nthreads or os.cpu_count() or 1
         r = L.or_finalize(self.h, model.dtfac_solid, model.dtfac_shell, model.dtmx,
                           model.dt2old, nt)
@@ -149,3 +160,21 @@ class OracleModel:
 
     def error(self):
         return lib().or_error(self.h)
+
+    def clear_links(self):
+        lib().or_rlink_clear(self.h)
+
+    def set_record(self, on=True):
+        lib().or_set_record(self.h, 1 if on else 0)
+
+    def record(self):
+        """Listing quantities of the last cycle (ECRIT's point of the
+        cycle): time, dt, energies (internal, kinetic, rotational kinetic,
+        hourglass), momentum, mass, controlling element."""
+        out = np.zeros(10)
+        el = np.zeros(1, np.int32)
+        lib().or_get_record(self.h, _ptr(out), _ptr(el))
+        keys = ("tt", "dt2", "eint", "ekin", "ekinr", "ehour", "xmom", "ymom", "zmom", "mass")
+        r = dict(zip(keys, out.tolist()))
+        r["neltst"] = int(el[0])
+        return r

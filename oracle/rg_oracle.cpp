@@ -8,9 +8,10 @@
 // so that no multiply-add is fused.
 //
 // Parity status: the reference engine cannot be built here (no Fortran
-// compiler; the starter also needs an un-vendored binary library), so this
-// restatement is pinned by analytic known-answer tests, not by outputs of the
-// reference engine -- parity against the reference itself is unpinned.
+// compiler; the starter also needs an un-vendored binary library).  The shell
+// path is pinned against outputs the reference engine wrote for its own QA
+// deck CRA2V44 (printed cycle table to every digit, time histories to ~1e-6
+// relative over 3375 cycles); the hexa path by analytic known-answer tests.
 //
 // Each block cites the reference file:line it follows (paths relative to the
 // OpenRadioss source tree).
@@ -70,6 +71,18 @@ struct Model {
   int error = 0;
   bool finalized = false;
   double ehour_total = 0;
+
+  // rigid links between nodes (engine /VEL/TRA, RLINK1)
+  struct Link {
+    std::vector<int> nodes;  // 0-based
+    int ic = 0, icr = 0;     // direction codes: 4 = x, 2 = y, 1 = z
+  };
+  std::vector<Link> links;
+
+  // listing quantities of the last cycle, taken where ECRIT runs (after the
+  // kinematic conditions, before VELOCITY)
+  bool record = false;
+  double out[10] = {};
 };
 
 // ----------------------------------------------------------------------------
@@ -661,6 +674,7 @@ int rwall_add(Shells *, const double *p0, const double *nrm, double dsearch);
 void rwall_apply(Shells *, int numnod, const double *X, double *V,
                  const double *A, double dt12);
 int get_state(const Shells *, int which, double *out);
+int set_frame(Shells *, int ishfram);
 }  // namespace rg_oracle_shell
 
 struct OrModelWrap {
@@ -1049,6 +1063,89 @@ int or_cycle(void *m, int ncycle) {
         M.V[n3] = M.V[n3] - dv * W.n[2];
       }
     }
+    // RLINK1 (constraints/general/rlink/rlink1.F): every node of a link
+    // takes the mass-weighted mean acceleration of the link in the linked
+    // directions (IC bits 4 = x, 2 = y, 1 = z), after the boundary
+    // conditions (resol.F:7322 BCS10, then :7355 RLINK10).
+    for (auto &L : M.links) {
+      if (L.ic != 0) {
+        double mass = 0, ax = 0, ay = 0, az = 0;
+        for (int n : L.nodes) {
+          mass = mass + M.MS[n];
+          ax = ax + M.MS[n] * M.A[3 * n];
+          ay = ay + M.MS[n] * M.A[3 * n + 1];
+          az = az + M.MS[n] * M.A[3 * n + 2];
+        }
+        if (mass != RG_ZERO) {
+          ax = ax / mass;
+          ay = ay / mass;
+          az = az / mass;
+          for (int n : L.nodes) {
+            if (L.ic & 1) M.A[3 * n + 2] = az;
+            if (L.ic & 2) M.A[3 * n + 1] = ay;
+            if (L.ic & 4) M.A[3 * n] = ax;
+          }
+        }
+      }
+      if (L.icr != 0 && rot) {
+        double iner = 0, ax = 0, ay = 0, az = 0;
+        for (int n : L.nodes) {
+          iner = iner + M.IN[n];
+          ax = ax + M.IN[n] * M.AR[3 * n];
+          ay = ay + M.IN[n] * M.AR[3 * n + 1];
+          az = az + M.IN[n] * M.AR[3 * n + 2];
+        }
+        if (iner != RG_ZERO) {
+          ax = ax / iner;
+          ay = ay / iner;
+          az = az / iner;
+          for (int n : L.nodes) {
+            if (L.icr & 1) M.AR[3 * n + 2] = az;
+            if (L.icr & 2) M.AR[3 * n + 1] = ay;
+            if (L.icr & 4) M.AR[3 * n] = ax;
+          }
+        }
+      }
+    }
+    // ECRIT (output/ecrit.F:193, 266-330): energies of the printout with the
+    // velocities brought to the current time, V + DT1/2 * A.
+    if (M.record) {
+      const double dt05 = RG_HALF * M.dt1;
+      double ek = 0, ekr = 0, xm = 0, ym = 0, zm = 0, mass = 0;
+      for (int n = 0; n < numnod; n++) {
+        const double vx = M.V[3 * n] + dt05 * M.A[3 * n];
+        const double vy = M.V[3 * n + 1] + dt05 * M.A[3 * n + 1];
+        const double vz = M.V[3 * n + 2] + dt05 * M.A[3 * n + 2];
+        ek = ek + (vx * vx + vy * vy + vz * vz) * RG_HALF * M.MS[n];
+        xm = xm + vx * M.MS[n];
+        ym = ym + vy * M.MS[n];
+        zm = zm + vz * M.MS[n];
+        mass = mass + M.MS[n];
+        if (rot) {
+          const double rx = M.VR[3 * n] + dt05 * M.AR[3 * n];
+          const double ry = M.VR[3 * n + 1] + dt05 * M.AR[3 * n + 1];
+          const double rz = M.VR[3 * n + 2] + dt05 * M.AR[3 * n + 2];
+          ekr = ekr + (rx * rx + ry * ry + rz * rz) * RG_HALF * M.IN[n];
+        }
+      }
+      double ei = 0, eh = 0;
+      for (int e = 0; e < M.numels; e++) {
+        ei += M.eint[e] * M.vol[e];
+        eh += M.ehou[e];
+      }
+      double sei = 0, seh = 0;
+      rg_oracle_shell::energy(w->sh, sei, seh);
+      M.out[0] = M.tt;
+      M.out[1] = M.dt2;
+      M.out[2] = ei + sei;
+      M.out[3] = ek;
+      M.out[4] = ekr;
+      M.out[5] = eh + seh;
+      M.out[6] = xm;
+      M.out[7] = ym;
+      M.out[8] = zm;
+      M.out[9] = mass;
+    }
     // VELOCITY (velocity.F:59-75), DEPLA (displacement.F:68-100)
 #pragma omp parallel for schedule(static) num_threads(M.nthreads)
     for (int n = 0; n < numnod; n++) {
@@ -1149,6 +1246,41 @@ int or_energy(void *m, double *eint, double *ekin, double *ekinr,
 }
 
 int or_error(void *m) { return ((OrModelWrap *)m)->m.error; }
+
+int or_shell_frame(void *m, int ishfram) {
+  return rg_oracle_shell::set_frame(((OrModelWrap *)m)->sh, ishfram);
+}
+
+int or_rlink_add(void *m, int nsn, const int *nodes, int ic, int icr) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (nsn <= 0 || !nodes || ic < 0 || ic > 7 || icr < 0 || icr > 7) return -1;
+  Model::Link L;
+  for (int i = 0; i < nsn; i++) {
+    if (nodes[i] < 1 || nodes[i] > M.numnod) return -2;
+    L.nodes.push_back(nodes[i] - 1);
+  }
+  L.ic = ic;
+  L.icr = icr;
+  M.links.push_back(L);
+  return (int)M.links.size() - 1;
+}
+
+int or_rlink_clear(void *m) {
+  ((OrModelWrap *)m)->m.links.clear();
+  return 0;
+}
+
+int or_set_record(void *m, int on) {
+  ((OrModelWrap *)m)->m.record = on != 0;
+  return 0;
+}
+
+int or_get_record(void *m, double *out, int *neltst) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (out) std::copy(M.out, M.out + 10, out);
+  if (neltst) *neltst = M.neltst;
+  return 0;
+}
 
 int or_get_shell_state(void *m, int which, double *out) {
   return rg_oracle_shell::get_state(((OrModelWrap *)m)->sh, which, out);

@@ -8,10 +8,14 @@
  * time the CPU baseline; the product never links, loads or calls it.
  *
  * Parity status: the reference engine cannot be built here (no Fortran
- * compiler), so this restatement is pinned by analytic known-answer tests
- * (rigid-body motion, constant-strain patch test, elastic wave speed,
- * energy conservation, Johnson-Cook uniaxial yield) rather than by outputs of
- * the reference engine itself.
+ * compiler).  The shell path (CFORC3, LAW2, PARITH/ON assembly, ACCELE, BCS,
+ * rigid link, VELOCITY / DEPLA, time step) is pinned against outputs of the
+ * reference engine itself: its QA deck CRA2V44 (768 shells, 3375 cycles over
+ * a run and a restart), whose printed cycle table the oracle reproduces to
+ * every printed digit and whose time histories to ~1e-6 relative
+ * (tests/test_oracle_cra2.py).  The hexa path is pinned by analytic
+ * known-answer tests (rigid-body motion, constant-strain patch test, elastic
+ * wave speed, energy conservation, Johnson-Cook uniaxial yield).
  *
  * Conventions follow the reference: nodal arrays are X(3,NUMNOD) (xyz
  * interleaved), IXS(11,NUMELS) columns hold {mat, n1..n8 (1-based), prop,
@@ -72,6 +76,21 @@ int or_get_hexa_state(void *m, int group, int which, double *out);
 int or_energy(void *m, double *eint, double *ekin, double *ekinr,
               double *ehour);
 int or_error(void *m);
+
+/* Local shell frame: 0 = symmetric convected frame (default), 2 = the
+ * version-4 frame of /SHFRA/V4 (CNVEC3, cnvec3.F:143-170). */
+int or_shell_frame(void *m, int ishfram);
+/* Rigid link (engine /VEL/TRA|ROT, RLINK1): nodes 1-based, ic / icr the
+ * translational / rotational direction bits (4 = x, 2 = y, 1 = z).  Applied
+ * after the boundary conditions of every cycle.  or_rlink_clear removes all
+ * links (a restart whose engine deck has no /VEL card). */
+int or_rlink_add(void *m, int nsn, const int *nodes, int ic, int icr);
+int or_rlink_clear(void *m);
+/* Listing record of the last cycle (what ECRIT prints): out[0..9] = TT, DT2,
+ * internal energy, kinetic energy and rotational kinetic energy of
+ * V + DT1/2 A, hourglass energy, x/y/z momentum, mass.  Off by default. */
+int or_set_record(void *m, int on);
+int or_get_record(void *m, double *out, int *neltst);
 /* Shell state: which = 0 FOR (5 x nc), 1 MOM (3 x nc), 2 THK, 3 EINT
  * (2 x nc), 4 OFF, 5 SIG (5 x npt x nc), 6 PLA (npt x nc), 7 HOUR (5 x nc). */
 int or_get_shell_state(void *m, int which, double *out);

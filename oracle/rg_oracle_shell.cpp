@@ -2,9 +2,10 @@
 //
 // Restates, per element and in the reference's expression order, the CFORC3
 // chain for the pinned formulation: Ishell=1 (IHBE=1, viscous/elastic
-// hourglass CHVIS3), Ismstr=4 (no small-strain reference storage), Ithick=1
-// (thickness update), NPT through-thickness points with the COQINI tables,
-// ISHFRAM=0 (CNVEC3 frame), Johnson-Cook plane stress (SIGEPS02C + M2CPLR)
+// hourglass CHVIS3), Ismstr=2/4 (no small-strain reference storage), Ithick=1
+// (current thickness) or 0 (initial thickness), NPT through-thickness points
+// with the COQINI tables, ISHFRAM=0 (symmetric CNVEC3 frame) or 2 (the
+// version-4 non-symmetric frame of /SHFRA/V4), Johnson-Cook plane stress (SIGEPS02C + M2CPLR)
 // with Iplas=1 (3 Newton iterations) or Iplas=0 (radial return), element
 // time step (NODADT=0, IDTMIN(3)=2), PARITH/ON slot writes (CUPDT3P).
 // Conventions: see rg_oracle.cpp.  Paths are relative to the OpenRadioss
@@ -60,9 +61,15 @@ struct Shells {
   std::vector<double> sig, pla, epsd;  // per IP: [npt][numelc] (max npt 5)
   std::vector<double> ehou;            // accumulated hourglass energy
   int nptmax = 5;
+  int ishfram = 0;                     // local frame (/SHFRA/V4: 2)
 };
 
 Shells *create() { return new Shells(); }
+int set_frame(Shells *s, int ishfram) {
+  if (ishfram != 0 && ishfram != 2) return -1;
+  s->ishfram = ishfram;
+  return 0;
+}
 void destroy(Shells *s) { delete s; }
 int numelc(const Shells *s) { return s->numelc; }
 const int *ixc(const Shells *s) { return s->ixc.data(); }
@@ -167,7 +174,8 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     for (int k = 0; k < 4; k++)
       for (int c = 0; c < 3; c++) vl[k][c] = vrl[k][c] = RG_ZERO;
   double thk0 = S->thke[e];
-  // ---- CNVEC3 (cnvec3.F:35), ISHFRAM = 0 ----
+  // ---- CNVEC3 (cnvec3.F:35), ISHFRAM = 0 (cnvec3.F:117-141) or 2
+  // (cnvec3.F:143-170) ----
   double e1x, e1y, e1z, e2x, e2y, e2z, e3x, e3y, e3z;
   {
     const double x21 = xg[1] - xg[0], x32 = xg[2] - xg[1], x34 = xg[2] - xg[3], x41 = xg[3] - xg[0];
@@ -182,6 +190,32 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     e3x = e1y * e2z - e1z * e2y;
     e3y = e1z * e2x - e1x * e2z;
     e3z = e1x * e2y - e1y * e2x;
+    if (S->ishfram == 2) {
+      // version-4 frame: e1 along the mean of the two x-sides, tilted by
+      // e2 x e3, then normalised; e2 = e3 x e1
+      double suma = e2x * e2x + e2y * e2y + e2z * e2z;
+      e1x = e1x * suma + e2y * e3z - e2z * e3y;
+      e1y = e1y * suma + e2z * e3x - e2x * e3z;
+      e1z = e1z * suma + e2x * e3y - e2y * e3x;
+      suma = e1x * e1x + e1y * e1y + e1z * e1z;
+      suma = RG_ONE / dmax(std::sqrt(suma), RG_EM20);
+      e1x = e1x * suma;
+      e1y = e1y * suma;
+      e1z = e1z * suma;
+      suma = e3x * e3x + e3y * e3y + e3z * e3z;
+      suma = RG_ONE / dmax(std::sqrt(suma), RG_EM20);
+      e3x = e3x * suma;
+      e3y = e3y * suma;
+      e3z = e3z * suma;
+      e2x = e3y * e1z - e3z * e1y;
+      e2y = e3z * e1x - e3x * e1z;
+      e2z = e3x * e1y - e3y * e1x;
+      suma = e2x * e2x + e2y * e2y + e2z * e2z;
+      suma = RG_ONE / dmax(std::sqrt(suma), RG_EM20);
+      e2x = e2x * suma;
+      e2y = e2y * suma;
+      e2z = e2z * suma;
+    } else {
     double suma = e3x * e3x + e3y * e3y + e3z * e3z;
     suma = RG_ONE / dmax(std::sqrt(suma), RG_EM20);
     e3x = e3x * suma;
@@ -201,6 +235,7 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     e2x = e3y * e1z - e3z * e1y;
     e2y = e3z * e1x - e3x * e1z;
     e2z = e3x * e1y - e3y * e1x;
+    }
   }
   // ---- CDERI3 (cderi3.F:30), ISMSTR = 4 ----
   double x2, y2, x3, y3, x4, y4, z2, px1, px2, py1, py2, area, vhx, vhy;
@@ -223,9 +258,10 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     vhx = (-x2 + x3 - x4) / area;
     vhy = (-y2 + y3 - y4) / area;
   }
-  // ---- CCOEF3 (ccoef3.F:30), ITHK > 0 ----
+  // ---- CCOEF3 (ccoef3.F:74-90): ITHK > 0 works on the current thickness,
+  // ITHK = 0 on the initial one (THK0 = THKE from CCOOR3, ccoor3.F:80) ----
   const double vol00 = thk0 * area;
-  thk0 = S->thk[e];
+  if (G.ithk > 0) thk0 = S->thk[e];
   const double vol0 = thk0 * area;
   const double thk02 = thk0 * thk0;
   const double rho = G.rho, ym = G.young, nu = G.nu, gmod = G.g, a11 = G.a11;
