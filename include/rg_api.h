@@ -101,6 +101,25 @@ int rg_shell_group_add(rg_ctx *ctx, int nel, const int *ixc, int npt,
 int rg_rwall_add(rg_ctx *ctx, const double *p0, const double *nrm,
                  double dsearch);
 
+/* Rigid link between nodes: the engine deck's /VEL/TRA|ROT card, applied by
+ * RLINK10 -> RLINK1 (engine/source/constraints/general/rlink/rlink10.F:38,
+ * rlink1.F) after the boundary conditions of every cycle (resol.F:7355).
+ * The nsn nodes (1-based) take the mass-weighted mean acceleration of the
+ * link in the directions of ic and the inertia-weighted mean rotational
+ * acceleration in those of icr (bits 4 = x, 2 = y, 1 = z; /VEL/TRA/XYZ is
+ * ic = 7).  Before rg_finalize; a node belongs to one link at most.
+ * Returns the link index. */
+int rg_rlink_add(rg_ctx *ctx, int nsn, const int *nodes, int ic, int icr);
+
+/* Switch link `link` on or off between cycles (a restart whose engine deck
+ * no longer has the /VEL card); ordered after the cycles already queued. */
+int rg_rlink_set_active(rg_ctx *ctx, int link, int active);
+
+/* Local shell frame of CNVEC3 (cnvec3.F:117-170): ISHFRAM 0 (symmetric
+ * convected frame, default) or 2 (the starter's /SHFRA/V4, contrl.F:495-498).
+ * Before rg_finalize. */
+int rg_set_shell_frame(rg_ctx *ctx, int ishfram);
+
 /* Optional: PARITH/ON tables from the engine (ADSKY(NUMNOD+1), IADS(8,
  * NUMELS), IADC(4,NUMELC), 1-based; FILLCNE order, starter/source/spmd/
  * domdec2.F:2046).  Without this call rg_finalize builds them in that order. */

@@ -23,6 +23,7 @@ using namespace rg;
 namespace {
 
 constexpr int NODE_NT = 256;
+constexpr int LINK_NT = 128;
 constexpr int DT_NT = 1024;
 constexpr int EN_BLOCKS = 304;  // 2 x 152 SMs, fixed: reductions are order-fixed
 constexpr int EN_NT = 256;
@@ -56,16 +57,96 @@ int dalloc(rg_ctx *c, T **p, size_t n) {
   return RG_OK;
 }
 
-// Node kernel: one thread per node (node_update in rg_node.cuh).
-template <bool F64, bool ROT>
+// Node kernels: one thread per node (node_update in rg_node.cuh); LINK:
+// the model has rigid links; the link-free variants are the hot path.
+template <bool F64, bool LINK>
 __global__ void __launch_bounds__(NODE_NT)
 node_kernel(NodeView N, const int *__restrict__ adsky, const void *__restrict__ fsky_,
             const void *__restrict__ fskyr_, const Time *__restrict__ T,
             const int *__restrict__ wall, const double *__restrict__ walls,
-            int *__restrict__ status) {
+            const dbl4 *__restrict__ lacc, int *__restrict__ status) {
   const int n = blockIdx.x * NODE_NT + threadIdx.x;
   if (n >= N.numnod) return;
-  node_update<F64, ROT>(N, adsky, fsky_, fskyr_, T, wall, walls, status, n);
+  node_update<F64, false, false, LINK>(N, adsky, fsky_, fskyr_, T, wall, walls, lacc, status, n);
+}
+
+template <bool F64, bool LINK>
+__global__ void __launch_bounds__(NODE_NT)
+node_kernel_rot(NodeView N, const int *__restrict__ adsky, const void *__restrict__ fsky_,
+                const void *__restrict__ fskyr_, const Time *__restrict__ T,
+                const int *__restrict__ wall, const double *__restrict__ walls,
+                const dbl4 *__restrict__ lacc, int *__restrict__ status) {
+  const int n = blockIdx.x * NODE_NT + threadIdx.x;
+  if (n >= N.numnod) return;
+  node_update<F64, true, false, LINK>(N, adsky, fsky_, fskyr_, T, wall, walls, lacc, status, n);
+}
+
+// Rigid links, RLINK1 (constraints/general/rlink/rlink1.F) as called by
+// RLINK10 after the boundary conditions: block l forms link l's mass (and
+// inertia) and the mass- (inertia-) weighted sums of its nodes'
+// accelerations -- each node's acceleration computed as the node kernel
+// computes it (ASSPAR4 sums, ACCELE, BCS) -- in a fixed order (strided
+// per-thread sums, then a fixed tree), and writes the common accelerations
+// (AX/MASS ...) that the node kernel gives the linked directions.  An
+// inactive link, or one of zero mass, writes direction bits 0 (no effect).
+template <bool F64, bool ROT>
+__global__ void __launch_bounds__(LINK_NT)
+rlink_kernel(NodeView N, const int *__restrict__ adsky, const void *__restrict__ fsky_,
+             const void *__restrict__ fskyr_, const int *__restrict__ lnodes,
+             const int *__restrict__ loff, const int4 *__restrict__ lic,
+             dbl4 *__restrict__ lacc, int *__restrict__ status) {
+  const int l = blockIdx.x;
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = loff[l] + threadIdx.x; i < loff[l + 1]; i += LINK_NT) {
+    const int n = lnodes[i];
+    double a0, a1, a2, r0, r1, r2;
+    node_assemble<F64, ROT, false>(adsky, fsky_, fskyr_, status, n, a0, a1, a2, r0, r1, r2);
+    const dbl4 x = N.X4[n];
+    const int code = (int)N.V4[n].w;
+    const double ms = N.D4[n].w;
+    a0 = __dmul_rn(a0, x.w);
+    a1 = __dmul_rn(a1, x.w);
+    a2 = __dmul_rn(a2, x.w);
+    if (code & 1) a0 = 0.0;
+    if (code & 2) a1 = 0.0;
+    if (code & 4) a2 = 0.0;
+    s[0] = __dadd_rn(s[0], ms);
+    s[1] = __dadd_rn(s[1], __dmul_rn(ms, a0));
+    s[2] = __dadd_rn(s[2], __dmul_rn(ms, a1));
+    s[3] = __dadd_rn(s[3], __dmul_rn(ms, a2));
+    if (ROT) {
+      const double rin = N.VR4[n].w, in = N.DR4[n].w;
+      r0 = __dmul_rn(r0, rin);
+      r1 = __dmul_rn(r1, rin);
+      r2 = __dmul_rn(r2, rin);
+      if (code & 8) r0 = 0.0;
+      if (code & 16) r1 = 0.0;
+      if (code & 32) r2 = 0.0;
+      s[4] = __dadd_rn(s[4], in);
+      s[5] = __dadd_rn(s[5], __dmul_rn(in, r0));
+      s[6] = __dadd_rn(s[6], __dmul_rn(in, r1));
+      s[7] = __dadd_rn(s[7], __dmul_rn(in, r2));
+    }
+  }
+  __shared__ double sh[8][LINK_NT];
+  for (int j = 0; j < 8; j++) sh[j][threadIdx.x] = s[j];
+  __syncthreads();
+  for (int o = LINK_NT / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int j = 0; j < 8; j++) sh[j][threadIdx.x] = __dadd_rn(sh[j][threadIdx.x], sh[j][threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int4 c = lic[l];
+    dbl4 t = mk4(0, 0, 0, 0), u = mk4(0, 0, 0, 0);
+    const double mass = sh[0][0], iner = sh[4][0];
+    if (c.z && c.x && mass != 0.0)
+      t = mk4(sh[1][0] / mass, sh[2][0] / mass, sh[3][0] / mass, (double)c.x);
+    if (ROT && c.z && c.y && iner != 0.0)
+      u = mk4(sh[5][0] / iner, sh[6][0] / iner, sh[7][0] / iner, (double)c.y);
+    lacc[2 * l] = t;
+    lacc[2 * l + 1] = u;
+  }
 }
 
 // Mixed form: refresh the FP32 copies from the FP64 node records (after a
@@ -415,22 +496,44 @@ int enqueue_elements(rg_ctx *c, int advance) {
   return RG_OK;
 }
 
-int enqueue_nodes(rg_ctx *c) {
+template <bool F64, bool ROT>
+void launch_nodes(rg_ctx *c) {
   const int nb = (c->numnod + NODE_NT - 1) / NODE_NT;
+  const void *fr = ROT ? c->d_fskyr : nullptr;
+  if (c->nlinks)
+    rlink_kernel<F64, ROT><<<c->nlinks, LINK_NT, 0, c->stream>>>(
+        c->nv, c->d_adsky, c->d_fsky, fr, c->d_lnodes, c->d_loff, c->d_lic, c->d_lacc,
+        c->d_status);
+  const dbl4 *lacc = c->d_lacc;
+  cudaStream_t s = c->stream;
+  if (ROT) {
+    if (c->nlinks)
+      node_kernel_rot<F64, true><<<nb, NODE_NT, 0, s>>>(c->nv, c->d_adsky, c->d_fsky, fr, c->d_time,
+                                                        c->d_wall, c->d_walls, lacc, c->d_status);
+    else
+      node_kernel_rot<F64, false><<<nb, NODE_NT, 0, s>>>(c->nv, c->d_adsky, c->d_fsky, fr, c->d_time,
+                                                         c->d_wall, c->d_walls, nullptr, c->d_status);
+  } else {
+    if (c->nlinks)
+      node_kernel<F64, true><<<nb, NODE_NT, 0, s>>>(c->nv, c->d_adsky, c->d_fsky, fr, c->d_time,
+                                                    c->d_wall, c->d_walls, lacc, c->d_status);
+    else
+      node_kernel<F64, false><<<nb, NODE_NT, 0, s>>>(c->nv, c->d_adsky, c->d_fsky, fr, c->d_time,
+                                                     c->d_wall, c->d_walls, nullptr, c->d_status);
+  }
+}
+
+int enqueue_nodes(rg_ctx *c) {
   if (c->prec == RG_PREC_FP64) {
     if (c->rot)
-      node_kernel<true, true><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, c->d_fsky, c->d_fskyr, c->d_time, c->d_wall, c->d_walls, c->d_status);
+      launch_nodes<true, true>(c);
     else
-      node_kernel<true, false><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, c->d_fsky, nullptr, c->d_time, c->d_wall, c->d_walls, c->d_status);
+      launch_nodes<true, false>(c);
   } else {
     if (c->rot)
-      node_kernel<false, true><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, c->d_fsky, c->d_fskyr, c->d_time, c->d_wall, c->d_walls, c->d_status);
+      launch_nodes<false, true>(c);
     else
-      node_kernel<false, false><<<nb, NODE_NT, 0, c->stream>>>(
-          c->nv, c->d_adsky, c->d_fsky, nullptr, c->d_time, c->d_wall, c->d_walls, c->d_status);
+      launch_nodes<false, false>(c);
   }
   return RG_OK;
 }
@@ -619,6 +722,46 @@ int rg_rwall_add(rg_ctx *c, const double *p0, const double *nrm, double dsearch)
   return (int)c->walls.size() - 1;
 }
 
+int rg_rlink_add(rg_ctx *c, int nsn, const int *nodes, int ic, int icr) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "rigid link added after rg_finalize");
+  if (c->numnod <= 0) return fail(c, RG_E_STATE, "rg_mesh_upload first");
+  if (nsn <= 0 || !nodes) return fail(c, RG_E_ARG, "rg_rlink_add: bad arguments");
+  if (ic < 0 || ic > 7 || icr < 0 || icr > 7)
+    return fail(c, RG_E_ARG, "rg_rlink_add: direction codes must be 0..7");
+  LinkHost L;
+  for (int i = 0; i < nsn; i++) {
+    if (nodes[i] < 1 || nodes[i] > c->numnod) return fail(c, RG_E_ARG, "rigid link node out of range");
+    L.nodes.push_back(nodes[i] - 1);
+  }
+  L.ic = ic;
+  L.icr = icr;
+  c->links.push_back(L);
+  return (int)c->links.size() - 1;
+}
+
+int rg_rlink_set_active(rg_ctx *c, int link, int active) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  if (link < 0 || link >= c->nlinks) return fail(c, RG_E_ARG, "no such rigid link");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  // ordered after the cycles already queued on the context's stream
+  const LinkHost &L = c->links[link];
+  c->h_link = make_int4(L.ic, L.icr, active ? 1 : 0, 0);
+  RG_CUDA(c, cudaMemcpyAsync(c->d_lic + link, &c->h_link, sizeof(int4), cudaMemcpyHostToDevice,
+                             c->stream));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return RG_OK;
+}
+
+int rg_set_shell_frame(rg_ctx *c, int ishfram) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "rg_set_shell_frame after rg_finalize");
+  if (ishfram != 0 && ishfram != 2) return fail(c, RG_E_UNSUP, "ISHFRAM must be 0 or 2");
+  c->shells.ishfram = ishfram;
+  return RG_OK;
+}
+
 int rg_skyline_set(rg_ctx *c, const int *adsky, const int *iads, const int *iadc) {
   if (!c || !adsky) return RG_E_ARG;
   if (c->finalized) return fail(c, RG_E_STATE, "skyline set after rg_finalize");
@@ -659,6 +802,14 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   if (!check_skyline(numnod, ne, nc, c->adsky, c->iads, c->iadc, c->lsky, why))
     return fail(c, RG_E_ARG, "skyline: " + why);
   int r;
+  // rigid links: 1-based link index per node, carried in the node code
+  c->nlinks = (int)c->links.size();
+  std::vector<int> lnk(numnod, 0);
+  for (int l = 0; l < c->nlinks; l++)
+    for (int n : c->links[l].nodes) {
+      if (lnk[n]) return fail(c, RG_E_ARG, "a node belongs to two rigid links");
+      lnk[n] = l + 1;
+    }
   // nodes
   // X4.w = 1/MS and VR4.w = 1/IN: ACCELE's RTMP = ONE/MS(N) evaluated once
   // (the same IEEE quotient), D4.w = MS and DR4.w = IN for the energies.
@@ -667,7 +818,8 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   for (int n = 0; n < numnod; n++) {
     const double ms = c->MS[n], in = c->IN[n];
     x4[n] = mk4(c->X[3 * n], c->X[3 * n + 1], c->X[3 * n + 2], ms > 0.0 ? 1.0 / ms : 0.0);
-    v4[n] = mk4(c->V[3 * n], c->V[3 * n + 1], c->V[3 * n + 2], (double)c->icodt[n]);
+    v4[n] = mk4(c->V[3 * n], c->V[3 * n + 1], c->V[3 * n + 2],
+                (double)(c->icodt[n] | (lnk[n] << RG_LINK_SHIFT)));
     // D4: displacement (FP64 form) or initial position (mixed form), MS
     z4[n] = c->prec == RG_PREC_MIXED
                 ? mk4(c->X[3 * n], c->X[3 * n + 1], c->X[3 * n + 2], ms)
@@ -802,6 +954,22 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     if ((r = dalloc(c, &c->d_walls, 6 * c->nwalls))) return r;
     RG_CUDA(c, cudaMemcpy(c->d_wall, wn.data(), numnod * sizeof(int), cudaMemcpyHostToDevice));
     RG_CUDA(c, cudaMemcpy(c->d_walls, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (c->nlinks) {
+    std::vector<int> ln, lo(1, 0);
+    std::vector<int4> li;
+    for (auto &L : c->links) {
+      ln.insert(ln.end(), L.nodes.begin(), L.nodes.end());
+      lo.push_back((int)ln.size());
+      li.push_back(make_int4(L.ic, L.icr, 1, 0));
+    }
+    if ((r = dalloc(c, &c->d_lnodes, ln.size()))) return r;
+    if ((r = dalloc(c, &c->d_loff, lo.size()))) return r;
+    if ((r = dalloc(c, &c->d_lic, li.size()))) return r;
+    if ((r = dalloc(c, &c->d_lacc, 2 * li.size()))) return r;
+    RG_CUDA(c, cudaMemcpy(c->d_lnodes, ln.data(), ln.size() * sizeof(int), cudaMemcpyHostToDevice));
+    RG_CUDA(c, cudaMemcpy(c->d_loff, lo.data(), lo.size() * sizeof(int), cudaMemcpyHostToDevice));
+    RG_CUDA(c, cudaMemcpy(c->d_lic, li.data(), li.size() * sizeof(int4), cudaMemcpyHostToDevice));
   }
   {
     const int ng = (c->nparts + DT_GROUP - 1) / DT_GROUP;

@@ -252,10 +252,10 @@ batch_kernel(const BatchDev<ER> B, const int phases) {
         const int n = nt.n0 + k * BNT + threadIdx.x;
         if (n < nn) {
           if (J.rot)
-            node_update<F64, true, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls,
+            node_update<F64, true, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                          J.status, n);
           else
-            node_update<F64, false, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls,
+            node_update<F64, false, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                           J.status, n);
         }
       }
@@ -289,10 +289,10 @@ batch_node_kernel(const BatchDev<ER> B) {
       const int n = nt.n0 + i;
       if (n < nn) {
         if (J.rot)
-          node_update<F64, true, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls,
+          node_update<F64, true, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                        J.status, n);
         else
-          node_update<F64, false, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls,
+          node_update<F64, false, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                         J.status, n);
       }
     }
@@ -639,6 +639,7 @@ int rg_batch_add(rg_batch *b, rg_ctx *c, int target_ncycle) {
   if (!b || !c) return RG_E_ARG;
   if (!c->finalized) return bfail(b, RG_E_STATE, "batch: job context not finalized");
   if (c->device != b->device) return bfail(b, RG_E_ARG, "batch: job on another device");
+  if (c->nlinks) return bfail(b, RG_E_UNSUP, "batch: jobs with rigid links run alone (rg_cycle)");
   bool any = false;
   for (auto *q : b->jobs) any = any || q;
   if (any && c->prec != b->prec)

@@ -22,11 +22,17 @@ struct WallHost {
   double p0[3], n[3], dsearch;
 };
 
+struct LinkHost {
+  std::vector<int> nodes;  // 0-based
+  int ic = 0, icr = 0;     // direction bits 4 = x, 2 = y, 1 = z
+};
+
 }  // namespace rg
 
 struct rg_ctx {
   typedef rg::HexaGroupHost HexaGroupHost;
   typedef rg::WallHost WallHost;
+  typedef rg::LinkHost LinkHost;
   typedef rg::ShellModelHost ShellModelHost;
   typedef rg::NodeView NodeView;
   typedef rg::Time Time;
@@ -50,6 +56,7 @@ struct rg_ctx {
   std::vector<HexaGroupHost> hg;
   ShellModelHost shells;  // rg_shell.h
   std::vector<WallHost> walls;
+  std::vector<LinkHost> links;
   std::vector<int> adsky, iads, iadc;  // 1-based as given / built
   bool skyline_given = false;
   int lsky = 0;
@@ -74,6 +81,13 @@ struct rg_ctx {
   int *d_wall = nullptr;       // per node: wall index or -1
   double *d_walls = nullptr;   // 6 doubles per wall (p0, n)
   int nwalls = 0;
+  // rigid links: node lists (concatenated, 0-based), offsets, (ic, icr,
+  // active, 0) per link, and the common accelerations (2 per link)
+  int nlinks = 0;
+  int *d_lnodes = nullptr, *d_loff = nullptr;
+  int4 *d_lic = nullptr;
+  rg::dbl4 *d_lacc = nullptr;
+  int4 h_link = {0, 0, 0, 0};  // source of rg_rlink_set_active's copy
   bool rot = false;
   // staging for forint_step / downloads
   double *d_stage = nullptr;   // 12 * numnod doubles

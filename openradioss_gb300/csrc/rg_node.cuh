@@ -7,6 +7,10 @@
 
 namespace rg {
 
+// node code: bits below RG_LINK_SHIFT hold the boundary code, the bits above
+// the 1-based rigid-link index
+constexpr int RG_LINK_SHIFT = 8;
+
 // ---------------------------------------------------------------------------
 // Node update: ASSPAR4 (asspar4.F:165-180) fixed-order slot sums, ACCELE
 // (accele.F:66-78), BCS10/BCS1V (bcs10.F:31), planar rigid wall, VELOCITY
@@ -46,18 +50,19 @@ __device__ __forceinline__ dbl4 ldcg4(const dbl4 *p) {
   return mk4(a.x, a.y, b.x, b.y);
 }
 
-// COH = true: the slots and the time-step scalars were written earlier in
+// ASSPAR4 sums of node n: A (and AR) = 0 + the node's slots in PARITH/ON
+// order; FP64 slots summed in FP64, the mixed form's FP32 slots in FP32 (no
+// reassociation) and widened.  COH = true: the slots were written earlier in
 // the same launch by other blocks, so they are read through L2.
-template <bool F64, bool ROT, bool COH = false>
-__device__ __forceinline__ void node_update(const NodeView &N, const int *__restrict__ adsky,
-                                            const void *__restrict__ fsky_,
-                                            const void *__restrict__ fskyr_,
-                                            const Time *__restrict__ T,
-                                            const int *__restrict__ wall,
-                                            const double *__restrict__ walls,
-                                            int *__restrict__ status, const int n) {
+template <bool F64, bool ROT, bool COH>
+__device__ __forceinline__ void node_assemble(const int *__restrict__ adsky,
+                                              const void *__restrict__ fsky_,
+                                              const void *__restrict__ fskyr_,
+                                              int *__restrict__ status, const int n,
+                                              double &a0, double &a1, double &a2,
+                                              double &r0, double &r1, double &r2) {
   const int k0 = __ldg(adsky + n), k1 = __ldg(adsky + n + 1);
-  double a0, a1, a2, r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  r0 = r1 = r2 = 0.0;
   if constexpr (F64) {
     // ASSPAR4: A = 0 + sum of the node's slots in PARITH/ON order, FP64
     const dbl4 *fsky = (const dbl4 *)fsky_;
@@ -102,6 +107,23 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     r1 = c1;
     r2 = c2;
   }
+}
+
+// COH = true: the slots and the time-step scalars were written earlier in
+// the same launch by other blocks, so they are read through L2.  LINK: the
+// model has rigid links; lacc holds their common accelerations (rlink
+// kernel).
+template <bool F64, bool ROT, bool COH = false, bool LINK = false>
+__device__ __forceinline__ void node_update(const NodeView &N, const int *__restrict__ adsky,
+                                            const void *__restrict__ fsky_,
+                                            const void *__restrict__ fskyr_,
+                                            const Time *__restrict__ T,
+                                            const int *__restrict__ wall,
+                                            const double *__restrict__ walls,
+                                            const dbl4 *__restrict__ lacc,
+                                            int *__restrict__ status, const int n) {
+  double a0, a1, a2, r0, r1, r2;
+  node_assemble<F64, ROT, COH>(adsky, fsky_, fskyr_, status, n, a0, a1, a2, r0, r1, r2);
   dbl4 x = ld4(N.X4 + n);
   dbl4 v = ld4(N.V4 + n);
   // FP64 form: D4 = displacement, MS.  Mixed form: D4 holds the initial
@@ -114,11 +136,23 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
   a0 = __dmul_rn(a0, x.w);
   a1 = __dmul_rn(a1, x.w);
   a2 = __dmul_rn(a2, x.w);
+  // node code: BCS bits 1/2/4 (x/y/z), 8/16/32 (rotations); above them the
+  // 1-based index of the node's rigid link (0: none)
   const int code = (int)v.w;
   if (code) {
     if (code & 1) a0 = 0.0;
     if (code & 2) a1 = 0.0;
     if (code & 4) a2 = 0.0;
+  }
+  // RLINK1 (rlink1.F), after the boundary conditions (resol.F:7322, 7355):
+  // the linked directions take the link's common acceleration
+  const int lk = LINK ? code >> RG_LINK_SHIFT : 0;
+  if (LINK && lk > 0) {
+    const dbl4 L = lacc[2 * (lk - 1)];
+    const int ic = (int)L.w;
+    if (ic & 4) a0 = L.x;
+    if (ic & 2) a1 = L.y;
+    if (ic & 1) a2 = L.z;
   }
   // RGWALL (constraints/general/rwall/rgwall.F:33), fixed infinite plane,
   // sliding: a slave node whose predicted position X + (V + A*DT12)*DT2 is
@@ -193,6 +227,13 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
       if (code & 8) r0 = 0.0;
       if (code & 16) r1 = 0.0;
       if (code & 32) r2 = 0.0;
+    }
+    if (LINK && lk > 0) {
+      const dbl4 L = lacc[2 * (lk - 1) + 1];
+      const int icr = (int)L.w;
+      if (icr & 4) r0 = L.x;
+      if (icr & 2) r1 = L.y;
+      if (icr & 1) r2 = L.z;
     }
     vr.x = __dadd_rn(vr.x, __dmul_rn(dt12, r0));
     vr.y = __dadd_rn(vr.y, __dmul_rn(dt12, r1));

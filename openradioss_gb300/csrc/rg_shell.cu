@@ -110,8 +110,8 @@ int shell_group_add(ShellModelHost &S, int numnod, int nel, const int *ixc, int 
     why = "shell: supported ISMSTR is 4 (2 accepted, run without the small-strain switch)";
     return RG_E_UNSUP;
   }
-  if (ithk <= 0) {
-    why = "shell: supported formulation is ITHK > 0 (thickness update)";
+  if (ithk < 0) {
+    why = "shell: ITHK must be 0 (initial thickness) or > 0 (current thickness)";
     return RG_E_UNSUP;
   }
   if (iparam[0] != 0 || uparam[7] != 0.0) {
@@ -134,6 +134,8 @@ int shell_group_add(ShellModelHost &S, int numnod, int nel, const int *ixc, int 
   P.nft = S.numelc;
   P.nel = nel;
   P.npt = npt;
+  P.ithk = ithk > 0 ? 1 : 0;
+  P.ishfram = 0;  // set for every group at finalize (a model-wide option)
   P.ipla = (int)geo[38];
   if (P.ipla != 0 && P.ipla != 1) {
     delete g;
@@ -282,6 +284,7 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
   for (auto *g : S.groups) {
     g->P.part_off = part_off;
     g->P.dtfac = dtfac;
+    g->P.ishfram = S.ishfram;
     shell_params_mirror(g->P);
     part_off += shell_blocks(g->P.nel);
   }

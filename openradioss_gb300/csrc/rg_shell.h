@@ -16,6 +16,7 @@ struct ShellModelHost {
   std::vector<double> thk0;             // initial thickness per shell
   std::vector<ShellGroupHost *> groups;
   int key0 = 0;                         // dt-order key of the first shell
+  int ishfram = 0;                      // local frame of every group (0 / 2)
   void *dev = nullptr;                  // device arrays (rg_shell.cu)
 };
 

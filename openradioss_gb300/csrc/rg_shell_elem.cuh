@@ -7,9 +7,9 @@
 // The arithmetic follows, step by step and in the same expression order,
 // the reference routines (paths relative to the OpenRadioss source tree):
 //   CCOOR3 gather            elements/shell/coque/ccoor3.F:31
-//   CNVEC3 convected frame   elements/shell/coque/cnvec3.F:35 (ISHFRAM = 0)
+//   CNVEC3 convected frame   elements/shell/coque/cnvec3.F:35 (ISHFRAM 0 or 2)
 //   CDERI3 local geometry    elements/shell/coque/cderi3.F:30 (ISMSTR = 4)
-//   CCOEF3 coefficients      elements/shell/coque/ccoef3.F:30 (ITHK > 0)
+//   CCOEF3 coefficients      elements/shell/coque/ccoef3.F:30 (ITHK 1 or 0)
 //   CDLEN3 length for dt     elements/shell/coque/cdlen3.F:30
 //   CDEFO3 membrane rates    elements/shell/coque/cdefo3.F:30 (IHBE <= 1)
 //   CCURV3 curvature rates   elements/shell/coque/ccurv3.F:30
@@ -34,11 +34,13 @@ namespace rg {
 
 struct ShellParams {
   int nft, nel, npt, ipla;
-  int part_off, pad;
+  int part_off;
+  int ishfram;  // local frame: 0 symmetric (default), 2 version-4 (/SHFRA/V4)
   double rho, young, nu, g, a11, ssp;
   double h1, h2, h3, srh1, srh2, srh3, dm, ish, fsh;
   double ca, cb, cn, ymax, cc, eps0, pm9;
-  int icc, vp, israte, pad2;
+  int icc, vp, israte;
+  int ithk;     // 1: current thickness in CCOEF3, 0: initial thickness
   double dtfac;
   // group constants derived once on the host (they are the same for every
   // element of the group): plane-stress moduli, 1/(1-NU), 1/(1+NU),
@@ -265,25 +267,53 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       e3x = e1y * e2z - e1z * e2y;
       e3y = e1z * e2x - e1x * e2z;
       e3z = e1x * e2y - e1y * e2x;
-      R suma = e3x * e3x + e3y * e3y + e3z * e3z;
-      suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
-      e3x = e3x * suma;
-      e3y = e3y * suma;
-      e3z = e3z * suma;
-      const R s1 = e1x * e1x + e1y * e1y + e1z * e1z;
-      const R s2 = e2x * e2x + e2y * e2y + e2z * e2z;
-      suma = sqrt(s1 / s2);
-      e1x = e1x + (e2y * e3z - e2z * e3y) * suma;
-      e1y = e1y + (e2z * e3x - e2x * e3z) * suma;
-      e1z = e1z + (e2x * e3y - e2y * e3x) * suma;
-      suma = e1x * e1x + e1y * e1y + e1z * e1z;
-      suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
-      e1x = e1x * suma;
-      e1y = e1y * suma;
-      e1z = e1z * suma;
-      e2x = e3y * e1z - e3z * e1y;
-      e2y = e3z * e1x - e3x * e1z;
-      e2z = e3x * e1y - e3y * e1x;
+      if (P.ishfram == 2) {
+        // version-4 non-symmetric frame (cnvec3.F:143-170): e1 scaled by
+        // |e2|^2 and tilted by e2 x e3 (unit e3 not yet formed), e2 = e3 x e1
+        R suma = e2x * e2x + e2y * e2y + e2z * e2z;
+        e1x = e1x * suma + e2y * e3z - e2z * e3y;
+        e1y = e1y * suma + e2z * e3x - e2x * e3z;
+        e1z = e1z * suma + e2x * e3y - e2y * e3x;
+        suma = e1x * e1x + e1y * e1y + e1z * e1z;
+        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        e1x = e1x * suma;
+        e1y = e1y * suma;
+        e1z = e1z * suma;
+        suma = e3x * e3x + e3y * e3y + e3z * e3z;
+        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        e3x = e3x * suma;
+        e3y = e3y * suma;
+        e3z = e3z * suma;
+        e2x = e3y * e1z - e3z * e1y;
+        e2y = e3z * e1x - e3x * e1z;
+        e2z = e3x * e1y - e3y * e1x;
+        suma = e2x * e2x + e2y * e2y + e2z * e2z;
+        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        e2x = e2x * suma;
+        e2y = e2y * suma;
+        e2z = e2z * suma;
+      } else {
+        // symmetric convected frame (cnvec3.F:117-141)
+        R suma = e3x * e3x + e3y * e3y + e3z * e3z;
+        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        e3x = e3x * suma;
+        e3y = e3y * suma;
+        e3z = e3z * suma;
+        const R s1 = e1x * e1x + e1y * e1y + e1z * e1z;
+        const R s2 = e2x * e2x + e2y * e2y + e2z * e2z;
+        suma = sqrt(s1 / s2);
+        e1x = e1x + (e2y * e3z - e2z * e3y) * suma;
+        e1y = e1y + (e2z * e3x - e2x * e3z) * suma;
+        e1z = e1z + (e2x * e3y - e2y * e3x) * suma;
+        suma = e1x * e1x + e1y * e1y + e1z * e1z;
+        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        e1x = e1x * suma;
+        e1y = e1y * suma;
+        e1z = e1z * suma;
+        e2x = e3y * e1z - e3z * e1y;
+        e2y = e3z * e1x - e3x * e1z;
+        e2z = e3x * e1y - e3y * e1x;
+      }
     }
     // ---- CDERI3 ----
     R x2, y2, x3, y3, x4, y4, px1, px2, py1, py2, area, inv_area, vhx, vhy;
@@ -306,9 +336,10 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       vhx = (-x2 + x3 - x4) * inv_area;
       vhy = (-y2 + y3 - y4) * inv_area;
     }
-    // ---- CCOEF3 (ITHK > 0) ----
+    // ---- CCOEF3: ITHK > 0 works on the current thickness, ITHK = 0 on the
+    // initial one (THKE, ccoor3.F:80) ----
     const double thk_cur = S.thk[e];
-    thk0 = (R)thk_cur;
+    if (P.ithk > 0) thk0 = (R)thk_cur;
     const R vol0 = thk0 * area;
     const R thk02 = thk0 * thk0;
     const R nu = PC(nu), ym = PC(young), gmod = PC(g), a11 = PC(a11), ssp = PC(ssp),
@@ -407,7 +438,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     R epsd_pg;
     {
       const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
-      const R th = thk0;
+      const R th = (R)thk_cur;  // GBUF%THK: the current thickness
       const R eps_k2 = (kxx * kxx + kyy * kyy + kxx * kyy + (R)RG_FOURTH * kxy * kxy) *
                        (R)RG_ONE_OVER_9 * th * th;
       const R eps_m2 =

@@ -80,6 +80,12 @@ class Engine:
         for (p0, nrm, ds) in m.rwalls:
             self._chk(L.rg_rwall_add(self.h, _p(np.asarray(p0, np.float64)),
                                      _p(np.asarray(nrm, np.float64)), float(ds)), "rg_rwall_add")
+        for (nodes, ic, icr) in getattr(m, "rlinks", []):
+            nodes = np.ascontiguousarray(nodes, np.int32)
+            self._chk(L.rg_rlink_add(self.h, len(nodes), _p(nodes), int(ic), int(icr)),
+                      "rg_rlink_add")
+        if getattr(m, "ishfram", 0):
+            self._chk(L.rg_set_shell_frame(self.h, int(m.ishfram)), "rg_set_shell_frame")
         if skyline is not None:
             adsky, iads, iadc = (np.ascontiguousarray(a, np.int32) for a in skyline)
             self._chk(L.rg_skyline_set(self.h, _p(adsky), _p(iads), _p(iadc)), "rg_skyline_set")
@@ -102,6 +108,11 @@ class Engine:
         self._chk(self.L.rg_cycle(self.h, int(n)), "rg_cycle")
         if sync:
             self.sync()
+
+    def set_link_active(self, link, active):
+        """Switch rigid link `link` on or off between cycles."""
+        self._chk(self.L.rg_rlink_set_active(self.h, int(link), 1 if active else 0),
+                  "rg_rlink_set_active")
 
     def sync(self):
         self._chk(self.L.rg_synchronize(self.h), "rg_synchronize")

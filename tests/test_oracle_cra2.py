@@ -15,29 +15,16 @@ cycle and the time histories to within the tolerances below, which are a few
 times the differences seen (IE 4e-7, KE 4e-8, DT 6e-7 relative; node
 displacements 1.3e-5, velocities 9e-4 absolute, on values of order 10).
 """
-import os
-
 import numpy as np
 import pytest
 
+from cra2_common import check_printed, check_time_history, load_deck, printed_ok, run_both
 from openradioss_gb300 import model as M
-
-HERE = os.path.dirname(os.path.abspath(__file__))
-FIX = os.path.join(HERE, "golden", "cra2.npz")
 
 
 @pytest.fixture(scope="module")
 def deck():
-    return dict(np.load(FIX))
-
-
-def printed_ok(ours, ref):
-    """ours rounds to the 4-significant-digit printed value ref."""
-    if ref == 0.0:
-        return abs(ours) < 5e-4
-    e = np.floor(np.log10(abs(ref)))
-    half_unit = 0.5 * 10.0 ** (e - 3)
-    return abs(ours - ref) <= half_unit * 1.02
+    return load_deck()
 
 
 def test_deck_masses_match_starter(deck):
@@ -60,32 +47,22 @@ def test_deck_masses_match_starter(deck):
 
 @pytest.fixture(scope="module")
 def run(deck):
-    """Both engine runs of the deck through the oracle: per cycle the
-    listing record and, before it, the nodal D and V (what the time history
-    samples at that cycle)."""
+    """Both engine runs of the deck through the oracle."""
     from oracle.oracle import OracleModel
 
-    m = M.model_from_deck(deck, "cra2")
-    o = OracleModel(m)
+    o = OracleModel(M.model_from_deck(deck, "cra2"))
     o.set_record(True)
-    tstop1, tstop2 = (float(t) for t in deck["run_tstop"])
-    nid = deck["th_node_ids"] - 1
-    recs = ([], [])
-    nodes = ([], [])
-    phase = 0
-    while True:
-        tt = o.time()["tt"]
-        if phase == 0 and tt >= tstop1:
-            o.clear_links()  # the restart deck has no /VEL card
-            phase = 1
-        if phase == 1 and tt >= tstop2:
-            break
-        nd = o.nodes()
+
+    def step():
         o.cycle(1)
         assert o.error() == 0
-        recs[phase].append(o.record())
-        nodes[phase].append(np.concatenate([nd["D"][:, nid].T, nd["V"][:, nid].T], axis=1))
-    return recs, nodes
+        return o.record()
+
+    def nodes_of():
+        nd = o.nodes()
+        return nd["D"], nd["V"]
+
+    return run_both(deck, step, o.clear_links, nodes_of, lambda: o.time()["tt"])
 
 
 def test_first_cycle_time_step(deck, run):
@@ -105,41 +82,12 @@ def test_cycle_counts(deck, run):
 
 @pytest.mark.parametrize("phase", [0, 1])
 def test_printed_table(deck, run, phase):
-    recs, _ = run
-    table = deck["out1" if phase == 0 else "out2"]
-    for row in table:
-        c = int(row[0])
-        r = recs[phase][c]
-        for key, col in (("tt", 1), ("dt2", 2), ("eint", 4), ("ekin", 5), ("ekinr", 6)):
-            assert printed_ok(r[key], row[col]), (phase, c, key, r[key], row[col])
-        assert r["neltst"] == int(row[3]), (phase, c, r["neltst"], row[3])
+    check_printed(deck, run[0], phase)
 
 
 @pytest.mark.parametrize("phase", [0, 1])
 def test_time_history(deck, run, phase):
-    recs, nodes = run
-    pre = "th1" if phase == 0 else "th2"
-    th_t, th_g, th_n = deck[pre + "_time"], deck[pre + "_glob"], deck[pre + "_node"]
-    tts = np.array([r["tt"] for r in recs[phase]], np.float32)
-    cols = [str(c) for c in deck["th_glob_columns"]]
-    tol = dict(IE=2e-6, KE=2e-7, XMOM=2e-7, MASS=1e-7, DT=3e-6, RKE=1e-4, HE=1e-5)
-    key = dict(IE="eint", KE="ekin", XMOM="xmom", MASS="mass", DT="dt2", RKE="ekinr", HE="ehour")
-    matched = 0
-    for k, t in enumerate(th_t):
-        # the time-history cycle: the one whose time matches the recorded
-        # one (times agree to a small fraction of a step)
-        c = int(np.argmin(np.abs(tts.astype(np.float64) - float(t))))
-        assert abs(float(tts[c]) - float(t)) <= 1e-3 * recs[phase][c]["dt2"], (phase, k, t, tts[c])
-        r = recs[phase][c]
-        for name, rel in tol.items():
-            ref = float(th_g[k][cols.index(name)])
-            if ref != 0.0:
-                assert abs(r[key[name]] - ref) <= rel * abs(ref), (phase, k, name, r[key[name]], ref)
-        dn = np.abs(nodes[phase][c] - th_n[k])
-        assert dn[:, :3].max() <= 5e-5, (phase, k, dn[:, :3].max())
-        assert dn[:, 3:].max() <= 5e-3, (phase, k, dn[:, 3:].max())
-        matched += 1
-    assert matched == len(th_t) == 50
+    check_time_history(deck, run[0], run[1], phase)
 
 
 def _printed_misses(deck, mutate, ncyc=1501):
