@@ -78,8 +78,11 @@ int rg_mesh_upload(rg_ctx *ctx, int numnod, const double *x, const double *v,
  * sforc3.F:60): nel elements, IXS(11,nel), law mtn (1 = M1LAW elastic,
  * 2 = M2LAW Johnson-Cook), PM / GEO columns (NPROPM >= 100, NPROPG >= 200
  * entries read), LAW2 mat_param%uparam(1:12) / iparam(1:4) (may be NULL for
- * LAW1).  Supported formulation: ISMSTR=4, JHBE=1 (Isolid=1), JCVT=0
- * (Iframe=1), Lagrangian.  Returns the group index (>= 0) or an error. */
+ * LAW1).  Supported formulation: ISMSTR=4, JHBE=1 (Isolid=1), Lagrangian,
+ * jcvt (the starter's JCVT): 0 (Iframe=1, Jaumann rate, SROTA3) or 1
+ * (co-rotational frame SRCOOR3 / SRROTA3, the starter's choice for 8-node
+ * Lagrangian bricks when Iframe is left to default, sgrtails.F:906-912).
+ * Returns the group index (>= 0) or an error. */
 int rg_hexa_group_add(rg_ctx *ctx, int nel, const int *ixs, int mtn,
                       const double *pm, const double *geo,
                       const double *uparam, const int *iparam, int ismstr,

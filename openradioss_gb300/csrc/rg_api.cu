@@ -645,8 +645,8 @@ int rg_hexa_group_add(rg_ctx *c, int nel, const int *ixs, int mtn,
   if (c->numnod <= 0) return fail(c, RG_E_STATE, "rg_mesh_upload first");
   if (nel <= 0 || !ixs || !pm || !geo) return fail(c, RG_E_ARG, "rg_hexa_group_add: bad arguments");
   if (mtn != 1 && mtn != 2) return fail(c, RG_E_UNSUP, "hexa: only LAW1 and LAW2");
-  if (ismstr != 4 || jhbe != 1 || jcvt != 0)
-    return fail(c, RG_E_UNSUP, "hexa: supported formulation is ISMSTR=4, JHBE=1, JCVT=0");
+  if (ismstr != 4 || jhbe != 1 || (jcvt != 0 && jcvt != 1))
+    return fail(c, RG_E_UNSUP, "hexa: supported formulation is ISMSTR=4, JHBE=1, JCVT=0 or 1");
   if (mtn == 2 && (!uparam || !iparam)) return fail(c, RG_E_ARG, "LAW2 needs uparam/iparam");
   for (int e = 0; e < nel; e++)
     for (int k = 1; k <= 8; k++) {
@@ -666,6 +666,7 @@ int rg_hexa_group_add(rg_ctx *c, int nel, const int *ixs, int mtn,
   P.qb = geo[14];
   P.vns1 = geo[15];
   P.vns2 = geo[16];
+  P.jcvt = jcvt;
   if (!(P.rho0 > 0.0)) return fail(c, RG_E_ARG, "PM(1) density must be > 0");
   // M1LAW / M2LAW: SSP = SQRT((ONEP333*G + C1)/RHO0), a group constant at OFF=1
   P.ssp1 = std::sqrt((RG_ONEP333 * (P.g * 1.0) + P.c1) / P.rho0);

@@ -145,7 +145,8 @@ struct HexaParams {
   double qh, qa, qb, vns1, vns2;  // GEO(13..17)
   double dtfac;            // DTFAC1(1)
   double ssp1;             // sqrt((1.333 G + C1) / RHO0): sound speed at OFF = 1
-  int has_cns, pad2;       // numerical damping GEO(16..17) set
+  int has_cns;             // numerical damping GEO(16..17) set
+  int jcvt;                // 0: Jaumann rate (Iframe=1), 1: co-rotational frame
   // LAW2 Johnson-Cook (mat_param%uparam / iparam)
   double ca, cb, cn, epmx, sigm0, cc, epdr, asrate, z3;
   int icc, vp, israte, pad;

@@ -8,7 +8,7 @@
 
 namespace rg {
 
-template <typename ER, int LAW, int NT, int MINB>
+template <typename ER, int LAW, int JCVT, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
             typename SlotT<ER>::type *__restrict__ fsky, DtPartials dp,
@@ -17,7 +17,7 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
   const int il = blockIdx.x * NT + threadIdx.x;
   R dtmine = (R)RG_EP06;
   int elmin = -1;
-  if (il < P.nel) hexa_element<ER, LAW>(P, A, N, fsky, T, status, il, dtmine, elmin);
+  if (il < P.nel) hexa_element<ER, LAW, JCVT>(P, A, N, fsky, T, status, il, dtmine, elmin);
   // per-block time-step candidate
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x,
                       dp.el + P.part_off + blockIdx.x);
@@ -31,11 +31,15 @@ static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
                        DtPartials dp, Time *T, int *status, const DtFinish &F,
                        cudaStream_t s) {
   constexpr int NT = 128;
-  // mixed form: 5 resident blocks per SM fit in 96 registers without
-  // spilling; the FP64 form needs its ~200 registers
+  // mixed form: 5 resident blocks per SM at 96 registers (a few dozen bytes
+  // per thread spill to L1: measured faster than 4 or 6 blocks); the FP64
+  // form needs its ~250 registers
   constexpr int MINB = std::is_same<ER, float>::value ? 5 : 1;
   const int nb = (P.nel + NT - 1) / NT;
-  hexa_kernel<ER, LAW, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);
+  if (P.jcvt)
+    hexa_kernel<ER, LAW, 1, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);
+  else
+    hexa_kernel<ER, LAW, 0, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);
 }
 
 int hexa_blocks(int nel) { return (nel + 127) / 128; }

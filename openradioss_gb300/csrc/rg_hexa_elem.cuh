@@ -8,6 +8,8 @@
 // the same expression order, the reference routines cited at each block
 // (paths relative to the OpenRadioss source tree):
 //   SCOOR3  gather                     elements/solid/solide/scoor3.F:38
+//   SRCOOR3 co-rotational frame (JCVT=1) elements/solid/solide/srcoor3.F:42,
+//           SREPISO3 / SORTHO3         srepiso3.F, sortho3.F
 //   SDERI3  Jacobian, volume, PX, PH   elements/solid/solide/sderi3.F:32-339
 //   SDLEN3  characteristic length      elements/solid/solide/sdlen3.F:39-172
 //   SDEFO3  strain rate, spin          elements/solid/solide/sdefo3.F:32-313
@@ -18,6 +20,8 @@
 //                                      materials/mat_share/mqviscb.F:44
 //   SHVIS3  viscous hourglass          elements/solid/solide/shvis3.F:31
 //   SFINT3  internal forces            elements/solid/solide/sfint3.F:257
+//   SRROTA3 forces back (JCVT=1)       elements/solid/solide/srrota3.F,
+//                                      sforc3.F:1634-1645
 //   SCUMU3P PARITH/ON slot writes      elements/solid/solide/scumu3p.F:37
 //
 // Two arithmetic forms come from one template:
@@ -46,7 +50,107 @@ __device__ __forceinline__ T fmin_(T a, T b) {
   return a < b ? a : b;
 }
 
-template <typename ER, int LAW>
+// Products and sums of the co-rotational frame and rotations: in the FP64
+// form rounded one operation at a time in the reference's order (no
+// contraction into multiply-adds), so that the frame -- a chain of
+// normalisations whose round-off the rotated coordinates amplify -- is the
+// same bits as a non-contracting CPU build; plain operators in FP32.
+template <typename R>
+__device__ __forceinline__ R mul_(R a, R b) {
+  if constexpr (sizeof(R) == 8) return __dmul_rn(a, b);
+  else return a * b;
+}
+template <typename R>
+__device__ __forceinline__ R add_(R a, R b) {
+  if constexpr (sizeof(R) == 8) return __dadd_rn(a, b);
+  else return a + b;
+}
+template <typename R>
+__device__ __forceinline__ R sub_(R a, R b) {
+  if constexpr (sizeof(R) == 8) return __dsub_rn(a, b);
+  else return a - b;
+}
+// a*x + b*y + c*z, left to right
+template <typename R>
+__device__ __forceinline__ R dot3_(R a, R x, R b, R y, R c, R z) {
+  return add_(add_(mul_(a, x), mul_(b, y)), mul_(c, z));
+}
+// a*b - c*d + e
+template <typename R>
+__device__ __forceinline__ R cross_add_(R a, R b, R c, R d, R e) {
+  return add_(sub_(mul_(a, b), mul_(c, d)), e);
+}
+template <typename R>
+__device__ __forceinline__ R inv_norm_(R a, R b, R c) {
+  R n = sqrt(dot3_(a, a, b, b, c, c));
+  if (n != (R)0) n = (R)1 / n;
+  return n;
+}
+
+// SREPISO3 + SORTHO3: the co-rotational frame of a hexa from its
+// isoparametric directions r, s, t, orthogonalised by three symmetric
+// iterations; R[3i+j] = Rij, column j = local axis j.  Only coordinate
+// differences enter, so relative coordinates give the same frame.
+template <typename R>
+__device__ __forceinline__ void hexa_frame(const R *x, const R *y, const R *z, R *Rm) {
+  const R x17 = x[6] - x[0], x28 = x[7] - x[1], x35 = x[4] - x[2], x46 = x[5] - x[3];
+  const R y17 = y[6] - y[0], y28 = y[7] - y[1], y35 = y[4] - y[2], y46 = y[5] - y[3];
+  const R z17 = z[6] - z[0], z28 = z[7] - z[1], z35 = z[4] - z[2], z46 = z[5] - z[3];
+  const R a17 = x17 + x46, a28 = x28 + x35;
+  const R b17 = y17 + y46, b28 = y28 + y35;
+  const R c17 = z17 + z46, c28 = z28 + z35;
+  const R rx = x17 + x28 - x35 - x46, ry = y17 + y28 - y35 - y46, rz = z17 + z28 - z35 - z46;
+  const R sx = a17 + a28, sy = b17 + b28, sz = c17 + c28;
+  const R tx = a17 - a28, ty = b17 - b28, tz = c17 - c28;
+  R aa = inv_norm_(rx, ry, rz);
+  R ux = mul_(rx, aa), uy = mul_(ry, aa), uz = mul_(rz, aa);
+  aa = inv_norm_(sx, sy, sz);
+  R vx = mul_(sx, aa), vy = mul_(sy, aa), vz = mul_(sz, aa);
+  aa = inv_norm_(tx, ty, tz);
+  R wx = mul_(tx, aa), wy = mul_(ty, aa), wz = mul_(tz, aa);
+#pragma unroll
+  for (int it = 0; it < 3; it++) {
+    const R e1x = cross_add_(vy, wz, vz, wy, ux), e1y = cross_add_(vz, wx, vx, wz, uy),
+            e1z = cross_add_(vx, wy, vy, wx, uz);
+    const R e2x = cross_add_(wy, uz, wz, uy, vx), e2y = cross_add_(wz, ux, wx, uz, vy),
+            e2z = cross_add_(wx, uy, wy, ux, vz);
+    const R e3x = cross_add_(uy, vz, uz, vy, wx), e3y = cross_add_(uz, vx, ux, vz, wy),
+            e3z = cross_add_(ux, vy, uy, vx, wz);
+    R bb = inv_norm_(e1x, e1y, e1z);
+    ux = mul_(e1x, bb);
+    uy = mul_(e1y, bb);
+    uz = mul_(e1z, bb);
+    bb = inv_norm_(e2x, e2y, e2z);
+    vx = mul_(e2x, bb);
+    vy = mul_(e2y, bb);
+    vz = mul_(e2z, bb);
+    bb = inv_norm_(e3x, e3y, e3z);
+    wx = mul_(e3x, bb);
+    wy = mul_(e3y, bb);
+    wz = mul_(e3z, bb);
+  }
+  R e3x = sub_(mul_(uy, vz), mul_(uz, vy)), e3y = sub_(mul_(uz, vx), mul_(ux, vz)),
+    e3z = sub_(mul_(ux, vy), mul_(uy, vx));
+  aa = inv_norm_(e3x, e3y, e3z);
+  e3x = mul_(e3x, aa);
+  e3y = mul_(e3y, aa);
+  e3z = mul_(e3z, aa);
+  Rm[0] = ux;
+  Rm[3] = uy;
+  Rm[6] = uz;
+  Rm[1] = sub_(mul_(e3y, uz), mul_(e3z, uy));
+  Rm[4] = sub_(mul_(e3z, ux), mul_(e3x, uz));
+  Rm[7] = sub_(mul_(e3x, uy), mul_(e3y, ux));
+  Rm[2] = e3x;
+  Rm[5] = e3y;
+  Rm[8] = e3z;
+}
+
+// JCVT = 0: Jaumann-rate formulation (Iframe=1); JCVT = 1: co-rotational
+// frame (Iframe=2, the default of 8-node Lagrangian bricks): coordinates and
+// velocities in the element frame, no spin, midpoint-corrected rates, the
+// stress kept in the frame, forces rotated back.
+template <typename ER, int LAW, int JCVT = 0>
 __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArrays<ER> &A,
                                              const NodeView &N,
                                              typename SlotT<ER>::type *__restrict__ fsky,
@@ -120,6 +224,23 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         x[k] = (c[k].hx - c[0].hx) + (c[k].lx - c[0].lx);
         y[k] = (c[k].hy - c[0].hy) + (c[k].ly - c[0].ly);
         z[k] = (c[k].hz - c[0].hz) + (c[k].lz - c[0].lz);
+      }
+    }
+
+    // ---- SRCOOR3 (JCVT = 1): frame, local coordinates and velocities --------
+    R Rm[9];
+    if constexpr (JCVT != 0) {
+      hexa_frame<R>(x, y, z, Rm);
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const R X = x[k], Y = y[k], Z = z[k];
+        x[k] = dot3_(Rm[0], X, Rm[3], Y, Rm[6], Z);
+        y[k] = dot3_(Rm[1], X, Rm[4], Y, Rm[7], Z);
+        z[k] = dot3_(Rm[2], X, Rm[5], Y, Rm[8], Z);
+        const R U = vx[k], V = vy[k], W = vz[k];
+        vx[k] = dot3_(Rm[0], U, Rm[3], V, Rm[6], W);
+        vy[k] = dot3_(Rm[1], U, Rm[4], V, Rm[7], W);
+        vz[k] = dot3_(Rm[2], U, Rm[5], V, Rm[8], W);
       }
     }
 
@@ -268,7 +389,7 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       deltax = (R)RG_FOUR * volr * (R)RG_ONE / sqrt(aream);
     }
 
-    // ---- SDEFO3 (JHBE=1, JCVT=0) ---------------------------------------------
+    // ---- SDEFO3 (JHBE=1) -------------------------------------------------------
     R dxx, dyy, dzz, d4, d5, d6, wxx, wyy, wzz;
     {
       const R vx17 = vx[0] - vx[6], vx28 = vx[1] - vx[7], vx35 = vx[2] - vx[4], vx46 = vx[3] - vx[5];
@@ -283,13 +404,28 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       const R dyz = pz[0] * vy17 + pz[1] * vy28 + pz[2] * vy35 + pz[3] * vy46;
       const R dzx = px[0] * vz17 + px[1] * vz28 + px[2] * vz35 + px[3] * vz46;
       const R dzy = py[0] * vz17 + py[1] * vz28 + py[2] * vz35 + py[3] * vz46;
-      d4 = dxy + dyx;
-      d5 = dyz + dzy;
-      d6 = dxz + dzx;
       const R dt1d2 = (R)RG_HALF * dt1;
-      wzz = dt1d2 * (dyx - dxy);
-      wyy = dt1d2 * (dxz - dzx);
-      wxx = dt1d2 * (dzy - dyz);
+      if constexpr (JCVT != 0) {
+        // sdefo3.F:158-205 (explicit): no spin, midpoint correction
+        const R exx = dxx, eyy = dyy, ezz = dzz;
+        wxx = wyy = wzz = (R)0;
+        dxx = dxx - dt1d2 * (exx * exx + dyx * dyx + dzx * dzx);
+        dyy = dyy - dt1d2 * (eyy * eyy + dzy * dzy + dxy * dxy);
+        dzz = dzz - dt1d2 * (ezz * ezz + dxz * dxz + dyz * dyz);
+        R aaa = dt1d2 * (exx * dxy + dyx * eyy + dzx * dzy);
+        d4 = (dxy - aaa) + (dyx - aaa);
+        aaa = dt1d2 * (eyy * dyz + dzy * ezz + dxy * dxz);
+        d5 = (dyz - aaa) + (dzy - aaa);
+        aaa = dt1d2 * (ezz * dzx + dxz * exx + dyz * dyx);
+        d6 = (dxz - aaa) + (dzx - aaa);
+      } else {
+        d4 = dxy + dyx;
+        d5 = dyz + dzy;
+        d6 = dxz + dzx;
+        wzz = dt1d2 * (dyx - dxy);
+        wyy = dt1d2 * (dxz - dzx);
+        wxx = dt1d2 * (dzy - dyz);
+      }
     }
 
     // ---- SRHO3 (Lagrangian) -------------------------------------------------
@@ -322,7 +458,11 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
     R s[6], sg[6];
 #pragma unroll
     for (int c = 0; c < 6; c++) s[c] = st_sig[c];
-    {
+    if constexpr (JCVT != 0) {
+      // SRMALLA3: the stress stays in the element frame
+#pragma unroll
+      for (int c = 0; c < 6; c++) sg[c] = s[c];
+    } else {
       const R q1 = (R)RG_TWO * s[3] * wzz;
       const R q2 = (R)RG_TWO * s[5] * wyy;
       const R q3 = (R)RG_TWO * s[4] * wxx;
@@ -611,6 +751,17 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         fint = s3 * pz[j] + s6 * px[j] + s5 * py[j];
         f[2][j] = f[2][j] - fint;
         f[2][pb[j]] = f[2][pb[j]] + fint;
+      }
+    }
+
+    // ---- SRROTA3 (JCVT = 1): forces back to the global frame, F = R F_loc ------
+    if constexpr (JCVT != 0) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const R fx = f[0][k], fy = f[1][k], fz = f[2][k];
+        f[0][k] = dot3_(Rm[0], fx, Rm[1], fy, Rm[2], fz);
+        f[1][k] = dot3_(Rm[3], fx, Rm[4], fy, Rm[5], fz);
+        f[2][k] = dot3_(Rm[6], fx, Rm[7], fy, Rm[8], fz);
       }
     }
 

@@ -69,7 +69,8 @@ class Engine:
             ixs = np.ascontiguousarray(g.ixs.T.reshape(-1), np.int32)
             self._chk(L.rg_hexa_group_add(self.h, g.ixs.shape[1], _p(ixs), g.mat["mtn"],
                                           _p(g.mat["pm"]), _p(g.geo), _p(g.mat["uparam"]),
-                                          _p(g.mat["iparam"]), 4, 1, 0), "rg_hexa_group_add")
+                                          _p(g.mat["iparam"]), 4, 1, getattr(g, "jcvt", 0)),
+                      "rg_hexa_group_add")
         for g in m.shells:
             ixc = np.ascontiguousarray(g.ixc.T.reshape(-1), np.int32)
             thk = np.ascontiguousarray(g.thk, np.float64)

@@ -151,6 +151,7 @@ class HexaGroupSpec:
     ixs: np.ndarray            # (11, nel) int32
     mat: dict
     geo: np.ndarray
+    jcvt: int = 0              # 0: Iframe=1 (Jaumann), 1: co-rotational frame
 
 
 @dataclass

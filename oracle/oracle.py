@@ -81,7 +81,7 @@ class OracleModel:
             r = L.or_hexa_group_add(self.h, g.ixs.shape[1],
                                     np.ascontiguousarray(g.ixs.T.reshape(-1), np.int32),
                                     g.mat["mtn"], g.mat["pm"], g.geo, g.mat["uparam"],
-                                    g.mat["iparam"], 4, 1, 0)
+                                    g.mat["iparam"], 4, 1, getattr(g, "jcvt", 0))
             if r < 0:
                 raise RuntimeError("or_hexa_group_add failed %d" % r)
         for g in model.shells:

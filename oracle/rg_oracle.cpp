@@ -103,7 +103,68 @@ struct HexaLocal {
   double s[6][MVSIZ];  // stress before rotation (SOLD)
   double ssp[MVSIZ], qnew[MVSIZ], ssp_eq[MVSIZ], sti[MVSIZ];
   double f[3][8][MVSIZ];
+  double r[9][MVSIZ];  // JCVT=1: element frame R11 R12 R13 R21 ... R33
 };
+
+// SREPISO3 + SORTHO3 (srepiso3.F, sortho3.F): the co-rotational frame of a
+// hexa from its isoparametric directions r, s, t (the JAC1-9 combinations),
+// orthogonalised by three symmetric iterations.  R(3i+j) holds Rij; column j
+// is local axis j (SORTHO3's E1X = R11, E2X = R12, E3X = R13, ...).
+static void hexa_frame(const double *x, const double *y, const double *z, double *R) {
+  const double x17 = x[6] - x[0], x28 = x[7] - x[1], x35 = x[4] - x[2], x46 = x[5] - x[3];
+  const double y17 = y[6] - y[0], y28 = y[7] - y[1], y35 = y[4] - y[2], y46 = y[5] - y[3];
+  const double z17 = z[6] - z[0], z28 = z[7] - z[1], z35 = z[4] - z[2], z46 = z[5] - z[3];
+  const double a17 = x17 + x46, a28 = x28 + x35;
+  const double b17 = y17 + y46, b28 = y28 + y35;
+  const double c17 = z17 + z46, c28 = z28 + z35;
+  const double rx = x17 + x28 - x35 - x46, ry = y17 + y28 - y35 - y46, rz = z17 + z28 - z35 - z46;
+  const double sx = a17 + a28, sy = b17 + b28, sz = c17 + c28;
+  const double tx = a17 - a28, ty = b17 - b28, tz = c17 - c28;
+  double aa = std::sqrt(rx * rx + ry * ry + rz * rz);
+  if (aa != RG_ZERO) aa = RG_ONE / aa;
+  double ux = rx * aa, uy = ry * aa, uz = rz * aa;
+  aa = std::sqrt(sx * sx + sy * sy + sz * sz);
+  if (aa != RG_ZERO) aa = RG_ONE / aa;
+  double vx = sx * aa, vy = sy * aa, vz = sz * aa;
+  aa = std::sqrt(tx * tx + ty * ty + tz * tz);
+  if (aa != RG_ZERO) aa = RG_ONE / aa;
+  double wx = tx * aa, wy = ty * aa, wz = tz * aa;
+  for (int it = 0; it < 3; it++) {
+    const double e1x = vy * wz - vz * wy + ux, e1y = vz * wx - vx * wz + uy,
+                 e1z = vx * wy - vy * wx + uz;
+    const double e2x = wy * uz - wz * uy + vx, e2y = wz * ux - wx * uz + vy,
+                 e2z = wx * uy - wy * ux + vz;
+    const double e3x = uy * vz - uz * vy + wx, e3y = uz * vx - ux * vz + wy,
+                 e3z = ux * vy - uy * vx + wz;
+    double bb = std::sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
+    if (bb != RG_ZERO) bb = RG_ONE / bb;
+    ux = e1x * bb;
+    uy = e1y * bb;
+    uz = e1z * bb;
+    bb = std::sqrt(e2x * e2x + e2y * e2y + e2z * e2z);
+    if (bb != RG_ZERO) bb = RG_ONE / bb;
+    vx = e2x * bb;
+    vy = e2y * bb;
+    vz = e2z * bb;
+    bb = std::sqrt(e3x * e3x + e3y * e3y + e3z * e3z);
+    if (bb != RG_ZERO) bb = RG_ONE / bb;
+    wx = e3x * bb;
+    wy = e3y * bb;
+    wz = e3z * bb;
+  }
+  const double e1x = ux, e1y = uy, e1z = uz;
+  double e3x = e1y * vz - e1z * vy, e3y = e1z * vx - e1x * vz, e3z = e1x * vy - e1y * vx;
+  aa = std::sqrt(e3x * e3x + e3y * e3y + e3z * e3z);
+  if (aa != RG_ZERO) aa = RG_ONE / aa;
+  e3x = e3x * aa;
+  e3y = e3y * aa;
+  e3z = e3z * aa;
+  const double e2x = e3y * e1z - e3z * e1y, e2y = e3z * e1x - e3x * e1z,
+               e2z = e3x * e1y - e3y * e1x;
+  R[0] = e1x; R[1] = e2x; R[2] = e3x;
+  R[3] = e1y; R[4] = e2y; R[5] = e3y;
+  R[6] = e1z; R[7] = e2z; R[8] = e3z;
+}
 
 void hexa_group(Model &M, const HexaGroup &G, double &dt2t, int &neltst) {
   HexaLocal L;
@@ -128,6 +189,31 @@ void hexa_group(Model &M, const HexaGroup &G, double &dt2t, int &neltst) {
         L.vx[k][i] = M.V[3 * n + 0];
         L.vy[k][i] = M.V[3 * n + 1];
         L.vz[k][i] = M.V[3 * n + 2];
+      }
+    }
+  }
+
+  // SRCOOR3 (srcoor3.F), JCVT=1: element frame, then coordinates and
+  // velocities in it (X_loc = R^T X; SRROTA3 with the transposed frame)
+  if (G.jcvt) {
+    for (int i = 0; i < nel; i++) {
+      double xs[8], ys[8], zs[8], R[9];
+      for (int k = 0; k < 8; k++) {
+        xs[k] = L.x[k][i];
+        ys[k] = L.y[k][i];
+        zs[k] = L.z[k][i];
+      }
+      hexa_frame(xs, ys, zs, R);
+      for (int c = 0; c < 9; c++) L.r[c][i] = R[c];
+      for (int k = 0; k < 8; k++) {
+        const double X = L.x[k][i], Y = L.y[k][i], Z = L.z[k][i];
+        L.x[k][i] = R[0] * X + R[3] * Y + R[6] * Z;
+        L.y[k][i] = R[1] * X + R[4] * Y + R[7] * Z;
+        L.z[k][i] = R[2] * X + R[5] * Y + R[8] * Z;
+        const double U = L.vx[k][i], V = L.vy[k][i], W = L.vz[k][i];
+        L.vx[k][i] = R[0] * U + R[3] * V + R[6] * W;
+        L.vy[k][i] = R[1] * U + R[4] * V + R[7] * W;
+        L.vz[k][i] = R[2] * U + R[5] * V + R[8] * W;
       }
     }
   }
@@ -271,12 +357,36 @@ void hexa_group(Model &M, const HexaGroup &G, double &dt2t, int &neltst) {
     L.dzx[i] = P_(px, 0) * vz17 + P_(px, 1) * vz28 + P_(px, 2) * vz35 + P_(px, 3) * vz46;
     L.dzy[i] = P_(py, 0) * vz17 + P_(py, 1) * vz28 + P_(py, 2) * vz35 + P_(py, 3) * vz46;
 #undef P_
-    L.d4[i] = L.dxy[i] + L.dyx[i];
-    L.d5[i] = L.dyz[i] + L.dzy[i];
-    L.d6[i] = L.dxz[i] + L.dzx[i];
-    L.wzz[i] = dt1d2 * (L.dyx[i] - L.dxy[i]);
-    L.wyy[i] = dt1d2 * (L.dxz[i] - L.dzx[i]);
-    L.wxx[i] = dt1d2 * (L.dzy[i] - L.dyz[i]);
+    if (G.jcvt) {
+      // JCVT /= 0, explicit (sdefo3.F:158-205): no spin; the midpoint
+      // correction of the rates
+      L.wxx[i] = L.wyy[i] = L.wzz[i] = RG_ZERO;
+      const double exx = L.dxx[i], eyy = L.dyy[i], ezz = L.dzz[i];
+      const double exy = L.dxy[i], eyx = L.dyx[i], exz = L.dxz[i];
+      const double ezx = L.dzx[i], eyz = L.dyz[i], ezy = L.dzy[i];
+      L.dxx[i] = L.dxx[i] - dt1d2 * (exx * exx + eyx * eyx + ezx * ezx);
+      L.dyy[i] = L.dyy[i] - dt1d2 * (eyy * eyy + ezy * ezy + exy * exy);
+      L.dzz[i] = L.dzz[i] - dt1d2 * (ezz * ezz + exz * exz + eyz * eyz);
+      double aaa = dt1d2 * (exx * exy + eyx * eyy + ezx * ezy);
+      L.dxy[i] = L.dxy[i] - aaa;
+      L.dyx[i] = L.dyx[i] - aaa;
+      L.d4[i] = L.dxy[i] + L.dyx[i];
+      aaa = dt1d2 * (eyy * eyz + ezy * ezz + exy * exz);
+      L.dyz[i] = L.dyz[i] - aaa;
+      L.dzy[i] = L.dzy[i] - aaa;
+      L.d5[i] = L.dyz[i] + L.dzy[i];
+      aaa = dt1d2 * (ezz * ezx + exz * exx + eyz * eyx);
+      L.dxz[i] = L.dxz[i] - aaa;
+      L.dzx[i] = L.dzx[i] - aaa;
+      L.d6[i] = L.dxz[i] + L.dzx[i];
+    } else {
+      L.d4[i] = L.dxy[i] + L.dyx[i];
+      L.d5[i] = L.dyz[i] + L.dzy[i];
+      L.d6[i] = L.dxz[i] + L.dzx[i];
+      L.wzz[i] = dt1d2 * (L.dyx[i] - L.dxy[i]);
+      L.wyy[i] = dt1d2 * (L.dxz[i] - L.dzx[i]);
+      L.wxx[i] = dt1d2 * (L.dzy[i] - L.dyz[i]);
+    }
   }
 
   // SRHO3 Lagrangian branch (srho3.F:140-150): VOLO = GBUF%VOL (initial)
@@ -289,10 +399,13 @@ void hexa_group(Model &M, const HexaGroup &G, double &dt2t, int &neltst) {
     M.eint[e] = M.eint[e] * M.vol[e];
   }
 
-  // SROTA3 (srota3.F:40-97): Jaumann rotation; S = stress before rotation
+  // SROTA3 (srota3.F:40-97): Jaumann rotation; S = stress before rotation.
+  // JCVT=1: SRMALLA3 (srmall3.F) only copies the stress, kept in the
+  // element frame.
   for (int i = 0; i < nel; i++) {
     const int e = nft + i;
     for (int c = 0; c < 6; c++) L.s[c][i] = SIG[c * NE + e];
+    if (G.jcvt) continue;
     const double s1 = L.s[0][i], s2 = L.s[1][i], s3 = L.s[2][i],
                  s4 = L.s[3][i], s5 = L.s[4][i], s6 = L.s[5][i];
     const double q1 = RG_TWO * s4 * L.wzz[i];
@@ -634,6 +747,23 @@ void hexa_group(Model &M, const HexaGroup &G, double &dt2t, int &neltst) {
     }
   }
 
+  // SRROTA3 (srrota3.F, sforc3.F:1634-1645), JCVT=1: forces back to the
+  // global frame, F = R F_loc
+  if (G.jcvt) {
+    for (int i = 0; i < nel; i++) {
+      const double *R = nullptr;
+      double Rl[9];
+      for (int c = 0; c < 9; c++) Rl[c] = L.r[c][i];
+      R = Rl;
+      for (int k = 0; k < 8; k++) {
+        const double fx = L.f[0][k][i], fy = L.f[1][k][i], fz = L.f[2][k][i];
+        L.f[0][k][i] = R[0] * fx + R[1] * fy + R[2] * fz;
+        L.f[1][k][i] = R[3] * fx + R[4] * fy + R[5] * fz;
+        L.f[2][k][i] = R[6] * fx + R[7] * fy + R[8] * fz;
+      }
+    }
+  }
+
   // SCUMU3P (scumu3p.F:37-664): zero deleted (OFFG<0) elements, STI/4,
   // write FSKY(1:3,K), FSKY(7,K) at K = IADS(k, e).
   for (int i = 0; i < nel; i++) {
@@ -734,7 +864,7 @@ int or_hexa_group_add(void *m, int nel, const int *ixs, int mtn,
   Model &M = ((OrModelWrap *)m)->m;
   if (M.finalized || nel <= 0) return -1;
   if (mtn != 1 && mtn != 2) return -2;
-  if (jcvt != 0 || jhbe != 1 || ismstr != 4) return -3;
+  if ((jcvt != 0 && jcvt != 1) || jhbe != 1 || ismstr != 4) return -3;
   // Split into MVSIZ-long groups like the starter (SGRTAILS).
   for (int s = 0; s < nel; s += MVSIZ) {
     HexaGroup G;

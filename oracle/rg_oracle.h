@@ -32,7 +32,9 @@ void or_model_free(void *m);
 
 /* Hexa group (SFORC3 path).  pm / geo are the material / property columns
  * (PM(1:NPROPM,imat), GEO(1:NPROPG,iprop)); uparam / iparam the LAW2
- * mat_param%uparam(1:12) / iparam(1:4).  Returns the group index or <0. */
+ * mat_param%uparam(1:12) / iparam(1:4); jcvt 0 (Iframe=1, Jaumann rate) or
+ * 1 (co-rotational frame, the default of 8-node Lagrangian bricks).
+ * Returns the group index or <0. */
 int or_hexa_group_add(void *m, int nel, const int *ixs, int mtn,
                       const double *pm, const double *geo,
                       const double *uparam, const int *iparam, int ismstr,
