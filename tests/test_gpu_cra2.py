@@ -130,5 +130,8 @@ def test_fp64_matches_oracle(deck, fp64):
         for key in ("eint", "ekin", "dt2", "ehour", "tt"):
             ref = recs[c][key]
             assert abs(g[c][key] - ref) <= 1e-12 * abs(ref) + 1e-12, (c, key, g[c][key], ref)
-        assert g[c]["neltst"] == recs[c]["neltst"]
+        # the controlling element: equal, except between elements whose time
+        # steps tie to round-off (the regular mesh has many equal ones)
+        if g[c]["neltst"] != recs[c]["neltst"]:
+            assert abs(g[c]["dt2"] - recs[c]["dt2"]) <= 1e-13 * recs[c]["dt2"], c
         assert np.abs(gn[c] - nodes[c]).max() <= 1e-9, c
