@@ -50,6 +50,7 @@ extern "C" {
 #define RG_ST_SLOT 4       /* skyline slot index out of range */
 #define RG_ST_DTMIN 8      /* time step below the configured minimum */
 #define RG_ST_BARRIER 16   /* batched kernel: grid barrier wait gave up */
+#define RG_ST_NODSTIF 32   /* nodal time step: node with no stiffness (DTNODA stop) */
 
 /* precision modes (rg_set_precision) */
 #define RG_PREC_FP64 0     /* plain form: everything in FP64 */
@@ -117,6 +118,16 @@ int rg_rlink_add(rg_ctx *ctx, int nsn, const int *nodes, int ic, int icr);
 /* Switch link `link` on or off between cycles (a restart whose engine deck
  * no longer has the /VEL card); ordered after the cycles already queued. */
 int rg_rlink_set_active(rg_ctx *ctx, int link, int active);
+
+/* Nodal time step (/DT/NODA: DTNODA, engine/source/time_step/dtnoda.F:37,
+ * called at resol.F:6066): the elements give only their stiffness (hexa STI
+ * of MQVISCB, shell STI / STIR of CHVIS3's nodal branch, no CDT3), and the
+ * cycle's step is the minimum over nodes of dtfac*sqrt(2*MS/STIFN) and, for
+ * shell models, dtfac*sqrt(2*IN/STIFR) -- dtfac = DTFAC1(11).  NELTST then
+ * holds the controlling node's number.  A step below dtmin (DTMIN1(11), 0 =
+ * none) raises RG_ST_DTMIN; a node without stiffness RG_ST_NODSTIF.  Before
+ * rg_finalize; models with it run alone (not in a batch). */
+int rg_set_nodal_dt(rg_ctx *ctx, double dtfac, double dtmin);
 
 /* Local shell frame of CNVEC3 (cnvec3.F:117-170): ISHFRAM 0 (symmetric
  * convected frame, default) or 2 (the starter's /SHFRA/V4, contrl.F:495-498).

@@ -29,6 +29,7 @@ SIGNATURES = [
     ("rg_rlink_add", _ip, [_vp, _ip, _vp, _ip, _ip]),
     ("rg_rlink_set_active", _ip, [_vp, _ip, _ip]),
     ("rg_set_shell_frame", _ip, [_vp, _ip]),
+    ("rg_set_nodal_dt", _ip, [_vp, _dp, _dp]),
     ("rg_skyline_set", _ip, [_vp, _vp, _vp, _vp]),
     ("rg_finalize", _ip, [_vp, _dp, _dp, _dp, _dp]),
     ("rg_skyline_get", _ip, [_vp, _vp, _vp, _vp, _vp]),

@@ -81,6 +81,59 @@ node_kernel_rot(NodeView N, const int *__restrict__ adsky, const void *__restric
   node_update<F64, true, false, LINK>(N, adsky, fsky_, fskyr_, T, wall, walls, lacc, status, n);
 }
 
+// Nodal time step, DTNODA (time_step/dtnoda.F:213-345, 443-470), NODADT > 0:
+// node n's step DTFAC1(11)*SQRT(2*MS/STIFN) and, for shell models,
+// DTFAC1(11)*SQRT(2*IN/STIFR), STIFN / STIFR the fixed-order sums of the
+// element stiffness slots (ASSPAR4).  A node with non-positive stiffness
+// raises RG_ST_NODSTIF (the reference stops).  Order keys: on ties the first
+// node of the translational pass wins, then the first of the rotational
+// pass (the strict '<' scans of DTNODA).  The block minima are reduced by
+// the last block, which applies the RESOL dt logic.
+template <bool F64, bool ROT>
+__global__ void __launch_bounds__(NODE_NT)
+nodal_dt_kernel(NodeView N, const int *__restrict__ adsky, const void *__restrict__ fsky_,
+                const void *__restrict__ fskyr_, const double dtfac, const double dtmin,
+                DtPartials dp, Time *__restrict__ T, int *__restrict__ status,
+                const DtFinish F) {
+  const int n = blockIdx.x * NODE_NT + threadIdx.x;
+  const int numnod = N.numnod;
+  double d = RG_EP06;
+  int k = -1;
+  if (n < numnod) {
+    double st = 0.0, sr = 0.0;
+    const int k0 = adsky[n], k1 = adsky[n + 1];
+    for (int q = k0; q < k1; q++) {
+      if constexpr (F64) {
+        st = __dadd_rn(st, ((const dbl4 *)fsky_)[q].w);
+        if (ROT) sr = __dadd_rn(sr, ((const dbl4 *)fskyr_)[q].w);
+      } else {
+        st = __dadd_rn(st, (double)__ldg(&((const float4 *)fsky_)[q].w));
+        if (ROT) sr = __dadd_rn(sr, (double)__ldg(&((const float4 *)fskyr_)[q].w));
+      }
+    }
+    const double ms = N.D4[n].w;
+    if (st <= 0.0) {
+      atomicOr(status, RG_ST_NODSTIF);
+    } else if (ms > 0.0) {
+      const double dn = __dmul_rn(dtfac, sqrt(__dmul_rn(2.0, ms) / st));
+      if (dn < dtmin) atomicOr(status, RG_ST_DTMIN);
+      dt_pair_min(d, k, dn, 2 * numnod - 1 - n);
+    }
+    if (ROT) {
+      const double in = N.DR4[n].w;
+      if (sr <= 0.0) {
+        atomicOr(status, RG_ST_NODSTIF);
+      } else if (in > 0.0) {
+        const double dn = __dmul_rn(dtfac, sqrt(__dmul_rn(2.0, in) / sr));
+        if (dn < dtmin) atomicOr(status, RG_ST_DTMIN);
+        dt_pair_min(d, k, dn, numnod - 1 - n);
+      }
+    }
+  }
+  block_dt_min<NODE_NT, double>(d, k, dp.dt + blockIdx.x, dp.el + blockIdx.x);
+  dt_finish_block<NODE_NT>(dp, F, blockIdx.x, T, status);
+}
+
 // Rigid links, RLINK1 (constraints/general/rlink/rlink1.F) as called by
 // RLINK10 after the boundary conditions: block l forms link l's mass (and
 // inertia) and the mass- (inertia-) weighted sums of its nodes'
@@ -472,12 +525,14 @@ int init_hexa_state(rg_ctx *c, HexaArrays<ER> &A) {
 // model without elements gets the stand-alone time-step kernel.
 int enqueue_elements(rg_ctx *c, int advance) {
   const DtPartials dp = c->dp;
-  if (c->nparts == 0) {
+  if (c->nparts == 0 && !c->nodadt) {
     dt_kernel<<<1, DT_NT, 0, c->stream>>>(dp, 0, c->d_ngl_all, c->d_time, c->d_status, advance);
     return RG_OK;
   }
   DtFinish F;
-  F.ctr = c->d_dtctr;
+  // under the nodal time step the elements give no step: no fused finish
+  // (the nodal dt kernel applies the cycle's step)
+  F.ctr = c->nodadt ? nullptr : c->d_dtctr;
   F.gdt = c->d_gdt;
   F.gel = c->d_gel;
   F.nparts = c->nparts;
@@ -500,6 +555,18 @@ template <bool F64, bool ROT>
 void launch_nodes(rg_ctx *c) {
   const int nb = (c->numnod + NODE_NT - 1) / NODE_NT;
   const void *fr = ROT ? c->d_fskyr : nullptr;
+  if (c->nodadt) {
+    DtFinish F;
+    F.ctr = c->d_nctr;
+    F.gdt = c->d_ngdt;
+    F.gel = c->d_ngel;
+    F.nparts = c->nnparts;
+    F.advance = 1;
+    F.ngl = c->d_ngl_nodes;
+    nodal_dt_kernel<F64, ROT><<<nb, NODE_NT, 0, c->stream>>>(
+        c->nv, c->d_adsky, c->d_fsky, fr, c->dtfac_noda, c->dtmin_noda, c->ndp, c->d_time,
+        c->d_status, F);
+  }
   if (c->nlinks)
     rlink_kernel<F64, ROT><<<c->nlinks, LINK_NT, 0, c->stream>>>(
         c->nv, c->d_adsky, c->d_fsky, fr, c->d_lnodes, c->d_loff, c->d_lic, c->d_lacc,
@@ -755,6 +822,17 @@ int rg_rlink_set_active(rg_ctx *c, int link, int active) {
   return RG_OK;
 }
 
+int rg_set_nodal_dt(rg_ctx *c, double dtfac, double dtmin) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "rg_set_nodal_dt after rg_finalize");
+  if (!(dtfac > 0.0) || dtmin < 0.0) return fail(c, RG_E_ARG, "rg_set_nodal_dt: bad factors");
+  c->nodadt = 1;
+  c->shells.nodadt = 1;
+  c->dtfac_noda = dtfac;
+  c->dtmin_noda = dtmin;
+  return RG_OK;
+}
+
 int rg_set_shell_frame(rg_ctx *c, int ishfram) {
   if (!c) return RG_E_ARG;
   if (c->finalized) return fail(c, RG_E_STATE, "rg_set_shell_frame after rg_finalize");
@@ -902,6 +980,7 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   for (auto &g : c->hg) {
     g.P.part_off = c->nparts;
     g.P.dtfac = dtfac_solid;
+    g.P.nodadt = c->nodadt;
     hexa_params_mirror(g.P);
     c->nparts += hexa_blocks(g.nel);
   }
@@ -929,7 +1008,7 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   t.dt2old = dt2old;
   t.dtmx = dtmx;
   t.dt2t = 0;
-  t.dtmin = 0;
+  t.dtmin = c->nodadt ? c->dtmin_noda : 0.0;
   if ((r = dalloc(c, &c->d_time, 1))) return r;
   RG_CUDA(c, cudaMemcpy(c->d_time, &t, sizeof(Time), cudaMemcpyHostToDevice));
   if ((r = dalloc(c, &c->d_status, 1))) return r;
@@ -979,6 +1058,26 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     if ((r = dalloc(c, &c->d_gel, std::max(ng, 1)))) return r;
     RG_CUDA(c, cudaMemset(c->d_dtctr, 0, (ng + 1) * sizeof(unsigned)));
   }
+  if (c->nodadt) {
+    c->nnparts = (numnod + NODE_NT - 1) / NODE_NT;
+    const int ng = (c->nnparts + DT_GROUP - 1) / DT_GROUP;
+    if ((r = dalloc(c, &c->ndp.dt, c->nnparts))) return r;
+    if ((r = dalloc(c, &c->ndp.el, c->nnparts))) return r;
+    if ((r = dalloc(c, &c->d_nctr, ng + 1))) return r;
+    if ((r = dalloc(c, &c->d_ngdt, ng))) return r;
+    if ((r = dalloc(c, &c->d_ngel, ng))) return r;
+    RG_CUDA(c, cudaMemset(c->d_nctr, 0, (ng + 1) * sizeof(unsigned)));
+    // order key -> node number: translational keys 2*numnod-1-n, rotational
+    // numnod-1-n
+    std::vector<int> nn(2 * (size_t)numnod);
+    for (int n = 0; n < numnod; n++) {
+      nn[2 * (size_t)numnod - 1 - n] = n + 1;
+      nn[numnod - 1 - n] = n + 1;
+    }
+    if ((r = dalloc(c, &c->d_ngl_nodes, nn.size()))) return r;
+    RG_CUDA(c, cudaMemcpy(c->d_ngl_nodes, nn.data(), nn.size() * sizeof(int),
+                          cudaMemcpyHostToDevice));
+  }
   if ((r = dalloc(c, &c->d_stage, 12 * (size_t)numnod + 16))) return r;
   RG_CUDA(c, cudaMallocHost((void **)&c->h_time, sizeof(Time)));
   if ((r = dalloc(c, &c->d_epart, 4 * EN_BLOCKS + 8))) return r;
@@ -1021,7 +1120,7 @@ int rg_cycle(rg_ctx *c, int ncycle) {
     cudaEventRecord(c->ev[0], c->stream);
     const DtPartials dp = c->dp;
     DtFinish F;
-    F.ctr = c->d_dtctr;
+    F.ctr = c->nodadt ? nullptr : c->d_dtctr;
     F.gdt = c->d_gdt;
     F.gel = c->d_gel;
     F.nparts = c->nparts;
@@ -1039,8 +1138,9 @@ int rg_cycle(rg_ctx *c, int ncycle) {
     shell_enqueue(c->shells, c->prec, c->nv, c->d_fsky, c->d_fskyr, dp, c->d_time, c->d_status,
                   F, c->stream);
     cudaEventRecord(c->ev[2], c->stream);
-    // the time-step reduction runs inside the last element block
-    if (c->nparts == 0)
+    // the time-step reduction runs inside the last element block (or the
+    // nodal dt kernel, launched with the node phase)
+    if (c->nparts == 0 && !c->nodadt)
       dt_kernel<<<1, DT_NT, 0, c->stream>>>(dp, 0, c->d_ngl_all, c->d_time, c->d_status, 1);
     cudaEventRecord(c->ev[3], c->stream);
     enqueue_nodes(c);

@@ -88,6 +88,16 @@ struct rg_ctx {
   int4 *d_lic = nullptr;
   rg::dbl4 *d_lacc = nullptr;
   int4 h_link = {0, 0, 0, 0};  // source of rg_rlink_set_active's copy
+  // nodal time step (/DT/NODA): per-node-block partials, their fused
+  // last-block reduction, and the key -> node number table
+  int nodadt = 0;
+  double dtfac_noda = 0.9, dtmin_noda = 0.0;
+  int nnparts = 0;
+  rg::DtPartials ndp{};
+  unsigned *d_nctr = nullptr;
+  double *d_ngdt = nullptr;
+  int *d_ngel = nullptr;
+  int *d_ngl_nodes = nullptr;
   bool rot = false;
   // staging for forint_step / downloads
   double *d_stage = nullptr;   // 12 * numnod doubles

@@ -149,7 +149,8 @@ struct HexaParams {
   int jcvt;                // 0: Jaumann rate (Iframe=1), 1: co-rotational frame
   // LAW2 Johnson-Cook (mat_param%uparam / iparam)
   double ca, cb, cn, epmx, sigm0, cc, epdr, asrate, z3;
-  int icc, vp, israte, pad;
+  int icc, vp, israte;
+  int nodadt;              // nodal time step: the element gives STI only
   double inv_rho0;         // 1/RHO0 (group constant)
   // FP32 copies of the coefficients above (the same round-to-nearest
   // conversion, done once on the host) for the mixed form, and the two

@@ -602,7 +602,8 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         sti = (rhoe * tidt) * (volr * tidt);
       }
       const R dtxd = PC(dtfac) * dtx;
-      if ((F64 ? voln > RG_ZERO : volr > (R)0) && (off != (R)0 && offg >= (R)0)) {
+      // under the nodal time step the element only gives STI (mqviscb.F:351)
+      if (!P.nodadt && (F64 ? voln > RG_ZERO : volr > (R)0) && (off != (R)0 && offg >= (R)0)) {
         // running minimum over the elements this thread handles; element
         // order key e, mapped to the user id by the time-step reduction
         dt_pair_min_t(dtmine, elmin, dtxd, e);

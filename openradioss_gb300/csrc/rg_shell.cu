@@ -285,6 +285,7 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
     g->P.part_off = part_off;
     g->P.dtfac = dtfac;
     g->P.ishfram = S.ishfram;
+    g->P.nodadt = S.nodadt;
     shell_params_mirror(g->P);
     part_off += shell_blocks(g->P.nel);
   }

@@ -17,6 +17,7 @@ struct ShellModelHost {
   std::vector<ShellGroupHost *> groups;
   int key0 = 0;                         // dt-order key of the first shell
   int ishfram = 0;                      // local frame of every group (0 / 2)
+  int nodadt = 0;                       // nodal time step (/DT/NODA)
   void *dev = nullptr;                  // device arrays (rg_shell.cu)
 };
 

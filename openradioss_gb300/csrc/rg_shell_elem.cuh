@@ -48,7 +48,8 @@ struct ShellParams {
   // coefficients of CHVIS3
   double a1, a2, inv1mnu, inv1pnu, inv_hmax, dtfac_ssp;
   double shf0, hA1, hA3, hA5, hA7, hA8;
-  int shf_const, pad3;
+  int shf_const;
+  int nodadt;   // nodal time step: STI / STIR for DTNODA, no element dt
   // FP32 copies for the mixed form (converted once on the host) and the
   // branch flags CC /= 0, DM /= 0 evaluated on the FP64 values
   struct {
@@ -620,6 +621,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     for (int c = 0; c < 3; c++) S.mom[c * nc + e] = momn[c];
     // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) ----
     R h11, h12, h13, h21, h22, h23, h31, h32, h33, hr4, hr5;
+    R sti_noda = (R)0, stir_noda = (R)0;
     {
       const R px1v = px1 * vhx, px2v = px2 * vhx, py1v = py1 * vhy, py2v = py2 * vhy;
       const R gama1 = off * ((R)RG_ONE - px1v - py1v);
@@ -654,6 +656,18 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       const R b1 = px1 * px1 + py1 * py1, b2 = px2 * px2 + py2 * py2;
       R hh2 = A8 * thk02 * td / (b1 + b2);
       if (S.degen[e]) h1q = h2q = h3q = hh1 = hh2 = (R)0;
+      if (P.nodadt) {
+        // nodal time step (chvis3.F:198-265, IGTYP=1): the element
+        // stiffness STI with the elastic hourglass term SCALE, and STIR
+        // (VISCMX = 1, ALPE = 1; the linear hourglass terms are 0)
+        const R scale = smax(smax(gama1 * gama1, gama2 * gama2), smax(gama3 * gama3, gama4 * gama4)) *
+                        dt1 * smax(smax(hh1, hh2), (R)0) / smax(dt1 * dt1, (R)RG_EM20);
+        if (off != (R)0) {
+          sti_noda = (R)0 + scale;
+          sti_noda = sti_noda + smax(b1, b2) * thk0 * a11 / area;
+          stir_noda = sti_noda * (thk02 * (R)RG_ONE_OVER_12 + area * (R)RG_ONE_OVER_9);
+        }
+      }
       R hg1 = vx[0] * gama1 + vx[1] * gama2 + vx[2] * gama3 + vx[3] * gama4;
       R hg2 = vy[0] * gama1 + vy[1] * gama2 + vy[2] * gama3 + vy[3] * gama4;
       R hou0 = st_hour[0] + hg1 * hh1;
@@ -687,9 +701,9 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       S.hour[4 * nc + e] = hr5;
       S.ehou[e] = st_ehou + (double)ehou;
     }
-    // ---- CDT3 ----
-    R sti;
-    {
+    // ---- CDT3 (not called under the nodal time step, cforc3.F:668) ----
+    R sti = sti_noda;
+    if (!P.nodadt) {
       const R dt = aldt * PC(dtfac_ssp);
       if (offg > (R)0 && off != (R)0) {
         // running minimum; reversed order key: the first element wins ties
@@ -763,7 +777,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       b.x = zero ? (R)0 : -M[0][k];
       b.y = zero ? (R)0 : -M[1][k];
       b.z = zero ? (R)0 : -M[2][k];
-      b.w = (R)0;  // STIR = 0 (element time step)
+      b.w = zero ? (R)0 : stir_noda;  // STIR: 0 under the element time step
       fsky[K] = a;
       fskyr[K] = b;
     }

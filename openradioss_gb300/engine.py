@@ -87,6 +87,9 @@ class Engine:
                       "rg_rlink_add")
         if getattr(m, "ishfram", 0):
             self._chk(L.rg_set_shell_frame(self.h, int(m.ishfram)), "rg_set_shell_frame")
+        if getattr(m, "nodal_dt", None):
+            dtfac, dtmin = m.nodal_dt
+            self._chk(L.rg_set_nodal_dt(self.h, float(dtfac), float(dtmin)), "rg_set_nodal_dt")
         if skyline is not None:
             adsky, iads, iadc = (np.ascontiguousarray(a, np.int32) for a in skyline)
             self._chk(L.rg_skyline_set(self.h, _p(adsky), _p(iads), _p(iadc)), "rg_skyline_set")

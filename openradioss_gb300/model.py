@@ -181,6 +181,7 @@ class Model:
     # bits 4 = x, 2 = y, 1 = z
     rlinks: list = field(default_factory=list)
     ishfram: int = 0           # local shell frame: 0 symmetric, 2 /SHFRA/V4
+    nodal_dt: tuple | None = None  # /DT/NODA: (DTFAC1(11), DTMIN1(11))
     dtfac_solid: float = 0.9
     dtfac_shell: float = 0.9
     dtmx: float = 1e30

@@ -57,6 +57,7 @@ def lib():
         L.or_rlink_add.argtypes = [vp, C.c_int, _ip, C.c_int, C.c_int]
         L.or_rlink_clear.argtypes = [vp]
         L.or_set_record.argtypes = [vp, C.c_int]
+        L.or_set_nodal_dt.argtypes = [vp, C.c_double, C.c_double]
         L.or_get_record.argtypes = [vp, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
@@ -102,6 +103,9 @@ class OracleModel:
                 raise RuntimeError("or_rlink_add failed")
         if L.or_shell_frame(self.h, model.ishfram) != 0:
             raise RuntimeError("or_shell_frame: unsupported ISHFRAM %d" % model.ishfram)
+        if getattr(model, "nodal_dt", None):
+            if L.or_set_nodal_dt(self.h, float(model.nodal_dt[0]), float(model.nodal_dt[1])) != 0:
+                raise RuntimeError("or_set_nodal_dt failed")
         nt = nthreads or os.cpu_count() or 1
         r = L.or_finalize(self.h, model.dtfac_solid, model.dtfac_shell, model.dtmx,
                           model.dt2old, nt)

@@ -79,6 +79,10 @@ struct Model {
   };
   std::vector<Link> links;
 
+  // nodal time step (/DT/NODA, DTNODA): DTFAC1(11), DTMIN1(11)
+  int nodadt = 0;
+  double dtfac_noda = RG_ZEP9, dtmin_noda = RG_ZERO;
+
   // listing quantities of the last cycle, taken where ECRIT runs (after the
   // kinematic conditions, before VELOCITY)
   bool record = false;
@@ -579,8 +583,9 @@ void hexa_group(Model &M, const HexaGroup &G, double &dt2t, int &neltst) {
       L.sti[i] = trho * tvol;
     }
     dtx = M.dtfac_solid * dtx;
-    // NODADT = 0: DT2T = min over live elements (mqviscb.F:520-535)
-    if (L.voln[i] > RG_ZERO && (L.off[i] != RG_ZERO && M.offg[e] >= RG_ZERO)) {
+    // NODADT = 0: DT2T = min over live elements (mqviscb.F:520-535); under
+    // the nodal time step the elements only provide STI (mqviscb.F:351)
+    if (!M.nodadt && L.voln[i] > RG_ZERO && (L.off[i] != RG_ZERO && M.offg[e] >= RG_ZERO)) {
       if (!(dtx > dt2t)) {
         dt2t = dtx;
         neltst = e;
@@ -805,6 +810,7 @@ void rwall_apply(Shells *, int numnod, const double *X, double *V,
                  const double *A, double dt12);
 int get_state(const Shells *, int which, double *out);
 int set_frame(Shells *, int ishfram);
+void set_nodadt(Shells *, int on);
 }  // namespace rg_oracle_shell
 
 struct OrModelWrap {
@@ -1123,6 +1129,39 @@ int or_cycle(void *m, int ncycle) {
       M.FRLAST[3 * n + 1] = r1;
       M.FRLAST[3 * n + 2] = r2;
     }
+    // DTNODA (time_step/dtnoda.F:213-345, 443-470), NODADT > 0: nodal time
+    // step DTFAC1(11)*SQRT(2*MS/STIFN) over the nodes with mass, then the
+    // rotational one DTFAC1(11)*SQRT(2*IN/STIFR); a node with non-positive
+    // stiffness stops the run (flagged here).  Strict '<' scans: on ties the
+    // first node of the translational pass, then of the rotational pass.
+    if (M.nodadt) {
+      for (int n = 0; n < numnod; n++) {
+        if (M.STIFN[n] <= RG_ZERO) {
+          M.error |= 32;
+        } else if (M.MS[n] > RG_ZERO) {
+          const double d = M.dtfac_noda * std::sqrt(RG_TWO * M.MS[n] / M.STIFN[n]);
+          if (d < M.dtmin_noda) M.error |= 8;
+          if (d < dt2t) {
+            dt2t = d;
+            neltst = n + 1;
+          }
+        }
+      }
+      if (rot) {
+        for (int n = 0; n < numnod; n++) {
+          if (M.STIFR[n] <= RG_ZERO) {
+            M.error |= 32;
+          } else if (M.IN[n] > RG_ZERO) {
+            const double d = M.dtfac_noda * std::sqrt(RG_TWO * M.IN[n] / M.STIFR[n]);
+            if (d < M.dtmin_noda) M.error |= 8;
+            if (d < dt2t) {
+              dt2t = d;
+              neltst = n + 1;
+            }
+          }
+        }
+      }
+    }
     // resol.F:6123-6127, 6352, 6494-6497
     if (dt2t < M.dt2) {
       M.dt2 = dt2t;
@@ -1376,6 +1415,16 @@ int or_energy(void *m, double *eint, double *ekin, double *ekinr,
 }
 
 int or_error(void *m) { return ((OrModelWrap *)m)->m.error; }
+
+int or_set_nodal_dt(void *m, double dtfac, double dtmin) {
+  auto *w = (OrModelWrap *)m;
+  if (w->m.finalized || !(dtfac > 0.0)) return -1;
+  w->m.nodadt = 1;
+  w->m.dtfac_noda = dtfac;
+  w->m.dtmin_noda = dtmin;
+  rg_oracle_shell::set_nodadt(w->sh, 1);
+  return 0;
+}
 
 int or_shell_frame(void *m, int ishfram) {
   return rg_oracle_shell::set_frame(((OrModelWrap *)m)->sh, ishfram);

@@ -79,6 +79,11 @@ int or_energy(void *m, double *eint, double *ekin, double *ekinr,
               double *ehour);
 int or_error(void *m);
 
+/* Nodal time step (/DT/NODA; DTNODA, time_step/dtnoda.F): elements give
+ * only their stiffness, the cycle's step is the minimum over nodes of
+ * dtfac*sqrt(2*MS/STIFN) (and 2*IN/STIFR for shell nodes).  Before
+ * or_finalize.  Error bits: 8 below dtmin, 32 node without stiffness. */
+int or_set_nodal_dt(void *m, double dtfac, double dtmin);
 /* Local shell frame: 0 = symmetric convected frame (default), 2 = the
  * version-4 frame of /SHFRA/V4 (CNVEC3, cnvec3.F:143-170). */
 int or_shell_frame(void *m, int ishfram);

@@ -62,9 +62,11 @@ struct Shells {
   std::vector<double> ehou;            // accumulated hourglass energy
   int nptmax = 5;
   int ishfram = 0;                     // local frame (/SHFRA/V4: 2)
+  int nodadt = 0;                      // nodal time step (/DT/NODA)
 };
 
 Shells *create() { return new Shells(); }
+void set_nodadt(Shells *s, int on) { s->nodadt = on; }
 int set_frame(Shells *s, int ishfram) {
   if (ishfram != 0 && ishfram != 2) return -1;
   s->ishfram = ishfram;
@@ -531,6 +533,7 @@ static void element(Shells *S, const Group &G, int e, const double *X,
   const double viscmx = std::sqrt(RG_ONE + RG_ZERO * RG_ZERO) - RG_ZERO;
   // ---- CHVIS3 (chvis3.F:32), ISMSTR = 4, IHBE = 1 ----
   double h11, h12, h13, h21, h22, h23, h31, h32, h33, b1x[4], b2x[4], ehou;
+  double sti_noda = RG_ZERO, stir_noda = RG_ZERO;
   {
     const double px1v = px1 * vhx, px2v = px2 * vhx, py1v = py1 * vhy, py2v = py2 * vhy;
     const double gama1 = off * (RG_ONE - px1v - py1v);
@@ -567,6 +570,21 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     const double b1 = px1 * px1 + py1 * py1, b2 = px2 * px2 + py2 * py2;
     double hh2 = A8 * thk02 * td / (b1 + b2);
     if (ix[3] == ix[4]) h1q = h1l = h2q = h2l = h3q = h3l = hh1 = hh2 = RG_ZERO;
+    if (S->nodadt) {
+      // nodal time step (chvis3.F:198-265, IGTYP=1, no adaptive meshing):
+      // element stiffness for DTNODA, with the hourglass stiffness SCALE
+      const double scale =
+          dmax(dmax(gama1 * gama1, gama2 * gama2), dmax(gama3 * gama3, gama4 * gama4)) * DT1 *
+          dmax(dmax(hh1 + h1l, hh2 + h2l), h3l) / dmax(DT1 * DT1, RG_EM20);
+      if (off == RG_ZERO) {
+        sti_noda = stir_noda = RG_ZERO;
+      } else {
+        const double vv = viscmx * viscmx * RG_ONE;  // VISCMX^2 * ALPE
+        sti_noda = RG_ZERO + scale;
+        sti_noda = sti_noda + dmax(b1, b2) * thk0 * a11 / (area * vv);
+        stir_noda = sti_noda * (thk02 * RG_ONE_OVER_12 + area * RG_ONE_OVER_9);
+      }
+    }
     double hg1 = vx[0] * gama1 + vx[1] * gama2 + vx[2] * gama3 + vx[3] * gama4;
     double hg2 = vy[0] * gama1 + vy[1] * gama2 + vy[2] * gama3 + vy[3] * gama4;
     HOU_(0, e) = HOU_(0, e) + hg1 * hh1;
@@ -602,9 +620,10 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     b2x[2] = HOU_(4, e) * off;
     b2x[3] = -HOU_(4, e) * off;
   }
-  // ---- CDT3 (cdt3.F:32): element time step, STI ----
-  double sti, stir;
-  {
+  // ---- CDT3 (cdt3.F:32): element time step, STI; not called under the
+  // nodal time step (cforc3.F:668, IDTMIN(3) = 0) ----
+  double sti = sti_noda, stir = stir_noda;
+  if (!S->nodadt) {
     aldt = aldt * viscmx / std::sqrt(RG_ONE);
     const double dt = dtfac * aldt / ssp;
     if (S->offg[e] > RG_ZERO && off != RG_ZERO && dt < dt2t) {
