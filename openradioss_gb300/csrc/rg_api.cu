@@ -208,7 +208,10 @@ __global__ void refresh_copies_kernel(NodeView N, int rot) {
   const int n = blockIdx.x * NODE_NT + threadIdx.x;
   if (n >= N.numnod) return;
   const dbl4 x = N.X4[n], v = N.V4[n];
-  N.XF[n] = split_hilo(x.x, x.y, x.z);
+  F8 c = split_hilo(x.x, x.y, x.z);
+  c.pad0 = __double2float_rn(x.w);                       // 1/MS
+  c.pad1 = rot ? __double2float_rn(N.VR4[n].w) : 0.f;    // 1/IN
+  N.XF[n] = c;
   N.VF[n] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y), __double2float_rn(v.z), 0.f);
   if (rot) {
     const dbl4 w = N.VR4[n];
@@ -343,7 +346,10 @@ __global__ void upload_nodes_kernel(NodeView N, const double *__restrict__ x,
   N.X4[i] = a;
   N.V4[i] = b;
   if (mixed) {
-    N.XF[i] = split_hilo(a.x, a.y, a.z);
+    F8 c = split_hilo(a.x, a.y, a.z);
+    c.pad0 = __double2float_rn(a.w);                             // 1/MS
+    c.pad1 = N.VR4 ? __double2float_rn(N.VR4[i].w) : 0.f;        // 1/IN
+    N.XF[i] = c;
     N.VF[i] = make_float4(__double2float_rn(b.x), __double2float_rn(b.y),
                           __double2float_rn(b.z), 0.f);
   }

@@ -252,10 +252,10 @@ batch_kernel(const BatchDev<ER> B, const int phases) {
         const int n = nt.n0 + k * BNT + threadIdx.x;
         if (n < nn) {
           if (J.rot)
-            node_update<F64, true, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
+            node_update<F64, true, true, false, false>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                          J.status, n);
           else
-            node_update<F64, false, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
+            node_update<F64, false, true, false, false>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                           J.status, n);
         }
       }
@@ -289,10 +289,10 @@ batch_node_kernel(const BatchDev<ER> B) {
       const int n = nt.n0 + i;
       if (n < nn) {
         if (J.rot)
-          node_update<F64, true, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
+          node_update<F64, true, true, false, false>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                        J.status, n);
         else
-          node_update<F64, false, true>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
+          node_update<F64, false, true, false, false>(J.nv, J.adsky, J.fsky, J.fskyr, J.T, J.wall, J.walls, nullptr,
                                         J.status, n);
       }
     }

@@ -44,7 +44,7 @@ struct Time {
 // (mixed form): the difference of two nodes' copies keeps FP32 relative
 // precision however far the nodes are from the origin.
 struct __align__(32) F8 {
-  float hx, hy, hz, pad0, lx, ly, lz, pad1;
+  float hx, hy, hz, pad0, lx, ly, lz, pad1;  // pad0 = 1/MS, pad1 = 1/IN (FP32)
 };
 
 struct NodeView {

@@ -19,6 +19,8 @@ constexpr int RG_LINK_SHIFT = 8;
 // multiply-add is fused and each node's result does not depend on the
 // launch configuration.
 // ---------------------------------------------------------------------------
+// (pad0, pad1 = 1/MS, 1/IN in FP32 for the mixed node update: set by the
+// callers)
 __device__ __forceinline__ F8 split_hilo(double x, double y, double z) {
   F8 c;
   c.hx = __double2float_rn(x);
@@ -50,11 +52,62 @@ __device__ __forceinline__ dbl4 ldcg4(const dbl4 *p) {
   return mk4(a.x, a.y, b.x, b.y);
 }
 
+// Mixed form, ASSPAR4 sums of node n: the FP32 slot forces summed in the
+// fixed PARITH/ON order in FP32 (explicit round-to-nearest adds: no
+// reassociation).  MLP: the first U slots of the node (all of them in a
+// regular mesh: 4 per shell node, 8 per hexa node) are loaded together
+// before the sums, so that their latencies overlap; further slots follow one
+// by one.  COH = true: the slots were written earlier in the same launch by
+// other blocks, so they are read through L2.
+template <bool ROT, bool COH, bool MLP>
+__device__ __forceinline__ void node_sums_f32(const int k0, const int k1,
+                                              const float4 *__restrict__ fsky,
+                                              const float4 *__restrict__ fskyr,
+                                              int *__restrict__ status, float &b0, float &b1,
+                                              float &b2, float &c0, float &c1, float &c2) {
+  b0 = b1 = b2 = c0 = c1 = c2 = 0.f;
+  constexpr int U = MLP ? (ROT ? 4 : 8) : 0;
+  float4 fa[U > 0 ? U : 1], ga[ROT && U > 0 ? U : 1];
+#pragma unroll
+  for (int j = 0; j < U; j++) {
+    if (k0 + j < k1) {
+      fa[j] = COH ? __ldcg(fsky + k0 + j) : __ldg(fsky + k0 + j);
+      if (ROT) ga[j] = COH ? __ldcg(fskyr + k0 + j) : __ldg(fskyr + k0 + j);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < U; j++) {
+    if (k0 + j < k1) {
+      b0 = __fadd_rn(b0, fa[j].x);
+      b1 = __fadd_rn(b1, fa[j].y);
+      b2 = __fadd_rn(b2, fa[j].z);
+      if (ROT) {
+        c0 = __fadd_rn(c0, ga[j].x);
+        c1 = __fadd_rn(c1, ga[j].y);
+        c2 = __fadd_rn(c2, ga[j].z);
+      }
+    }
+  }
+  for (int k = k0 + U; k < k1; k++) {
+    const float4 f = COH ? __ldcg(fsky + k) : __ldg(fsky + k);
+    b0 = __fadd_rn(b0, f.x);
+    b1 = __fadd_rn(b1, f.y);
+    b2 = __fadd_rn(b2, f.z);
+    if (ROT) {
+      const float4 g = COH ? __ldcg(fskyr + k) : __ldg(fskyr + k);
+      c0 = __fadd_rn(c0, g.x);
+      c1 = __fadd_rn(c1, g.y);
+      c2 = __fadd_rn(c2, g.z);
+    }
+  }
+  if (!(isfinite(b0) && isfinite(b1) && isfinite(b2))) atomicOr(status, RG_ST_NAN);
+}
+
 // ASSPAR4 sums of node n: A (and AR) = 0 + the node's slots in PARITH/ON
-// order; FP64 slots summed in FP64, the mixed form's FP32 slots in FP32 (no
-// reassociation) and widened.  COH = true: the slots were written earlier in
-// the same launch by other blocks, so they are read through L2.
-template <bool F64, bool ROT, bool COH>
+// order; FP64 slots summed in FP64, the mixed form's FP32 slots in FP32 and
+// widened.  COH = true: the slots were written earlier in the same launch by
+// other blocks, so they are read through L2.
+template <bool F64, bool ROT, bool COH, bool MLP = true>
 __device__ __forceinline__ void node_assemble(const int *__restrict__ adsky,
                                               const void *__restrict__ fsky_,
                                               const void *__restrict__ fskyr_,
@@ -64,7 +117,6 @@ __device__ __forceinline__ void node_assemble(const int *__restrict__ adsky,
   const int k0 = __ldg(adsky + n), k1 = __ldg(adsky + n + 1);
   r0 = r1 = r2 = 0.0;
   if constexpr (F64) {
-    // ASSPAR4: A = 0 + sum of the node's slots in PARITH/ON order, FP64
     const dbl4 *fsky = (const dbl4 *)fsky_;
     const dbl4 *fskyr = (const dbl4 *)fskyr_;
     a0 = a1 = a2 = 0.0;
@@ -82,24 +134,9 @@ __device__ __forceinline__ void node_assemble(const int *__restrict__ adsky,
     }
     if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicOr(status, RG_ST_NAN);
   } else {
-    // mixed form: FP32 element forces summed in the same fixed order in
-    // FP32 (explicit round-to-nearest adds: no reassociation), then FP64
-    const float4 *fsky = (const float4 *)fsky_;
-    const float4 *fskyr = (const float4 *)fskyr_;
-    float b0 = 0.f, b1 = 0.f, b2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
-    for (int k = k0; k < k1; k++) {
-      const float4 f = COH ? __ldcg(fsky + k) : __ldg(fsky + k);
-      b0 = __fadd_rn(b0, f.x);
-      b1 = __fadd_rn(b1, f.y);
-      b2 = __fadd_rn(b2, f.z);
-      if (ROT) {
-        const float4 g = COH ? __ldcg(fskyr + k) : __ldg(fskyr + k);
-        c0 = __fadd_rn(c0, g.x);
-        c1 = __fadd_rn(c1, g.y);
-        c2 = __fadd_rn(c2, g.z);
-      }
-    }
-    if (!(isfinite(b0) && isfinite(b1) && isfinite(b2))) atomicOr(status, RG_ST_NAN);
+    float b0, b1, b2, c0, c1, c2;
+    node_sums_f32<ROT, COH, MLP>(k0, k1, (const float4 *)fsky_, (const float4 *)fskyr_, status,
+                                 b0, b1, b2, c0, c1, c2);
     a0 = b0;
     a1 = b1;
     a2 = b2;
@@ -112,8 +149,9 @@ __device__ __forceinline__ void node_assemble(const int *__restrict__ adsky,
 // COH = true: the slots and the time-step scalars were written earlier in
 // the same launch by other blocks, so they are read through L2.  LINK: the
 // model has rigid links; lacc holds their common accelerations (rlink
-// kernel).
-template <bool F64, bool ROT, bool COH = false, bool LINK = false>
+// kernel).  MLP: load a node's first slots together (more registers; off in
+// the batched kernels, which are held to their register budgets).
+template <bool F64, bool ROT, bool COH = false, bool LINK = false, bool MLP = true>
 __device__ __forceinline__ void node_update(const NodeView &N, const int *__restrict__ adsky,
                                             const void *__restrict__ fsky_,
                                             const void *__restrict__ fskyr_,
@@ -122,8 +160,27 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
                                             const double *__restrict__ walls,
                                             const dbl4 *__restrict__ lacc,
                                             int *__restrict__ status, const int n) {
-  double a0, a1, a2, r0, r1, r2;
-  node_assemble<F64, ROT, COH>(adsky, fsky_, fskyr_, status, n, a0, a1, a2, r0, r1, r2);
+  double a0, a1, a2, r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  F8 xf;  // mixed form: FP32 position copy; pad0 / pad1 = 1/MS, 1/IN in FP32
+  if constexpr (F64) {
+    node_assemble<F64, ROT, COH, MLP>(adsky, fsky_, fskyr_, status, n, a0, a1, a2, r0, r1, r2);
+  } else {
+    float b0, b1, b2, c0, c1, c2;
+    node_sums_f32<ROT, COH, MLP>(__ldg(adsky + n), __ldg(adsky + n + 1),
+                                 (const float4 *)fsky_, (const float4 *)fskyr_, status, b0, b1,
+                                 b2, c0, c1, c2);
+    xf = N.XF[n];
+    // ACCELE on the FP32 force sums: F * (1/MS) rounded once in FP32, then
+    // widened (the forces carry FP32 precision already)
+    a0 = (double)__fmul_rn(b0, xf.pad0);
+    a1 = (double)__fmul_rn(b1, xf.pad0);
+    a2 = (double)__fmul_rn(b2, xf.pad0);
+    if (ROT) {
+      r0 = (double)__fmul_rn(c0, xf.pad1);
+      r1 = (double)__fmul_rn(c1, xf.pad1);
+      r2 = (double)__fmul_rn(c2, xf.pad1);
+    }
+  }
   dbl4 x = ld4(N.X4 + n);
   dbl4 v = ld4(N.V4 + n);
   // FP64 form: D4 = displacement, MS.  Mixed form: D4 holds the initial
@@ -133,9 +190,11 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
   const double dt12 = COH ? __ldcg(&T->dt12) : T->dt12;
   const double dt2 = COH ? __ldcg(&T->dt2) : T->dt2;
   // ACCELE: A = A * (1/MS); X4.w holds 1/MS (0 when MS <= 0, giving A = 0)
-  a0 = __dmul_rn(a0, x.w);
-  a1 = __dmul_rn(a1, x.w);
-  a2 = __dmul_rn(a2, x.w);
+  if constexpr (F64) {
+    a0 = __dmul_rn(a0, x.w);
+    a1 = __dmul_rn(a1, x.w);
+    a2 = __dmul_rn(a2, x.w);
+  }
   // node code: BCS bits 1/2/4 (x/y/z), 8/16/32 (rotations); above them the
   // 1-based index of the node's rigid link (0: none)
   const int code = (int)v.w;
@@ -207,22 +266,27 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     x.z = fma(dt2, v.z, x.z);
     // the FP32 hi/lo copy advances by the FP32-rounded increment with an
     // exact two-sum (no FP64 split of the new position)
-    F8 c = N.XF[n];
-    ff_add(c.hx, c.lx, __double2float_rn(__dmul_rn(dt2, v.x)));
-    ff_add(c.hy, c.ly, __double2float_rn(__dmul_rn(dt2, v.y)));
-    ff_add(c.hz, c.lz, __double2float_rn(__dmul_rn(dt2, v.z)));
-    N.XF[n] = c;
-    N.VF[n] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y),
-                          __double2float_rn(v.z), 0.f);
+    // increment DT2 * V formed in FP32 from the FP32 velocity copy (one
+    // rounding more than the FP64 product: below the copy's resolution)
+    const float vfx = __double2float_rn(v.x), vfy = __double2float_rn(v.y),
+                vfz = __double2float_rn(v.z);
+    const float dt2f = __double2float_rn(dt2);
+    ff_add(xf.hx, xf.lx, __fmul_rn(dt2f, vfx));
+    ff_add(xf.hy, xf.ly, __fmul_rn(dt2f, vfy));
+    ff_add(xf.hz, xf.lz, __fmul_rn(dt2f, vfz));
+    N.XF[n] = xf;
+    N.VF[n] = make_float4(vfx, vfy, vfz, 0.f);
   }
   st4(N.X4 + n, x);
   st4(N.V4 + n, v);
   if constexpr (F64) st4(N.D4 + n, d);
   if (ROT) {
     dbl4 vr = ld4(N.VR4 + n);
-    r0 = __dmul_rn(r0, vr.w);
-    r1 = __dmul_rn(r1, vr.w);
-    r2 = __dmul_rn(r2, vr.w);
+    if constexpr (F64) {
+      r0 = __dmul_rn(r0, vr.w);
+      r1 = __dmul_rn(r1, vr.w);
+      r2 = __dmul_rn(r2, vr.w);
+    }
     if (code) {
       if (code & 8) r0 = 0.0;
       if (code & 16) r1 = 0.0;
@@ -235,9 +299,15 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
       if (icr & 2) r1 = L.y;
       if (icr & 1) r2 = L.z;
     }
-    vr.x = __dadd_rn(vr.x, __dmul_rn(dt12, r0));
-    vr.y = __dadd_rn(vr.y, __dmul_rn(dt12, r1));
-    vr.z = __dadd_rn(vr.z, __dmul_rn(dt12, r2));
+    if constexpr (F64) {
+      vr.x = __dadd_rn(vr.x, __dmul_rn(dt12, r0));
+      vr.y = __dadd_rn(vr.y, __dmul_rn(dt12, r1));
+      vr.z = __dadd_rn(vr.z, __dmul_rn(dt12, r2));
+    } else {
+      vr.x = fma(dt12, r0, vr.x);
+      vr.y = fma(dt12, r1, vr.y);
+      vr.z = fma(dt12, r2, vr.z);
+    }
     st4(N.VR4 + n, vr);
     if constexpr (!F64)
       N.VRF[n] = make_float4(__double2float_rn(vr.x), __double2float_rn(vr.y),
