@@ -31,10 +31,10 @@ static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
                        DtPartials dp, Time *T, int *status, const DtFinish &F,
                        cudaStream_t s) {
   constexpr int NT = 128;
-  // mixed form: 5 resident blocks per SM at 96 registers (a few dozen bytes
-  // per thread spill to L1: measured faster than 4 or 6 blocks); the FP64
+  // mixed form: 6 resident blocks per SM at 80 registers (about 100 bytes
+  // per thread spill to L1: measured faster than 4, 5 or 7 blocks); the FP64
   // form needs its ~250 registers
-  constexpr int MINB = std::is_same<ER, float>::value ? 5 : 1;
+  constexpr int MINB = std::is_same<ER, float>::value ? 6 : 1;
   const int nb = (P.nel + NT - 1) / NT;
   if (P.jcvt)
     hexa_kernel<ER, LAW, 1, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);

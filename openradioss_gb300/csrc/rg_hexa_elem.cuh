@@ -668,6 +668,19 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
     }
 
     // ---- SHVIS3 (JHBE >= 1) ----------------------------------------------------
+    // Mixed form: the node velocities are read again (the read-only FP32
+    // copies, in L1/L2 since the gather) rather than held in registers
+    // through the material update -- fewer live values, fewer spills.
+    if constexpr (!F64 && JCVT == 0) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const float4 vk = ldf4(N.VF + nc[k]);
+        const bool z0 = offg0 < (R)0;
+        vx[k] = z0 ? 0.f : vk.x;
+        vy[k] = z0 ? 0.f : vk.y;
+        vz[k] = z0 ? 0.f : vk.z;
+      }
+    }
     R f[3][8];
     {
       const R caq = (R)RG_FOURTH * off * PC(qh);
