@@ -97,3 +97,31 @@ def test_shell_mixed_vs_fp64(Engine):
     err_e = np.max(np.abs(e32 - e64)) / np.max(np.abs(e64))
     print("shell mixed: displacement %.2e peak force %.2e internal energy %.2e" % (err_d, err_p, err_e))
     assert err_d < 1e-4 and err_p < 1e-4 and err_e < 1e-4
+
+
+@pytest.mark.parametrize("ishfram,ithk,iplas,npt", [
+    (2, 1, 1, 5), (2, 0, 0, 3), (0, 0, 1, 3), (2, 1, 0, 1), (0, 1, 1, 2)])
+def test_formulation_combinations(Engine, oracle_lib, ishfram, ithk, iplas, npt):
+    """The shell options one at a time and together (local frame 0 / 2,
+    current / initial thickness, iterative / radial-return plasticity, 1-5
+    points), on a deforming crash box against the oracle: first-cycle forces
+    1e-12, 150-cycle trajectories 1e-10."""
+    m = M.crash_box(n_side=5, n_len=12, v0=40.0, vpert=2.0, npt=npt)
+    m.ishfram = ishfram
+    g = m.shells[0]
+    g.ithk = ithk
+    g.geo[38] = iplas
+    e = Engine(m)
+    o = oracle_lib.OracleModel(m, nthreads=2)
+    e.cycle(1)
+    o.cycle(1)
+    fg, fo = e.forces(), o.nodes()
+    assert rel(fg["F"], fo["F"]) < 1e-12
+    assert rel(fg["FR"], fo["FR"]) < 1e-12
+    e.cycle(149)
+    o.cycle(149)
+    ng, no = e.nodes(), o.nodes()
+    assert rel(ng["X"] - m.X, no["X"] - m.X) < 1e-10
+    assert rel(ng["VR"], no["VR"]) < 1e-10
+    # thickness (updated in both ITHK modes by the material)
+    assert rel(e.shell_state(2, m.numelc), o.shell_state(2, m.numelc)) < 1e-10
