@@ -180,6 +180,13 @@ class Model:
     # rigid links (engine /VEL/TRA|ROT): (1-based nodes, ic, icr), direction
     # bits 4 = x, 2 = y, 1 = z
     rlinks: list = field(default_factory=list)
+    # rigid bodies (/RBODY, after the starter's set-up, rbody_init):
+    # (1-based main node, 1-based secondary nodes, principal axes as rows
+    # (3, 3), principal inertia (3,))
+    rbodies: list = field(default_factory=list)
+    # concentrated loads (/CLOAD): (1-based node, direction 0..5, abscissa
+    # scale, ordinate scale, curve abscissae, curve ordinates)
+    cloads: list = field(default_factory=list)
     ishfram: int = 0           # local shell frame: 0 symmetric, 2 /SHFRA/V4
     nodal_dt: tuple | None = None  # /DT/NODA: (DTFAC1(11), DTMIN1(11))
     dtfac_solid: float = 0.9
@@ -507,4 +514,109 @@ def model_from_deck(d, name="deck", with_links=True):
     if with_links and len(d["rlink_nodes"]):
         m.rlinks = [(np.asarray(d["rlink_nodes"], np.int32), 7, 0)]
     m.ishfram = 2 if int(d["shfra_v4"]) else 0
+    return m
+
+
+def rbody_init(X, MS, IN, main, nodes, ispher=2):
+    """The starter's rigid-body set-up INIRBY
+    (starter/source/constraints/general/rbody/inirby.F) for a body without
+    added mass or inertia, skew or sensor, centre-of-mass flag ICOG = 1:
+    the main node (1-based) moves to the centre of mass of itself (a zero
+    mass counts as 1e-20) and the secondary nodes (1-based); the inertia
+    tensor about it collects the main node's shifted mass, the secondary
+    masses and their nodal inertia; its principal values below 1e-3 of the
+    largest gain 0.1 of the largest (ISPHER = 2, the reader's default);
+    MS(main) becomes the body mass and IN(main) the smallest principal
+    inertia.  X, MS, IN are updated in place.  Returns the principal axes as
+    rows (right-handed) and the principal inertia."""
+    m = int(main) - 1
+    sec = np.asarray(nodes, np.int64) - 1
+    ms_loc, in_loc = MS[sec].copy(), IN[sec].copy()
+    if MS[m] == 0.0:
+        MS[m] = 1e-20
+    J = np.eye(3) * IN[m]
+    xmg = MS[m]
+    xg = X[:, m].copy()
+    masrb = MS[m] + ms_loc.sum()
+    X[:, m] = (X[:, m] * MS[m] + (X[:, sec] * ms_loc).sum(axis=1)) / masrb
+    r = xg - X[:, m]
+    J += xmg * (np.dot(r, r) * np.eye(3) - np.outer(r, r))
+    for k in range(len(sec)):
+        r = X[:, sec[k]] - X[:, m]
+        J += in_loc[k] * np.eye(3) + ms_loc[k] * (np.dot(r, r) * np.eye(3) - np.outer(r, r))
+    w, v = np.linalg.eigh(J)
+    if ispher == 2 and w.min() <= 1e-3 * w.max():
+        w = np.where(w / w.max() < 1e-3, w + 0.1 * w.max(), w)
+    axes = v.T.copy()
+    if np.linalg.det(axes) < 0:
+        axes[2] = -axes[2]
+    MS[m] = masrb
+    IN[m] = w.min()
+    return axes, w, J
+
+
+def hexa_model_from_deck(d, name="deck"):
+    """Model of a hexa deck held as arrays (the layout written by
+    tests/golden/make_h101.py: nodes, /BRICK parts, /MAT/ELAST, /PROP/SOLID,
+    /DEF_SOLID, /BCS, /FUNCT + /CLOAD, /RBODY), with the starter's decisions
+    for it:
+
+    * properties (starter/source/properties/solid/hm_read_prop14.F:276-288):
+      Isolid 0 -> the /DEF_SOLID value; Iframe 0 -> the /DEF_SOLID value, and
+      Iframe 2 is the co-rotational frame (JCVT = 1 in the engine); Ismstr 0
+      -> 4; qa, qb, h 0 -> 1.1, 0.05, 0.1;
+    * masses: SMASS3 lumping rho V / 8 of every brick;
+    * rigid bodies: rbody_init (INIRBY).
+
+    Node ids are mapped to 1-based indices in the order of the /NODE card;
+    elements keep their user ids.  One hexa group per part, in part order.
+    """
+    node_id = np.asarray(d["node_id"])
+    index = {int(n): k + 1 for k, n in enumerate(node_id)}
+    to_idx = np.vectorize(lambda n: index[int(n)], otypes=[np.int32])
+    X = np.ascontiguousarray(np.asarray(d["X"], np.float64).T)
+    numnod = X.shape[1]
+    mats = {int(r[0]): r for r in np.asarray(d["mat"])}
+    pcols = [str(c) for c in d["prop_columns"]]
+    props = {int(r[0]): dict(zip(pcols, r)) for r in np.asarray(d["prop"])}
+    isolid_d, ismstr_d, _, iframe_d = (int(v) for v in d["def_solid"])
+    ms = np.zeros(numnod)
+    groups = []
+    bid, bpart, bnodes = (np.asarray(d[k]) for k in ("brick_id", "brick_part", "brick_nodes"))
+    for p, mid, pid in zip(d["part_id"], d["part_mat"], d["part_prop"]):
+        sel = np.nonzero(bpart == p)[0]
+        _, rho, young, nu = mats[int(mid)]
+        pr = props[int(pid)]
+        isolid = int(pr["Isolid"]) or isolid_d or 1
+        iframe = int(pr["Iframe"]) or iframe_d
+        ismstr = int(pr["Ismstr"]) or ismstr_d or 4
+        if isolid != 1 or ismstr != 4 or iframe not in (1, 2):
+            raise ValueError("only Isolid = 1, Ismstr = 4 bricks are supported")
+        ixs = np.zeros((11, len(sel)), np.int32)
+        ixs[0] = int(mid)
+        ixs[1:9] = to_idx(bnodes[sel]).T
+        ixs[9] = int(pid)
+        ixs[10] = bid[sel]
+        lumped_mass_hexa(X, ixs, rho, ms)
+        geo = solid_prop(qa=pr["qa"] or 1.1, qb=pr["qb"] or 0.05, qh=pr["h"] or 0.1)
+        groups.append(HexaGroupSpec(ixs, law1(rho, young, nu), geo, jcvt=iframe - 1))
+    icodt = np.zeros(numnod, np.int32)
+    off = np.asarray(d["bcs_offsets"])
+    bn = to_idx(np.asarray(d["bcs_nodes"]))
+    for k, (tra, rot) in enumerate(zip(d["bcs_tra"], d["bcs_rot"])):
+        icodt[bn[off[k]:off[k + 1]] - 1] |= _code_bits(str(tra), 1) | _code_bits(str(rot), 8)
+    inr = np.zeros(numnod)
+    rbodies = []
+    off = np.asarray(d["rbody_offsets"])
+    rn = np.asarray(d["rbody_nodes"])
+    for k, main in enumerate(d["rbody_main"]):
+        nodes = to_idx(rn[off[k]:off[k + 1]])
+        axes, inertia, _ = rbody_init(X, ms, inr, index[int(main)], nodes)
+        rbodies.append((index[int(main)], nodes, axes, inertia))
+    fx, fy = np.asarray(d["funct1"], np.float64).T
+    fcx, fcy = (float(v) for v in d["cload_scale"])
+    cloads = [(index[int(n)], int(d["cload_dir"]), fcx, fcy, fx, fy) for n in d["cload_nodes"]]
+    m = Model(name, X, np.zeros_like(X), ms, icodt, hexa=groups, IN=inr)
+    m.rbodies = rbodies
+    m.cloads = cloads
     return m

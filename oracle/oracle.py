@@ -59,6 +59,9 @@ def lib():
         L.or_set_record.argtypes = [vp, C.c_int]
         L.or_set_nodal_dt.argtypes = [vp, C.c_double, C.c_double]
         L.or_get_record.argtypes = [vp, C.c_void_p, C.c_void_p]
+        L.or_rbody_add.argtypes = [vp, C.c_int, C.c_int, _ip, _dp, _dp]
+        L.or_cload_add.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                   _dp, _dp]
         _lib = L
     return _lib
 
@@ -95,6 +98,19 @@ class OracleModel:
                 raise RuntimeError("or_shell_group_add failed %d" % r)
         if model.IN is not None:
             L.or_set_inertia(self.h, np.ascontiguousarray(model.IN, np.float64))
+        for (main, nodes, axes, inertia) in getattr(model, "rbodies", []):
+            r = L.or_rbody_add(self.h, int(main), len(nodes),
+                               np.ascontiguousarray(nodes, np.int32),
+                               np.ascontiguousarray(axes, np.float64).reshape(-1),
+                               np.ascontiguousarray(inertia, np.float64))
+            if r < 0:
+                raise RuntimeError("or_rbody_add failed %d" % r)
+        for (node, dr, fcx, fcy, xs, ys) in getattr(model, "cloads", []):
+            xs = np.ascontiguousarray(xs, np.float64)
+            r = L.or_cload_add(self.h, int(node), int(dr), float(fcx), float(fcy), len(xs), xs,
+                               np.ascontiguousarray(ys, np.float64))
+            if r < 0:
+                raise RuntimeError("or_cload_add failed %d" % r)
         for (p0, nrm, ds) in model.rwalls:
             L.or_rwall_add(self.h, np.asarray(p0, np.float64), np.asarray(nrm, np.float64), ds)
         for (nodes, ic, icr) in model.rlinks:
@@ -175,10 +191,11 @@ class OracleModel:
         """Listing quantities of the last cycle (ECRIT's point of the
         cycle): time, dt, energies (internal, kinetic, rotational kinetic,
         hourglass), momentum, mass, controlling element."""
-        out = np.zeros(10)
+        out = np.zeros(11)
         el = np.zeros(1, np.int32)
         lib().or_get_record(self.h, _ptr(out), _ptr(el))
-        keys = ("tt", "dt2", "eint", "ekin", "ekinr", "ehour", "xmom", "ymom", "zmom", "mass")
+        keys = ("tt", "dt2", "eint", "ekin", "ekinr", "ehour", "xmom", "ymom", "zmom", "mass",
+                "wfext")
         r = dict(zip(keys, out.tolist()))
         r["neltst"] = int(el[0])
         return r

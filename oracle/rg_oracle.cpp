@@ -8,10 +8,14 @@
 // so that no multiply-add is fused.
 //
 // Parity status: the reference engine cannot be built here (no Fortran
-// compiler; the starter also needs an un-vendored binary library).  The shell
-// path is pinned against outputs the reference engine wrote for its own QA
-// deck CRA2V44 (printed cycle table to every digit, time histories to ~1e-6
-// relative over 3375 cycles); the hexa path by analytic known-answer tests.
+// compiler; the starter also needs an un-vendored binary library).  Both
+// element paths are pinned against outputs the reference engine wrote for
+// its own QA decks: the shell path by CRA2V44 (printed cycle table to every
+// digit, time histories to ~1e-6 relative over 3375 cycles), the hexa path
+// (LAW1, co-rotational frame, viscous hourglass) by H101 (six cantilevers
+// with rigid-body tips under concentrated loads: printed table to every
+// digit, energies and tip motions to ~1e-7 over 847 cycles).  Rigid bodies
+// and concentrated loads are here to run that deck.
 //
 // Each block cites the reference file:line it follows (paths relative to the
 // OpenRadioss source tree).
@@ -83,10 +87,32 @@ struct Model {
   int nodadt = 0;
   double dtfac_noda = RG_ZEP9, dtmin_noda = RG_ZERO;
 
+  // rigid bodies (/RBODY; starter INIRBY done by the caller: the main node
+  // sits at the centre of mass with MS = body mass, IN = smallest principal
+  // inertia)
+  struct Body {
+    int main = 0;            // 0-based
+    std::vector<int> nodes;  // secondary nodes, 0-based
+    double R[9] = {};        // principal axes, rows e1 e2 e3 (RBY(1:9))
+    double I[3] = {};        // principal inertia (RBY(10:12))
+  };
+  std::vector<Body> bodies;
+  std::vector<char> secondary;  // 1: secondary node of a rigid body, 2: main
+
+  // concentrated loads (/CLOAD): node (0-based), direction 0..5 (x y z, then
+  // rotations), abscissa / ordinate scales, load curve points
+  struct Load {
+    int node = 0, dir = 0;
+    double fcx = 1, fcy = 1;
+    std::vector<double> x, y;
+  };
+  std::vector<Load> loads;
+  double wfext = 0;  // external work of the loads (OUTPUT%TH%WFEXT)
+
   // listing quantities of the last cycle, taken where ECRIT runs (after the
   // kinematic conditions, before VELOCITY)
   bool record = false;
-  double out[10] = {};
+  double out[11] = {};
 };
 
 // ----------------------------------------------------------------------------
@@ -1049,19 +1075,171 @@ int or_get_skyline(void *m, int *adsky, int *iads, int *iadc, int *lsky) {
   return 0;
 }
 
+}  // extern "C"
+
+namespace {
+
+// FINTER (tools/curve/finter.F): piecewise-linear load curve; a one-point
+// curve is constant; outside the abscissa range the end segments extend
+// linearly.  The value is taken from the nearer end of the segment.
+double finter(const std::vector<double> &x, const std::vector<double> &y, double t) {
+  const size_t n = x.size();
+  if (n == 1) return y[0];
+  size_t i = 1;
+  while (i < n - 1 && x[i] - t < RG_ZERO) i++;
+  const double div0 = x[i] - x[i - 1];
+  const double div = std::copysign(std::max(std::fabs(div0), 1e-16), div0);
+  const double deri = (y[i] - y[i - 1]) / div;
+  const double dx1 = t - x[i - 1], dx2 = x[i] - t;
+  return dx1 <= dx2 ? y[i - 1] + dx1 * deri : y[i] - dx2 * deri;
+}
+
+// ROTBMR (tools/skew/rotbmr.F): turn the principal frame by the rotation
+// vector dt*vi given in that frame (Rodrigues' formula, the matrix scaled by
+// |r|^2 with |r|^2 >= 1e-10), renormalise e1, e2 and take e3 = e1 x e2.
+void rotbmr(const double vi[3], double R[9], double dt) {
+  const double rx = dt * vi[0], ry = dt * vi[1], rz = dt * vi[2];
+  const double r2 = std::max(1e-10, rx * rx + ry * ry + rz * rz);
+  const double r = std::sqrt(r2);
+  const double cm1 = RG_ONE - std::cos(r);
+  const double c = std::cos(r) * r2;
+  const double s = std::sin(r) * r;
+  const double e11 = rx * rx * cm1 + c, e22 = ry * ry * cm1 + c;
+  const double e12 = rx * ry * cm1 + rz * s, e21 = rx * ry * cm1 - rz * s;
+  const double e13 = rx * rz * cm1 - ry * s, e23 = ry * rz * cm1 + rx * s;
+  double a[3], b[3];
+  for (int k = 0; k < 3; k++) {
+    a[k] = R[k] * e11 + R[3 + k] * e12 + R[6 + k] * e13;
+    b[k] = R[k] * e21 + R[3 + k] * e22 + R[6 + k] * e23;
+  }
+  const double na = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  const double nb = std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+  for (int k = 0; k < 3; k++) {
+    a[k] = a[k] / na;
+    b[k] = b[k] / nb;
+  }
+  R[0] = a[0], R[1] = a[1], R[2] = a[2];
+  R[3] = b[0], R[4] = b[1], R[5] = b[2];
+  R[6] = a[1] * b[2] - a[2] * b[1];
+  R[7] = a[2] * b[0] - a[0] * b[2];
+  R[8] = a[0] * b[1] - a[1] * b[0];
+}
+
+// RBYFOR / RGBODFP (constraints/general/rbody/rbyfor.F, rgbodfp.F), after
+// the slot assembly: the secondary nodes' forces, moments about the main
+// node and stiffnesses go to the main node (summed in secondary order; the
+// reference's PARITH/ON sum is order-independent, SUM_6_FLOAT); then, with
+// no rotational condition on the main node (ICODR = 0) and a non-spherical
+// body, the frame turns by VR*DT1 and the moment becomes the pseudo moment
+// IN(M)/I_k (M_k + (I_l - I_m) w_l w_m) in the principal frame, so that
+// ACCELE's AR = moment / IN(M) is the Euler angular acceleration.
+void rbyfor(Model &M, Model::Body &B) {
+  const int m = B.main;
+  for (int k = 0; k < 3; k++) B.I[k] = std::max(B.I[k], M.IN[m]);
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const double xm = M.X[3 * m], ym = M.X[3 * m + 1], zm = M.X[3 * m + 2];
+  for (int n : B.nodes) {
+    const double rx = M.X[3 * n] - xm, ry = M.X[3 * n + 1] - ym, rz = M.X[3 * n + 2] - zm;
+    const double dd = rx * rx + ry * ry + rz * rz;
+    const double f0 = M.A[3 * n], f1 = M.A[3 * n + 1], f2 = M.A[3 * n + 2];
+    s[0] = s[0] + M.STIFN[n];
+    s[1] = s[1] + (M.STIFR[n] + dd * M.STIFN[n]);
+    s[2] = s[2] + f0;
+    s[3] = s[3] + f1;
+    s[4] = s[4] + f2;
+    s[5] = s[5] + (M.AR[3 * n] + ry * f2 - rz * f1);
+    s[6] = s[6] + (M.AR[3 * n + 1] + rz * f0 - rx * f2);
+    s[7] = s[7] + (M.AR[3 * n + 2] + rx * f1 - ry * f0);
+  }
+  M.STIFN[m] = M.STIFN[m] + s[0];
+  M.STIFR[m] = M.STIFR[m] + s[1];
+  for (int k = 0; k < 3; k++) {
+    M.A[3 * m + k] = M.A[3 * m + k] + s[2 + k];
+    M.AR[3 * m + k] = M.AR[3 * m + k] + s[5 + k];
+  }
+  double *R = B.R, *vr = &M.VR[3 * m], *am = &M.AR[3 * m];
+  const double wa[3] = {am[0], am[1], am[2]};
+  double vi[3];
+  for (int k = 0; k < 3; k++) vi[k] = R[3 * k] * vr[0] + R[3 * k + 1] * vr[1] + R[3 * k + 2] * vr[2];
+  rotbmr(vi, R, M.dt1);
+  double ap[3];
+  for (int k = 0; k < 3; k++) ap[k] = R[3 * k] * wa[0] + R[3 * k + 1] * wa[1] + R[3 * k + 2] * wa[2];
+  ap[0] = ap[0] + (B.I[1] - B.I[2]) * vi[1] * vi[2];
+  ap[1] = ap[1] + (B.I[2] - B.I[0]) * vi[2] * vi[0];
+  ap[2] = ap[2] + (B.I[0] - B.I[1]) * vi[0] * vi[1];
+  double w[3];
+  for (int k = 0; k < 3; k++) w[k] = ap[k] * M.IN[m] / B.I[k];
+  for (int k = 0; k < 3; k++) am[k] = R[k] * w[0] + R[3 + k] * w[1] + R[6 + k] * w[2];
+  for (int n : B.nodes) {
+    M.STIFN[n] = RG_EM20;
+    M.STIFR[n] = RG_EM20;
+  }
+}
+
+// RBYVIT / RGBODV (rbyvit.F, rgbodv.F), more than two secondary nodes: every
+// secondary node gets the accelerations that make VELOCITY give it the rigid
+// motion of the main node, V(M) + A(M)*DT12 + W x r + DT2/2 W x (W x r) and
+// W, with W = VR(M) + AR(M)*DT12.  Returns 1 when DT2*|VR(M)| > 1.
+int rgbodv(Model &M, const Model::Body &B) {
+  const int m = B.main;
+  const double *vrm = &M.VR[3 * m];
+  int err = 0;
+  if (M.dt2 * M.dt2 * (vrm[0] * vrm[0] + vrm[1] * vrm[1] + vrm[2] * vrm[2]) > RG_ONE) err = 1;
+  const double vg0 = vrm[0] + M.AR[3 * m] * M.dt12;
+  const double vg1 = vrm[1] + M.AR[3 * m + 1] * M.dt12;
+  const double vg2 = vrm[2] + M.AR[3 * m + 2] * M.dt12;
+  const double usdt = RG_ONE / M.dt12;
+  const double am0 = M.A[3 * m], am1 = M.A[3 * m + 1], am2 = M.A[3 * m + 2];
+  const double *vm = &M.V[3 * m];
+  const double xm = M.X[3 * m], ym = M.X[3 * m + 1], zm = M.X[3 * m + 2];
+  const double h = RG_HALF * M.dt2;
+  for (int n : B.nodes) {
+    M.AR[3 * n] = (vg0 - M.VR[3 * n]) * usdt;
+    M.AR[3 * n + 1] = (vg1 - M.VR[3 * n + 1]) * usdt;
+    M.AR[3 * n + 2] = (vg2 - M.VR[3 * n + 2]) * usdt;
+    const double rx = M.X[3 * n] - xm, ry = M.X[3 * n + 1] - ym, rz = M.X[3 * n + 2] - zm;
+    const double vx1 = vg1 * rz - vg2 * ry;
+    const double vx2 = vg2 * rx - vg0 * rz;
+    const double vx3 = vg0 * ry - vg1 * rx;
+    M.A[3 * n] = am0 + (vm[0] + vx1 + h * (vg1 * vx3 - vg2 * vx2) - M.V[3 * n]) * usdt;
+    M.A[3 * n + 1] = am1 + (vm[1] + vx2 + h * (vg2 * vx1 - vg0 * vx3) - M.V[3 * n + 1]) * usdt;
+    M.A[3 * n + 2] = am2 + (vm[2] + vx3 + h * (vg0 * vx2 - vg1 * vx1) - M.V[3 * n + 2]) * usdt;
+  }
+  return err;
+}
+
+}  // namespace
+
+extern "C" {
+
 // One explicit cycle in RESOL order (engine/source/engine/resol.F).
 int or_cycle(void *m, int ncycle) {
   auto *w = (OrModelWrap *)m;
   Model &M = w->m;
   if (!M.finalized) return -1;
   const int numnod = M.numnod;
-  const bool rot = rg_oracle_shell::numelc(w->sh) > 0;
+  const bool shells = rg_oracle_shell::numelc(w->sh) > 0;
+  const bool rot = shells || !M.bodies.empty();
   for (int c = 0; c < ncycle; c++) {
     // resol.F:2721-2722, 2826: DT1 = DT2, DT2 = 1e6, DT2T = DT2
     M.dt1 = M.dt2;
     M.dt2 = RG_EP06;
     double dt2t = M.dt2;
     int neltst = 0;
+    // FORCE (loads/general/force.F90, PARITH/ON branch): a concentrated
+    // load adds FCY * F(TT * FCX) to its node; the external work of the
+    // cycle is 1/2 (F(TT - DT1) + F(TT)) * V, times the new DT2 once the
+    // time step is known (resol.F:6508).  Here the load enters the node's
+    // sum ahead of the element slots.
+    double wfexc = RG_ZERO;
+    for (auto &L : M.loads) {
+      const double a0 = L.fcy * finter(L.x, L.y, (M.tt - M.dt1) * L.fcx);
+      const double aa = L.fcy * finter(L.x, L.y, M.tt * L.fcx);
+      double *acc = L.dir < 3 ? &M.A[3 * L.node + L.dir] : &M.AR[3 * L.node + L.dir - 3];
+      const double vel = L.dir < 3 ? M.V[3 * L.node + L.dir] : M.VR[3 * L.node + L.dir - 3];
+      *acc = *acc + aa;
+      wfexc = wfexc + RG_HALF * (a0 + aa) * vel;
+    }
     // FORINT: element groups (OpenMP over groups, forint.F:339).  Each
     // group reports the minimum of DTFAC1*DTX and the last element (group
     // order) attaining it; ties across groups resolve to the larger global
@@ -1084,7 +1262,7 @@ int or_cycle(void *m, int ncycle) {
         eidx = gel[g];
       }
     if (eidx >= 0) neltst = M.ixs[11 * eidx + 10];
-    if (rot) {
+    if (shells) {
       int err = 0;
       double d = dt2t;
       int el = neltst;
@@ -1129,6 +1307,8 @@ int or_cycle(void *m, int ncycle) {
       M.FRLAST[3 * n + 1] = r1;
       M.FRLAST[3 * n + 2] = r2;
     }
+    // RBYFOR (resol.F:5714), before the nodal time step
+    for (auto &B : M.bodies) rbyfor(M, B);
     // DTNODA (time_step/dtnoda.F:213-345, 443-470), NODADT > 0: nodal time
     // step DTFAC1(11)*SQRT(2*MS/STIFN) over the nodes with mass, then the
     // rotational one DTFAC1(11)*SQRT(2*IN/STIFR); a node with non-positive
@@ -1170,6 +1350,7 @@ int or_cycle(void *m, int ncycle) {
     M.dt2 = std::min(std::min(M.dt2, RG_SP_1P1 * M.dt2old), M.dtmx);
     M.dt2old = M.dt2;
     M.dt12 = RG_HALF * (M.dt1 + M.dt2);
+    M.wfext = M.wfext + wfexc * M.dt2;
     // ACCELE (accele.F:66-78)
 #pragma omp parallel for schedule(static) num_threads(M.nthreads)
     for (int n = 0; n < numnod; n++) {
@@ -1276,12 +1457,32 @@ int or_cycle(void *m, int ncycle) {
         }
       }
     }
+    // RBYVIT (resol.F:7849), after the boundary conditions
+    for (auto &B : M.bodies)
+      if (rgbodv(M, B)) M.error |= 64;
     // ECRIT (output/ecrit.F:193, 266-330): energies of the printout with the
-    // velocities brought to the current time, V + DT1/2 * A.
+    // velocities brought to the current time, V + DT1/2 * A.  RBYCOR /
+    // RGBCOR (rbycor.F, rgbcor.F:213-380) take the secondary nodes of rigid
+    // bodies out of the sums and count a body's rotation with its principal
+    // inertia: 1/2 sum_k I_k (R W)_k^2, W = VR(M) + DT1/2 AR(M).
     if (M.record) {
       const double dt05 = RG_HALF * M.dt1;
       double ek = 0, ekr = 0, xm = 0, ym = 0, zm = 0, mass = 0;
+      for (const auto &B : M.bodies) {
+        const int n = B.main;
+        const double *R = B.R;
+        const double wx = M.VR[3 * n] + dt05 * M.AR[3 * n];
+        const double wy = M.VR[3 * n + 1] + dt05 * M.AR[3 * n + 1];
+        const double wz = M.VR[3 * n + 2] + dt05 * M.AR[3 * n + 2];
+        for (int k = 0; k < 3; k++) {
+          const double vi = R[3 * k] * wx + R[3 * k + 1] * wy + R[3 * k + 2] * wz;
+          ekr = ekr + RG_HALF * B.I[k] * vi * vi;
+        }
+      }
       for (int n = 0; n < numnod; n++) {
+        // role: 0 free node, 1 rigid-body secondary, 2 rigid-body main
+        const int role = M.secondary.empty() ? 0 : M.secondary[n];
+        if (role == 1) continue;
         const double vx = M.V[3 * n] + dt05 * M.A[3 * n];
         const double vy = M.V[3 * n + 1] + dt05 * M.A[3 * n + 1];
         const double vz = M.V[3 * n + 2] + dt05 * M.A[3 * n + 2];
@@ -1290,7 +1491,7 @@ int or_cycle(void *m, int ncycle) {
         ym = ym + vy * M.MS[n];
         zm = zm + vz * M.MS[n];
         mass = mass + M.MS[n];
-        if (rot) {
+        if (rot && role == 0) {
           const double rx = M.VR[3 * n] + dt05 * M.AR[3 * n];
           const double ry = M.VR[3 * n + 1] + dt05 * M.AR[3 * n + 1];
           const double rz = M.VR[3 * n + 2] + dt05 * M.AR[3 * n + 2];
@@ -1314,6 +1515,7 @@ int or_cycle(void *m, int ncycle) {
       M.out[7] = ym;
       M.out[8] = zm;
       M.out[9] = mass;
+      M.out[10] = M.wfext;
     }
     // VELOCITY (velocity.F:59-75), DEPLA (displacement.F:68-100)
 #pragma omp parallel for schedule(static) num_threads(M.nthreads)
@@ -1444,6 +1646,49 @@ int or_rlink_add(void *m, int nsn, const int *nodes, int ic, int icr) {
   return (int)M.links.size() - 1;
 }
 
+int or_rbody_add(void *m, int main, int nsn, const int *nodes, const double *axes,
+                 const double *inertia) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (M.finalized || nsn <= 2 || !nodes || !axes || !inertia || main < 1 || main > M.numnod)
+    return -1;
+  if (M.secondary.empty()) M.secondary.assign(M.numnod, 0);
+  Model::Body B;
+  B.main = main - 1;
+  if (M.secondary[B.main]) return -2;
+  for (int i = 0; i < nsn; i++) {
+    const int n = nodes[i] - 1;
+    if (n < 0 || n >= M.numnod || n == B.main || M.secondary[n]) return -2;
+    B.nodes.push_back(n);
+  }
+  for (int k = 0; k < 9; k++) B.R[k] = axes[k];
+  for (int k = 0; k < 3; k++) {
+    if (!(inertia[k] > RG_ZERO)) return -1;
+    B.I[k] = inertia[k];
+  }
+  if (!(M.IN[B.main] > RG_ZERO) || !(M.MS[B.main] > RG_ZERO)) return -3;
+  for (int n : B.nodes) M.secondary[n] = 1;
+  M.secondary[B.main] = 2;
+  M.bodies.push_back(B);
+  return (int)M.bodies.size() - 1;
+}
+
+int or_cload_add(void *m, int node, int dir, double fcx, double fcy, int npts,
+                 const double *x, const double *y) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (node < 1 || node > M.numnod || dir < 0 || dir > 5 || npts < 1 || !x || !y) return -1;
+  for (int i = 1; i < npts; i++)
+    if (!(x[i] > x[i - 1])) return -1;
+  Model::Load L;
+  L.node = node - 1;
+  L.dir = dir;
+  L.fcx = fcx;
+  L.fcy = fcy;
+  L.x.assign(x, x + npts);
+  L.y.assign(y, y + npts);
+  M.loads.push_back(L);
+  return (int)M.loads.size() - 1;
+}
+
 int or_rlink_clear(void *m) {
   ((OrModelWrap *)m)->m.links.clear();
   return 0;
@@ -1456,7 +1701,7 @@ int or_set_record(void *m, int on) {
 
 int or_get_record(void *m, double *out, int *neltst) {
   Model &M = ((OrModelWrap *)m)->m;
-  if (out) std::copy(M.out, M.out + 10, out);
+  if (out) std::copy(M.out, M.out + 11, out);
   if (neltst) *neltst = M.neltst;
   return 0;
 }

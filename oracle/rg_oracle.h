@@ -13,9 +13,13 @@
  * reference engine itself: its QA deck CRA2V44 (768 shells, 3375 cycles over
  * a run and a restart), whose printed cycle table the oracle reproduces to
  * every printed digit and whose time histories to ~1e-6 relative
- * (tests/test_oracle_cra2.py).  The hexa path is pinned by analytic
- * known-answer tests (rigid-body motion, constant-strain patch test, elastic
- * wave speed, energy conservation, Johnson-Cook uniaxial yield).
+ * (tests/test_oracle_cra2.py).  The hexa path (LAW1, co-rotational frame,
+ * viscous hourglass) is pinned the same way by the QA deck H101 (six
+ * cantilevers with rigid-body tips under concentrated loads, 847 cycles:
+ * printed table to every digit, energies and tip motions to ~1e-7,
+ * tests/test_oracle_h101.py), and by analytic known-answer tests
+ * (rigid-body motion, constant-strain patch test, elastic wave speed,
+ * energy conservation, Johnson-Cook uniaxial yield).
  *
  * Conventions follow the reference: nodal arrays are X(3,NUMNOD) (xyz
  * interleaved), IXS(11,NUMELS) columns hold {mat, n1..n8 (1-based), prop,
@@ -93,9 +97,24 @@ int or_shell_frame(void *m, int ishfram);
  * links (a restart whose engine deck has no /VEL card). */
 int or_rlink_add(void *m, int nsn, const int *nodes, int ic, int icr);
 int or_rlink_clear(void *m);
-/* Listing record of the last cycle (what ECRIT prints): out[0..9] = TT, DT2,
- * internal energy, kinetic energy and rotational kinetic energy of
- * V + DT1/2 A, hourglass energy, x/y/z momentum, mass.  Off by default. */
+/* Rigid body (/RBODY; RBYFOR, RBYVIT, RBYCOR): main node and nsn > 2
+ * secondary nodes (1-based); the caller has done the starter's INIRBY: the
+ * main node sits at the centre of mass with MS = body mass and IN = the
+ * smallest principal inertia; axes = principal directions as rows (RBY(1:9),
+ * right-handed), inertia = principal inertia (RBY(10:12)).  Before
+ * or_finalize; or_set_inertia must come first.  Error bit 64: a body turns
+ * more than one radian in a step. */
+int or_rbody_add(void *m, int main, int nsn, const int *nodes,
+                 const double *axes, const double *inertia);
+/* Concentrated load (/CLOAD; FORCE): node 1-based, dir 0..2 force x/y/z,
+ * 3..5 moment; the load curve (npts increasing abscissae, FINTER) is read at
+ * TT * fcx and scaled by fcy.  Its external work enters the listing record. */
+int or_cload_add(void *m, int node, int dir, double fcx, double fcy, int npts,
+                 const double *x, const double *y);
+/* Listing record of the last cycle (what ECRIT prints): out[0..10] = TT,
+ * DT2, internal energy, kinetic energy and rotational kinetic energy of
+ * V + DT1/2 A, hourglass energy, x/y/z momentum, mass, external work of the
+ * concentrated loads.  Off by default. */
 int or_set_record(void *m, int on);
 int or_get_record(void *m, double *out, int *neltst);
 /* Shell state: which = 0 FOR (5 x nc), 1 MOM (3 x nc), 2 THK, 3 EINT
