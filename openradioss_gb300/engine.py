@@ -35,7 +35,16 @@ class RgError(RuntimeError):
 class Engine:
     """One model resident on one GPU (an rg_ctx)."""
 
-    def __init__(self, model, device=0, precision=RG_PREC_FP64, skyline=None):
+    def __init__(self, model, device=0, precision=RG_PREC_FP64, skyline=None,
+                 elements_only=False):
+        """elements_only: the model's rigid bodies and concentrated loads
+        (model.rbodies, model.cloads), which the CUDA path does not run, are
+        left to the caller's own nodal update, and only the FORINT-level
+        call (forint_step) is open; without it such a model is refused."""
+        if (getattr(model, "rbodies", None) or getattr(model, "cloads", None)) and not elements_only:
+            raise RgError("rigid bodies and concentrated loads are not on the CUDA path: "
+                          "use elements_only=True with forint_step")
+        self.elements_only = elements_only
         self.L = _lib.lib()
         self.model = model
         self.precision = precision
@@ -109,6 +118,8 @@ class Engine:
 
     # ---- stepping --------------------------------------------------------
     def cycle(self, n=1, sync=True):
+        if self.elements_only:
+            raise RgError("an elements_only engine runs forint_step only")
         self._chk(self.L.rg_cycle(self.h, int(n)), "rg_cycle")
         if sync:
             self.sync()

@@ -4,7 +4,8 @@ Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` use this module, and only as a checker / reported baseline;
 the product never imports it.  See rg_oracle.cpp for what it restates and
 its parity status (shell path pinned against the reference engine's own
-outputs for its QA deck CRA2V44; hexa path by analytic known-answer tests).
+outputs for its QA deck CRA2V44, hexa path for its QA deck H101; both also
+by analytic known-answer tests).
 """
 from __future__ import annotations
 
@@ -23,9 +24,10 @@ _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
 def build(force=False):
-    """Compile the oracle with its Makefile (g++, -ffp-contract=off)."""
-    if force or not os.path.exists(_LIB):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle with its Makefile (g++, -ffp-contract=off); make
+    rebuilds it whenever a source is newer than the library, and a failed
+    compile raises instead of leaving an older library in use."""
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB
 
 
@@ -60,6 +62,7 @@ def lib():
         L.or_set_nodal_dt.argtypes = [vp, C.c_double, C.c_double]
         L.or_get_record.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.or_rbody_add.argtypes = [vp, C.c_int, C.c_int, _ip, _dp, _dp]
+        L.or_set_forces.argtypes = [vp] + [C.c_void_p] * 4 + [C.c_double, C.c_int]
         L.or_cload_add.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                    _dp, _dp]
         _lib = L
@@ -180,6 +183,16 @@ class OracleModel:
 
     def error(self):
         return lib().or_error(self.h)
+
+    def set_forces(self, f, stifn, dt2t, neltst, fr=None, stifr=None):
+        """Assembled element forces for the next cycle(1) (F and FR as (N, 3)
+        or (3*N,) arrays in node-major order, STIFN, STIFR (N,)), with the
+        element time step: the cycle skips its own element groups."""
+        c = lambda a: None if a is None else np.ascontiguousarray(a, np.float64).reshape(-1)
+        f, stifn, fr, stifr = c(f), c(stifn), c(fr), c(stifr)
+        if lib().or_set_forces(self.h, _ptr(f), _ptr(stifn), _ptr(fr), _ptr(stifr), float(dt2t),
+                               int(neltst)) != 0:
+            raise RuntimeError("or_set_forces failed")
 
     def clear_links(self):
         lib().or_rlink_clear(self.h)

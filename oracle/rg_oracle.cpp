@@ -109,6 +109,13 @@ struct Model {
   std::vector<Load> loads;
   double wfext = 0;  // external work of the loads (OUTPUT%TH%WFEXT)
 
+  // forces supplied from outside for the next cycle (or_set_forces): the
+  // cycle then skips its element groups and assembly
+  bool ext = false;
+  std::vector<double> ext_f, ext_fr, ext_stifn, ext_stifr;
+  double ext_dt2t = 0;
+  int ext_neltst = 0;
+
   // listing quantities of the last cycle, taken where ECRIT runs (after the
   // kinematic conditions, before VELOCITY)
   bool record = false;
@@ -1244,7 +1251,7 @@ int or_cycle(void *m, int ncycle) {
     // group reports the minimum of DTFAC1*DTX and the last element (group
     // order) attaining it; ties across groups resolve to the larger global
     // element index, i.e. the sequential-order result of MQVISCB.
-    const int ng = (int)M.hg.size();
+    const int ng = M.ext ? 0 : (int)M.hg.size();
     std::vector<double> gdt(ng, RG_EP06);
     std::vector<int> gel(ng, -1);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(M.nthreads)
@@ -1262,7 +1269,11 @@ int or_cycle(void *m, int ncycle) {
         eidx = gel[g];
       }
     if (eidx >= 0) neltst = M.ixs[11 * eidx + 10];
-    if (shells) {
+    if (M.ext && M.ext_dt2t < dt2t) {
+      dt2t = M.ext_dt2t;
+      neltst = M.ext_neltst;
+    }
+    if (shells && !M.ext) {
       int err = 0;
       double d = dt2t;
       int el = neltst;
@@ -1281,7 +1292,19 @@ int or_cycle(void *m, int ncycle) {
       double a0 = M.A[3 * n], a1 = M.A[3 * n + 1], a2 = M.A[3 * n + 2];
       double r0 = M.AR[3 * n], r1 = M.AR[3 * n + 1], r2 = M.AR[3 * n + 2];
       double st = RG_ZERO, sr = RG_ZERO;
-      for (int k = M.adsky[n] - 1; k < M.adsky[n + 1] - 1; k++) {
+      if (M.ext) {
+        a0 = a0 + M.ext_f[3 * n];
+        a1 = a1 + M.ext_f[3 * n + 1];
+        a2 = a2 + M.ext_f[3 * n + 2];
+        st = M.ext_stifn[n];
+        if (!M.ext_fr.empty()) {
+          r0 = r0 + M.ext_fr[3 * n];
+          r1 = r1 + M.ext_fr[3 * n + 1];
+          r2 = r2 + M.ext_fr[3 * n + 2];
+        }
+        if (!M.ext_stifr.empty()) sr = M.ext_stifr[n];
+      }
+      for (int k = M.adsky[n] - 1; k < (M.ext ? M.adsky[n] - 1 : M.adsky[n + 1] - 1); k++) {
         const double *fs = &M.fsky[8 * k];
         a0 = a0 + fs[0];
         a1 = a1 + fs[1];
@@ -1538,6 +1561,7 @@ int or_cycle(void *m, int ncycle) {
     // resol.F:8603-8611 (double accumulation), NCYCLE + 1
     M.tt = M.tt + M.dt2;
     M.ncycle++;
+    M.ext = false;
   }
   return M.error;
 }
@@ -1687,6 +1711,21 @@ int or_cload_add(void *m, int node, int dir, double fcx, double fcy, int npts,
   L.y.assign(y, y + npts);
   M.loads.push_back(L);
   return (int)M.loads.size() - 1;
+}
+
+int or_set_forces(void *m, const double *f, const double *stifn, const double *fr,
+                  const double *stifr, double dt2t, int neltst) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (!M.finalized || !f || !stifn) return -1;
+  const size_t n3 = 3 * (size_t)M.numnod;
+  M.ext_f.assign(f, f + n3);
+  M.ext_stifn.assign(stifn, stifn + M.numnod);
+  if (fr) M.ext_fr.assign(fr, fr + n3); else M.ext_fr.clear();
+  if (stifr) M.ext_stifr.assign(stifr, stifr + M.numnod); else M.ext_stifr.clear();
+  M.ext_dt2t = dt2t;
+  M.ext_neltst = neltst;
+  M.ext = true;
+  return 0;
 }
 
 int or_rlink_clear(void *m) {

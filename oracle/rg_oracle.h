@@ -111,6 +111,14 @@ int or_rbody_add(void *m, int main, int nsn, const int *nodes,
  * TT * fcx and scaled by fcy.  Its external work enters the listing record. */
 int or_cload_add(void *m, int node, int dir, double fcx, double fcy, int npts,
                  const double *x, const double *y);
+/* Element forces from outside for the next cycle (a FORINT done elsewhere,
+ * e.g. by the CUDA path's rg_forint_step): F(3,NUMNOD) and STIFN (FR,
+ * STIFR may be NULL) are the assembled element forces, dt2t / neltst the
+ * element time step and its element.  The next or_cycle(m, 1) skips its own
+ * element groups and slot sums and runs the rest of RESOL (loads, rigid
+ * bodies, ACCELE, conditions, listing, VELOCITY, DEPLA) on these. */
+int or_set_forces(void *m, const double *f, const double *stifn, const double *fr,
+                  const double *stifr, double dt2t, int neltst);
 /* Listing record of the last cycle (what ECRIT prints): out[0..10] = TT,
  * DT2, internal energy, kinetic energy and rotational kinetic energy of
  * V + DT1/2 A, hourglass energy, x/y/z momentum, mass, external work of the

@@ -240,7 +240,7 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     }
   }
   // ---- CDERI3 (cderi3.F:30), ISMSTR = 4 ----
-  double x2, y2, x3, y3, x4, y4, z2, px1, px2, py1, py2, area, vhx, vhy;
+  double x2, y2, x3, y3, x4, y4, px1, px2, py1, py2, area, vhx, vhy;
   {
     const double x21 = xg[1] - xg[0], y21 = yg[1] - yg[0], z21 = zg[1] - zg[0];
     const double x31 = xg[2] - xg[0], y31 = yg[2] - yg[0], z31 = zg[2] - zg[0];
@@ -251,7 +251,6 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     x3 = e1x * x31 + e1y * y31 + e1z * z31;
     x4 = e1x * x41 + e1y * y41 + e1z * z41;
     y4 = e2x * x41 + e2y * y41 + e2z * z41;
-    z2 = e3x * x21 + e3y * y21 + e3z * z21;
     px1 = RG_HALF * (y2 - y4);
     py1 = RG_HALF * (x4 - x2);
     px2 = RG_HALF * y3;
@@ -309,7 +308,6 @@ static void element(Shells *S, const Group &G, int e, const double *X,
     const double vz13 = vz[0] - vz[2], vz24 = vz[1] - vz[3];
     eyz = py1 * vz13 + py2 * vz24;
     exz = px1 * vz13 + px2 * vz24;
-    z2 = RG_ZERO;
     const double dt1v4 = RG_FOURTH * DT1;
     const double tmp2a = py2 + py1;
     const double tmp3a = std::copysign(dmax(std::fabs(tmp2a), RG_EM20), tmp2a);

@@ -110,3 +110,38 @@ def test_planted_change_breaks_match(deck, change):
         check_printed(deck, m, recs)
     with pytest.raises(AssertionError):
         check_time_history(deck, recs, nodes)
+
+
+def test_external_forces_hook(deck):
+    """or_set_forces (the hook the CUDA path's FORINT-level call feeds, see
+    tests/test_gpu_h101.py): a second oracle that takes the first one's
+    assembled element forces and element step every cycle instead of
+    computing its own follows it bit for bit through the rigid bodies and
+    loads."""
+    from oracle.oracle import OracleModel
+
+    a = OracleModel(M.hexa_model_from_deck(deck, "h101"), nthreads=1)
+    m = M.hexa_model_from_deck(deck, "h101")
+    b = OracleModel(m, nthreads=1)
+    loaded = np.array([c[0] for c in m.cloads]) - 1
+    for _ in range(200):
+        a.cycle(1)
+        nd, t = a.nodes(), a.time()
+        f = nd["F"].T.copy()
+        f[loaded] = 0.0          # F holds the loads; b adds its own
+        b.set_forces(f, nd["STIFN"], t["dt2"], t["neltst"])
+        b.cycle(1)
+    na, nb = a.nodes(), b.nodes()
+    assert np.array_equal(na["X"], nb["X"]) and np.array_equal(na["V"], nb["V"])
+    assert np.array_equal(na["VR"], nb["VR"])
+    assert a.time()["tt"] == b.time()["tt"]
+
+
+def test_cuda_engine_refuses_rigid_bodies(deck):
+    """The CUDA path does not run rigid bodies or concentrated loads: an
+    Engine for such a model is refused unless it is opened for the
+    FORINT-level call only (the caller runs the nodal update)."""
+    from openradioss_gb300.engine import Engine, RgError
+
+    with pytest.raises(RgError):
+        Engine(M.hexa_model_from_deck(deck, "h101"))
