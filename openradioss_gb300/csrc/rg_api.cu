@@ -1003,8 +1003,17 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
                             c->nparts, alloc_fn, why)))
       return fail(c, r, "shell set-up: " + why);
   }
-  if ((r = dalloc(c, &c->dp.dt, std::max(c->nparts, 1)))) return r;
-  if ((r = dalloc(c, &c->dp.el, std::max(c->nparts, 1)))) return r;
+  // the partial arrays also hold one slot per 128-element tile of every
+  // group: the batched kernel writes a job's partials in that layout, which
+  // has more slots than a balanced FP64 shell launch
+  {
+    int tiles = 0;
+    for (auto &g : c->hg) tiles += hexa_blocks(g.nel);
+    tiles += shell_tile_count(c->shells);
+    c->nparts_cap = std::max(c->nparts, tiles);
+  }
+  if ((r = dalloc(c, &c->dp.dt, std::max(c->nparts_cap, 1)))) return r;
+  if ((r = dalloc(c, &c->dp.el, std::max(c->nparts_cap, 1)))) return r;
   // time scalars
   Time t{};
   t.tt = 0;

@@ -431,7 +431,7 @@ int rebuild(rg_batch *b) {
       for (int t = 0; t < ntl_g; t++) tiles.push_back({BK_SHELL + P->npt - 1, gi, t, part + t});
       part += ntl_g;
     }
-    if (part > c->nparts) return bfail(b, RG_E_STATE, "batch: dt partial count exceeds the job's");
+    if (part > c->nparts_cap) return bfail(b, RG_E_STATE, "batch: dt partial count exceeds the job's");
     J.nparts = part;
     jobs.push_back(J);
     for (int n0 = 0; n0 < c->numnod; n0 += nt) ntl.push_back({j, n0});

@@ -74,7 +74,8 @@ struct rg_ctx {
   Time *d_time = nullptr;
   int *d_status = nullptr;
   DtPartials dp{};
-  int nparts = 0;
+  int nparts = 0;       // dt partials written by a cycle's element launches
+  int nparts_cap = 0;   // slots allocated (also the batched kernel's tiles)
   unsigned *d_dtctr = nullptr;  // fused dt: [1 + groups] completion counters
   double *d_gdt = nullptr;      // fused dt: group minima
   int *d_gel = nullptr;

@@ -36,22 +36,11 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              Time *__restrict__ T, int key0, int nc_total, int *__restrict__ status,
              const DtFinish F) {
   typedef ER R;
+  const int il = blockIdx.x * NT + threadIdx.x;
   R dtmine = (R)RG_EP06;
   int elmin = -1;
-  // warp tasks of 32 consecutive elements: with wtasks = 0 each warp does
-  // the one task of its own 32 threads (element = block * NT + thread);
-  // otherwise block b takes tasks [b W / nblk, (b+1) W / nblk), so that every
-  // SM of a one-wave launch gets the same work
-  int t0 = blockIdx.x * (NT / 32), t1 = t0 + NT / 32;
-  if (P.wtasks) {
-    t0 = (int)(((long long)blockIdx.x * P.wtasks) / gridDim.x);
-    t1 = (int)(((long long)(blockIdx.x + 1) * P.wtasks) / gridDim.x);
-  }
-  for (int t = t0 + (int)(threadIdx.x >> 5); t < t1; t += NT / 32) {
-    const int il = t * 32 + (int)(threadIdx.x & 31);
-    if (il < P.nel)
-      shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin);
-  }
+  if (il < P.nel)
+    shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin);
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
   if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
 }
@@ -91,7 +80,7 @@ static void launch_shell(const ShellParams &P, const ShellArrays<ER> &A, const N
                          void *fsky, void *fskyr, DtPartials dp, Time *T, int key0,
                          int nct, int *status, const DtFinish &F, cudaStream_t s) {
   typedef typename SlotT<ER>::type ST;
-  const int nb = P.nblk;
+  const int nb = shell_blocks(P.nel);
   ST *f = (ST *)fsky, *fr = (ST *)fskyr;
   switch (P.npt) {
     case 1: shell_kernel<ER, 1, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
@@ -251,41 +240,10 @@ static int init_arrays(ShellModelHost &S, ShellArrays<ER> &A) {
   return 0;
 }
 
-// resident blocks per SM of the shell kernel for NPT points
-template <typename ER>
-static int shell_resident(int npt) {
-  int r = 0;
-  cudaError_t e;
-  switch (npt) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 1, SHELL_NT>, SHELL_NT, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 2, SHELL_NT>, SHELL_NT, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 3, SHELL_NT>, SHELL_NT, 0); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 4, SHELL_NT>, SHELL_NT, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 5, SHELL_NT>, SHELL_NT, 0); break;
-  }
-  return e == cudaSuccess && r > 0 ? r : 1;
-}
-
-// Launch layout of a group.  The FP64 kernel is bound by the FP64 pipe,
-// whose time per SM is the work placed on it: when a group needs more than
-// one wave of resident blocks, one wave of blocks shares its warp tasks
-// evenly (one element per thread would leave some SMs a block more than
-// others).  The mixed kernel is bound by memory latency, which the extra
-// warps of one element per thread hide better.
-static void shell_layout(ShellParams &P, int prec) {
-  P.nblk = shell_blocks(P.nel);
-  P.wtasks = 0;
-  if (prec != RG_PREC_FP64) return;
-  int dev = 0, nsm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
-    return;
-  const int wave = nsm * shell_resident<double>(P.npt);
-  const int w = (P.nel + 31) / 32;
-  if (w > wave * (SHELL_NT / 32)) {
-    P.nblk = wave;
-    P.wtasks = w;
-  }
+int shell_tile_count(const ShellModelHost &S) {
+  int n = 0;
+  for (auto *g : S.groups) n += shell_blocks(g->P.nel);
+  return n;
 }
 
 int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc, int key0,
@@ -335,8 +293,7 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
     g->P.ishfram = S.ishfram;
     g->P.nodadt = S.nodadt;
     shell_params_mirror(g->P);
-    shell_layout(g->P, prec);
-    part_off += g->P.nblk;
+    part_off += shell_blocks(g->P.nel);
   }
   return RG_OK;
 }

@@ -52,6 +52,8 @@ void shell_free(ShellModelHost &S);
 struct ShellParams;
 const void *shell_device_arrays(const ShellModelHost &S, int prec);
 int shell_group_count(const ShellModelHost &S);
+// 128-element tiles over all shell groups (one dt partial each)
+int shell_tile_count(const ShellModelHost &S);
 const ShellParams *shell_group_params(const ShellModelHost &S, int g);
 
 }  // namespace rg

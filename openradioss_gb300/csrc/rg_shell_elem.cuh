@@ -35,9 +35,6 @@ namespace rg {
 struct ShellParams {
   int nft, nel, npt, ipla;
   int part_off;
-  // launch layout: nblk blocks; wtasks = 0: one element per thread, else the
-  // group's wtasks 32-element warp tasks spread evenly over the blocks
-  int nblk, wtasks;
   int ishfram;  // local frame: 0 symmetric (default), 2 version-4 (/SHFRA/V4)
   double rho, young, nu, g, a11, ssp;
   double h1, h2, h3, srh1, srh2, srh3, dm, ish, fsh;
