@@ -36,11 +36,31 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              Time *__restrict__ T, int key0, int nc_total, int *__restrict__ status,
              const DtFinish F) {
   typedef ER R;
-  const int il = blockIdx.x * NT + threadIdx.x;
   R dtmine = (R)RG_EP06;
   int elmin = -1;
-  if (il < P.nel)
-    shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin);
+  // warp tasks of 32 consecutive elements.  wtasks = 0: each warp does the
+  // one task of its own threads (element = block * NT + thread).  Otherwise
+  // (FP64 groups of more than one wave) warps take tasks from a counter
+  // until none is left: the FP64 kernel is bound by the FP64 pipe, and
+  // dynamic tasks keep every SM's share equal even when plastic elements
+  // cost more.  Results do not depend on which warp takes which task.
+  const int lane = threadIdx.x & 31;
+  int t = blockIdx.x * (NT / 32) + (int)(threadIdx.x >> 5);
+  bool first = true;
+  for (;;) {
+    if (P.wtasks) {
+      int g = 0;
+      if (lane == 0) g = (int)atomicAdd(P.qctr, 1u);
+      t = __shfl_sync(0xffffffffu, g, 0);
+      if (t >= P.wtasks) break;
+    } else {
+      if (!first) break;
+      first = false;
+    }
+    const int il = t * 32 + lane;
+    if (il < P.nel)
+      shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin);
+  }
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
   if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
 }
@@ -80,7 +100,8 @@ static void launch_shell(const ShellParams &P, const ShellArrays<ER> &A, const N
                          void *fsky, void *fskyr, DtPartials dp, Time *T, int key0,
                          int nct, int *status, const DtFinish &F, cudaStream_t s) {
   typedef typename SlotT<ER>::type ST;
-  const int nb = shell_blocks(P.nel);
+  const int nb = P.nblk;
+  if (P.wtasks) cudaMemsetAsync(P.qctr, 0, sizeof(unsigned), s);
   ST *f = (ST *)fsky, *fr = (ST *)fskyr;
   switch (P.npt) {
     case 1: shell_kernel<ER, 1, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
@@ -246,6 +267,21 @@ int shell_tile_count(const ShellModelHost &S) {
   return n;
 }
 
+// resident blocks per SM of the shell kernel for NPT points
+template <typename ER>
+static int shell_resident(int npt) {
+  int r = 0;
+  cudaError_t e;
+  switch (npt) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 1, SHELL_NT>, SHELL_NT, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 2, SHELL_NT>, SHELL_NT, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 3, SHELL_NT>, SHELL_NT, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 4, SHELL_NT>, SHELL_NT, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 5, SHELL_NT>, SHELL_NT, 0); break;
+  }
+  return e == cudaSuccess && r > 0 ? r : 1;
+}
+
 int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc, int key0,
                    double dtfac, int &part_off, const DevAlloc &alloc, std::string &why) {
   (void)X;
@@ -293,7 +329,24 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
     g->P.ishfram = S.ishfram;
     g->P.nodadt = S.nodadt;
     shell_params_mirror(g->P);
-    part_off += shell_blocks(g->P.nel);
+    // FP64 groups needing more than one wave of resident blocks: one wave
+    // taking warp tasks from a counter (the mixed kernel, latency bound,
+    // keeps one element per thread and the extra warps that hide latency)
+    g->P.nblk = shell_blocks(g->P.nel);
+    g->P.wtasks = 0;
+    if (prec == RG_PREC_FP64) {
+      int dev = 0, nsm = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      const int wave = nsm * shell_resident<double>(g->P.npt);
+      const int w = (g->P.nel + 31) / 32;
+      if (nsm > 0 && w > wave * (SHELL_NT / 32)) {
+        if ((r = alloc((void **)&g->P.qctr, sizeof(unsigned)))) return r;
+        g->P.nblk = wave;
+        g->P.wtasks = w;
+      }
+    }
+    part_off += g->P.nblk;
   }
   return RG_OK;
 }

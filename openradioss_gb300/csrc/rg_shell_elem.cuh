@@ -35,6 +35,11 @@ namespace rg {
 struct ShellParams {
   int nft, nel, npt, ipla;
   int part_off;
+  // launch layout: nblk blocks; wtasks = 0: one element per thread, else
+  // the group's wtasks 32-element warp tasks, taken by the warps of one wave
+  // of resident blocks from the counter qctr (zeroed before each launch)
+  unsigned *qctr;
+  int nblk, wtasks;
   int ishfram;  // local frame: 0 symmetric (default), 2 version-4 (/SHFRA/V4)
   double rho, young, nu, g, a11, ssp;
   double h1, h2, h3, srh1, srh2, srh3, dm, ish, fsh;
