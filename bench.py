@@ -171,6 +171,16 @@ def fp64_roofline(kkey, ne, ms, device):
             "peak_kind": "measured (rg_fp64_peak: dependent FMA chains, all SMs)"}
 
 
+# DRAM bytes of one launch of the workload's element kernel
+# (dram__bytes_read.sum + dram__bytes_write.sum), from the ncu captures whose
+# commands and figures are in profiles/shell_kernel_crash_box_120k.md and
+# profiles/hexa_kernel_block128_jc.md
+NCU_TRAFFIC = {
+    "crash_box_120k_jc": {"f64": 73.9e6 + 33.6e6, "mixed": 42.9e6 + 0.9e6},
+    "hexa_block_128_jc": {"f64": 506.7e6 + 685.1e6, "mixed": 388.4e6 + 354.4e6},
+}
+
+
 def run_ours(args, rank, world, local_rank):
     from openradioss_gb300.engine import Engine, RG_PREC_FP64, RG_PREC_MIXED
     wl = args.workload
@@ -278,13 +288,8 @@ def run_ours(args, rank, world, local_rank):
     ach = res64["elem_bytes"] * ne / (k64 * 1e-3) / 1e9
     k32 = res32["kt"][kk]
     ach32 = res32["elem_bytes"] * ne / (k32 * 1e-3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "hexa_traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get(wl)
-        except Exception:
-            traffic = None
+    traffic = NCU_TRAFFIC.get(wl, {}).get("f64")
+    traffic32 = NCU_TRAFFIC.get(wl, {}).get("mixed")
     line = {
         "metric": "element-updates/s",
         "value": value,
@@ -316,7 +321,7 @@ def run_ours(args, rank, world, local_rank):
                 "d2h_bytes_per_step": (8 if model.shells else 4) * 8 * model.numnod},
         "gpu_launches": (len(model.hexa) + len(model.shells) + 2) * args.steps,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": ach / hbm_peak, "traffic": traffic,
+                     "frac": ach / hbm_peak, "traffic": traffic, "traffic_unit": "bytes per launch (ncu)",
                      "kernel": "%s_kernel<double>" % kk,
                      "bytes_per_element": res64["elem_bytes"], "ms_per_launch": k64,
                      "peak_kind": peak_kind,
@@ -329,6 +334,7 @@ def run_ours(args, rank, world, local_rank):
                           "kernel_ms": res32["kt"],
                           "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm_peak,
                                        "unit": "GB/s", "frac": ach32 / hbm_peak,
+                                       "traffic": traffic32,
                                        "bytes_per_element": res32["elem_bytes"]}},
         "clocks": res64["clocks"],
         "device_status": [res64["status"], res32["status"]],
