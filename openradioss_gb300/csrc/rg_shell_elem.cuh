@@ -184,6 +184,27 @@ __device__ __forceinline__ T smin(T a, T b) {
   return a < b ? a : b;
 }
 
+// 1 / MAX(SQRT(S), EM20) of CNVEC3's normalisations.  FP64 form: one
+// reciprocal square root (a square root and a division each cost about ten
+// instructions of the FP64 pipe, which bounds the FP64 kernel); below
+// EM20^2 the value 1/EM20 as in the reference.  FP32 form: as written.
+template <typename R>
+__device__ __forceinline__ R inv_norm_em20(const R s) {
+  if constexpr (std::is_same<R, double>::value)
+    return s > RG_EM20 * RG_EM20 ? rsqrt(s) : RG_ONE / RG_EM20;
+  else
+    return (R)RG_ONE / smax(sqrt(s), (R)RG_EM20);
+}
+
+// SQRT(S1 / S2) (CNVEC3); FP64 form as S1 * RSQRT(S1 * S2).
+template <typename R>
+__device__ __forceinline__ R sqrt_ratio(const R s1, const R s2) {
+  if constexpr (std::is_same<R, double>::value)
+    return s1 > 0.0 ? s1 * rsqrt(s1 * s2) : sqrt(s1 / s2);
+  else
+    return sqrt(s1 / s2);
+}
+
 template <typename ER, int NPT>
 __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellArrays<ER> &S,
                                               const NodeView &N,
@@ -281,12 +302,12 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         e1y = e1y * suma + e2z * e3x - e2x * e3z;
         e1z = e1z * suma + e2x * e3y - e2y * e3x;
         suma = e1x * e1x + e1y * e1y + e1z * e1z;
-        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        suma = inv_norm_em20(suma);
         e1x = e1x * suma;
         e1y = e1y * suma;
         e1z = e1z * suma;
         suma = e3x * e3x + e3y * e3y + e3z * e3z;
-        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        suma = inv_norm_em20(suma);
         e3x = e3x * suma;
         e3y = e3y * suma;
         e3z = e3z * suma;
@@ -294,25 +315,25 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         e2y = e3z * e1x - e3x * e1z;
         e2z = e3x * e1y - e3y * e1x;
         suma = e2x * e2x + e2y * e2y + e2z * e2z;
-        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        suma = inv_norm_em20(suma);
         e2x = e2x * suma;
         e2y = e2y * suma;
         e2z = e2z * suma;
       } else {
         // symmetric convected frame (cnvec3.F:117-141)
         R suma = e3x * e3x + e3y * e3y + e3z * e3z;
-        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        suma = inv_norm_em20(suma);
         e3x = e3x * suma;
         e3y = e3y * suma;
         e3z = e3z * suma;
         const R s1 = e1x * e1x + e1y * e1y + e1z * e1z;
         const R s2 = e2x * e2x + e2y * e2y + e2z * e2z;
-        suma = sqrt(s1 / s2);
+        suma = sqrt_ratio(s1, s2);
         e1x = e1x + (e2y * e3z - e2z * e3y) * suma;
         e1y = e1y + (e2z * e3x - e2x * e3z) * suma;
         e1z = e1z + (e2x * e3y - e2y * e3x) * suma;
         suma = e1x * e1x + e1y * e1y + e1z * e1z;
-        suma = (R)RG_ONE / smax(sqrt(suma), (R)RG_EM20);
+        suma = inv_norm_em20(suma);
         e1x = e1x * suma;
         e1y = e1y * suma;
         e1z = e1z * suma;
