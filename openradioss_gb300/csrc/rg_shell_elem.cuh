@@ -414,15 +414,23 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       const R dt1v4 = (R)RG_FOURTH * dt1;
       const R tmp2a = py2 + py1;
       const R tmp3a = copysign(smax(fabs(tmp2a), (R)RG_EM20), tmp2a);
-      const R tmp1a = dt1v4 * (vz13 - vz24) * (vz13 - vz24) / tmp3a;
+      const R tmp1b = px2 - px1;
+      const R tmp3b = copysign(smax(fabs(tmp1b), (R)RG_EM20), tmp1b);
+      // FP64 form: the two divisions share one reciprocal (FP64-pipe work)
+      R tmp1a, tmp2b;
+      if constexpr (F64) {
+        const R rab = (R)RG_ONE / (tmp3a * tmp3b);
+        tmp1a = dt1v4 * (vz13 - vz24) * (vz13 - vz24) * (tmp3b * rab);
+        tmp2b = dt1v4 * (vz13 + vz24) * (vz13 + vz24) * (tmp3a * rab);
+      } else {
+        tmp1a = dt1v4 * (vz13 - vz24) * (vz13 - vz24) / tmp3a;
+        tmp2b = dt1v4 * (vz13 + vz24) * (vz13 + vz24) / tmp3b;
+      }
       R vx13 = vx[0] - vx[2], vx24 = vx[1] - vx[3];
       vx13 = vx13 - tmp1a;
       vx24 = vx24 + tmp1a;
       exx = px1 * vx13 + px2 * vx24;
       exy = py1 * vx13 + py2 * vx24;
-      const R tmp1b = px2 - px1;
-      const R tmp3b = copysign(smax(fabs(tmp1b), (R)RG_EM20), tmp1b);
-      const R tmp2b = dt1v4 * (vz13 + vz24) * (vz13 + vz24) / tmp3b;
       R vy13 = vy[0] - vy[2], vy24 = vy[1] - vy[3];
       vy13 = vy13 + tmp2b;
       vy24 = vy24 + tmp2b;
@@ -648,6 +656,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) ----
     R h11, h12, h13, h21, h22, h23, h31, h32, h33, hr4, hr5;
     R sti_noda = (R)0, stir_noda = (R)0;
+    R inv_divm = (R)0;  // FP64 form: 1 / MAX(ALDT^2, EM20), formed with HH2
     {
       const R px1v = px1 * vhx, px2v = px2 * vhx, py1v = py1 * vhy, py2v = py2 * vhy;
       const R gama1 = off * ((R)RG_ONE - px1v - py1v);
@@ -680,7 +689,17 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       const R td = thk0 * dt1;
       R hh1 = A7 * td;
       const R b1 = px1 * px1 + py1 * py1, b2 = px2 * px2 + py2 * py2;
-      R hh2 = A8 * thk02 * td / (b1 + b2);
+      R hh2;
+      if constexpr (F64) {
+        // FP64 form: HH2's division and CDT3's 1 / MAX(ALDT^2, EM20) share
+        // one reciprocal (FP64-pipe work)
+        const R divm = smax(aldt * aldt, (R)RG_EM20);
+        const R rq = (R)RG_ONE / ((b1 + b2) * divm);
+        hh2 = A8 * thk02 * td * (divm * rq);
+        inv_divm = (b1 + b2) > (R)0 ? (b1 + b2) * rq : (R)RG_ONE / divm;
+      } else {
+        hh2 = A8 * thk02 * td / (b1 + b2);
+      }
       if (S.degen[e]) h1q = h2q = h3q = hh1 = hh2 = (R)0;
       if (P.nodadt) {
         // nodal time step (chvis3.F:198-265, IGTYP=1): the element
@@ -736,8 +755,12 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         // (strict < in CDT3)
         dt_pair_min_t(dtmine, elmin, dt, key0 + (nc_total - 1 - e));
       }
-      const R divm = smax(aldt * aldt, (R)RG_EM20);
-      sti = (R)RG_HALF * vol0 * ym / divm;
+      if constexpr (F64) {
+        sti = (R)RG_HALF * vol0 * ym * inv_divm;
+      } else {
+        const R divm = smax(aldt * aldt, (R)RG_EM20);
+        sti = (R)RG_HALF * vol0 * ym / divm;
+      }
       sti = (R)RG_ZEP81 * sti * off;
     }
     // ---- CFINT3 ----
