@@ -47,6 +47,9 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
   const int lane = threadIdx.x & 31;
   int t = blockIdx.x * (NT / 32) + (int)(threadIdx.x >> 5);
   bool first = true;
+  const double DT1 = T->dt2;
+  const R dt1r = (R)DT1;
+  const R dtinv = dt1r / smax(dt1r * dt1r, (R)RG_EM20);
   for (;;) {
     if (P.wtasks) {
       int g = 0;
@@ -59,7 +62,8 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     }
     const int il = t * 32 + lane;
     if (il < P.nel)
-      shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin);
+      shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin, DT1,
+                             dtinv);
   }
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
   if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);

@@ -212,13 +212,16 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
                                               typename SlotT<ER>::type *__restrict__ fskyr,
                                               const Time *__restrict__ T, const int key0,
                                               const int nc_total, const int il, ER &dtmine,
-                                              int &elmin) {
+                                              int &elmin, const double DT1in = -1.0,
+                                              const ER dtinv_in = (ER)0) {
   typedef ER R;
   constexpr bool F64 = std::is_same<ER, double>::value;
   const int nc = S.nc;
   {
     const int e = P.nft + il;
-    const double DT1 = T->dt2;
+    // DT1 and DT1/MAX(DT1^2, EM20) are the same for every element: a caller
+    // looping over elements passes them (DT1in >= 0) to form them once
+    const double DT1 = DT1in >= 0.0 ? DT1in : T->dt2;
     const R dt1 = (R)DT1;
     // ---- CCOOR3 ----
     int nn[4];
@@ -344,6 +347,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     }
     // ---- CDERI3 ----
     R x2, y2, x3, y3, x4, y4, px1, px2, py1, py2, area, inv_area, vhx, vhy;
+    R area2_m56 = (R)0;  // FP64 form: CDLEN3's AREA^2 / MAX(AL5, AL6, EM20)
     {
       const R x21 = xg[1] - xg[0], y21 = yg[1] - yg[0], z21 = zg[1] - zg[0];
       const R x31 = xg[2] - xg[0], y31 = yg[2] - yg[0], z31 = zg[2] - zg[0];
@@ -359,7 +363,18 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       px2 = (R)RG_HALF * y3;
       py2 = -(R)RG_HALF * x3;
       area = smax((R)RG_TWO * (py2 * px1 - py1 * px2), (R)RG_EM20);
-      inv_area = (R)RG_ONE / area;
+      if constexpr (F64) {
+        // 1/AREA and CDLEN3's AREA^2 / MAX(AL5, AL6, EM20) from one
+        // reciprocal (FP64-pipe work)
+        const R al5c = (x4 - x2) * (x4 - x2) + (y4 - y2) * (y4 - y2);
+        const R al6c = x3 * x3 + y3 * y3;
+        const R m56 = smax(smax(al5c, al6c), (R)RG_EM20);
+        const R r = (R)RG_ONE / (area * m56);
+        inv_area = m56 * r;
+        area2_m56 = area * area * (area * r);
+      } else {
+        inv_area = (R)RG_ONE / area;
+      }
       vhx = (-x2 + x3 - x4) * inv_area;
       vhy = (-y2 + y3 - y4) * inv_area;
     }
@@ -392,7 +407,11 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       R almin = smin(smin(al1, al2), al4);
       const R alquad = smin(smin(al3, al5), al6);
       if (al3 != (R)0) almin = smin(almin, alquad);
-      const R dtdyn = area * area / smax(smax(al5, al6), (R)RG_EM20);
+      R dtdyn;
+      if constexpr (F64)
+        dtdyn = area2_m56;
+      else
+        dtdyn = area * area / smax(smax(al5, al6), (R)RG_EM20);
       aldt = smax(dtdyn, almin);
       const R dthour = (R)RG_HALF * (almin + aldt) * PC(inv_hmax);
       if (dthour < aldt) aldt = dthour;
@@ -472,7 +491,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     // element strain rate (ASRATE = 1)
     R epsd_pg;
     {
-      const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
+      const R dtinv = DT1in >= 0.0 ? dtinv_in : dt1 / smax(dt1 * dt1, (R)RG_EM20);
       const R th = (R)thk_cur;  // GBUF%THK: the current thickness
       const R eps_k2 = (kxx * kxx + kyy * kyy + kxx * kyy + (R)RG_FOURTH * kxy * kxy) *
                        (R)RG_ONE_OVER_9 * th * th;
@@ -632,7 +651,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     }
     S.thk[e] = thkn > RG_EM30 ? thkn : RG_EM30;
     if (P.f.dm_nz) {
-      const R dtinv = dt1 / smax(dt1 * dt1, (R)RG_EM20);
+      const R dtinv = DT1in >= 0.0 ? dtinv_in : dt1 / smax(dt1 * dt1, (R)RG_EM20);
       const R visc = ((R)RG_ONEP414 * PC(dm)) * ssp * sqrt(area) * dtinv * rho;
       forn[0] = forn[0] + visc * (exx + (R)RG_HALF * eyy);
       forn[1] = forn[1] + visc * (eyy + (R)RG_HALF * exx);
