@@ -22,7 +22,12 @@ using namespace rg;
 
 namespace {
 
-constexpr int NODE_NT = 256;
+// Node kernels: 64-thread blocks.  The node update is bound by the FP64
+// pipe (FP64 form) or by conversions on it (mixed form), so its time per SM
+// is the number of blocks placed there; a model of 120k nodes in 256-thread
+// blocks put 4 blocks on some SMs and 3 on the rest (64: 0.0286 -> 0.0245 ms
+// FP64, 0.0183 -> 0.0163 ms mixed).  At least DT_GROUP threads (nodal dt).
+constexpr int NODE_NT = 64;
 constexpr int LINK_NT = 128;
 constexpr int DT_NT = 1024;
 constexpr int EN_BLOCKS = 304;  // 2 x 152 SMs, fixed: reductions are order-fixed
