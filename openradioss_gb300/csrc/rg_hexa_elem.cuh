@@ -386,7 +386,11 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
         const R area = ee * gg - ff * ff;
         aream = fmax_(area, aream);
       }
-      deltax = (R)RG_FOUR * volr * (R)RG_ONE / sqrt(aream);
+      // FP64 form: one reciprocal square root (the FP64 pipe bounds it)
+      if constexpr (F64)
+        deltax = (R)RG_FOUR * volr * rsqrt(aream);
+      else
+        deltax = (R)RG_FOUR * volr * (R)RG_ONE / sqrt(aream);
     }
 
     // ---- SDEFO3 (JHBE=1) -------------------------------------------------------
@@ -595,10 +599,22 @@ __device__ __forceinline__ void hexa_element(const HexaParams &P, const HexaArra
       }
       qnew = rhoe * ad * al * (qaa * al + qb * ssp);
       const R ssp_eq = fmax_((R)RG_EM20, qx + sqrt(qx * qx + ssp * ssp));
-      const R dtx = deltax / ssp_eq;
+      R dtx, tidt64 = (R)0;
+      if constexpr (F64) {
+        // DTX = DELTAX / SSP_EQ and 1/DTX from one reciprocal
+        const R rd = (R)RG_ONE / (deltax * ssp_eq);
+        dtx = deltax * deltax * rd;
+        tidt64 = ssp_eq * ssp_eq * rd;
+      } else {
+        dtx = deltax / ssp_eq;
+      }
       sti = (R)0;
       if (!(off == (R)0 || offg < (R)0)) {
-        const R tidt = (R)RG_ONE / dtx;
+        R tidt;
+        if constexpr (F64)
+          tidt = tidt64;
+        else
+          tidt = (R)RG_ONE / dtx;
         sti = (rhoe * tidt) * (volr * tidt);
       }
       const R dtxd = PC(dtfac) * dtx;
