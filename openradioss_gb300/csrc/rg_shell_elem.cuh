@@ -619,12 +619,29 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
             dpla_i = dpla_j;
             const R pla_i = pla + dpla_i;
             const R yld_i = pla_i == (R)0 ? smin(ymax, ca) : smin(ymax, ca + cb * exp(PC(cn) * log(pla_i)));
-            dr = (R)RG_HALF * ym * dpla_i / yld_i;
-            Pp = (R)RG_ONE / ((R)RG_ONE + dr * nu1);
-            Qq = (R)RG_ONE / ((R)RG_ONE + (R)RG_THREE * dr * nu2);
+            // FP64 form: the two divisions by YLD_I, and P and Q, each from
+            // one reciprocal (FP64-pipe work of the plastic points)
+            R inv_y = (R)0;
+            if constexpr (F64) {
+              inv_y = (R)RG_ONE / yld_i;
+              dr = (R)RG_HALF * ym * dpla_i * inv_y;
+              const R dp = (R)RG_ONE + dr * nu1;
+              const R dq = (R)RG_ONE + (R)RG_THREE * dr * nu2;
+              const R rpq = (R)RG_ONE / (dp * dq);
+              Pp = dq * rpq;
+              Qq = dp * rpq;
+            } else {
+              dr = (R)RG_HALF * ym * dpla_i / yld_i;
+              Pp = (R)RG_ONE / ((R)RG_ONE + dr * nu1);
+              Qq = (R)RG_ONE / ((R)RG_ONE + (R)RG_THREE * dr * nu2);
+            }
             const R p2 = Pp * Pp, q2 = Qq * Qq;
             const R f = A * p2 + B * q2 - yld_i * yld_i;
-            const R df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) / yld_i - h2 * yld_i;
+            R df;
+            if constexpr (F64)
+              df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) * inv_y - h2 * yld_i;
+            else
+              df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) / yld_i - h2 * yld_i;
             dpla_j = dpla_i > (R)0 ? smax((R)0, dpla_i - f / df) : (R)0;
           }
           pla = pla + dpla_i;
