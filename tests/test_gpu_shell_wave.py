@@ -4,9 +4,9 @@ A crash box of 41,600 shells (more than the 152 SMs x 2 blocks x 128
 threads of one wave of the FP64 shell kernel, so blocks are scheduled in
 several rounds) against the oracle -- forces of the first cycles within
 1e-12, trajectories within 1e-10, time step and controlling element equal --
-and the same model stepped by the batched kernel (which writes the job's
+the same model stepped by the batched kernel (which writes the job's
 time-step partials in its own tile layout) within 1e-10 of the single
-model.
+model, and the FORINT-level call equal bit for bit to the device cycle.
 """
 import numpy as np
 import pytest
@@ -57,3 +57,32 @@ def test_batch_with_a_job_larger_than_one_wave():
         e = Engine(m)
         e.cycle(10)
         assert close(got[i], state(e), 1e-10), i
+
+
+def test_forint_step_matches_device_cycle_beyond_one_wave():
+    """The FORINT-level call (warp tasks on the same layout) returns the
+    device-resident cycle's assembled forces, moments, stiffness and element
+    step bit for bit on the model larger than one wave."""
+    from openradioss_gb300.engine import Engine
+
+    m = model()
+    e1 = Engine(m)
+    e1.cycle(5)
+    nd = e1.nodes()
+    t = e1.time()
+    e1.cycle(1)
+    ref = e1.forces()
+    e2 = Engine(m)
+    e2.cycle(5)
+    x = np.ascontiguousarray(nd["X"].T)
+    v = np.ascontiguousarray(nd["V"].T)
+    vr = np.ascontiguousarray(nd["VR"].T)
+    fr = np.empty_like(x)
+    sr = np.empty(m.numnod)
+    f, st, dt2t, el = e2.forint_step(x, v, t["dt2"], vr=vr, fr=fr, stifr=sr)
+    assert np.array_equal(f.T, ref["F"])
+    assert np.array_equal(fr.T, ref["FR"])
+    assert np.array_equal(st, ref["STIFN"])
+    assert el == e1.time()["neltst"] and dt2t > 0
+    e1.close()
+    e2.close()
