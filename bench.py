@@ -268,10 +268,12 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_job and args.forms == "both" and JOB_CYCLES.get(wl):
         for prec in forms:
             e = Engine(model, device=local_rank, precision=prec)
-            jms = e.time_cycles(JOB_CYCLES[wl])
+            # the whole job is seconds long: its clock record has many samples
+            with Clocks(local_rank) as jclk:
+                jms = e.time_cycles(JOB_CYCLES[wl])
             jobs[prec] = dict(cycles=JOB_CYCLES[wl], seconds=jms * 1e-3,
                               element_updates_s=ne * JOB_CYCLES[wl] / (jms * 1e-3),
-                              status=e.status())
+                              status=e.status(), clocks=jclk.summary())
             e.close()
 
     if args.forms != "both":
