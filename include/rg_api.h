@@ -218,13 +218,20 @@ int rg_time_cycles_cold(rg_ctx *ctx, int ncycle, unsigned long long flush_bytes,
  * sizes are refused with RG_E_SIZE before any device work.  For callers that
  * must not allocate at that moment (a serving loop whose HBM budget is fully
  * reserved; an engine that accounts its own device memory).  Synchronous, on
- * the legacy default stream: the arrays must be complete when it is called.
- * Nothing in the scratch needs to start at zero (each call overwrites the
- * partials it reads); the scratch is shared per device, so calls that
- * overlap in time on one device race and must be serialised by the caller.
- * The first call on a device looks the scratch address up
- * (cudaGetSymbolAddress); make it before starting any stream capture on that
- * device.  No counterpart in the reference (its energy sums are host loops). */
+ * the legacy default stream, which is not ordered after a context's own
+ * (non-blocking) stream: call rg_synchronize(ctx) -- or synchronise whatever
+ * stream produced the arrays -- before this call, or it races with the
+ * cycles still queued.  Nothing in the scratch needs to start at zero (each
+ * call overwrites the partials it reads); the scratch is shared per device,
+ * so calls that overlap in time on one device race and must be serialised by
+ * the caller.  The first call on a device looks the scratch address up
+ * (cudaGetSymbolAddress); with CUDA's default lazy module loading that is
+ * when the library's module, and the 512 KB scratch with it, is loaded onto
+ * the device, so the first call does take device memory: make one warm-up
+ * call per device while there is still room (before reserving the whole HBM
+ * budget) and before starting any stream capture on that device; later calls
+ * allocate nothing.  No counterpart in the reference (its energy sums are
+ * host loops). */
 #define RG_NOALLOC_NODES_PER_BLOCK 1024
 #define RG_NOALLOC_MAX_BLOCKS 65536
 int rg_kinetic_energy_noalloc(int device, int numnod, const double *d_v,
@@ -241,8 +248,13 @@ int rg_fp64_peak(int device, double *fma_per_s);
  * the same arithmetic form together: one persistent cooperative kernel per
  * cycle (element tiles of every job -> grid barrier -> per-job time step ->
  * grid barrier -> node tiles of every job), captured in a CUDA graph.  Each
- * job keeps its own state, time step and cycle target; a job's results are
- * bitwise those of rg_cycle on it alone.  While a context is in a batch,
+ * job keeps its own state, time step and cycle target.  Within the batched
+ * kernel a job's results are bitwise the same under every launch
+ * configuration, schedule and batch composition; against rg_cycle on the
+ * job alone (separately compiled kernels, whose multiply-add contraction may
+ * differ) they agree within 1e-10 (FP64) / 1e-4 (mixed form) of the job's
+ * displacement and velocity scales, and the job reaches exactly its cycle
+ * target.  While a context is in a batch,
  * only the batch advances it; read its results with the rg_download_* calls
  * after rg_batch_synchronize.  No counterpart in the reference (its engine
  * runs one model per process); the per-job cycle is the RESOL loop body. */
@@ -268,6 +280,22 @@ int rg_batch_time_cycles(rg_batch *b, int ncycle, double *ms);
 /* ncycle[slot] = the job's cycle count after the last batched cycle (-1 for
  * a free slot); bstatus = batch status (RG_ST_BARRIER), cleared. */
 int rg_batch_progress(rg_batch *b, int *ncycle, int nslots, int *bstatus);
+/* Status word (RG_ST_* bits) of every job's own context after the batch's
+ * queued cycles: status[slot], 0 for a free slot; the words are left set
+ * (the job's rg_status reads and clears its own).  A job whose word is raised
+ * can be removed (rg_batch_remove) while the other jobs go on: jobs share no
+ * data.  No counterpart in the reference (one model per process; its
+ * engine stops the run, MSTOP / TSTOP, resol.F). */
+int rg_batch_job_status(rg_batch *b, int *status, int nslots);
+/* Test hook of the batched kernel's bounded grid barrier: spin_limit naps of
+ * 64 ns before a waiting block gives up (0 = the default, about a second),
+ * and block late_block (-1 = none) made to arrive at every barrier after
+ * late_us microseconds (at most 1e6) of sleep.  With a limit shorter than
+ * the delay the waits run out: the kernel records RG_ST_BARRIER (read by
+ * rg_batch_progress) and returns; the cycle's results are void, the batch
+ * stays usable.  Nothing waits without a bound, nothing faults. */
+int rg_batch_set_barrier_test(rg_batch *b, unsigned spin_limit, int late_block,
+                              unsigned late_us);
 /* Autotuner: times each candidate configuration ({ktile, knode,
  * blocks_per_sm, schedule} rows; NULL = built-in list) for trial_cycles on
  * the batch's jobs with their state saved and restored, keeps the fastest.

@@ -64,6 +64,8 @@ SIGNATURES = [
     ("rg_batch_synchronize", _ip, [_vp]),
     ("rg_batch_time_cycles", _ip, [_vp, _ip, _vp]),
     ("rg_batch_progress", _ip, [_vp, _vp, _ip, _vp]),
+    ("rg_batch_job_status", _ip, [_vp, _vp, _ip]),
+    ("rg_batch_set_barrier_test", _ip, [_vp, C.c_uint, _ip, C.c_uint]),
     ("rg_batch_autotune", _ip, [_vp, _ip, _vp, _ip, _vp]),
 ]
 

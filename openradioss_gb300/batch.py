@@ -86,6 +86,21 @@ class Batch:
                                            C.byref(st)), "rg_batch_progress")
         return {s: int(nc[s]) for s in self.slots}, st.value
 
+    def job_status(self):
+        """{slot: status word} of the jobs' own contexts (RG_ST_* bits),
+        read after the queued cycles and left set."""
+        n = max(self.slots) + 1 if self.slots else 1
+        st = np.zeros(n, np.int32)
+        self._chk(self.L.rg_batch_job_status(self.h, st.ctypes.data_as(C.c_void_p), n),
+                  "rg_batch_job_status")
+        return {s: int(st[s]) for s in self.slots}
+
+    def set_barrier_test(self, spin_limit=0, late_block=-1, late_us=0):
+        """Test hook of the bounded grid barrier (see rg_batch_set_barrier_test);
+        the defaults switch it off."""
+        self._chk(self.L.rg_batch_set_barrier_test(self.h, int(spin_limit), int(late_block),
+                                                    int(late_us)), "rg_batch_set_barrier_test")
+
     def autotune(self, trial_cycles=5, candidates=None):
         """Time candidate launch configurations ({ktile, knode,
         blocks_per_sm, schedule} rows; None = the built-in list) on this

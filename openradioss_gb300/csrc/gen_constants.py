@@ -15,6 +15,7 @@ The generated header is committed; nothing at build or run time reads the
 reference.
 """
 import math
+import os
 import re
 import sys
 
@@ -53,7 +54,11 @@ def evaluate(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # root of the OpenRadioss source tree: first argument or OPENRADIOSS_SRC
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("OPENRADIOSS_SRC")
+    if not ref:
+        sys.exit("usage: gen_constants.py <root of the OpenRadioss source tree> "
+                 "(or set OPENRADIOSS_SRC)")
     env = evaluate(ref + "/common_source/modules/constant_mod.F")
     out = [
         "// Generated by gen_constants.py from the reference's constant module",

@@ -89,13 +89,23 @@ struct BatchDev {
   GridBar *bar;
   int *bstatus;    // batch status word (RG_ST_BARRIER)
   int njobs, ntiles, nntiles, ktile, knode, pad;
+  // barrier wait limit (64 ns naps) and the test hook: block late_block
+  // (-1: none) arrives at every barrier after late_naps naps of 1 us
+  unsigned spin_limit, late_naps;
+  int late_block, pad2;
 };
 
 // Grid-wide barrier for a cooperative launch (all blocks co-resident).  The
 // wait is bounded: on give-up the block records RG_ST_BARRIER and goes on.
-__device__ __forceinline__ void grid_barrier(GridBar *bar, int *bstatus) {
+// The counters of the barrier and of the work queues are re-armed before
+// every cycle (batch_reset_counters), so a cycle whose barrier gave up leaves
+// nothing behind for the next one.
+__device__ __forceinline__ void grid_barrier(GridBar *bar, int *bstatus, unsigned spin_limit,
+                                             int late_block, unsigned late_naps) {
   __syncthreads();
   if (threadIdx.x == 0) {
+    if ((int)blockIdx.x == late_block)
+      for (unsigned i = 0; i < late_naps; i++) __nanosleep(1000);  // bounded delay
     const unsigned g = atomicOr(&bar->gen, 0u);
     __threadfence();
     if (atomicAdd(&bar->count, 1u) == gridDim.x - 1) {
@@ -105,7 +115,7 @@ __device__ __forceinline__ void grid_barrier(GridBar *bar, int *bstatus) {
     } else {
       unsigned it = 0;
       while (atomicOr(&bar->gen, 0u) == g) {
-        if (++it > BAR_SPIN_LIMIT) {
+        if (++it > spin_limit) {
           atomicOr(bstatus, RG_ST_BARRIER);
           break;
         }
@@ -208,7 +218,8 @@ batch_kernel(const BatchDev<ER> B, const int phases) {
       __syncthreads();
     }
   }
-  if ((phases & 1) && (phases & 6)) grid_barrier(B.bar, B.bstatus);
+  if ((phases & 1) && (phases & 6))
+    grid_barrier(B.bar, B.bstatus, B.spin_limit, B.late_block, B.late_naps);
 
   // ---- phase 2: time step of each job ----------------------------------------
   if (phases & 2) {
@@ -237,7 +248,8 @@ batch_kernel(const BatchDev<ER> B, const int phases) {
     // the element counter is free again (phase 1 ended before this phase)
     if (blockIdx.x == 0 && threadIdx.x == 0) B.ctr[0] = 0u;
   }
-  if ((phases & 2) && (phases & 4)) grid_barrier(B.bar, B.bstatus);
+  if ((phases & 2) && (phases & 4))
+    grid_barrier(B.bar, B.bstatus, B.spin_limit, B.late_block, B.late_naps);
 
   // ---- phase 3: node tiles -----------------------------------------------------
   if (phases & 4) {
@@ -299,10 +311,16 @@ batch_node_kernel(const BatchDev<ER> B) {
   }
 }
 
-// The node counter is reset by the first phase of the next cycle's launch
-// sequence: a separate one-thread kernel keeps the rule simple for both
-// schedules.
-__global__ void batch_reset_node_counter(unsigned *ctr) { ctr[1] = 0u; }
+// The work counters and the barrier's arrival count are re-armed before each
+// cycle's launch sequence by a separate one-thread kernel (stream order puts
+// it after the previous cycle's last kernel): the rule is the same for both
+// schedules, and a cycle whose barrier wait gave up cannot leave a stale count
+// to the next one.  In a healthy run all three are zero already.
+__global__ void batch_reset_counters(unsigned *ctr, GridBar *bar) {
+  ctr[0] = 0u;
+  ctr[1] = 0u;
+  bar->count = 0u;
+}
 
 }  // namespace rg
 
@@ -317,6 +335,9 @@ struct rg_batch {
   std::vector<int> target;      // per slot
   // launch configuration
   int ktile = 1, knode = 1, blocks_per_sm = 0, schedule = 0;  // 0 persistent, 1 three launches
+  // grid barrier wait limit and its test hook (rg_batch_set_barrier_test)
+  unsigned spin_limit = BAR_SPIN_LIMIT, late_naps = 0;
+  int late_block = -1;
   int max_blocks_per_sm = 0, nsm = 0;
   // device descriptors
   void *d_jobs = nullptr;
@@ -500,6 +521,9 @@ BatchDev<ER> dev_view(rg_batch *b) {
   D.nntiles = b->nntiles;
   D.ktile = b->ktile;
   D.knode = b->knode;
+  D.spin_limit = b->spin_limit;
+  D.late_block = b->late_block;
+  D.late_naps = b->late_naps;
   return D;
 }
 
@@ -528,7 +552,7 @@ int enqueue(rg_batch *b) {
   const int bps = b->blocks_per_sm > 0 ? std::min(b->blocks_per_sm, b->max_blocks_per_sm)
                                        : b->max_blocks_per_sm;
   const int grid = std::max(1, bps * b->nsm);
-  batch_reset_node_counter<<<1, 1, 0, b->stream>>>(b->d_ctr);
+  batch_reset_counters<<<1, 1, 0, b->stream>>>(b->d_ctr, b->d_bar);
   if (b->schedule == 0) {
     cudaLaunchConfig_t cfg;
     std::memset(&cfg, 0, sizeof(cfg));
@@ -767,6 +791,37 @@ int rg_batch_progress(rg_batch *b, int *ncycle, int nslots, int *bstatus) {
     }
   }
   if (bstatus) *bstatus = st;
+  return RG_OK;
+}
+
+// Status word of every job (RG_ST_* bits of its own context, 0 for a free
+// slot), read after the batch's queued cycles and left set: the job's own
+// rg_status still reads and clears it.  One small copy per job.
+int rg_batch_job_status(rg_batch *b, int *status, int nslots) {
+  if (!b || !status || nslots < 0) return RG_E_ARG;
+  RB_CUDA(b, cudaSetDevice(b->device));
+  for (int s = 0; s < nslots; s++) status[s] = 0;
+  const int n = std::min(nslots, (int)b->jobs.size());
+  for (int s = 0; s < n; s++)
+    if (b->jobs[s])
+      RB_CUDA(b, cudaMemcpyAsync(status + s, b->jobs[s]->d_status, sizeof(int),
+                                 cudaMemcpyDeviceToHost, b->stream));
+  RB_CUDA(b, cudaStreamSynchronize(b->stream));
+  return RG_OK;
+}
+
+// Test hook of the bounded grid barrier: spin_limit naps of 64 ns before a
+// block gives up (0 = the default), and block late_block (-1 = none) made to
+// arrive at every barrier after late_us microseconds of sleep.  With a limit
+// shorter than the delay the other blocks' waits run out, the kernel records
+// RG_ST_BARRIER and returns; nothing hangs and nothing faults.
+int rg_batch_set_barrier_test(rg_batch *b, unsigned spin_limit, int late_block,
+                              unsigned late_us) {
+  if (!b || late_us > 1000000u) return RG_E_ARG;
+  b->spin_limit = spin_limit ? spin_limit : BAR_SPIN_LIMIT;
+  b->late_block = late_block;
+  b->late_naps = late_block >= 0 ? late_us : 0u;
+  b->dirty = true;
   return RG_OK;
 }
 

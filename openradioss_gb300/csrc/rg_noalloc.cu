@@ -15,6 +15,19 @@
 // Nothing in it has to start at zero: every call overwrites the partials it
 // reads.  The scratch is shared by all callers on a device, so two calls that
 // overlap in time on one device race: callers serialise them.
+//
+// The scratch is part of this library's device module.  With CUDA's lazy
+// module loading (the default) the module -- and with it the 512 KB array --
+// is loaded on the device when the first call looks the scratch address up,
+// so that first call does take device memory.  A caller that must not
+// allocate later makes one warm-up call per device while it still has room
+// (at context creation, before it reserves its HBM budget); every later call
+// allocates nothing.
+//
+// The kernels run on the legacy default stream.  Contexts of this library
+// run on their own non-blocking streams, so the arrays of a context must be
+// complete first: call rg_synchronize(ctx), or synchronise whatever stream
+// produced the arrays, before this call.
 #include "../../include/rg_api.h"
 
 #include <cuda_runtime.h>
@@ -112,7 +125,11 @@ namespace {
 constexpr int PK_CHAINS = 8;
 constexpr int PK_ITERS = 4096;
 
-__global__ void __launch_bounds__(256) fp64_fma_kernel(double *out, double a, double b) {
+// sink of the FMA chains (never written in practice), apart from the
+// kinetic-energy scratch
+static __device__ double g_fp64_sink;
+
+__global__ void __launch_bounds__(256) fp64_fma_kernel(double a, double b) {
   double c[PK_CHAINS];
 #pragma unroll
   for (int k = 0; k < PK_CHAINS; k++) c[k] = threadIdx.x * 1e-3 + k;
@@ -123,27 +140,25 @@ __global__ void __launch_bounds__(256) fp64_fma_kernel(double *out, double a, do
   double s = 0.0;
 #pragma unroll
   for (int k = 0; k < PK_CHAINS; k++) s += c[k];
-  if (s == 12345.678) out[blockIdx.x] = s;  // keeps the chains live
+  if (s == 12345.678) g_fp64_sink = s;  // keeps the chains live
 }
 }  // namespace
 
 extern "C" int rg_fp64_peak(int device, double *fma_per_s) {
-  if (!fma_per_s || device < 0) return RG_E_ARG;
+  if (!fma_per_s || device < 0 || device >= NA_MAX_DEVICES) return RG_E_ARG;
   int prev = -1;
   if (cudaGetDevice(&prev) != cudaSuccess) return RG_E_CUDA;
   if (prev != device && cudaSetDevice(device) != cudaSuccess) return RG_E_CUDA;
   int nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
   const int blocks = nsm * 8;
-  double *scr = nullptr;
-  int r = scratch_for(device, &scr);
+  int r = RG_OK;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (r == RG_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
-    r = RG_E_CUDA;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) r = RG_E_CUDA;
   if (r == RG_OK) {
-    fp64_fma_kernel<<<blocks, 256>>>(scr, 0.999999, 1e-9);  // warm-up
+    fp64_fma_kernel<<<blocks, 256>>>(0.999999, 1e-9);  // warm-up
     cudaEventRecord(e0);
-    fp64_fma_kernel<<<blocks, 256>>>(scr, 0.999999, 1e-9);
+    fp64_fma_kernel<<<blocks, 256>>>(0.999999, 1e-9);
     cudaEventRecord(e1);
     float ms = 0.f;
     if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)

@@ -11,7 +11,13 @@ of ``step_cycles`` cycles it
   the running batch with its own cycle target;
 * retires the jobs whose cycle count reached their target: their results are
   read back, their device memory is released, and the freed slot and bytes go
-  to the next waiting requests.
+  to the next waiting requests;
+* retires as failed, at once, a job whose own device status word is raised
+  (negative volume, non-finite acceleration, time step below its minimum:
+  the conditions on which the reference engine stops its run) -- the other
+  jobs share no data with it and go on unchanged.  A batch-level failure (a
+  grid barrier that gave up) voids the step for every running job: they are
+  all retired as failed, and the server goes on with the waiting requests.
 
 While the GPU runs a step, the host prepares the next admissions (upload
 and set-up), so requests that arrive while others are on the GPU overlap
@@ -80,6 +86,8 @@ class JobRecord:
     elements: int = 0
     device_bytes: int = 0
     result: dict = field(default_factory=dict)
+    failed: bool = False
+    status: int = 0
 
     @property
     def latency(self):
@@ -106,6 +114,7 @@ class Server:
         self.running = {}     # slot -> (Engine, JobRecord, reserved bytes)
         self.waiting = []     # heap of Request (arrival order)
         self.done = []
+        self.failed = []
         self.max_used = 0
 
     def submit(self, key, model, ncycles, arrival):
@@ -157,6 +166,28 @@ class Server:
             self.done.append(rec)
         return len(fin)
 
+    def _retire_failed(self, jstat, bstatus):
+        """Retire, as failed, every job whose status word is raised (every
+        running job when the batch status is): removed from the batch,
+        memory released, record kept with its status."""
+        bad = [s for s in self.running if bstatus or jstat.get(s, 0)]
+        if not bad:
+            return 0
+        self.batch.sync()
+        now = self._clock()
+        for s in bad:
+            e, rec, need = self.running.pop(s)
+            self.batch.remove(s)
+            rec.finished = now
+            rec.failed = True
+            rec.status = int(jstat.get(s, 0)) | int(bstatus)
+            rec.result = dict(time=e.time(), status=rec.status)
+            e.status()  # clear the word the job's context kept
+            e.close()
+            self.used -= need
+            self.failed.append(rec)
+        return len(bad)
+
     def _clock(self):
         return time.perf_counter() - self.t0
 
@@ -168,7 +199,7 @@ class Server:
         total = len(self.waiting)
         self.t0 = time.perf_counter()
         steps = 0
-        while len(self.done) < total:
+        while len(self.done) + len(self.failed) < total:
             now = self._clock()
             if self.running:
                 # launch a step; admissions prepared meanwhile overlap with it
@@ -176,16 +207,17 @@ class Server:
                 steps += 1
                 self._admit(self._clock())
                 prog, st = self.batch.progress()
-                if st:
-                    raise RuntimeError("batched kernel status %d" % st)
+                self._retire_failed(self.batch.job_status(), st)
                 self._retire(prog)
             else:
                 if self.waiting and self.waiting[0].arrival > now:
                     time.sleep(min(0.05, self.waiting[0].arrival - now))
                 self._admit(self._clock())
         makespan = self._clock()
-        lat = np.array([r.latency for r in self.done])
-        return dict(jobs=total, makespan_s=makespan, jobs_per_h=3600.0 * total / makespan,
+        lat = np.array([r.latency for r in self.done]) if self.done else np.zeros(1)
+        ok = len(self.done)
+        return dict(jobs=total, completed=ok, failed=len(self.failed), makespan_s=makespan,
+                    jobs_per_h=3600.0 * ok / makespan,
                     p50_latency_s=float(np.percentile(lat, 50)),
                     p99_latency_s=float(np.percentile(lat, 99)),
                     mean_latency_s=float(lat.mean()), steps=steps,

@@ -27,6 +27,7 @@ The deck is (C) Siemens, licensed CC BY-NC 4.0 (header of CRA2V44_0000.rad);
 the fixture carries its numbers for parity testing only.
 
 Usage:  python tests/golden/make_cra2.py [path to the cra2 QA directory]
+        (or OPENRADIOSS_SRC=<root of the OpenRadioss tree> python tests/golden/make_cra2.py)
 """
 from __future__ import annotations
 
@@ -37,8 +38,23 @@ import sys
 
 import numpy as np
 
-DEFAULT_DIR = "/root/reference/qa-tests/miniqa/RESTART/cra2"
+# inside an OpenRadioss source tree, given by the command line or by the
+# OPENRADIOSS_SRC environment variable (the tree's root)
+QA_SUBDIR = "qa-tests/miniqa/RESTART/cra2"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cra2.npz")
+
+
+def qa_dir(subdir):
+    """The QA directory to read: the first command-line argument, else
+    subdir inside the OpenRadioss tree named by OPENRADIOSS_SRC; neither
+    given is an error (no machine path is assumed)."""
+    if len(sys.argv) > 1:
+        return sys.argv[1]
+    root = os.environ.get("OPENRADIOSS_SRC")
+    if not root:
+        sys.exit("give the QA directory as the first argument, or set OPENRADIOSS_SRC "
+                 "to the root of an OpenRadioss source tree")
+    return os.path.join(root, subdir)
 
 
 def read_blocks(path):
@@ -250,7 +266,7 @@ def parse_th(path, ngv=12, npart=3, npv=8, nnode=3, nnv=6):
 
 
 def main():
-    qa = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_DIR
+    qa = qa_dir(QA_SUBDIR)
     dd = os.path.join(qa, "data")
     rd = os.path.join(qa, "reference")
     d = parse_starter(os.path.join(dd, "CRA2V44_0000.rad"))

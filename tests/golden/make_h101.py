@@ -26,6 +26,7 @@ The deck is (C) Siemens, licensed CC BY-NC 4.0 (header of
 CONV_ELS_0000.rad); the fixture carries its numbers for parity testing only.
 
 Usage:  python tests/golden/make_h101.py [path to the H101 QA directory]
+        (or OPENRADIOSS_SRC=<root of the OpenRadioss tree> python tests/golden/make_h101.py)
 """
 from __future__ import annotations
 
@@ -38,9 +39,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from make_cra2 import find, fortran_records, grnod, ints, nums, one, read_blocks  # noqa: E402
+from make_cra2 import find, fortran_records, grnod, ints, nums, one, qa_dir, read_blocks  # noqa: E402,E501
 
-DEFAULT_DIR = "/root/reference/qa-tests/miniqa/SOLIDES/nv_elts/poutre_flex/flexion/H101"
+# inside an OpenRadioss source tree, given by the command line or by the
+# OPENRADIOSS_SRC environment variable (the tree's root)
+QA_SUBDIR = "qa-tests/miniqa/SOLIDES/nv_elts/poutre_flex/flexion/H101"
 OUT = os.path.join(HERE, "h101.npz")
 
 
@@ -209,7 +212,7 @@ def parse_th(path, ngv=12, nnode=6, nnv=6):
 
 
 def main():
-    qa = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_DIR
+    qa = qa_dir(QA_SUBDIR)
     dd = os.path.join(qa, "data")
     rd = os.path.join(qa, "reference")
     d = parse_starter(os.path.join(dd, "CONV_ELS_0000.rad"))

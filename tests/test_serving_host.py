@@ -10,10 +10,13 @@ from openradioss_gb300 import serving as S
 
 class FakeEngine:
     live = 0
+    # model name -> (cycle at which the job's status word is raised, bits)
+    fail_at = {}
 
     def __init__(self, model, device=0, precision=1):
         self.model = model
         self.nc = 0
+        self.word = 0
         FakeEngine.live += 1
 
     def info(self):
@@ -26,7 +29,8 @@ class FakeEngine:
         return {}
 
     def status(self):
-        return 0
+        w, self.word = self.word, 0
+        return w
 
     def close(self):
         FakeEngine.live -= 1
@@ -51,12 +55,21 @@ class FakeBatch:
     def remove(self, s):
         self.slots.pop(s)
 
+    bstatus = 0
+
     def cycle(self, n):
         for e, t in self.slots.values():
             e.nc = min(t, e.nc + n)
+            f = FakeEngine.fail_at.get(e.model.name)
+            if f and e.nc >= f[0]:
+                e.word |= f[1]
 
     def progress(self):
-        return {s: e.nc for s, (e, t) in self.slots.items()}, 0
+        st, FakeBatch.bstatus = FakeBatch.bstatus, 0
+        return {s: e.nc for s, (e, t) in self.slots.items()}, st
+
+    def job_status(self):
+        return {s: e.word for s, (e, t) in self.slots.items()}
 
     def sync(self):
         pass
@@ -70,6 +83,8 @@ def fakes(monkeypatch):
     monkeypatch.setattr(S, "Engine", FakeEngine)
     monkeypatch.setattr(S, "Batch", FakeBatch)
     FakeEngine.live = 0
+    FakeEngine.fail_at = {}
+    FakeBatch.bstatus = 0
     yield
 
 
@@ -97,6 +112,49 @@ def test_slot_limit_and_order(fakes):
     assert srv.batch.max_live == 2
     adm = sorted(srv.done, key=lambda r: r.admitted)
     assert [r.key for r in adm] == sorted(r.key for r in adm)  # FIFO admission
+
+
+def test_failed_job_is_retired_and_others_finish(fakes):
+    """A job whose status word is raised (here a non-finite acceleration at
+    its cycle 100) is retired as failed at the end of that step, its memory
+    released, and every other job still reaches its target."""
+    jobs = small_jobs()
+    for k, m, n, a in jobs:
+        m.name = "job%d" % k
+    FakeEngine.fail_at = {"job3": (100, 2)}
+    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50)
+    st = srv.run(jobs)
+    assert st["failed"] == 1 and st["completed"] == 5
+    assert [r.key for r in srv.failed] == [3]
+    assert srv.failed[0].status == 2 and srv.failed[0].failed
+    assert srv.failed[0].result["time"]["ncycle"] == 100
+    assert sorted(r.key for r in srv.done) == [0, 1, 2, 4, 5]
+    assert all(r.result["time"]["ncycle"] == jobs[r.key][2] for r in srv.done)
+    assert srv.used == 0 and FakeEngine.live == 0
+
+
+def test_batch_failure_retires_the_running_jobs(fakes):
+    """A batch-level failure (grid barrier gave up) voids the step of every
+    running job: they are retired as failed and the server serves the
+    requests that arrive afterwards."""
+    jobs = small_jobs()[:2] + [(9, M.crash_box(n_side=3, n_len=4, seed=9), 100, 0.3)]
+
+    class OnceBatch(FakeBatch):
+        fired = False
+
+        def cycle(self, n):
+            super().cycle(n)
+            if not OnceBatch.fired:
+                OnceBatch.fired = True
+                FakeBatch.bstatus = 16
+
+    S.Batch = OnceBatch
+    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50)
+    st = srv.run(jobs)
+    assert sorted(r.key for r in srv.failed) == [0, 1]
+    assert all(r.status & 16 for r in srv.failed)
+    assert [r.key for r in srv.done] == [9]
+    assert st["completed"] == 1 and srv.used == 0 and FakeEngine.live == 0
 
 
 def test_oversize_job_is_refused(fakes):
