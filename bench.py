@@ -4,14 +4,24 @@
 A *step* is one explicit cycle of the whole model (every element group ->
 PARITH/ON assembly -> time step -> nodal update) with the model resident in
 HBM.  ``value`` is element-updates/s (elements x cycles / device seconds,
-CUDA events on the library's stream); ``e2e`` is the same metric through the
-FORINT-level C-ABI call with host buffers (X, V uploaded and assembled
-forces + STIFN downloaded every step).  The headline form is the plain FP64
-path; the mixed FP32-element / FP64-nodal form is reported beside it.
+CUDA events on the library's stream, every cycle from cold L2) of the plain
+FP64 form on the crash box of 120,120 shells; the mixed FP32-element /
+FP64-nodal form is reported beside it.  ``e2e`` is the same metric through
+the library's whole-cycle call with host node buffers (rg_cycle_host: X, V,
+VR read from pinned host memory, X, V, VR, D written back, every step).
+
+The same line carries, for the other single-GPU configurations, summaries
+measured in the same run: the 20^3 bar impact (LAW1, 1,000 cycles) and the
+128^3 Johnson-Cook block (2,000 cycles), each with both forms' full-length
+job runs and the mixed form's error against the FP64 run (displacement,
+peak force, internal energy and its growth); the batched sweep of 64
+crash-box variants and the Poisson serving stream, both against sequential
+runs of the same jobs, all at full length.
 
 ``--impl reference`` times the reference algorithm's CPU path -- the CPU
 restatement under oracle/ (the reference engine itself cannot be built
-without a Fortran compiler) -- on all host cores, on the same workload.
+without a Fortran compiler) -- on all host cores, on the same workload and
+the same cycle window as the GPU's timed region.
 
 Multi-GPU: replicas only (independent models, weak scaling, barrier and
 max-over-ranks timing), launched by torchrun.
@@ -48,6 +58,9 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "crash_box_120k_jc"
 # full run length of each configuration (the "job")
 JOB_CYCLES = {"crash_box_120k_jc": 20000, "hexa_block_128_jc": 2000, "bar_impact_20_law1": 1000}
+# printouts of a job run (forces, energies, displacement) for the error curve
+JOB_PRINTOUTS = 40
+L2_FLUSH_BYTES = 256 << 20  # twice the GB300 L2
 
 
 def peaks():
@@ -56,6 +69,16 @@ def peaks():
         d = json.load(open(p))
         return d.get("hbm_gbs", 6800.0), "measured"
     return 6800.0, "fallback"
+
+
+def profile_json(name):
+    p = os.path.join(ROOT, "profiles", name)
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return {}
+    return {}
 
 
 class Clocks:
@@ -121,6 +144,25 @@ def replica_value(units_per_rank, world, seconds):
     return world * units_per_rank / seconds
 
 
+def workload_config(wl, model, world):
+    """The workload as both arms describe it (the same dict in the GPU line
+    and in the reference arm's line)."""
+    hexa = bool(model.hexa)
+    law2 = bool(model.shells) or model.hexa[0].mat["mtn"] == 2
+    return {"workload": wl, "elements": model.numels + model.numelc, "nodes": model.numnod,
+            "law": "LAW2 Johnson-Cook" if law2 else "LAW1",
+            "formulation": ("one-point hexa Isolid=1 Iframe=1 Ismstr=4, viscous hourglass"
+                            if hexa else
+                            "Belytschko-Tsay shell Ishell=1 Ismstr=4 Ithick=1 NPT=5 Iplas=1, "
+                            "planar sliding rigid wall") + ", PARITH/ON",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "window": "each arm times cycles W+1 .. W+K of a fresh model (W warm-up cycles)"
+                      + ("; at W=5, K=20 the box is still moving to the wall (elastic): the "
+                         "full 20,000-cycle job (contact, buckling, plasticity) is timed in "
+                         "'job'" if not hexa else ""),
+            "l2": "GPU arm: L2 flushed (256 MB written) before every timed cycle"}
+
+
 def element_bytes(model, prec):
     """Algorithmic DRAM bytes of one element-kernel launch over the model,
     and per node of one node-kernel launch, from the implemented arrays
@@ -158,70 +200,145 @@ def element_bytes(model, prec):
     return rd + wr, node, "shell"
 
 
-def fp64_roofline(kkey, ne, ms, device):
-    """The plain form's element kernel against the FP64 pipe: FP64
-    instructions per launch over its time, against the measured FMA rate."""
+def fp64_peak(device=0):
+    """Measured FP64 fused multiply-add rate of the device (thread instr/s)."""
+    import ctypes as C
+    from openradioss_gb300 import _lib
+    v = C.c_double()
+    r = _lib.lib().rg_fp64_peak(device, C.byref(v))
+    return v.value if r == 0 else None
+
+
+def fp64_roofline(wl, kkey, ne, ms, device):
+    """The plain form's element kernel against the FP64 pipe, from
+    algorithmic operation counts: the FP64 flops per element the reference
+    algorithm performs in the timed window (op-counting build of the CPU
+    oracle, committed in profiles/fp64_op_counts.json) x elements over the
+    kernel's measured time, against twice the measured FMA instruction rate
+    (an FMA is two flops).  The FP64 instructions the kernel executes per
+    element (ncu) are given beside, with their ratio to the algorithmic
+    operations."""
     pk = fp64_peak(device)
-    n = FP64_INSTR_PER_ELEMENT.get(kkey)
-    if not pk or not n:
+    cnt = profile_json("fp64_op_counts.json").get("windows", {}).get(wl, {}).get(kkey)
+    if not pk or not cnt:
         return None
-    ach = n * ne / (ms * 1e-3)
-    return {"bound": "fp64 pipe", "achieved": ach, "peak": pk, "unit": "FP64 thread instr/s",
-            "frac": ach / pk, "instr_per_element": n,
-            "peak_kind": "measured (rg_fp64_peak: dependent FMA chains, all SMs)"}
+    flops = cnt["flops"]
+    ach = flops * ne / (ms * 1e-3)
+    out = {"bound": "fp64 pipe", "achieved": ach, "peak": 2.0 * pk, "unit": "FP64 flop/s",
+           "frac": ach / (2.0 * pk), "flops_per_element": flops,
+           "ops_per_element": {k: cnt[k] for k in ("add", "mul", "div", "sqrt", "pow", "log",
+                                                   "exp", "cmp", "minmax")},
+           "counts_from": "profiles/fp64_op_counts.json (python oracle/opcount_report.py)",
+           "peak_kind": "measured: 2 x rg_fp64_peak (dependent FMA chains on all SMs)"}
+    ex = profile_json("element_kernel_ncu.json").get(wl, {}).get("f64", {})
+    if ex.get("fp64_instr_per_element"):
+        n = ex["fp64_instr_per_element"]
+        algo = sum(cnt[k] for k in ("add", "mul", "div", "sqrt", "pow", "log", "exp", "cmp",
+                                    "minmax"))
+        out["executed_fp64_instr_per_element"] = n
+        out["executed_over_algorithmic_ops"] = n / algo
+        out["fp64_pipe_frac_executed"] = n * ne / (ms * 1e-3) / pk
+    return out
 
 
-# DRAM bytes of one launch of the workload's element kernel
-# (dram__bytes_read.sum + dram__bytes_write.sum), from the ncu captures whose
-# commands and figures are in profiles/shell_kernel_crash_box_120k.md and
-# profiles/hexa_kernel_block128_jc.md
-NCU_TRAFFIC = {
-    "crash_box_120k_jc": {"f64": 73.9e6 + 33.6e6, "mixed": 42.9e6 + 0.9e6},
-    "hexa_block_128_jc": {"f64": 506.7e6 + 685.1e6, "mixed": 388.4e6 + 354.4e6},
-}
+def ncu_traffic(wl, form):
+    d = profile_json("element_kernel_ncu.json").get(wl, {}).get(form)
+    return (d["dram_read"] + d["dram_write"]) if d else None
 
 
-def run_ours(args, rank, world, local_rank):
-    from openradioss_gb300.engine import Engine, RG_PREC_FP64, RG_PREC_MIXED
-    wl = args.workload
-    model = WORKLOADS[wl]()
+def support_nodes(model):
+    """Nodes whose summed internal force is the model's impact force: the
+    fixed face of a hexa model, the row of a crash box at the wall."""
+    if model.hexa:
+        return np.nonzero(model.icodt != 0)[0]
+    z = model.X[2]
+    return np.nonzero(z <= z.min() + 1e-9)[0]
+
+
+def job_run(model, prec, cycles, device, printouts=JOB_PRINTOUTS):
+    """The configuration's full-length run (back-to-back graph launches, the
+    state evolving through contact and plasticity) in printout chunks, each
+    chunk timed with CUDA events on the library's stream (the printouts --
+    forces, energies, displacements -- fall between the timed spans)."""
+    from openradioss_gb300.engine import Engine
+    e = Engine(model, device=device, precision=prec)
+    sup = support_nodes(model)
+    every = max(1, cycles // printouts)
+    # displacements are kept at every dstride-th printout and the last
+    dstride = max(1, printouts // 10)
+    ms, curve, done, i = 0.0, [], 0, 0
+    with Clocks(device) as clk:
+        while done < cycles:
+            k = min(every, cycles - done)
+            ms += e.time_cycles(k)
+            done += k
+            f = e.forces()["F"]
+            en = e.energy()
+            keep_d = (i % dstride == dstride - 1) or done >= cycles
+            curve.append({"cycle": done, "reaction": float(abs(f[2, sup].sum())),
+                          "fmax": float(np.max(np.linalg.norm(f, axis=0))),
+                          "eint": en["eint"], "d": e.displacement() if keep_d else None})
+            i += 1
     ne = model.numels + model.numelc
-    hbm_peak, peak_kind = peaks()
-    out = {}
-    dist = world > 1
-    if dist:
-        import torch
-        import torch.distributed as tdist
+    out = dict(cycles=cycles, seconds=ms * 1e-3, element_updates_s=ne * cycles / (ms * 1e-3),
+               status=e.status(), clocks=clk.summary(), printout_every=every)
+    e.close()
+    return out, curve
 
-    def barrier():
-        if dist:
-            tdist.barrier()
 
-    def max_over_ranks(x):
-        return reduce_max(x, "cuda:%d" % local_rank) if dist else x
+def mixed_error(c64, c32):
+    """Mixed-form error against the FP64 run of the same job: relative
+    displacement error (final, and its largest over the printouts), peak
+    impact-force and peak nodal-force errors over the printouts, largest
+    internal-energy error, and the growth of the errors printout by
+    printout (all relative to the FP64 quantity's largest magnitude)."""
+    dmax = max(float(np.max(np.abs(c["d"]))) for c in c64 if c["d"] is not None) or 1.0
+    emax = max(abs(c["eint"]) for c in c64) or 1.0
+    rmax = max(c["reaction"] for c in c64) or 1.0
+    growth = []
+    for a, b in zip(c64, c32):
+        dd = (float(np.max(np.abs(b["d"] - a["d"]))) / dmax if a["d"] is not None
+              else None)
+        growth.append([a["cycle"], dd, abs(b["eint"] - a["eint"]) / emax,
+                       abs(b["reaction"] - a["reaction"]) / rmax])
+    p64r, p32r = max(c["reaction"] for c in c64), max(c["reaction"] for c in c32)
+    p64f, p32f = max(c["fmax"] for c in c64), max(c["fmax"] for c in c32)
+    return {"displacement_final": growth[-1][1],
+            "displacement_max": max(g[1] for g in growth if g[1] is not None),
+            "peak_impact_force": abs(p32r - p64r) / p64r if p64r else None,
+            "peak_nodal_force": abs(p32f - p64f) / p64f if p64f else None,
+            "internal_energy_max": max(g[2] for g in growth),
+            "peak_impact_force_n": p64r,
+            "growth_columns": ["cycle", "displacement", "internal_energy", "impact_force"],
+            "growth": [[g[0]] + [None if x is None else "%.3e" % x for x in g[1:]]
+                       for g in growth]}
 
-    forms = [RG_PREC_FP64, RG_PREC_MIXED] if args.forms == "both" else (
-        [RG_PREC_FP64] if args.forms == "f64" else [RG_PREC_MIXED])
+
+def measure_forms(wl, model, args, world, local_rank, forms, barrier, max_over_ranks):
+    """Cold-L2 timed cycles, warm back-to-back cycles and per-kernel times
+    of each arithmetic form, every measurement from the same state (W cycles
+    after set-up)."""
+    from openradioss_gb300.engine import Engine
+
     def fresh(prec):
-        # every measurement starts from the same state: W cycles after set-up
         e = Engine(model, device=local_rank, precision=prec)
         e.cycle(args.warmup)
         e.sync()
         return e
 
+    out = {}
     for prec in forms:
         eng = fresh(prec)
         barrier()
         with Clocks(local_rank) as clk:
-            # every timed cycle starts from cold L2 (256 MB written before it)
             ms = eng.time_cycles_cold(args.steps, L2_FLUSH_BYTES)
         ms = max_over_ranks(ms)
         st = eng.status()
+        dev_bytes = eng.info()["device_bytes"]
         eng.close()
         eng = fresh(prec)
         ms_warm = eng.time_cycles(args.steps)
         eng.close()
-        # per-kernel times (event-bracketed launches, same stream, cold L2)
         eng = fresh(prec)
         eng.time_cycles_cold(0, L2_FLUSH_BYTES)
         eng.set_timing(True)
@@ -232,10 +349,47 @@ def run_ours(args, rank, world, local_rank):
         eng.close()
         eb, nb, kkey = element_bytes(model, prec)
         out[prec] = dict(ms=ms, ms_warm=ms_warm, clocks=clk.summary(), kt=kt, status=st,
-                         elem_bytes=eb, node_bytes=nb, kkey=kkey)
-    # e2e: FORINT-level call with pinned host buffers (headline form), from
-    # the same state
-    eng = fresh(forms[0])
+                         elem_bytes=eb, node_bytes=nb, kkey=kkey, dev_bytes=dev_bytes)
+    return out
+
+
+def e2e_cycle_host(model, prec, args, local_rank, barrier, max_over_ranks):
+    """Whole cycles through rg_cycle_host with registered host buffers:
+    every step X, V (VR) go host -> device and X, V (VR), D come back.
+    Returns (seconds for K steps, h2d bytes, d2h bytes per step)."""
+    from openradioss_gb300.engine import Engine
+    e = Engine(model, device=local_rank, precision=prec)
+    e.cycle(args.warmup)
+    nd = e.nodes()
+    n = model.numnod
+    x = np.ascontiguousarray(nd["X"].T)
+    v = np.ascontiguousarray(nd["V"].T)
+    vr = np.ascontiguousarray(nd["VR"].T) if model.shells else None
+    d = np.empty((n, 3))
+    bufs = [a for a in (x, v, vr, d) if a is not None]
+    for a in bufs:
+        e.host_register(a)
+    for _ in range(3):
+        e.cycle_host(x, v, vr, x_out=x, v_out=v, vr_out=vr, d_out=d)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e.cycle_host(x, v, vr, x_out=x, v_out=v, vr_out=vr, d_out=d)
+    s = max_over_ranks(time.perf_counter() - t0)
+    for a in bufs:
+        e.host_unregister(a)
+    e.close()
+    nin = 3 if model.shells else 2
+    return s, nin * 24 * n, (nin + 1) * 24 * n
+
+
+def e2e_forint(model, prec, args, local_rank):
+    """The FORINT-level drop-in call (elements + PARITH/ON assembly; the
+    engine keeps its nodal update) with registered host buffers: seconds for
+    K calls."""
+    from openradioss_gb300.engine import Engine
+    eng = Engine(model, device=local_rank, precision=prec)
+    eng.cycle(args.warmup)
     nd = eng.nodes()
     x = np.ascontiguousarray(nd["X"].T)
     v = np.ascontiguousarray(nd["V"].T)
@@ -251,37 +405,89 @@ def run_ours(args, rank, world, local_rank):
     for a in bufs:
         eng.host_register(a)
     dt1 = eng.time()["dt2"]
-    for _ in range(max(1, args.warmup)):
+    for _ in range(3):
         eng.forint_step(x, v, dt1, vr=vr, f=f, stifn=stf, fr=fr, stifr=stfr)
-    barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         eng.forint_step(x, v, dt1, vr=vr, f=f, stifn=stf, fr=fr, stifr=stfr)
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    s = time.perf_counter() - t0
     for a in bufs:
         eng.host_unregister(a)
-    dev_bytes = eng.info()["device_bytes"]
     eng.close()
-    # the whole job of the configuration (its full cycle count, back to back
-    # graph launches, state evolving: contact, plasticity)
-    jobs = {}
-    if not args.no_job and args.forms == "both" and JOB_CYCLES.get(wl):
-        for prec in forms:
-            e = Engine(model, device=local_rank, precision=prec)
-            # the whole job is seconds long: its clock record has many samples
-            with Clocks(local_rank) as jclk:
-                jms = e.time_cycles(JOB_CYCLES[wl])
-            jobs[prec] = dict(cycles=JOB_CYCLES[wl], seconds=jms * 1e-3,
-                              element_updates_s=ne * JOB_CYCLES[wl] / (jms * 1e-3),
-                              status=e.status(), clocks=jclk.summary())
-            e.close()
+    return s
 
+
+def workload_summary(wl, args, device, with_jobs=True):
+    """One single-GPU configuration measured in both forms (cold-L2 cycles,
+    kernel times, element-kernel roofline) and, with_jobs, its full-length
+    job runs with the mixed form's error against the FP64 run."""
+    from openradioss_gb300.engine import RG_PREC_FP64, RG_PREC_MIXED
+    model = WORKLOADS[wl]()
+    ne = model.numels + model.numelc
+    hbm_peak, peak_kind = peaks()
+    res = measure_forms(wl, model, args, 1, device, [RG_PREC_FP64, RG_PREC_MIXED],
+                        lambda: None, lambda x: x)
+    out = {"config": workload_config(wl, model, 1)}
+    for prec, name in ((RG_PREC_FP64, "f64"), (RG_PREC_MIXED, "mixed")):
+        r = res[prec]
+        k = r["kt"][r["kkey"]]
+        ach = r["elem_bytes"] * ne / (k * 1e-3) / 1e9
+        out[name] = {"element_updates_s": ne * args.steps / (r["ms"] * 1e-3),
+                     "ms_per_step": r["ms"] / args.steps, "kernel_ms": r["kt"],
+                     "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak,
+                                  "unit": "GB/s", "frac": ach / hbm_peak,
+                                  "traffic": ncu_traffic(wl, name),
+                                  "kernel": "%s_kernel<%s>" % (r["kkey"], "double" if prec == 0
+                                                               else "float"),
+                                  "bytes_per_element": r["elem_bytes"], "peak_kind": peak_kind},
+                     "status": r["status"]}
+    out["mixed_speedup"] = out["mixed"]["element_updates_s"] / out["f64"]["element_updates_s"]
+    kk = res[RG_PREC_FP64]["kkey"]
+    out["fp64_roofline"] = fp64_roofline(wl, kk, ne, res[RG_PREC_FP64]["kt"][kk], device)
+    if with_jobs and JOB_CYCLES.get(wl):
+        j64, c64 = job_run(model, RG_PREC_FP64, JOB_CYCLES[wl], device)
+        j32, c32 = job_run(model, RG_PREC_MIXED, JOB_CYCLES[wl], device)
+        out["job"] = {"f64": j64, "mixed": j32, "mixed_speedup": j64["seconds"] / j32["seconds"],
+                      "mixed_error_vs_f64": mixed_error(c64, c32)}
+    return out
+
+
+def run_ours(args, rank, world, local_rank):
+    from openradioss_gb300.engine import RG_PREC_FP64, RG_PREC_MIXED
+    wl = args.workload
+    model = WORKLOADS[wl]()
+    ne = model.numels + model.numelc
+    hbm_peak, peak_kind = peaks()
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+
+    def max_over_ranks(x):
+        return reduce_max(x, "cuda:%d" % local_rank) if dist else x
+
+    forms = [RG_PREC_FP64, RG_PREC_MIXED] if args.forms == "both" else (
+        [RG_PREC_FP64] if args.forms == "f64" else [RG_PREC_MIXED])
+    out = measure_forms(wl, model, args, world, local_rank, forms, barrier, max_over_ranks)
     if args.forms != "both":
         res = out[forms[0]]
-        line = {"metric": "element-updates/s", "forms": args.forms,
-                "value": world * ne * args.steps / (res["ms"] * 1e-3),
-                "kernel_ms": res["kt"], "e2e_s": e2e_s}
-        return line
+        return {"metric": "element-updates/s", "forms": args.forms,
+                "value": world * ne * args.steps / (res["ms"] * 1e-3), "kernel_ms": res["kt"]}
+    # e2e: whole cycles with host node buffers, both forms (headline: FP64)
+    e2e = {}
+    for prec in forms:
+        s, hb, db = e2e_cycle_host(model, prec, args, local_rank, barrier, max_over_ranks)
+        e2e[prec] = dict(s=s, h2d=hb, d2h=db)
+    forint_s = e2e_forint(model, RG_PREC_FP64, args, local_rank)
+    jobs = {}
+    if not args.no_job and JOB_CYCLES.get(wl):
+        j64, c64 = job_run(model, RG_PREC_FP64, JOB_CYCLES[wl], local_rank)
+        j32, c32 = job_run(model, RG_PREC_MIXED, JOB_CYCLES[wl], local_rank)
+        jobs = {"f64": j64, "mixed": j32, "mixed_speedup": j64["seconds"] / j32["seconds"],
+                "mixed_error_vs_f64": mixed_error(c64, c32)}
     res64, res32 = out[RG_PREC_FP64], out[RG_PREC_MIXED]
     value = replica_value(ne * args.steps, world, res64["ms"] * 1e-3)
     value32 = replica_value(ne * args.steps, world, res32["ms"] * 1e-3)
@@ -290,8 +496,7 @@ def run_ours(args, rank, world, local_rank):
     ach = res64["elem_bytes"] * ne / (k64 * 1e-3) / 1e9
     k32 = res32["kt"][kk]
     ach32 = res32["elem_bytes"] * ne / (k32 * 1e-3) / 1e9
-    traffic = NCU_TRAFFIC.get(wl, {}).get("f64")
-    traffic32 = NCU_TRAFFIC.get(wl, {}).get("mixed")
+    groups = len(model.hexa) + len(model.shells)
     line = {
         "metric": "element-updates/s",
         "value": value,
@@ -305,30 +510,27 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded mesh and velocity field of the named shape)",
-        "config": {"workload": wl, "elements": ne, "nodes": model.numnod,
-                   "law": "LAW2 Johnson-Cook" if (model.shells or model.hexa[0].mat["mtn"] == 2)
-                   else "LAW1",
-                   "formulation": ("one-point hexa Isolid=1 Iframe=1 Ismstr=4, viscous "
-                                   "hourglass" if model.hexa else
-                                   "Belytschko-Tsay shell Ishell=1 Ismstr=4 Ithick=1 NPT=5 "
-                                   "Iplas=1, planar sliding rigid wall") + ", PARITH/ON",
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "L2 flushed (256 MB written) before every timed cycle; model "
-                         "state %.2f GB" % (dev_bytes / 1e9),
-                   "state": "every measurement starts %d cycles after set-up" % args.warmup},
-        "e2e": {"value": world * ne * args.steps / e2e_s, "unit": "element-updates/s",
-                "transfer": "inputs: registered host buffers read in place by the upload "
-                            "kernel; outputs: DMA copies from the device staging buffer",
-                "h2d_bytes_per_step": (3 if model.shells else 2) * 3 * 8 * model.numnod,
-                "d2h_bytes_per_step": (8 if model.shells else 4) * 8 * model.numnod},
-        "gpu_launches": (len(model.hexa) + len(model.shells) + 2) * args.steps,
+        "config": workload_config(wl, model, world),
+        "e2e": {"value": world * ne * args.steps / e2e[RG_PREC_FP64]["s"],
+                "unit": "element-updates/s",
+                "call": "rg_cycle_host: whole cycle (elements, PARITH/ON assembly, time step, "
+                        "nodal update) with host node buffers",
+                "transfer": "inputs X, V, VR read in place from registered (pinned) host "
+                            "buffers by the upload kernel; outputs X, V, VR, D by DMA copies",
+                "h2d_bytes_per_step": e2e[RG_PREC_FP64]["h2d"],
+                "d2h_bytes_per_step": e2e[RG_PREC_FP64]["d2h"],
+                "mixed": world * ne * args.steps / e2e[RG_PREC_MIXED]["s"],
+                "forint_level_f64": world * ne * args.steps / forint_s},
+        # per timed cycle: one element kernel per group + one node kernel
+        "gpu_launches": (groups + 1) * args.steps,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": ach / hbm_peak, "traffic": traffic, "traffic_unit": "bytes per launch (ncu)",
+                     "frac": ach / hbm_peak, "traffic": ncu_traffic(wl, "f64"),
+                     "traffic_unit": "DRAM bytes per launch (ncu capture, profiles/)",
                      "kernel": "%s_kernel<double>" % kk,
                      "bytes_per_element": res64["elem_bytes"], "ms_per_launch": k64,
                      "peak_kind": peak_kind,
-                     "note": "FP64 form is FP64-pipe bound on GB300; see fp64_roofline"},
-        "fp64_roofline": fp64_roofline(kk, ne, k64, local_rank),
+                     "note": "the FP64 form is bound by the FP64 pipe on GB300: fp64_roofline"},
+        "fp64_roofline": fp64_roofline(wl, kk, ne, k64, local_rank),
         "kernel_ms": res64["kt"],
         "l2_warm_back_to_back": {"f64": world * ne * args.steps / (res64["ms_warm"] * 1e-3),
                                  "mixed": world * ne * args.steps / (res32["ms_warm"] * 1e-3)},
@@ -336,50 +538,31 @@ def run_ours(args, rank, world, local_rank):
                           "kernel_ms": res32["kt"],
                           "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm_peak,
                                        "unit": "GB/s", "frac": ach32 / hbm_peak,
-                                       "traffic": traffic32,
+                                       "traffic": ncu_traffic(wl, "mixed"),
                                        "bytes_per_element": res32["elem_bytes"]}},
+        "device_bytes": res64["dev_bytes"],
         "clocks": res64["clocks"],
         "device_status": [res64["status"], res32["status"]],
     }
     if jobs:
-        line["job"] = {("f64" if p == RG_PREC_FP64 else "mixed"): j for p, j in jobs.items()}
-        if len(jobs) == 2:
-            line["job"]["mixed_speedup"] = jobs[RG_PREC_FP64]["seconds"] / jobs[RG_PREC_MIXED]["seconds"]
+        line["job"] = jobs
     if rank == 0 and not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(wl, args.cpu_sample)
+        line["cpu_baseline"] = cpu_baseline(wl, args.warmup, args.steps)
     return line
 
-
-L2_FLUSH_BYTES = 256 << 20  # twice the GB300 L2
-
-# FP64 thread instructions per element of the plain form's element kernels at
-# the benchmark's state (5 cycles after set-up), counted with ncu
-# (smsp__sass_thread_inst_executed_op_fp64_pred_on / elements per launch).
-FP64_INSTR_PER_ELEMENT = {"shell": 967.0, "hexa": 1030.0}
-
-
-def fp64_peak(device=0):
-    """Measured FP64 fused multiply-add rate of the device (thread instr/s)."""
-    import ctypes as C
-    from openradioss_gb300 import _lib
-    v = C.c_double()
-    r = _lib.lib().rg_fp64_peak(device, C.byref(v))
-    return v.value if r == 0 else None
 
 SWEEP_JOBS = 64
 SWEEP_CYCLES_PER_JOB = 2000
 
 
-def run_sweep(args, njobs=SWEEP_JOBS, timed_cycles=None, device=0):
+def run_sweep(args, njobs=SWEEP_JOBS, cycles=SWEEP_CYCLES_PER_JOB, device=0):
     """Batched crash-box sweep: njobs seeded variants (5k-60k shells each)
     stepped together in one persistent kernel per cycle (autotuned launch
-    shape), against the same jobs run one after another, alone, in the plain
-    FP64 form.  A job is SWEEP_CYCLES_PER_JOB cycles; the timed region is
-    timed_cycles cycles of every job and jobs/h is scaled from it."""
+    shape), against the same jobs run one after another alone, each form
+    at full length (cycles per job, from a fresh model)."""
     from openradioss_gb300.batch import Batch
     from openradioss_gb300.engine import Engine
     models = M.crash_box_sweep(njobs)
-    K = timed_cycles or args.steps
     ne = sum(m.numels + m.numelc for m in models)
     hbm_peak, peak_kind = peaks()
     seq = {}
@@ -387,60 +570,69 @@ def run_sweep(args, njobs=SWEEP_JOBS, timed_cycles=None, device=0):
         tot = 0.0
         for m in models:
             e = Engine(m, device=device, precision=prec)
-            e.cycle(args.warmup)
-            tot += e.time_cycles(K)
+            tot += e.time_cycles(cycles)
             e.close()
         seq[prec] = tot
     bat = {}
     for prec in (0, 1):
+        # autotune on a throw-away copy of the jobs, then time fresh jobs
         es = [Engine(m, device=device, precision=prec) for m in models]
         b = Batch(device)
         for e in es:
             b.add(e)
-        b.cycle(args.warmup)
-        b.sync()
         cfg = b.autotune(trial_cycles=3)
-        b.cycle(args.warmup)
+        b.close()
+        for e in es:
+            e.close()
+        es = [Engine(m, device=device, precision=prec) for m in models]
+        b = Batch(device)
+        for e in es:
+            b.add(e, cycles)
+        b.set_config(cfg["ktile"], cfg["knode"], cfg["blocks_per_sm"], cfg["schedule"])
         with Clocks(device) as clk:
-            ms = b.time_cycles(K)
+            ms = b.time_cycles(cycles)
         prog, st = b.progress()
         bat[prec] = dict(ms=ms, cfg=cfg, status=st, clocks=clk.summary(),
-                         status_jobs=sum(e.status() for e in es))
+                         status_jobs=sum(e.status() for e in es),
+                         all_at_target=all(p == cycles for p in prog.values()))
         b.close()
         for e in es:
             e.close()
 
     def jobs_h(ms):
-        return njobs * 3600.0 / (ms * 1e-3 * SWEEP_CYCLES_PER_JOB / K)
+        return njobs * 3600.0 / (ms * 1e-3)
 
     eb32 = sum(element_bytes(m, 1)[0] * m.numelc for m in models)
-    ach = eb32 / (bat[1]["ms"] * 1e-3 / K) / 1e9
+    ach = eb32 / (bat[1]["ms"] * 1e-3 / cycles) / 1e9
     return {
         "metric": "jobs/h",
         "value": jobs_h(bat[1]["ms"]),
         "unit": "jobs/h",
         "n_gpus": 1,
-        "steps": K,
-        "warmup": args.warmup,
-        "ms_per_step": bat[1]["ms"] / K,
+        "steps": cycles,
+        "warmup": 0,
+        "ms_per_step": bat[1]["ms"] / cycles,
         "higher_is_better": True,
         "dtype": "f32 element / f64 nodal",
         "data": "synthetic (64 seeded crash-box variants)",
         "config": {"workload": "crash_box_sweep_64", "jobs": njobs, "elements": ne,
                    "elements_per_job": [min(m.numelc for m in models),
                                         max(m.numelc for m in models)],
-                   "cycles_per_job": SWEEP_CYCLES_PER_JOB,
-                   "note": "jobs/h scaled from %d timed cycles of every job" % K},
+                   "cycles_per_job": cycles,
+                   "timing": "every job run at full length from a fresh model, in every "
+                             "arm; device time (CUDA events)"},
         "batched_mixed": {"jobs_h": jobs_h(bat[1]["ms"]),
-                          "element_updates_s": ne * K / (bat[1]["ms"] * 1e-3),
-                          "autotuned": bat[1]["cfg"]},
+                          "element_updates_s": ne * cycles / (bat[1]["ms"] * 1e-3),
+                          "autotuned": bat[1]["cfg"], "all_at_target": bat[1]["all_at_target"]},
         "batched_fp64": {"jobs_h": jobs_h(bat[0]["ms"]),
-                         "element_updates_s": ne * K / (bat[0]["ms"] * 1e-3),
-                         "autotuned": bat[0]["cfg"]},
+                         "element_updates_s": ne * cycles / (bat[0]["ms"] * 1e-3),
+                         "autotuned": bat[0]["cfg"], "all_at_target": bat[0]["all_at_target"]},
         "sequential_fp64": {"jobs_h": jobs_h(seq[0]),
-                            "element_updates_s": ne * K / (seq[0] * 1e-3)},
+                            "element_updates_s": ne * cycles / (seq[0] * 1e-3)},
         "sequential_mixed": {"jobs_h": jobs_h(seq[1]),
-                             "element_updates_s": ne * K / (seq[1] * 1e-3)},
+                             "element_updates_s": ne * cycles / (seq[1] * 1e-3)},
+        "batching_gain_fp64": seq[0] / bat[0]["ms"],
+        "batching_gain_mixed": seq[1] / bat[1]["ms"],
         "speedup_vs_sequential_plain": seq[0] / bat[1]["ms"],
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": ach / hbm_peak, "peak_kind": peak_kind,
@@ -461,25 +653,27 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
     """Serving stream: njobs seeded requests (50/50 shell crash boxes of
     2k-150k elements and hexa impact blocks of 2k-200k elements, 2,000-20,000
     cycles each) arriving as a Poisson process of SERVE_RATE jobs/s, admitted
-    by HBM budget into a continuously batched mixed-form run.  Beside it, the
-    same jobs as sequential plain FP64 runs alone (GPU time of each job from a
-    timed 50-cycle sample scaled to its cycle count)."""
+    by HBM budget into a continuously batched mixed-form run.  Beside it the
+    same jobs run alone one after another at full length, in the plain FP64
+    form and in the mixed form (device time of every job)."""
     from openradioss_gb300.engine import Engine
     from openradioss_gb300.serving import Server, poisson_arrivals
     jobs = [M.serving_job(k) for k in range(njobs)]
     arr = poisson_arrivals(njobs, SERVE_RATE, seed=7)
-    seq = 0.0
-    for m, n in jobs:
-        e = Engine(m, device=device, precision=0)
-        e.cycle(3)
-        seq += e.time_cycles(50) * 1e-3 * n / 50.0
-        e.close()
+    seq = {}
+    for prec in (0, 1):
+        tot = 0.0
+        for m, n in jobs:
+            e = Engine(m, device=device, precision=prec)
+            tot += e.time_cycles(n) * 1e-3
+            e.close()
+        seq[prec] = tot
     srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device)
     with Clocks(device) as clk:
         st = srv.run([(k, m, n, float(a)) for k, ((m, n), a) in enumerate(zip(jobs, arr))])
-    bad = sum(1 for r in srv.done if r.result.get("status", 0))
+    bad = sum(1 for r in srv.done if r.result.get("status", 0)) + len(srv.failed)
     srv.close()
-    seq_jobs_h = 3600.0 * njobs / seq
+    seq_jobs_h = {p: 3600.0 * njobs / seq[p] for p in seq}
     ne = [m.numels + m.numelc for m, _ in jobs]
     return {
         "metric": "jobs/h",
@@ -492,64 +686,60 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
         "config": {"workload": "serving_mix", "jobs": njobs, "arrival_rate_per_s": SERVE_RATE,
                    "elements_per_job": [min(ne), max(ne)],
                    "cycles_per_job": [min(n for _, n in jobs), max(n for _, n in jobs)],
-                   "hbm_budget_gb": SERVE_BUDGET / 2 ** 30, "step_cycles": 100},
+                   "hbm_budget_gb": SERVE_BUDGET / 2 ** 30, "step_cycles": 100,
+                   "sequential": "every job run alone at full length (device time)"},
+        "completed": st["completed"], "failed": st["failed"],
         "p50_latency_s": st["p50_latency_s"],
         "p99_latency_s": st["p99_latency_s"],
         "mean_latency_s": st["mean_latency_s"],
         "makespan_s": st["makespan_s"],
         "element_updates_s": st["element_updates"] / st["makespan_s"],
         "max_used_gb": st["max_used_bytes"] / 2 ** 30,
-        "sequential_fp64_jobs_h": seq_jobs_h,
-        "speedup_vs_sequential_plain": st["jobs_per_h"] / seq_jobs_h,
+        "sequential_fp64_jobs_h": seq_jobs_h[0],
+        "sequential_mixed_jobs_h": seq_jobs_h[1],
+        "speedup_vs_sequential_plain": st["jobs_per_h"] / seq_jobs_h[0],
+        "speedup_vs_sequential_mixed": st["jobs_per_h"] / seq_jobs_h[1],
         "jobs_with_device_status": bad,
         "clocks": clk.summary(),
     }
 
 
-def cpu_baseline(wl, sample_s, threads=None):
-    """Time the CPU restatement (oracle/) on the host cores: a bounded
-    sample of the same workload."""
+def cpu_window(wl, warmup, steps, threads=None):
+    """Time the CPU restatement (oracle/) on the host cores over the GPU's
+    timed window: a fresh model, W warm-up cycles, then K timed cycles."""
     from oracle.oracle import OracleModel
     model = WORKLOADS[wl]()
     nt = threads or os.cpu_count() or 1
     o = OracleModel(model, nthreads=nt)
+    o.cycle(warmup)
     t0 = time.perf_counter()
-    o.cycle(1)
-    t1 = time.perf_counter() - t0
-    # bounded sample: about sample_s seconds of CPU work
-    n = max(3, min(5000, int(sample_s / max(t1, 1e-6))))
-    t0 = time.perf_counter()
-    o.cycle(n)
+    o.cycle(steps)
     dt = time.perf_counter() - t0
     ne = model.numels + model.numelc
-    return {"value": ne * n / dt, "unit": "element-updates/s", "cores": nt,
-            "kind": "port", "sample": "%s, %d cycles after 1 warm-up cycle (%.1f s)" % (wl, n, dt)}
+    return model, nt, dt, ne * steps / dt
+
+
+def cpu_baseline(wl, warmup, steps):
+    model, nt, dt, v = cpu_window(wl, warmup, steps)
+    return {"value": v, "unit": "element-updates/s", "cores": nt, "kind": "port",
+            "sample": "%s, cycles %d-%d of a fresh model (the GPU's timed window), %.1f s"
+                      % (wl, warmup + 1, warmup + steps, dt)}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    from oracle.oracle import OracleModel
     wl = args.workload
-    model = WORKLOADS[wl]()
-    nt = os.cpu_count() or 1
-    o = OracleModel(model, nthreads=nt)
-    o.cycle(1)
-    # each step: one cycle of the workload (bounded sample)
-    for _ in range(args.warmup):
-        o.cycle(1)
-    t0 = time.perf_counter()
-    o.cycle(args.steps)
-    dt = time.perf_counter() - t0
-    v = (model.numels + model.numelc) * args.steps / dt
+    model, nt, dt, v = cpu_window(wl, args.warmup, args.steps)
     return {"metric": "element-updates/s", "value": v, "unit": "element-updates/s",
             "impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl, "elements": model.numels + model.numelc,
-                       "nodes": model.numnod},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh and velocity "
+            "field of the named shape)",
+            "config": workload_config(wl, model, world),
             "cpu_baseline": {"value": v, "unit": "element-updates/s", "cores": nt, "kind": "port",
-                             "sample": "%s, %d cycles" % (wl, args.steps)},
+                             "sample": "%s, cycles %d-%d of a fresh model" % (
+                                 wl, args.warmup + 1, args.warmup + args.steps)},
             "e2e": {"value": v, "unit": "element-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "note": "reference engine not buildable here (no Fortran compiler); "
@@ -569,8 +759,8 @@ def main():
                     help="skip the full-length job runs of the configuration")
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the batched-sweep and serving summaries of the default run")
-    ap.add_argument("--cpu-sample", type=float, default=15.0,
-                    help="seconds of CPU work in the cpu_baseline sample")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other single-GPU configurations' summaries")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="both", choices=["both", "f64", "mixed"],
                     help="arithmetic forms to run (profiling runs pick one)")
@@ -598,16 +788,22 @@ def main():
             print(json.dumps(line, default=float), flush=True)
         return
     line = run_ours(args, rank, world, local_rank)
-    if rank == 0 and world == 1 and not args.no_sweep:
-        sw = run_sweep(args, timed_cycles=20)
-        line["batched_sweep"] = {k: sw[k] for k in (
-            "batched_mixed", "batched_fp64", "sequential_fp64", "sequential_mixed",
-            "speedup_vs_sequential_plain", "config", "device_status")}
-        sv = run_serving(args)
-        line["serving"] = {k: sv[k] for k in (
-            "value", "unit", "p50_latency_s", "p99_latency_s", "sequential_fp64_jobs_h",
-            "speedup_vs_sequential_plain", "element_updates_s", "config",
-            "jobs_with_device_status")}
+    if rank == 0 and world == 1 and args.forms == "both":
+        if not args.no_configs:
+            line["configs"] = {w: workload_summary(w, args, local_rank, not args.no_job)
+                               for w in WORKLOADS if w != args.workload}
+        if not args.no_sweep:
+            sw = run_sweep(args)
+            line["batched_sweep"] = {k: sw[k] for k in (
+                "value", "unit", "batched_mixed", "batched_fp64", "sequential_fp64",
+                "sequential_mixed", "batching_gain_fp64", "batching_gain_mixed",
+                "speedup_vs_sequential_plain", "config", "device_status", "roofline")}
+            sv = run_serving(args)
+            line["serving"] = {k: sv[k] for k in (
+                "value", "unit", "completed", "failed", "p50_latency_s", "p99_latency_s",
+                "sequential_fp64_jobs_h", "sequential_mixed_jobs_h",
+                "speedup_vs_sequential_plain", "speedup_vs_sequential_mixed",
+                "element_updates_s", "makespan_s", "config", "jobs_with_device_status")}
     if rank == 0:
         print(json.dumps(line, default=float), flush=True)
     if world > 1:

@@ -165,6 +165,22 @@ int rg_synchronize(rg_ctx *ctx);
 int rg_forint_step(rg_ctx *ctx, const double *x, const double *v,
                    const double *vr, double dt1, double *f, double *stifn,
                    double *fr, double *stifr, double *dt2t, int *neltst);
+/* Whole cycle with host node buffers, for an engine that keeps X, V on the
+ * host for its other work (outputs, contact) but lets the device do the
+ * complete explicit cycle: x, v (and vr) -- both or neither -- replace the
+ * device's node positions and velocities, one cycle of rg_cycle runs
+ * (elements, PARITH/ON assembly, RESOL time step, ACCELE, BCS, rigid walls,
+ * VELOCITY, DEPLA), and the new X, V (VR, D = displacement) are written to
+ * the *_out buffers (any may be NULL; they may alias the inputs), *dt2 = the
+ * cycle's step.  Synchronous.  The device keeps the time-step record and the
+ * element state.  In the mixed form the element volumes are re-anchored to
+ * the given coordinates, as in rg_forint_step.  Registered host buffers
+ * (rg_host_register) are read in place.  The reference's GPU shell path
+ * moves the same arrays each cycle (shell_gpu_global_upload_nodes,
+ * shell_gpu_driver.cu:149-185) but leaves the nodal update on the host. */
+int rg_cycle_host(rg_ctx *ctx, const double *x, const double *v, const double *vr,
+                  double *x_out, double *v_out, double *vr_out, double *d_out,
+                  double *dt2);
 int rg_host_register(rg_ctx *ctx, void *ptr, unsigned long long bytes);
 int rg_host_unregister(rg_ctx *ctx, void *ptr);
 

@@ -36,6 +36,7 @@ SIGNATURES = [
     ("rg_cycle", _ip, [_vp, _ip]),
     ("rg_synchronize", _ip, [_vp]),
     ("rg_forint_step", _ip, [_vp, _vp, _vp, _vp, _dp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("rg_cycle_host", _ip, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("rg_host_register", _ip, [_vp, _vp, C.c_ulonglong]),
     ("rg_host_unregister", _ip, [_vp, _vp]),
     ("rg_download_nodes", _ip, [_vp, _vp, _vp, _vp, _vp]),

@@ -339,7 +339,9 @@ __global__ void upload_nodes_kernel(NodeView N, const double *__restrict__ x,
                                     const double *__restrict__ vr, int mixed,
                                     Time *__restrict__ T, double dt1) {
   const int i = blockIdx.x * NODE_NT + threadIdx.x;
-  if (i == 0) T->dt2 = dt1;  // DT1 of this call: the element kernels read Time::dt2
+  // DT1 of a FORINT-level call (the element kernels read Time::dt2); a
+  // whole-cycle upload passes dt1 < 0 and keeps the device's time step
+  if (i == 0 && dt1 >= 0.0) T->dt2 = dt1;
   if (i >= N.numnod) return;
   dbl4 a = N.X4[i], b = N.V4[i];
   a.x = x[3 * i];
@@ -1268,6 +1270,72 @@ int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
   if (dt2t) *dt2t = c->h_time->dt2t;
   if (neltst) *neltst = c->h_time->neltst;
+  return RG_OK;
+}
+
+// Whole device cycle with host node buffers: X, V (VR) uploaded as in
+// rg_forint_step, one cycle of the captured graph (elements, PARITH/ON
+// assembly, time step, nodal update), X, V (VR, D) and the cycle's step
+// returned through the staging buffer by DMA copies.
+int rg_cycle_host(rg_ctx *c, const double *x, const double *v, const double *vr,
+                  double *x_out, double *v_out, double *vr_out, double *d_out, double *dt2) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  if ((x == nullptr) != (v == nullptr))
+    return fail(c, RG_E_ARG, "rg_cycle_host: give both X and V, or neither");
+  if (c->timing) return fail(c, RG_E_STATE, "rg_cycle_host: event timing is on");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  const int n = c->numnod;
+  const int nb = (n + NODE_NT - 1) / NODE_NT;
+  const size_t n3 = 3 * (size_t)n;
+  double *st = c->d_stage;
+  if (x) {
+    const bool rot_in = vr && c->rot;
+    const double *dx = device_view(x), *dv = device_view(v);
+    const double *dvr = rot_in ? device_view(vr) : nullptr;
+    if (!dx) {
+      RG_CUDA(c, cudaMemcpyAsync(st, x, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      dx = st;
+    }
+    if (!dv) {
+      RG_CUDA(c, cudaMemcpyAsync(st + n3, v, n3 * sizeof(double), cudaMemcpyHostToDevice,
+                                 c->stream));
+      dv = st + n3;
+    }
+    if (rot_in && !dvr) {
+      RG_CUDA(c, cudaMemcpyAsync(st + 2 * n3, vr, n3 * sizeof(double), cudaMemcpyHostToDevice,
+                                 c->stream));
+      dvr = st + 2 * n3;
+    }
+    upload_nodes_kernel<<<nb, NODE_NT, 0, c->stream>>>(
+        c->nv, dx, dv, dvr, c->prec == RG_PREC_MIXED ? 1 : 0, c->d_time, -1.0);
+    // the mixed form's FP64 element volumes follow the given coordinates
+    if (c->prec == RG_PREC_MIXED && c->numels > 0)
+      launch_hexa_prev_volume(c->h32, c->nv, c->d_time, c->stream);
+  }
+  RG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+  struct {
+    double *dst;
+    dbl4 *src;
+  } items[4] = {{x_out, c->nv.X4}, {v_out, c->nv.V4}, {vr_out, c->rot ? c->nv.VR4 : nullptr},
+                {d_out, c->nv.D4}};
+  for (int k = 0; k < 4; k++) {
+    if (!items[k].dst) continue;
+    double *sk = st + k * n3;  // 12 * numnod doubles of staging: one slice per array
+    if (!items[k].src)
+      RG_CUDA(c, cudaMemsetAsync(sk, 0, n3 * sizeof(double), c->stream));
+    else if (items[k].src == c->nv.D4 && c->prec == RG_PREC_MIXED)
+      unpack_disp_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, c->nv.X4, c->nv.D4, sk);
+    else
+      unpack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, items[k].src, sk);
+    RG_CUDA(c, cudaMemcpyAsync(items[k].dst, sk, n3 * sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+  }
+  RG_CUDA(c, cudaMemcpyAsync(c->h_time, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost,
+                             c->stream));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  RG_CUDA(c, cudaGetLastError());
+  if (dt2) *dt2 = c->h_time->dt2;
   return RG_OK;
 }
 

@@ -151,6 +151,19 @@ class Engine:
                                         C.byref(el)), "rg_forint_step")
         return f, stifn, dt2t.value, el.value
 
+    def cycle_host(self, x=None, v=None, vr=None, x_out=None, v_out=None, vr_out=None,
+                   d_out=None):
+        """One whole cycle with host node buffers (rg_cycle_host): x, v (vr)
+        as (N, 3) arrays replace the device's nodes when given; the new
+        X, V (VR, D) go to the *_out arrays given.  Returns the cycle's
+        step."""
+        if self.elements_only:
+            raise RgError("an elements_only engine runs forint_step only")
+        dt2 = C.c_double()
+        self._chk(self.L.rg_cycle_host(self.h, _p(x), _p(v), _p(vr), _p(x_out), _p(v_out),
+                                       _p(vr_out), _p(d_out), C.byref(dt2)), "rg_cycle_host")
+        return dt2.value
+
     def host_register(self, a):
         self._chk(self.L.rg_host_register(self.h, _p(a), a.nbytes), "rg_host_register")
 
@@ -164,6 +177,13 @@ class Engine:
         self._chk(self.L.rg_download_nodes(self.h, _p(out["X"]), _p(out["V"]), _p(out["D"]),
                                            _p(out["VR"])), "rg_download_nodes")
         return {k: a.reshape(n, 3).T.copy() for k, a in out.items()}
+
+    def displacement(self):
+        """D(3, N): the nodes' displacement from their initial position."""
+        n = self.model.numnod
+        d = np.zeros(3 * n)
+        self._chk(self.L.rg_download_nodes(self.h, None, None, _p(d), None), "rg_download_nodes")
+        return d.reshape(n, 3).T.copy()
 
     def forces(self):
         n = self.model.numnod

@@ -17,7 +17,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "_build", "librg_oracle.so")
+_LIB_COUNT = os.path.join(_HERE, "_build", "librg_oracle_count.so")
 _lib = None
+_lib_count = None
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -35,7 +37,25 @@ def lib():
     global _lib
     if _lib is None:
         build()
-        L = C.CDLL(_LIB)
+        _lib = _declare(C.CDLL(_LIB))
+    return _lib
+
+
+def count_lib():
+    """The op-counting build of the oracle (rg_opcount.h): same entry points
+    plus or_opcount_get / or_opcount_reset; run it with one thread."""
+    global _lib_count
+    if _lib_count is None:
+        subprocess.run(["make", "-s", "-C", _HERE, "opcount"], check=True)
+        L = _declare(C.CDLL(_LIB_COUNT))
+        L.or_opcount_get.argtypes = [C.c_void_p]
+        L.or_opcount_reset.argtypes = []
+        _lib_count = L
+    return _lib_count
+
+
+def _declare(L):
+    if True:
         vp = C.c_void_p
         L.or_model_new.restype = vp
         L.or_model_new.argtypes = [C.c_int, _dp, _dp, _dp, _ip]
@@ -65,8 +85,7 @@ def lib():
         L.or_set_forces.argtypes = [vp] + [C.c_void_p] * 4 + [C.c_double, C.c_int]
         L.or_cload_add.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                    _dp, _dp]
-        _lib = L
-    return _lib
+    return L
 
 
 def _ptr(a):
@@ -76,8 +95,9 @@ def _ptr(a):
 class OracleModel:
     """A model stepped by the CPU oracle."""
 
-    def __init__(self, model, nthreads=None):
-        L = lib()
+    def __init__(self, model, nthreads=None, library=None):
+        L = library or lib()
+        self.L = L
         self.model = model
         n = model.numnod
         X = np.ascontiguousarray(model.X.T.reshape(-1))
@@ -133,11 +153,11 @@ class OracleModel:
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().or_model_free(self.h)
+            self.L.or_model_free(self.h)
             self.h = None
 
     def cycle(self, n=1):
-        return lib().or_cycle(self.h, n)
+        return self.L.or_cycle(self.h, n)
 
     def skyline(self):
         m = self.model
@@ -145,14 +165,14 @@ class OracleModel:
         iads = np.zeros(8 * max(m.numels, 1), np.int32)
         iadc = np.zeros(4 * max(m.numelc, 1), np.int32)
         lsky = np.zeros(1, np.int32)
-        lib().or_get_skyline(self.h, _ptr(adsky), _ptr(iads), _ptr(iadc), _ptr(lsky))
+        self.L.or_get_skyline(self.h, _ptr(adsky), _ptr(iads), _ptr(iadc), _ptr(lsky))
         return adsky, iads[:8 * m.numels], iadc[:4 * m.numelc], int(lsky[0])
 
     def nodes(self):
         n = self.model.numnod
         out = {k: np.zeros(3 * n) for k in ("X", "V", "D", "VR", "F", "FR")}
         out["STIFN"] = np.zeros(n)
-        lib().or_get_nodes(self.h, _ptr(out["X"]), _ptr(out["V"]), _ptr(out["D"]),
+        self.L.or_get_nodes(self.h, _ptr(out["X"]), _ptr(out["V"]), _ptr(out["D"]),
                            _ptr(out["VR"]), _ptr(out["F"]), _ptr(out["STIFN"]),
                            _ptr(out["FR"]))
         for k in ("X", "V", "D", "VR", "F", "FR"):
@@ -162,27 +182,27 @@ class OracleModel:
     def time(self):
         tt, dt1, dt2 = (np.zeros(1) for _ in range(3))
         nc, el = np.zeros(1, np.int32), np.zeros(1, np.int32)
-        lib().or_get_time(self.h, _ptr(tt), _ptr(dt1), _ptr(dt2), _ptr(nc), _ptr(el))
+        self.L.or_get_time(self.h, _ptr(tt), _ptr(dt1), _ptr(dt2), _ptr(nc), _ptr(el))
         return dict(tt=tt[0], dt1=dt1[0], dt2=dt2[0], ncycle=int(nc[0]), neltst=int(el[0]))
 
     def hexa_state(self, which):
         ne = self.model.numels
         out = np.zeros(6 * ne if which == 0 else ne)
-        lib().or_get_hexa_state(self.h, 0, which, out)
+        self.L.or_get_hexa_state(self.h, 0, which, out)
         return out.reshape(6, ne) if which == 0 else out
 
     def shell_state(self, which, size):
         out = np.zeros(size)
-        lib().or_get_shell_state(self.h, which, out)
+        self.L.or_get_shell_state(self.h, which, out)
         return out
 
     def energy(self):
         v = [np.zeros(1) for _ in range(4)]
-        lib().or_energy(self.h, *[_ptr(a) for a in v])
+        self.L.or_energy(self.h, *[_ptr(a) for a in v])
         return dict(eint=v[0][0], ekin=v[1][0], ekinr=v[2][0], ehour=v[3][0])
 
     def error(self):
-        return lib().or_error(self.h)
+        return self.L.or_error(self.h)
 
     def set_forces(self, f, stifn, dt2t, neltst, fr=None, stifr=None):
         """Assembled element forces for the next cycle(1) (F and FR as (N, 3)
@@ -190,15 +210,15 @@ class OracleModel:
         element time step: the cycle skips its own element groups."""
         c = lambda a: None if a is None else np.ascontiguousarray(a, np.float64).reshape(-1)
         f, stifn, fr, stifr = c(f), c(stifn), c(fr), c(stifr)
-        if lib().or_set_forces(self.h, _ptr(f), _ptr(stifn), _ptr(fr), _ptr(stifr), float(dt2t),
+        if self.L.or_set_forces(self.h, _ptr(f), _ptr(stifn), _ptr(fr), _ptr(stifr), float(dt2t),
                                int(neltst)) != 0:
             raise RuntimeError("or_set_forces failed")
 
     def clear_links(self):
-        lib().or_rlink_clear(self.h)
+        self.L.or_rlink_clear(self.h)
 
     def set_record(self, on=True):
-        lib().or_set_record(self.h, 1 if on else 0)
+        self.L.or_set_record(self.h, 1 if on else 0)
 
     def record(self):
         """Listing quantities of the last cycle (ECRIT's point of the
@@ -206,7 +226,7 @@ class OracleModel:
         hourglass), momentum, mass, controlling element."""
         out = np.zeros(11)
         el = np.zeros(1, np.int32)
-        lib().or_get_record(self.h, _ptr(out), _ptr(el))
+        self.L.or_get_record(self.h, _ptr(out), _ptr(el))
         keys = ("tt", "dt2", "eint", "ekin", "ekinr", "ehour", "xmom", "ymom", "zmom", "mass",
                 "wfext")
         r = dict(zip(keys, out.tolist()))

@@ -1228,6 +1228,7 @@ int or_cycle(void *m, int ncycle) {
   const bool shells = rg_oracle_shell::numelc(w->sh) > 0;
   const bool rot = shells || !M.bodies.empty();
   for (int c = 0; c < ncycle; c++) {
+    RG_OPCOUNT_PHASE(0);
     // resol.F:2721-2722, 2826: DT1 = DT2, DT2 = 1e6, DT2T = DT2
     M.dt1 = M.dt2;
     M.dt2 = RG_EP06;
@@ -1254,6 +1255,7 @@ int or_cycle(void *m, int ncycle) {
     const int ng = M.ext ? 0 : (int)M.hg.size();
     std::vector<double> gdt(ng, RG_EP06);
     std::vector<int> gel(ng, -1);
+    RG_OPCOUNT_PHASE(1);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(M.nthreads)
     for (int g = 0; g < ng; g++) {
       double d = RG_EP06;
@@ -1262,6 +1264,7 @@ int or_cycle(void *m, int ncycle) {
       gdt[g] = d;
       gel[g] = el;
     }
+    RG_OPCOUNT_PHASE(0);
     int eidx = -1;
     for (int g = 0; g < ng; g++)
       if (gel[g] >= 0 && !(gdt[g] > dt2t)) {
@@ -1287,6 +1290,7 @@ int or_cycle(void *m, int ncycle) {
       }
     }
     // ASSPAR4 (asspar4.F:165-180): fixed-order slot sums
+    RG_OPCOUNT_PHASE(3);
 #pragma omp parallel for schedule(static) num_threads(M.nthreads)
     for (int n = 0; n < numnod; n++) {
       double a0 = M.A[3 * n], a1 = M.A[3 * n + 1], a2 = M.A[3 * n + 2];

@@ -26,6 +26,15 @@
  * user id}, IXC(7,NUMELC) hold {mat, n1..n4, prop, user id}.
  */
 #pragma once
+
+// Phase marks of the op-counting build (rg_opcount.h); nothing elsewhere.
+#ifndef RG_OPCOUNT_PHASE
+#ifdef RG_OPCOUNT
+#define RG_OPCOUNT_PHASE(p) (rg_count::phase = (p))
+#else
+#define RG_OPCOUNT_PHASE(p) ((void)0)
+#endif
+#endif
 #ifdef __cplusplus
 extern "C" {
 #endif

@@ -15,6 +15,15 @@
 #include <vector>
 
 #include "../openradioss_gb300/csrc/rg_constants.h"
+
+// Phase marks of the op-counting build (rg_opcount.h); nothing elsewhere.
+#ifndef RG_OPCOUNT_PHASE
+#ifdef RG_OPCOUNT
+#define RG_OPCOUNT_PHASE(p) (rg_count::phase = (p))
+#else
+#define RG_OPCOUNT_PHASE(p) ((void)0)
+#endif
+#endif
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -708,6 +717,7 @@ void step(Shells *S, const double *X, const double *V, const double *VR,
   const int ng = (int)S->groups.size();
   std::vector<double> gdt(ng, RG_EP06);
   std::vector<int> gel(ng, -1);
+  RG_OPCOUNT_PHASE(2);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
   for (int g = 0; g < ng; g++) {
     const Group &G = S->groups[g];
@@ -718,6 +728,7 @@ void step(Shells *S, const double *X, const double *V, const double *VR,
     gdt[g] = d;
     gel[g] = el;
   }
+  RG_OPCOUNT_PHASE(0);
   // CDT3 keeps the first element attaining the minimum (strict <)
   int best = -1;
   double bd = dt2t;

@@ -46,3 +46,50 @@ def test_forint_registered_equals_staged(kind, prec):
         if a[i] is not None:
             assert np.array_equal(a[i], b[i]), i
     assert a[4] == b[4] and a[5] == b[5]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("kind", ["shell", "hexa"])
+def test_cycle_host_equals_device_cycle(kind, prec):
+    """The whole-cycle call with host node buffers (rg_cycle_host), fed each
+    cycle with its own previous output from registered buffers, follows the
+    device-resident cycle: bitwise in the FP64 form (the upload writes back
+    the same values), within the mixed form's tolerance there (its element
+    volumes are re-anchored to the given coordinates), over 20 cycles, with
+    the same time step sequence (FP64)."""
+    from openradioss_gb300.engine import Engine
+    m = (M.crash_box(n_side=5, n_len=10, vpert=1.0) if kind == "shell"
+         else M.large_block(n=8, seed=2))
+    n = m.numnod
+    e1 = Engine(m, precision=prec)
+    e2 = Engine(m, precision=prec)
+    e1.cycle(5)
+    e2.cycle(5)
+    nd = e2.nodes()
+    x = np.ascontiguousarray(nd["X"].T)
+    v = np.ascontiguousarray(nd["V"].T)
+    vr = np.ascontiguousarray(nd["VR"].T) if kind == "shell" else None
+    d = np.empty((n, 3))
+    for a in (x, v, vr, d):
+        if a is not None:
+            e2.host_register(a)
+    for _ in range(20):
+        e1.cycle(1)
+        dt2 = e2.cycle_host(x, v, vr, x_out=x, v_out=v, vr_out=vr, d_out=d)
+        if prec == 0:
+            assert dt2 == e1.time()["dt2"]
+    for a in (x, v, vr, d):
+        if a is not None:
+            e2.host_unregister(a)
+    n1 = e1.nodes()
+    if prec == 0:
+        assert np.array_equal(x.T, n1["X"]) and np.array_equal(v.T, n1["V"])
+        assert np.array_equal(d.T, n1["D"])
+        if kind == "shell":
+            assert np.array_equal(vr.T, n1["VR"])
+    else:
+        sd = np.max(np.abs(n1["X"] - m.X))
+        assert np.max(np.abs(x.T - n1["X"])) <= 1e-4 * sd
+        assert np.max(np.abs(v.T - n1["V"])) <= 1e-4 * np.max(np.abs(n1["V"]))
+    assert e2.time()["ncycle"] == e1.time()["ncycle"] == 25
+    assert e1.status() == 0 and e2.status() == 0
