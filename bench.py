@@ -286,6 +286,31 @@ def job_run(model, prec, cycles, device, printouts=JOB_PRINTOUTS):
     return out, curve
 
 
+def one_ulp(model):
+    """The model with every initial coordinate moved by one ulp: its FP64 run
+    against the unperturbed one measures the problem's own sensitivity to
+    round-off, the yardstick of the mixed form's error."""
+    import copy
+    mp = copy.deepcopy(model)
+    mp.X = np.nextafter(model.X, np.inf)
+    return mp
+
+
+def job_pair(model, cycles, device):
+    """Full-length FP64 and mixed runs of a configuration, and an FP64 run
+    from the one-ulp-perturbed start: times, and the mixed form's error
+    beside the FP64 form's own round-off drift."""
+    from openradioss_gb300.engine import RG_PREC_FP64, RG_PREC_MIXED
+    j64, c64 = job_run(model, RG_PREC_FP64, cycles, device)
+    j32, c32 = job_run(model, RG_PREC_MIXED, cycles, device)
+    _, c64p = job_run(one_ulp(model), RG_PREC_FP64, cycles, device)
+    return {"f64": j64, "mixed": j32, "mixed_speedup": j64["seconds"] / j32["seconds"],
+            "mixed_error_vs_f64": mixed_error(c64, c32),
+            "fp64_one_ulp_drift": mixed_error(c64, c64p),
+            "note": "fp64_one_ulp_drift: the FP64 run from coordinates moved by one ulp "
+                    "against the FP64 run -- the round-off sensitivity of the problem"}
+
+
 def mixed_error(c64, c32):
     """Mixed-form error against the FP64 run of the same job: relative
     displacement error (final, and its largest over the printouts), peak
@@ -445,10 +470,7 @@ def workload_summary(wl, args, device, with_jobs=True):
     kk = res[RG_PREC_FP64]["kkey"]
     out["fp64_roofline"] = fp64_roofline(wl, kk, ne, res[RG_PREC_FP64]["kt"][kk], device)
     if with_jobs and JOB_CYCLES.get(wl):
-        j64, c64 = job_run(model, RG_PREC_FP64, JOB_CYCLES[wl], device)
-        j32, c32 = job_run(model, RG_PREC_MIXED, JOB_CYCLES[wl], device)
-        out["job"] = {"f64": j64, "mixed": j32, "mixed_speedup": j64["seconds"] / j32["seconds"],
-                      "mixed_error_vs_f64": mixed_error(c64, c32)}
+        out["job"] = job_pair(model, JOB_CYCLES[wl], device)
     return out
 
 
@@ -484,10 +506,7 @@ def run_ours(args, rank, world, local_rank):
     forint_s = e2e_forint(model, RG_PREC_FP64, args, local_rank)
     jobs = {}
     if not args.no_job and JOB_CYCLES.get(wl):
-        j64, c64 = job_run(model, RG_PREC_FP64, JOB_CYCLES[wl], local_rank)
-        j32, c32 = job_run(model, RG_PREC_MIXED, JOB_CYCLES[wl], local_rank)
-        jobs = {"f64": j64, "mixed": j32, "mixed_speedup": j64["seconds"] / j32["seconds"],
-                "mixed_error_vs_f64": mixed_error(c64, c32)}
+        jobs = job_pair(model, JOB_CYCLES[wl], local_rank)
     res64, res32 = out[RG_PREC_FP64], out[RG_PREC_MIXED]
     value = replica_value(ne * args.steps, world, res64["ms"] * 1e-3)
     value32 = replica_value(ne * args.steps, world, res32["ms"] * 1e-3)
@@ -547,7 +566,15 @@ def run_ours(args, rank, world, local_rank):
     if jobs:
         line["job"] = jobs
     if rank == 0 and not args.no_cpu_baseline and world == 1:
+        # the baseline legs: the CPU restatement on the host cores, and (shell
+        # workloads) the reference's own CUDA shell path on this GPU
         line["cpu_baseline"] = cpu_baseline(wl, args.warmup, args.steps)
+        if model.shells:
+            try:
+                line["reference_gpu_shell"] = reference_gpu_shell(model, args, local_rank,
+                                                                  res64["kt"]["shell"])
+            except Exception as ex:  # the comparator is optional
+                line["reference_gpu_shell"] = {"unavailable": repr(ex)[:200]}
     return line
 
 
@@ -660,14 +687,25 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
     from openradioss_gb300.serving import Server, poisson_arrivals
     jobs = [M.serving_job(k) for k in range(njobs)]
     arr = poisson_arrivals(njobs, SERVE_RATE, seed=7)
-    seq = {}
+    seq, per_job = {}, {}
     for prec in (0, 1):
-        tot = 0.0
+        ts = []
         for m, n in jobs:
             e = Engine(m, device=device, precision=prec)
-            tot += e.time_cycles(n) * 1e-3
+            ts.append(e.time_cycles(n) * 1e-3)
             e.close()
-        seq[prec] = tot
+        per_job[prec] = ts
+        seq[prec] = sum(ts)
+
+    def fifo_latency(ts):
+        """Latencies of a server running one job at a time, first come first
+        served, on the same arrivals (each job taking its measured time)."""
+        free, lat = 0.0, []
+        for a, t in sorted(zip(arr, ts)):
+            start = max(free, float(a))
+            free = start + t
+            lat.append(free - float(a))
+        return float(np.percentile(lat, 50)), float(np.percentile(lat, 99))
     srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device)
     with Clocks(device) as clk:
         st = srv.run([(k, m, n, float(a)) for k, ((m, n), a) in enumerate(zip(jobs, arr))])
@@ -697,11 +735,95 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
         "max_used_gb": st["max_used_bytes"] / 2 ** 30,
         "sequential_fp64_jobs_h": seq_jobs_h[0],
         "sequential_mixed_jobs_h": seq_jobs_h[1],
+        "fifo_one_at_a_time_latency_s": {
+            "fp64": dict(zip(("p50", "p99"), fifo_latency(per_job[0]))),
+            "mixed": dict(zip(("p50", "p99"), fifo_latency(per_job[1]))),
+            "note": "the same arrivals served one job at a time, first come first served, "
+                    "each job taking its measured solo device time"},
         "speedup_vs_sequential_plain": st["jobs_per_h"] / seq_jobs_h[0],
         "speedup_vs_sequential_mixed": st["jobs_per_h"] / seq_jobs_h[1],
         "jobs_with_device_status": bad,
         "clocks": clk.summary(),
     }
+
+
+def reference_gpu_shell(model, args, device, ours_kernel_ms):
+    """Baseline leg: the reference's own CUDA shell path (its unmodified
+    shell_*_kernel.cu and shell_gpu_driver.cu, built for sm_103a in double
+    precision; oracle/ref_gpu.py) timed on this GPU on the same shells and
+    node state as ours -- a speed comparator, not a parity check.  Two
+    states, each held fixed for W + K steps as in a FORINT-level call: the
+    state of the timed window (W cycles after set-up) and the same with a
+    seeded N(0, 2 m/s) velocity perturbation, under which the points go
+    plastic.  Beside each: our FORINT-level call (rg_forint_step: the same
+    uploads, elements with PARITH/ON assembly, the same downloads) on the
+    same state, and our element kernel's device time per cycle."""
+    import tempfile
+    from openradioss_gb300.engine import Engine
+    from oracle import ref_gpu
+    why = ref_gpu.available()
+    if why:
+        return {"unavailable": why}
+    g = model.shells[0]
+    mt = g.mat
+    e = Engine(model, device=device, precision=0)
+    e.cycle(args.warmup)
+    nd = e.nodes()
+    dt = e.time()["dt2"]
+    e.close()
+    pm = mt["pm"]
+    rng = np.random.default_rng(11)
+    out = {"what": "reference CUDA shell path (shell_gpu_driver.h:302-477, MYREAL8, ISMSTR=2, "
+                   "IPLA=1, NPT=5) vs ours on the same shells and fixed node state",
+           "numelc": model.numelc, "steps": args.steps}
+    for name, dv in (("window_state", 0.0), ("perturbed_plastic", 2.0)):
+        X = np.ascontiguousarray(nd["X"].T)
+        V = np.ascontiguousarray(nd["V"].T + (rng.normal(0.0, dv, nd["V"].T.shape) if dv else 0.0))
+        VR = np.ascontiguousarray(nd["VR"].T)
+        req = dict(ixc4=(g.ixc[1:5] - 1).astype(np.int32), thk=g.thk, X=X, V=V, VR=VR,
+                   # E, nu, rho; Johnson-Cook A, B, n, C, eps0 (mat_param%uparam 1-3, 6-7)
+                   mat=np.array([pm[19], pm[20], pm[0], mt["uparam"][0], mt["uparam"][1],
+                                 mt["uparam"][2], mt["uparam"][5], mt["uparam"][6]]),
+                   # membrane, flexural, rotational hourglass (GEO(13:15))
+                   hg=np.array([g.geo[12], g.geo[13], g.geo[14]]), dt=dt, nwarm=args.warmup,
+                   nsteps=args.steps)
+        with tempfile.TemporaryDirectory() as td:
+            fn = os.path.join(td, "req.npz")
+            np.savez(fn, **req)
+            r = subprocess.run([sys.executable, "-m", "oracle.ref_gpu", fn], cwd=ROOT,
+                               capture_output=True, text=True, timeout=900)
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode != 0 or not lines:
+            out[name] = {"unavailable": "reference comparator exited %d: %s" % (
+                r.returncode, (r.stderr or r.stdout).strip().splitlines()[-1:])}
+            continue
+        ref = json.loads(lines[-1])
+        # ours: the FORINT-level call on the same fixed state
+        e = Engine(model, device=device, precision=0)
+        e.cycle(args.warmup)
+        f, fr = np.empty_like(X), np.empty_like(X)
+        st, sr = np.empty(model.numnod), np.empty(model.numnod)
+        bufs = [X, V, VR, f, fr, st, sr]
+        for a in bufs:
+            e.host_register(a)
+        for _ in range(args.warmup):
+            e.forint_step(X, V, dt, vr=VR, f=f, stifn=st, fr=fr, stifr=sr)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e.forint_step(X, V, dt, vr=VR, f=f, stifn=st, fr=fr, stifr=sr)
+        ours_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+        for a in bufs:
+            e.host_unregister(a)
+        e.close()
+        d = {"reference_kernels_ms_per_step": ref["kernels_ms_per_step"],
+             "reference_full_step_ms": ref["full_step_ms"],
+             "ours_forint_step_ms": ours_ms,
+             "speedup_full_step": ref["full_step_ms"] / ours_ms}
+        if name == "window_state":
+            d["ours_shell_kernel_ms"] = ours_kernel_ms
+            d["speedup_kernels"] = ref["kernels_ms_per_step"] / ours_kernel_ms
+        out[name] = d
+    return out
 
 
 def cpu_window(wl, warmup, steps, threads=None):
@@ -802,6 +924,7 @@ def main():
             line["serving"] = {k: sv[k] for k in (
                 "value", "unit", "completed", "failed", "p50_latency_s", "p99_latency_s",
                 "sequential_fp64_jobs_h", "sequential_mixed_jobs_h",
+                "fifo_one_at_a_time_latency_s",
                 "speedup_vs_sequential_plain", "speedup_vs_sequential_mixed",
                 "element_updates_s", "makespan_s", "config", "jobs_with_device_status")}
     if rank == 0:

@@ -754,6 +754,10 @@ int rg_hexa_group_add(rg_ctx *c, int nel, const int *ixs, int mtn,
   if (mtn == 2) {
     if (iparam[0] != 0 || uparam[7] != 0.0)
       return fail(c, RG_E_UNSUP, "LAW2: Zerilli or kinematic hardening not supported");
+    // adiabatic heating needs a temperature per element (M2LAW's TSTAR):
+    // not carried by the hexa path, refused rather than ignored
+    if (pm[68] > 0.0)
+      return fail(c, RG_E_UNSUP, "hexa LAW2: thermal softening (rho*Cp > 0) not supported");
     P.icc = iparam[1];
     P.vp = iparam[2];
     P.israte = iparam[3];

@@ -84,6 +84,25 @@ __device__ __forceinline__ void st4(dbl4 *__restrict__ p, dbl4 v) { *p = v; }
 __device__ __forceinline__ F8 ldF8(const F8 *__restrict__ p) { return *p; }
 __device__ __forceinline__ float4 ldf4(const float4 *__restrict__ p) { return __ldg(p); }
 
+// Asynchronous global -> shared copies of one thread's own values (sm_80+
+// cp.async): issued early, they fetch element state while the thread
+// computes, without holding registers; cp_async_wait_all() makes them
+// visible to the issuing thread.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // Block-level (min dt, element) reduction; ties keep the larger element
 // order key (the last element attaining the minimum in sequential order).
 __device__ __forceinline__ void dt_pair_min(double &d, int &k, double d2,

@@ -26,16 +26,27 @@ struct ShellDev {
   double *epart = nullptr;  // energy partials
 };
 
-// mixed form: 4 resident blocks per SM (128 registers); FP64: as many as
-// its ~250 registers allow
+// Resident blocks per SM of the mixed kernel (its register budget); the
+// FP64 kernel takes as many as its ~250 registers allow.
+#ifndef RG_SHELL_MIXED_MINB
+#define RG_SHELL_MIXED_MINB 4
+#endif
+
+// The mixed form stages each element's state in shared memory (cp.async at
+// the start of the element, shell_element<..., STAGE>): the DRAM reads of the
+// state overlap the node gathers and the geometry without holding registers.
 template <typename ER, int NPT, int NT>
-__global__ void __launch_bounds__(NT, sizeof(ER) == 4 ? 4 : 1)
+__global__ void __launch_bounds__(NT, sizeof(ER) == 4 ? RG_SHELL_MIXED_MINB : 1)
 shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              typename SlotT<ER>::type *__restrict__ fsky,
              typename SlotT<ER>::type *__restrict__ fskyr, DtPartials dp,
              Time *__restrict__ T, int key0, int nc_total, int *__restrict__ status,
              const DtFinish F) {
   typedef ER R;
+  constexpr bool STG = sizeof(ER) == 4;
+  static_assert(!STG || NT == SHELL_STG_NT, "staging slots are laid out for 128 threads");
+  __shared__ float s_stg[STG ? ShellStage<NPT>::nfloat * NT : 1];
+  __shared__ double s_stgd[STG ? ShellStage<NPT>::ndouble * NT : 1];
   R dtmine = (R)RG_EP06;
   int elmin = -1;
   // warp tasks of 32 consecutive elements.  wtasks = 0: each warp does the
@@ -62,8 +73,8 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     }
     const int il = t * 32 + lane;
     if (il < P.nel)
-      shell_element<ER, NPT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin, DT1,
-                             dtinv);
+      shell_element<ER, NPT, STG>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin,
+                                  DT1, dtinv, s_stg, s_stgd);
   }
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
   if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
@@ -139,8 +150,19 @@ int shell_group_add(ShellModelHost &S, int numnod, int nel, const int *ixc, int 
     why = "shell: ITHK must be 0 (initial thickness) or > 0 (current thickness)";
     return RG_E_UNSUP;
   }
-  if (iparam[0] != 0 || uparam[7] != 0.0) {
-    why = "shell LAW2: Zerilli or kinematic hardening not supported";
+  if (iparam[0] != 0) {
+    why = "shell LAW2: Zerilli-Armstrong (IFORM = 1) not supported";
+    return RG_E_UNSUP;
+  }
+  if (uparam[7] < 0.0 || uparam[7] > 1.0) {
+    why = "shell LAW2: FISOKIN must be in [0, 1]";
+    return RG_E_ARG;
+  }
+  // ductile rupture (SIGEPS02C: OFF = 4/5 once PLA >= EPMX, then the
+  // layer-failure bookkeeping of MULAWC) is not built: a finite EPMX is
+  // refused rather than ignored (the reader's default is 1e20, never reached)
+  if (uparam[3] < 1e20) {
+    why = "shell LAW2: ductile rupture (finite EPS_p_max) not supported";
     return RG_E_UNSUP;
   }
   for (int e = 0; e < nel; e++) {
@@ -162,9 +184,9 @@ int shell_group_add(ShellModelHost &S, int numnod, int nel, const int *ixc, int 
   P.ithk = ithk > 0 ? 1 : 0;
   P.ishfram = 0;  // set for every group at finalize (a model-wide option)
   P.ipla = (int)geo[38];
-  if (P.ipla != 0 && P.ipla != 1) {
+  if (P.ipla != 0 && P.ipla != 1 && P.ipla != 2) {
     delete g;
-    why = "shell LAW2: Iplas 0 or 1 supported";
+    why = "shell LAW2: Iplas 0, 1 or 2 supported";
     return RG_E_UNSUP;
   }
   P.rho = pm[0];
@@ -192,6 +214,14 @@ int shell_group_add(ShellModelHost &S, int numnod, int nel, const int *ixc, int 
   P.cc = uparam[5];
   P.eps0 = uparam[6];
   P.pm9 = uparam[8];
+  P.fisokin = uparam[7];
+  P.m_exp = uparam[9] != 0.0 ? uparam[9] : 1.0;
+  // thermal parameters of the material (PM(69) rho*Cp, PM(79) T_r, PM(80)
+  // T_melt; mat_param%therm): softening needs adiabatic heating
+  P.rhocp = pm[68];
+  P.tref = pm[78];
+  P.tmelt = pm[79];
+  P.thermal = (P.rhocp > 0.0 && P.tmelt > P.tref) ? 1 : 0;
   if (P.srh1 != 0.0 || P.srh2 != 0.0 || P.srh3 != 0.0) {
     delete g;
     why = "shell: linear hourglass viscosity (GEO(18..20)) not supported";
@@ -222,10 +252,15 @@ void shell_user_ids(const ShellModelHost &S, int *out) {
 }
 
 template <typename ER>
-static int alloc_arrays(ShellArrays<ER> &A, int nc, const DevAlloc &alloc) {
+static int alloc_arrays(ShellArrays<ER> &A, int nc, const DevAlloc &alloc, bool kin,
+                        bool therm) {
   auto get = [&](void **p, size_t bytes) { return alloc(p, bytes); };
   int r = 0;
   A.nc = nc;
+  A.sigbak = nullptr;
+  A.temp = nullptr;
+  if (kin && (r = get((void **)&A.sigbak, 15 * (size_t)nc * sizeof(ER)))) return r;
+  if (therm && (r = get((void **)&A.temp, 5 * (size_t)nc * sizeof(ER)))) return r;
   if ((r = get((void **)&A.offg, nc * sizeof(ER)))) return r;
   if ((r = get((void **)&A.thke, nc * sizeof(ER)))) return r;
   if ((r = get((void **)&A.thk, nc * sizeof(double)))) return r;
@@ -262,6 +297,18 @@ static int init_arrays(ShellModelHost &S, ShellArrays<ER> &A) {
       cp(A.epsd, zero.data(), 5 * (size_t)nc * sizeof(ER)) ||
       cp(A.ehou, zd.data(), nc * sizeof(double)))
     return RG_E_CUDA;
+  if (A.sigbak) {
+    std::vector<ER> z15(15 * (size_t)nc, (ER)0);
+    if (cp(A.sigbak, z15.data(), z15.size() * sizeof(ER))) return RG_E_CUDA;
+  }
+  if (A.temp) {
+    // each point starts at its material's T_r (the buffer's TINI)
+    std::vector<ER> t(5 * (size_t)nc, (ER)0);
+    for (auto *g : S.groups)
+      for (int p = 0; p < 5; p++)
+        for (int i = 0; i < g->P.nel; i++) t[(size_t)p * nc + g->P.nft + i] = (ER)g->P.tref;
+    if (cp(A.temp, t.data(), t.size() * sizeof(ER))) return RG_E_CUDA;
+  }
   return 0;
 }
 
@@ -313,14 +360,19 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
     why = "copy of shell tables failed";
     return RG_E_CUDA;
   }
+  bool kin = false, therm = false;
+  for (auto *g : S.groups) {
+    kin = kin || g->P.fisokin > 0.0;
+    therm = therm || g->P.thermal;
+  }
   if (prec == RG_PREC_FP64) {
-    if ((r = alloc_arrays(D->a64, nc, alloc))) return r;
+    if ((r = alloc_arrays(D->a64, nc, alloc, kin, therm))) return r;
     D->a64.ix = D->ix;
     D->a64.iadc = D->iadc;
     D->a64.degen = D->degen;
     if ((r = init_arrays(S, D->a64))) return r;
   } else {
-    if ((r = alloc_arrays(D->a32, nc, alloc))) return r;
+    if ((r = alloc_arrays(D->a32, nc, alloc, kin, therm))) return r;
     D->a32.ix = D->ix;
     D->a32.iadc = D->iadc;
     D->a32.degen = D->degen;
@@ -406,6 +458,18 @@ int shell_download(ShellModelHost &S, int prec, int which, double *out, std::str
     case 5: return fetch(a.sig, b.sig, 5 * (size_t)npt * n, false);
     case 6: return fetch(a.pla, b.pla, (size_t)npt * n, false);
     case 7: return fetch(a.hour, b.hour, 5 * n, false);
+    case 8:  // back stress per point [npt][3][n] (zero without kinematic hardening)
+      if (!(prec == RG_PREC_FP64 ? (const void *)a.sigbak : (const void *)b.sigbak)) {
+        std::fill(out, out + 3 * (size_t)npt * n, 0.0);
+        return 0;
+      }
+      return fetch(a.sigbak, b.sigbak, 3 * (size_t)npt * n, false);
+    case 9:  // temperature per point [npt][n] (T_r without adiabatic heating)
+      if (!(prec == RG_PREC_FP64 ? (const void *)a.temp : (const void *)b.temp)) {
+        std::fill(out, out + (size_t)npt * n, S.groups[0]->P.tref);
+        return 0;
+      }
+      return fetch(a.temp, b.temp, (size_t)npt * n, false);
   }
   why = "unknown shell state index";
   return RG_E_ARG;

@@ -55,6 +55,11 @@ struct ShellParams {
   double shf0, hA1, hA3, hA5, hA7, hA8;
   int shf_const;
   int nodadt;   // nodal time step: STI / STIR for DTNODA, no element dt
+  // kinematic / mixed hardening (FISOKIN, m2cplr.F:115-121, 289-363) and
+  // Johnson-Cook thermal softening with adiabatic heating (T* from each
+  // point's temperature, sigeps02c.F:125, 226-229; thermal = rho*Cp > 0)
+  double fisokin, m_exp, tref, tmelt, rhocp;
+  int thermal;
   // FP32 copies for the mixed form (converted once on the host) and the
   // branch flags CC /= 0, DM /= 0 evaluated on the FP64 values
   struct {
@@ -62,6 +67,7 @@ struct ShellParams {
     float ca, cb, cn, ymax, cc, eps0, pm9, dtfac;
     float a1, a2, inv1mnu, inv1pnu, inv_hmax, dtfac_ssp;
     float shf0, hA1, hA3, hA5, hA7, hA8;
+    float fisokin, m_exp, tref, tmelt, rhocp;
     int cc_nz, dm_nz;
   } f;
 };
@@ -118,6 +124,11 @@ inline void shell_params_mirror(ShellParams &P) {
   P.f.eps0 = (float)P.eps0;
   P.f.pm9 = (float)P.pm9;
   P.f.dtfac = (float)P.dtfac;
+  P.f.fisokin = (float)P.fisokin;
+  P.f.m_exp = (float)P.m_exp;
+  P.f.tref = (float)P.tref;
+  P.f.tmelt = (float)P.tmelt;
+  P.f.rhocp = (float)P.rhocp;
   P.f.cc_nz = P.cc != 0.0;
   P.f.dm_nz = P.dm != 0.0;
 }
@@ -135,6 +146,8 @@ struct ShellArrays {
   double *eint;           // [2][nc]
   ER *sig, *pla, *epsd;   // [npt][5][nc], [npt][nc], [npt][nc]
   double *ehou;           // [nc]
+  ER *sigbak;             // back stress [npt][3][nc] (FISOKIN > 0), else null
+  ER *temp;               // temperature [npt][nc] (thermal groups), else null
 };
 
 
@@ -205,7 +218,21 @@ __device__ __forceinline__ R sqrt_ratio(const R s1, const R s2) {
     return sqrt(s1 / s2);
 }
 
-template <typename ER, int NPT>
+// Shared-memory staging of a block's element state (mixed form, single-model
+// kernel): per thread of a SHELL_STG_NT-thread block, the float components
+// [forc 5 | mom 3 | hour 5 | gstr 8 | sig 5*NPT | pla NPT | epsd NPT] and the
+// doubles [eint 2 | ehou], component-major (slot = component * NT + thread).
+constexpr int SHELL_STG_NT = 128;
+constexpr int SG_FORC = 0, SG_MOM = 5, SG_HOUR = 8, SG_GSTR = 13, SG_SIG = 21;
+template <int NPT>
+struct ShellStage {
+  static constexpr int nfloat = 21 + 7 * NPT;
+  static constexpr int pla = SG_SIG + 5 * NPT;
+  static constexpr int epsd = SG_SIG + 6 * NPT;
+  static constexpr int ndouble = 3;
+};
+
+template <typename ER, int NPT, bool STAGE = false>
 __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellArrays<ER> &S,
                                               const NodeView &N,
                                               typename SlotT<ER>::type *__restrict__ fsky,
@@ -213,9 +240,13 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
                                               const Time *__restrict__ T, const int key0,
                                               const int nc_total, const int il, ER &dtmine,
                                               int &elmin, const double DT1in = -1.0,
-                                              const ER dtinv_in = (ER)0) {
+                                              const ER dtinv_in = (ER)0,
+                                              float *__restrict__ stg = nullptr,
+                                              double *__restrict__ stgd = nullptr) {
   typedef ER R;
   constexpr bool F64 = std::is_same<ER, double>::value;
+  static_assert(!(STAGE && F64), "shared-memory staging is the mixed form's");
+  typedef ShellStage<NPT> SG;
   const int nc = S.nc;
   {
     const int e = P.nft + il;
@@ -223,6 +254,31 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     // looping over elements passes them (DT1in >= 0) to form them once
     const double DT1 = DT1in >= 0.0 ? DT1in : T->dt2;
     const R dt1 = (R)DT1;
+    const int tid = threadIdx.x;
+    // staged form: the whole element state is requested now, into this
+    // thread's shared-memory slots, and waited for at its first use (CSTRA3)
+    if constexpr (STAGE) {
+      constexpr int NT = SHELL_STG_NT;
+#pragma unroll
+      for (int c = 0; c < 5; c++) cp_async4(stg + (SG_FORC + c) * NT + tid, S.forc + c * nc + e);
+#pragma unroll
+      for (int c = 0; c < 3; c++) cp_async4(stg + (SG_MOM + c) * NT + tid, S.mom + c * nc + e);
+#pragma unroll
+      for (int c = 0; c < 5; c++) cp_async4(stg + (SG_HOUR + c) * NT + tid, S.hour + c * nc + e);
+#pragma unroll
+      for (int c = 0; c < 8; c++) cp_async4(stg + (SG_GSTR + c) * NT + tid, S.gstr + c * nc + e);
+#pragma unroll
+      for (int c = 0; c < 5 * NPT; c++) cp_async4(stg + (SG_SIG + c) * NT + tid, S.sig + c * nc + e);
+#pragma unroll
+      for (int it = 0; it < NPT; it++) {
+        cp_async4(stg + (SG::pla + it) * NT + tid, S.pla + it * nc + e);
+        cp_async4(stg + (SG::epsd + it) * NT + tid, S.epsd + it * nc + e);
+      }
+      cp_async8(stgd + 0 * NT + tid, S.eint + e);
+      cp_async8(stgd + 1 * NT + tid, S.eint + nc + e);
+      cp_async8(stgd + 2 * NT + tid, S.ehou + e);
+      cp_async_commit();
+    }
     // ---- CCOOR3 ----
     int nn[4];
 #pragma unroll
@@ -275,13 +331,18 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     // Element state read up front, ahead of the first store (the compiler
     // must assume the state arrays may alias): the loads overlap the gathers.
     R st_forc[5], st_mom[3], st_hour[5];
+    double st_eint0 = 0.0, st_eint1 = 0.0, st_ehou = 0.0;
+    if constexpr (!STAGE) {
 #pragma unroll
-    for (int c = 0; c < 5; c++) st_forc[c] = S.forc[c * nc + e];
+      for (int c = 0; c < 5; c++) st_forc[c] = S.forc[c * nc + e];
 #pragma unroll
-    for (int c = 0; c < 3; c++) st_mom[c] = S.mom[c * nc + e];
+      for (int c = 0; c < 3; c++) st_mom[c] = S.mom[c * nc + e];
 #pragma unroll
-    for (int c = 0; c < 5; c++) st_hour[c] = S.hour[c * nc + e];
-    const double st_eint0 = S.eint[e], st_eint1 = S.eint[nc + e], st_ehou = S.ehou[e];
+      for (int c = 0; c < 5; c++) st_hour[c] = S.hour[c * nc + e];
+      st_eint0 = S.eint[e];
+      st_eint1 = S.eint[nc + e];
+      st_ehou = S.ehou[e];
+    }
     // ---- CNVEC3 ----
     R e1x, e1y, e1z, e2x, e2y, e2z, e3x, e3y, e3z;
     {
@@ -485,8 +546,15 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       kyy = kyy * fac1;
       kxy = kxy * fac1;
       const R inc[8] = {exx, eyy, exy, eyz, exz, kxx, kyy, kxy};
+      if constexpr (STAGE) {
+        cp_async_wait_all();
 #pragma unroll
-      for (int c = 0; c < 8; c++) S.gstr[c * nc + e] = S.gstr[c * nc + e] + inc[c];
+        for (int c = 0; c < 8; c++)
+          S.gstr[c * nc + e] = stg[(SG_GSTR + c) * SHELL_STG_NT + tid] + inc[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 8; c++) S.gstr[c * nc + e] = S.gstr[c * nc + e] + inc[c];
+      }
     }
     // element strain rate (ASRATE = 1)
     R epsd_pg;
@@ -500,196 +568,14 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       epsd_pg = sqrt(eps_k2 + eps_m2) * dtinv;
       S.epsdg[e] = epsd_pg;
     }
-    // ---- MULAWC: through-thickness loop (SIGEPS02C / M2CPLR) ----
-    R forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
-    R degmb = st_forc[0] * exx + st_forc[1] * eyy + st_forc[2] * exy + st_forc[3] * eyz +
-              st_forc[4] * exz;
-    R degfx = st_mom[0] * kxx + st_mom[1] * kyy + st_mom[2] * kxy;
-    double thkn = thk_cur;
-    R asrate = (R)RG_ONE;
-    if (P.israte > 0) {
-      if constexpr (F64)
-        asrate = smin((R)RG_ONE, (R)(P.pm9 * DT1));
-      else
-        asrate = smin(1.f, P.f.pm9 * dt1);
+    // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) and CDT3, ahead of MULAWC: they
+    // read no result of the material update, so the local velocities and
+    // rotation rates are dead before the through-thickness loop ----
+    if constexpr (STAGE) {
+#pragma unroll
+      for (int c = 0; c < 5; c++) st_hour[c] = stg[(SG_HOUR + c) * SHELL_STG_NT + tid];
+      st_ehou = stgd[2 * SHELL_STG_NT + tid];
     }
-    const R a1 = PC(a1);
-    const R a2 = PC(a2);
-    const R epdr = smax(PC(eps0) * dt1, (R)RG_EM20);
-    // LOG(EPSP/EPDR) of the previous point: the points usually share one
-    // strain rate (ASRATE = 1), and an equal argument gives the same value
-    R memo_epsp = (R)-1, memo_log = (R)0;
-    // point state: point it+1 is loaded while point it is computed
-    R nx_sig[5], nx_ep, nx_pla;
-#pragma unroll
-    for (int c = 0; c < 5; c++) nx_sig[c] = S.sig[(c)*nc + e];
-    nx_ep = S.epsd[e];
-    nx_pla = S.pla[e];
-#pragma unroll
-    for (int it = 0; it < NPT; it++) {
-      R sn[5];
-#pragma unroll
-      for (int c = 0; c < 5; c++) sn[c] = nx_sig[c];
-      R ep = nx_ep;
-      const R pla_in = nx_pla;
-      if (it + 1 < NPT) {
-        const int q5 = ((it + 1) * 5) * nc + e;
-#pragma unroll
-        for (int c = 0; c < 5; c++) nx_sig[c] = S.sig[q5 + c * nc];
-        nx_ep = S.epsd[(it + 1) * nc + e];
-        nx_pla = S.pla[(it + 1) * nc + e];
-      }
-      const R thkly = pcoef<R>(c_wfd[NPT - 1][it], c_wf[NPT - 1][it]);
-      const R thklyl = thkly * thk0;
-      const R wmc = pcoef<R>(c_wmd[NPT - 1][it], c_wm[NPT - 1][it]);
-      const R zt = pcoef<R>(c_z0d[NPT - 1][it], c_z0[NPT - 1][it]) * thk0;
-      const R depsxx = exx + zt * kxx;
-      const R depsyy = eyy + zt * kyy;
-      const R depsxy = exy + zt * kxy;
-      const int ip5 = (it * 5) * nc + e;
-      R epsdot;
-      if (P.vp == 2) {
-        ep = asrate * epsd_pg + ((R)RG_ONE - asrate) * ep;
-        S.epsd[it * nc + e] = ep;
-        epsdot = ep * dt1;
-      } else {
-        epsdot = ep * dt1;
-      }
-      R ezz = (R)0;
-      R ca = PC(ca), cb = PC(cb), ymax = PC(ymax);
-      sn[0] = sn[0] + a1 * depsxx + a2 * depsyy;
-      sn[1] = sn[1] + a2 * depsxx + a1 * depsyy;
-      sn[2] = sn[2] + gmod * depsxy;
-      sn[3] = sn[3] + gs * eyz;
-      sn[4] = sn[4] + gs * exz;
-      if (P.f.cc_nz) {
-        R epsp = epsdot;
-        if (P.israte == 0 && P.vp == 2)
-          epsp = smax(smax(fabs(depsxx), fabs(depsyy)), (R)RG_HALF * fabs(depsxy));
-        epsp = smax(epsp, epdr);
-        R logep;
-        if (epsp == memo_epsp) {
-          logep = memo_log;
-        } else {
-          logep = log(epsp / epdr);
-          memo_epsp = epsp;
-          memo_log = logep;
-        }
-        R q = ((R)RG_ONE + PC(cc) * logep);
-        q = smax(q, (R)RG_EM20);
-        ca = ca * q;
-        cb = cb * q;
-        if (P.icc == 1) ymax = ymax * q;
-      }
-      R pla = pla_in;
-      R yld = pla == (R)0 ? ca : ca + cb * exp(PC(cn) * log(pla));
-      yld = smin(yld, ymax);
-      if (P.ipla == 0) {
-        const R svm = sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2]);
-        const R r = smin((R)RG_ONE, yld / (svm + (R)RG_EM15));
-        if (r < (R)RG_ONE) {
-          sn[0] = sn[0] * r;
-          sn[1] = sn[1] * r;
-          sn[2] = sn[2] * r;
-          const R dpla = off * smax((R)0, (svm - yld) / ym);
-          const R s1 = (R)RG_HALF * (sn[0] + sn[1]);
-          ezz = dpla * s1 / yld;
-          pla = pla + dpla;
-        }
-      } else {
-        const R s1 = sn[0] + sn[1];
-        const R s2 = sn[0] - sn[1];
-        const R s3 = sn[2];
-        const R A = (R)RG_FOURTH * s1 * s1;
-        const R B = (R)RG_THREE_OVER_4 * s2 * s2 + (R)RG_THREE * s3 * s3;
-        // SVM > YLD tested on the squares (YLD >= 0): the square root is
-        // only taken at yielding points
-        if (A + B > yld * yld && off == (R)RG_ONE) {
-          const R svm = sqrt(A + B);
-          const R nu1 = PC(inv1mnu);
-          const R nu2 = PC(inv1pnu);
-          const R h = yld >= ymax ? (R)0 : PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
-          R dpla_j = (svm - yld) / ((R)RG_THREE * gmod + h);
-          const R anu1 = A * nu1;
-          const R bnu2 = (R)RG_THREE * B * nu2;
-          const R h2 = (R)RG_TWO * h;
-          R dpla_i = 0, Pp = 1, Qq = 1, dr = 0;
-#pragma unroll
-          for (int n = 0; n < 3; n++) {
-            dpla_i = dpla_j;
-            const R pla_i = pla + dpla_i;
-            const R yld_i = pla_i == (R)0 ? smin(ymax, ca) : smin(ymax, ca + cb * exp(PC(cn) * log(pla_i)));
-            // FP64 form: the two divisions by YLD_I, and P and Q, each from
-            // one reciprocal (FP64-pipe work of the plastic points)
-            R inv_y = (R)0;
-            if constexpr (F64) {
-              inv_y = (R)RG_ONE / yld_i;
-              dr = (R)RG_HALF * ym * dpla_i * inv_y;
-              const R dp = (R)RG_ONE + dr * nu1;
-              const R dq = (R)RG_ONE + (R)RG_THREE * dr * nu2;
-              const R rpq = (R)RG_ONE / (dp * dq);
-              Pp = dq * rpq;
-              Qq = dp * rpq;
-            } else {
-              dr = (R)RG_HALF * ym * dpla_i / yld_i;
-              Pp = (R)RG_ONE / ((R)RG_ONE + dr * nu1);
-              Qq = (R)RG_ONE / ((R)RG_ONE + (R)RG_THREE * dr * nu2);
-            }
-            const R p2 = Pp * Pp, q2 = Qq * Qq;
-            const R f = A * p2 + B * q2 - yld_i * yld_i;
-            R df;
-            if constexpr (F64)
-              df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) * inv_y - h2 * yld_i;
-            else
-              df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) / yld_i - h2 * yld_i;
-            dpla_j = dpla_i > (R)0 ? smax((R)0, dpla_i - f / df) : (R)0;
-          }
-          pla = pla + dpla_i;
-          const R t1 = (sn[0] + sn[1]) * Pp;
-          const R t2 = (sn[0] - sn[1]) * Qq;
-          sn[0] = (R)RG_HALF * (t1 + t2);
-          sn[1] = (R)RG_HALF * (t1 - t2);
-          sn[2] = sn[2] * Qq;
-          ezz = dr * t1 / ym;
-        }
-      }
-      S.pla[it * nc + e] = pla;
-      ezz = -(depsxx + depsyy) * nu - ((R)RG_ONE - (R)RG_TWO * nu) * ezz;
-      ezz = ezz * PC(inv1mnu);
-      thkn = thkn + (double)(ezz * thklyl * off);
-#pragma unroll
-      for (int c = 0; c < 5; c++) {
-        S.sig[ip5 + c * nc] = sn[c];
-        forn[c] = forn[c] + thkly * sn[c];
-      }
-      momn[0] = momn[0] + wmc * sn[0];
-      momn[1] = momn[1] + wmc * sn[1];
-      momn[2] = momn[2] + wmc * sn[2];
-    }
-    S.thk[e] = thkn > RG_EM30 ? thkn : RG_EM30;
-    if (P.f.dm_nz) {
-      const R dtinv = DT1in >= 0.0 ? dtinv_in : dt1 / smax(dt1 * dt1, (R)RG_EM20);
-      const R visc = ((R)RG_ONEP414 * PC(dm)) * ssp * sqrt(area) * dtinv * rho;
-      forn[0] = forn[0] + visc * (exx + (R)RG_HALF * eyy);
-      forn[1] = forn[1] + visc * (eyy + (R)RG_HALF * exx);
-      forn[2] = forn[2] + visc * exy * (R)RG_THIRD;
-    }
-#pragma unroll
-    for (int c = 0; c < 5; c++) forn[c] = forn[c] * off;
-#pragma unroll
-    for (int c = 0; c < 3; c++) momn[c] = momn[c] * off;
-    degmb = degmb + forn[0] * exx + forn[1] * eyy + forn[2] * exy + forn[3] * eyz + forn[4] * exz;
-    degfx = degfx + momn[0] * kxx + momn[1] * kyy + momn[2] * kxy;
-    {
-      const R vol2 = (R)RG_HALF * vol0;
-      S.eint[e] = st_eint0 + (double)(degmb * vol2);
-      S.eint[nc + e] = st_eint1 + (double)(degfx * thk0 * vol2);
-    }
-#pragma unroll
-    for (int c = 0; c < 5; c++) S.forc[c * nc + e] = forn[c];
-#pragma unroll
-    for (int c = 0; c < 3; c++) S.mom[c * nc + e] = momn[c];
-    // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) ----
     R h11, h12, h13, h21, h22, h23, h31, h32, h33, hr4, hr5;
     R sti_noda = (R)0, stir_noda = (R)0;
     R inv_divm = (R)0;  // FP64 form: 1 / MAX(ALDT^2, EM20), formed with HH2
@@ -799,6 +685,315 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       }
       sti = (R)RG_ZEP81 * sti * off;
     }
+    // ---- MULAWC: through-thickness loop (SIGEPS02C / M2CPLR) ----
+    R forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
+    if constexpr (STAGE) {
+#pragma unroll
+      for (int c = 0; c < 5; c++) st_forc[c] = stg[(SG_FORC + c) * SHELL_STG_NT + tid];
+#pragma unroll
+      for (int c = 0; c < 3; c++) st_mom[c] = stg[(SG_MOM + c) * SHELL_STG_NT + tid];
+    }
+    R degmb = st_forc[0] * exx + st_forc[1] * eyy + st_forc[2] * exy + st_forc[3] * eyz +
+              st_forc[4] * exz;
+    R degfx = st_mom[0] * kxx + st_mom[1] * kyy + st_mom[2] * kxy;
+    double thkn = thk_cur;
+    R asrate = (R)RG_ONE;
+    if (P.israte > 0) {
+      if constexpr (F64)
+        asrate = smin((R)RG_ONE, (R)(P.pm9 * DT1));
+      else
+        asrate = smin(1.f, P.f.pm9 * dt1);
+    }
+    const R a1 = PC(a1);
+    const R a2 = PC(a2);
+    const R epdr = smax(PC(eps0) * dt1, (R)RG_EM20);
+    // LOG(EPSP/EPDR) of the previous point: the points usually share one
+    // strain rate (ASRATE = 1), and an equal argument gives the same value
+    R memo_epsp = (R)-1, memo_log = (R)0;
+    R sigy_acc = (R)0;  // SIGY: YLD / NPT summed over the points so far
+    // point state: point it+1 is loaded while point it is computed
+    R nx_sig[5], nx_ep = (R)0, nx_pla = (R)0;
+    if constexpr (!STAGE) {
+#pragma unroll
+      for (int c = 0; c < 5; c++) nx_sig[c] = S.sig[(c)*nc + e];
+      nx_ep = S.epsd[e];
+      nx_pla = S.pla[e];
+    }
+#pragma unroll
+    for (int it = 0; it < NPT; it++) {
+      R sn[5];
+      R ep, pla_in;
+      if constexpr (STAGE) {
+        // the staged point state (shared memory, this thread's slots)
+#pragma unroll
+        for (int c = 0; c < 5; c++) sn[c] = stg[(SG_SIG + it * 5 + c) * SHELL_STG_NT + tid];
+        ep = stg[(SG::epsd + it) * SHELL_STG_NT + tid];
+        pla_in = stg[(SG::pla + it) * SHELL_STG_NT + tid];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 5; c++) sn[c] = nx_sig[c];
+        ep = nx_ep;
+        pla_in = nx_pla;
+        if (it + 1 < NPT) {
+          const int q5 = ((it + 1) * 5) * nc + e;
+#pragma unroll
+          for (int c = 0; c < 5; c++) nx_sig[c] = S.sig[q5 + c * nc];
+          nx_ep = S.epsd[(it + 1) * nc + e];
+          nx_pla = S.pla[(it + 1) * nc + e];
+        }
+      }
+      const R thkly = pcoef<R>(c_wfd[NPT - 1][it], c_wf[NPT - 1][it]);
+      const R thklyl = thkly * thk0;
+      const R wmc = pcoef<R>(c_wmd[NPT - 1][it], c_wm[NPT - 1][it]);
+      const R zt = pcoef<R>(c_z0d[NPT - 1][it], c_z0[NPT - 1][it]) * thk0;
+      const R depsxx = exx + zt * kxx;
+      const R depsyy = eyy + zt * kyy;
+      const R depsxy = exy + zt * kxy;
+      const int ip5 = (it * 5) * nc + e;
+      R epsdot;
+      if (P.vp == 2) {
+        ep = asrate * epsd_pg + ((R)RG_ONE - asrate) * ep;
+        S.epsd[it * nc + e] = ep;
+        epsdot = ep * dt1;
+      } else {
+        epsdot = ep * dt1;
+      }
+      R ezz = (R)0;
+      R ca = PC(ca), cb = PC(cb), ymax = PC(ymax);
+      // T* of the point (sigeps02c.F:125), 0 without adiabatic heating
+      R tstar = (R)0;
+      if (P.thermal) tstar = smax((R)0, (S.temp[it * nc + e] - PC(tref)) / (PC(tmelt) - PC(tref)));
+      // kinematic hardening: the predictor works on the shifted stress
+      // (m2cplr.F:115-121)
+      const bool kin = P.fisokin > 0.0;
+      R sgb[3] = {(R)0, (R)0, (R)0};
+      if (kin) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          sgb[c] = S.sigbak[(it * 3 + c) * nc + e];
+          sn[c] = sn[c] - sgb[c];
+        }
+      }
+      sn[0] = sn[0] + a1 * depsxx + a2 * depsyy;
+      sn[1] = sn[1] + a2 * depsxx + a1 * depsyy;
+      sn[2] = sn[2] + gmod * depsxy;
+      sn[3] = sn[3] + gs * eyz;
+      sn[4] = sn[4] + gs * exz;
+      if (P.f.cc_nz) {
+        R epsp = epsdot;
+        if (P.israte == 0 && P.vp == 2)
+          epsp = smax(smax(fabs(depsxx), fabs(depsyy)), (R)RG_HALF * fabs(depsxy));
+        epsp = smax(epsp, epdr);
+        R logep;
+        if (epsp == memo_epsp) {
+          logep = memo_log;
+        } else {
+          logep = log(epsp / epdr);
+          memo_epsp = epsp;
+          memo_log = logep;
+        }
+        R q = ((R)RG_ONE + PC(cc) * logep);
+        if (tstar != (R)0) q = q * ((R)RG_ONE - exp(PC(m_exp) * log(tstar)));
+        q = smax(q, (R)RG_EM20);
+        ca = ca * q;
+        cb = cb * q;
+        if (P.icc == 1) ymax = ymax * q;
+      } else if (tstar != (R)0) {
+        // CC = 0: thermal softening alone (m2cplr.F:169-178)
+        R q = (R)RG_ONE - exp(PC(m_exp) * log(tstar));
+        q = smax(q, (R)RG_EM20);
+        ca = ca * q;
+        cb = cb * q;
+      }
+      R pla = pla_in;
+      R yld;
+      if (kin)
+        yld = pla == (R)0 ? ca : ca + cb * ((R)RG_ONE - PC(fisokin)) * exp(PC(cn) * log(pla));
+      else
+        yld = pla == (R)0 ? ca : ca + cb * exp(PC(cn) * log(pla));
+      yld = smin(yld, ymax);
+      R h = (R)0, dpla_pt = (R)0;  // hardening modulus and DPLA of the point
+      if (P.ipla == 0) {
+        const R svm = sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2]);
+        const R r = smin((R)RG_ONE, yld / (svm + (R)RG_EM15));
+        if (r < (R)RG_ONE) {
+          sn[0] = sn[0] * r;
+          sn[1] = sn[1] * r;
+          sn[2] = sn[2] * r;
+          const R dpla = off * smax((R)0, (svm - yld) / ym);
+          const R s1 = (R)RG_HALF * (sn[0] + sn[1]);
+          ezz = dpla * s1 / yld;
+          pla = pla + dpla;
+          dpla_pt = dpla;
+          if (kin && yld < ymax) h = PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
+        }
+      } else if (P.ipla == 2) {
+        // m2cplr.F:380-445: projection along an approximate normal, then a
+        // radial return to the yield stress advanced by H * DPLA
+        const R svm2 = sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2];
+        const R yld2 = yld * yld;
+        if (svm2 > yld2 && off == (R)RG_ONE) {
+          const R svm = sqrt(svm2);
+          h = yld >= ymax ? (R)0 : PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
+          const R aa = (svm2 - yld2) /
+                       ((R)RG_FIVE * svm2 + (R)RG_THREE * (-(sn[0] * sn[1]) + sn[2] * sn[2]));
+          const R s1 = ((R)RG_ONE - (R)RG_TWO * aa) * sn[0] + aa * sn[1];
+          const R s2 = aa * sn[0] + ((R)RG_ONE - (R)RG_TWO * aa) * sn[1];
+          const R s3 = ((R)RG_ONE - (R)RG_THREE * aa) * sn[2];
+          sn[0] = s1;
+          sn[1] = s2;
+          sn[2] = s3;
+          const R dpla = off * (svm - yld) / ((R)RG_THREE * gmod + h);
+          pla = pla + dpla;
+          yld = yld + h * dpla;
+          dpla_pt = dpla;
+          const R svmn = sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2]);
+          const R r = smin((R)RG_ONE, yld / smax((R)RG_EM20, svmn));
+          sn[0] = sn[0] * r;
+          sn[1] = sn[1] * r;
+          sn[2] = sn[2] * r;
+          ezz = dpla * (R)RG_HALF * (sn[0] + sn[1]) / yld;
+        }
+      } else {
+        const R s1 = sn[0] + sn[1];
+        const R s2 = sn[0] - sn[1];
+        const R s3 = sn[2];
+        const R A = (R)RG_FOURTH * s1 * s1;
+        const R B = (R)RG_THREE_OVER_4 * s2 * s2 + (R)RG_THREE * s3 * s3;
+        // SVM > YLD tested on the squares (YLD >= 0): the square root is
+        // only taken at yielding points
+        if (A + B > yld * yld && off == (R)RG_ONE) {
+          const R svm = sqrt(A + B);
+          const R nu1 = PC(inv1mnu);
+          const R nu2 = PC(inv1pnu);
+          h = yld >= ymax ? (R)0 : PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
+          R dpla_j = (svm - yld) / ((R)RG_THREE * gmod + h);
+          // isotropic Newton (FISOKIN = 0), or the kinematic / mixed one with
+          // modified NU1, NU2 and the isotropic part of H (m2cplr.F:324-336)
+          R anu1 = A * nu1;
+          R bnu2 = (R)RG_THREE * B * nu2;
+          R h2 = (R)RG_TWO * h;
+          R nu11 = (R)0, nu21 = (R)0, beta = (R)RG_ONE;
+          if (kin) {
+            const R bh = h * PC(fisokin);
+            const R hi = h - bh;
+            const R hk = (R)RG_TWO_THIRD * bh;
+            const R aaa = (R)RG_THREE * hk / ym;
+            nu11 = nu1 + aaa;
+            nu21 = (R)RG_THREE * nu2 + aaa;
+            anu1 = A * nu11;
+            bnu2 = B * nu21;
+            h2 = (R)RG_TWO * hi;
+            beta = (R)RG_ONE - PC(fisokin);
+          }
+          R dpla_i = 0, Pp = 1, Qq = 1, dr = 0;
+#pragma unroll
+          for (int n = 0; n < 3; n++) {
+            dpla_i = dpla_j;
+            const R pla_i = pla + dpla_i;
+            R yld_i;
+            if (pla_i == (R)0)
+              yld_i = smin(ymax, ca);
+            else if (kin)
+              yld_i = smin(ymax, ca + beta * cb * exp(PC(cn) * log(pla_i)));
+            else
+              yld_i = smin(ymax, ca + cb * exp(PC(cn) * log(pla_i)));
+            // FP64 form: the two divisions by YLD_I, and P and Q, each from
+            // one reciprocal (FP64-pipe work of the plastic points)
+            R inv_y = (R)0;
+            if constexpr (F64) {
+              inv_y = (R)RG_ONE / yld_i;
+              dr = (R)RG_HALF * ym * dpla_i * inv_y;
+              const R dp = (R)RG_ONE + dr * (kin ? nu11 : nu1);
+              const R dq = kin ? (R)RG_ONE + dr * nu21 : (R)RG_ONE + (R)RG_THREE * dr * nu2;
+              const R rpq = (R)RG_ONE / (dp * dq);
+              Pp = dq * rpq;
+              Qq = dp * rpq;
+            } else {
+              dr = (R)RG_HALF * ym * dpla_i / yld_i;
+              Pp = (R)RG_ONE / ((R)RG_ONE + dr * (kin ? nu11 : nu1));
+              Qq = kin ? (R)RG_ONE / ((R)RG_ONE + dr * nu21)
+                       : (R)RG_ONE / ((R)RG_ONE + (R)RG_THREE * dr * nu2);
+            }
+            const R p2 = Pp * Pp, q2 = Qq * Qq;
+            const R f = A * p2 + B * q2 - yld_i * yld_i;
+            R df;
+            if constexpr (F64)
+              df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) * inv_y - h2 * yld_i;
+            else
+              df = -(anu1 * p2 * Pp + bnu2 * q2 * Qq) * (ym - dr * h2) / yld_i - h2 * yld_i;
+            dpla_j = dpla_i > (R)0 ? smax((R)0, dpla_i - f / df) : (R)0;
+          }
+          pla = pla + dpla_i;
+          dpla_pt = dpla_i;
+          const R t1 = (sn[0] + sn[1]) * Pp;
+          const R t2 = (sn[0] - sn[1]) * Qq;
+          sn[0] = (R)RG_HALF * (t1 + t2);
+          sn[1] = (R)RG_HALF * (t1 - t2);
+          sn[2] = sn[2] * Qq;
+          ezz = dr * t1 / ym;
+          // kinematic: YLD from the new PLA, H kept (m2cplr.F:465-476)
+          if (kin) yld = pla == (R)0 ? ca : smin(ymax, ca + beta * cb * exp(PC(cn) * log(pla)));
+        }
+      }
+      // kinematic / mixed hardening: back stress update, stress shifted back
+      // (m2cplr.F:477-490)
+      if (kin) {
+        const R alpha = PC(fisokin) * h * dpla_pt / yld;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          sgb[c] = sgb[c] + alpha * sn[c];
+          sn[c] = sn[c] + sgb[c];
+          S.sigbak[(it * 3 + c) * nc + e] = sgb[c];
+        }
+      }
+      // SIGEPS02C: SIGY accumulates YLD / NPT over the points so far, and
+      // this point's adiabatic heating uses that running sum
+      // (sigeps02c.F:197-199, 226-229; SIGY zeroed per group, mulawc.F90:577)
+      if (P.thermal) {
+        sigy_acc = sigy_acc + yld / (R)NPT;
+        S.temp[it * nc + e] = S.temp[it * nc + e] + sigy_acc * dpla_pt / PC(rhocp);
+      }
+      S.pla[it * nc + e] = pla;
+      ezz = -(depsxx + depsyy) * nu - ((R)RG_ONE - (R)RG_TWO * nu) * ezz;
+      ezz = ezz * PC(inv1mnu);
+      thkn = thkn + (double)(ezz * thklyl * off);
+#pragma unroll
+      for (int c = 0; c < 5; c++) {
+        S.sig[ip5 + c * nc] = sn[c];
+        forn[c] = forn[c] + thkly * sn[c];
+      }
+      momn[0] = momn[0] + wmc * sn[0];
+      momn[1] = momn[1] + wmc * sn[1];
+      momn[2] = momn[2] + wmc * sn[2];
+    }
+    S.thk[e] = thkn > RG_EM30 ? thkn : RG_EM30;
+    if (P.f.dm_nz) {
+      const R dtinv = DT1in >= 0.0 ? dtinv_in : dt1 / smax(dt1 * dt1, (R)RG_EM20);
+      const R visc = ((R)RG_ONEP414 * PC(dm)) * ssp * sqrt(area) * dtinv * rho;
+      forn[0] = forn[0] + visc * (exx + (R)RG_HALF * eyy);
+      forn[1] = forn[1] + visc * (eyy + (R)RG_HALF * exx);
+      forn[2] = forn[2] + visc * exy * (R)RG_THIRD;
+    }
+#pragma unroll
+    for (int c = 0; c < 5; c++) forn[c] = forn[c] * off;
+#pragma unroll
+    for (int c = 0; c < 3; c++) momn[c] = momn[c] * off;
+    degmb = degmb + forn[0] * exx + forn[1] * eyy + forn[2] * exy + forn[3] * eyz + forn[4] * exz;
+    degfx = degfx + momn[0] * kxx + momn[1] * kyy + momn[2] * kxy;
+    if constexpr (STAGE) {
+      st_eint0 = stgd[0 * SHELL_STG_NT + tid];
+      st_eint1 = stgd[1 * SHELL_STG_NT + tid];
+    }
+    {
+      const R vol2 = (R)RG_HALF * vol0;
+      S.eint[e] = st_eint0 + (double)(degmb * vol2);
+      S.eint[nc + e] = st_eint1 + (double)(degfx * thk0 * vol2);
+    }
+#pragma unroll
+    for (int c = 0; c < 5; c++) S.forc[c * nc + e] = forn[c];
+#pragma unroll
+    for (int c = 0; c < 3; c++) S.mom[c * nc + e] = momn[c];
     // ---- CFINT3 ----
     R F[3][4], M[3][4];
     {

@@ -67,9 +67,12 @@ def law1(rho, young, nu):
 
 
 def law2(rho, young, nu, a, b, n, c=0.0, eps0=1.0, epsmax=0.0, sigmax=0.0,
-         m_exp=0.0, vp=0, icc=0, fcut=0.0):
+         m_exp=0.0, vp=0, icc=0, fcut=0.0, fisokin=0.0, rhocp=0.0, tref=0.0, tmelt=0.0):
     """/MAT/PLAS_JOHNS (LAW2, Johnson-Cook) with the reader's defaults
-    (starter/source/materials/mat/mat002/hm_read_mat02_jc.F90:100-135)."""
+    (starter/source/materials/mat/mat002/hm_read_mat02_jc.F90:100-200,
+    249-251, 329-349): FISOKIN in uparam(8), the thermal parameters in
+    PM(69) = rho Cp, PM(79) = T_r (300 when not positive), PM(80) = T_melt
+    (1e20 when 0)."""
     pm = np.zeros(NPROPM)
     g, bulk = _g_bulk(young, nu)
     if n == 0.0:
@@ -99,8 +102,13 @@ def law2(rho, young, nu, a, b, n, c=0.0, eps0=1.0, epsmax=0.0, sigmax=0.0,
     _plane_stress(pm, young, nu, rho)
     pm[37], pm[38], pm[39] = a, b, n
     pm[88] = rho
+    if tref <= 0.0:
+        tref = 300.0
+    if tmelt == 0.0:
+        tmelt = 1e20
+    pm[68], pm[78], pm[79] = rhocp, tref, tmelt
     up = np.zeros(NUPARAM)
-    up[:10] = [a, b, n, epsmax, sigmax, c, eps0, 0.0, asrate, m_exp]
+    up[:10] = [a, b, n, epsmax, sigmax, c, eps0, fisokin, asrate, m_exp]
     ip = np.zeros(NIPARAM, np.int32)
     ip[:4] = [0, icc, vp, israte]
     return dict(mtn=2, pm=pm, uparam=up, iparam=ip)

@@ -937,6 +937,7 @@ int or_hexa_group_add(void *m, int nel, const int *ixs, int mtn,
       G.asrate = uparam[8];
       G.z3 = uparam[9];
       if (G.iform != 0 || G.fisokin != 0.0) return -4;
+      if (pm[68] > 0.0) return -4;  // adiabatic heating: no element temperature
     }
     M.hg.push_back(G);
   }

@@ -58,6 +58,10 @@ struct Group {
   double ca = 0, cb = 0, cn = 1, epmx = 0, ymax = 0, cc = 0, eps0 = 1, fisokin = 0;
   double pm9 = 0;
   int icc = 1, vp = 2, israte = 0;
+  // Johnson-Cook thermal softening (mat_param%therm, uparam(10)): adiabatic
+  // heating when RHOCP > 0, each point starting at TREF (allocbuf_auto.F:189)
+  double m_exp = 1, tref = 300, tmelt = 1e20, rhocp = 0;
+  int thermal = 0;
 };
 
 struct Shells {
@@ -68,6 +72,9 @@ struct Shells {
   // state (element SoA)
   std::vector<double> offg, thk, thke, forc, mom, eint, hour, gstr, epsdg;
   std::vector<double> sig, pla, epsd;  // per IP: [npt][numelc] (max npt 5)
+  std::vector<double> sigbak;          // back stress per IP: [npt][3][numelc]
+  std::vector<double> temp;            // temperature per IP: [npt][numelc]
+  bool temp_init = false;
   std::vector<double> ehou;            // accumulated hourglass energy
   int nptmax = 5;
   int ishfram = 0;                     // local frame (/SHFRA/V4: 2)
@@ -117,7 +124,12 @@ int group_add(Shells *S, int nel, const int *ixc, int npt, const double *pm,
   G.ish = geo[36];
   G.fsh = geo[37];
   G.ipla = (int)geo[38];
-  if (iparam[0] != 0 || uparam[7] != 0.0) return -4;
+  if (iparam[0] != 0) return -4;  // Zerilli-Armstrong (IFORM = 1) not restated
+  if (uparam[7] < 0.0 || uparam[7] > 1.0) return -4;
+  // ductile rupture (SIGEPS02C EPMX test and MULAWC's layer failure) is not
+  // restated: a finite EPMX is refused (the reader's default 1e20 is never
+  // reached)
+  if (uparam[3] < 1e20) return -4;
   G.icc = iparam[1];
   G.vp = iparam[2];
   G.israte = iparam[3];
@@ -129,6 +141,12 @@ int group_add(Shells *S, int nel, const int *ixc, int npt, const double *pm,
   G.cc = uparam[5];
   G.eps0 = uparam[6];
   G.pm9 = uparam[8];
+  G.fisokin = uparam[7];
+  G.m_exp = uparam[9] != 0.0 ? uparam[9] : 1.0;
+  G.rhocp = pm[68];
+  G.tref = pm[78];
+  G.tmelt = pm[79];
+  G.thermal = (G.rhocp > 0.0 && G.tmelt > G.tref) ? 1 : 0;
   S->groups.push_back(G);
   S->ixc.insert(S->ixc.end(), ixc, ixc + 7 * (size_t)nel);
   S->numelc += nel;
@@ -146,6 +164,8 @@ int group_add(Shells *S, int nel, const int *ixc, int npt, const double *pm,
   S->pla.resize(5 * (size_t)n, 0.0);
   S->epsd.resize(5 * (size_t)n, 0.0);
   S->ehou.resize(n, 0.0);
+  S->sigbak.resize(5 * 3 * (size_t)n, 0.0);
+  S->temp.resize(5 * (size_t)n, G.tref);
   return (int)S->groups.size() - 1;
 }
 
@@ -158,6 +178,8 @@ int group_add(Shells *S, int nel, const int *ixc, int npt, const double *pm,
 #define SIG_(c, p, e) S->sig[((size_t)(p) * 5 + (c)) * S->numelc + (e)]
 #define PLA_(p, e) S->pla[(size_t)(p) * S->numelc + (e)]
 #define EPS_(p, e) S->epsd[(size_t)(p) * S->numelc + (e)]
+#define SGB_(c, p, e) S->sigbak[((size_t)(p) * 3 + (c)) * S->numelc + (e)]
+#define TMP_(p, e) S->temp[(size_t)(p) * S->numelc + (e)]
 
 static inline double dmax(double a, double b) { return a > b ? a : b; }
 static inline double dmin(double a, double b) { return a < b ? a : b; }
@@ -390,6 +412,7 @@ static void element(Shells *S, const Group &G, int e, const double *X,
   double forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
   const double asrate = G.israte > 0 ? dmin(RG_ONE, G.pm9 * DT1) : RG_ONE;
   const int npt = G.npt;
+  double sigy_acc = RG_ZERO;
   for (int it = 0; it < npt; it++) {
     const double thkly = (double)WFT[npt - 1][it];
     const double thklyl = thkly * thk0;
@@ -416,10 +439,23 @@ static void element(Shells *S, const Group &G, int e, const double *X,
         epsdot = ep * DT1;  // VP = 1: previous filtered plastic rate
       }
     }
+    // SIGEPS02C: T* from the point's temperature (sigeps02c.F:125; JC, the
+    // point buffer starts at TINI = TREF, allocbuf_auto.F:189)
+    double tstar = RG_ZERO;
+    if (G.thermal) tstar = dmax(RG_ZERO, (TMP_(it, e) - G.tref) / (G.tmelt - G.tref));
     // M2CPLR (materials/mat/mat002/m2cplr.F:29)
     double ezz = RG_ZERO;
     double ca = G.ca, cb = G.cb, ymax = G.ymax, h = RG_ZERO;
+    double dpla = RG_ZERO;
+    const double fisokin = G.fisokin;
     for (int c = 0; c < 5; c++) sn[c] = so[c];
+    // kinematic hardening: the predictor works on the shifted stress
+    // (m2cplr.F:115-121)
+    if (fisokin > RG_ZERO) {
+      sn[0] = sn[0] - SGB_(0, it, e);
+      sn[1] = sn[1] - SGB_(1, it, e);
+      sn[2] = sn[2] - SGB_(2, it, e);
+    }
     sn[0] = sn[0] + a1 * depsxx + a2 * depsyy;
     sn[1] = sn[1] + a2 * depsxx + a1 * depsyy;
     sn[2] = sn[2] + gg * depsxy;
@@ -432,18 +468,28 @@ static void element(Shells *S, const Group &G, int e, const double *X,
         epsp = dmax(dmax(std::fabs(depsxx), std::fabs(depsyy)), RG_HALF * std::fabs(depsxy));
       epsp = dmax(epsp, epdr);
       logep = std::log(epsp / epdr);
-      double q = (RG_ONE + G.cc * logep);
+      double q;
+      if (tstar == RG_ZERO)
+        q = (RG_ONE + G.cc * logep);
+      else
+        q = (RG_ONE + G.cc * logep) * (RG_ONE - std::exp(G.m_exp * std::log(tstar)));
       q = dmax(q, RG_EM20);
       ca = ca * q;
       cb = cb * q;
       if (G.icc == 1) ymax = ymax * q;
+    } else if (tstar != RG_ZERO) {
+      // CC = 0: thermal softening alone (m2cplr.F:169-178)
+      double q = RG_ONE - std::exp(G.m_exp * std::log(tstar));
+      q = dmax(q, RG_EM20);
+      ca = ca * q;
+      cb = cb * q;
     }
     double &pla = PLA_(it, e);
     double yld;
     if (pla == RG_ZERO)
       yld = ca;
     else
-      yld = ca + cb * (RG_ONE - G.fisokin) * std::exp(G.cn * std::log(pla));
+      yld = ca + cb * (RG_ONE - fisokin) * std::exp(G.cn * std::log(pla));
     yld = dmin(yld, ymax);
     if (G.ipla == 0) {
       const double svm = std::sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + RG_THREE * sn[2] * sn[2]);
@@ -452,10 +498,44 @@ static void element(Shells *S, const Group &G, int e, const double *X,
         sn[0] = sn[0] * r;
         sn[1] = sn[1] * r;
         sn[2] = sn[2] * r;
-        const double dpla = off * dmax(RG_ZERO, (svm - yld) / young);
+        dpla = off * dmax(RG_ZERO, (svm - yld) / young);
         const double s1 = RG_HALF * (sn[0] + sn[1]);
         ezz = dpla * s1 / yld;
         pla = pla + dpla;
+        if (yld >= ymax)
+          h = RG_ZERO;
+        else
+          h = G.cn * cb * std::exp((G.cn - RG_ONE) * std::log(pla + RG_EM07));
+      }
+    } else if (G.ipla == 2) {
+      // m2cplr.F:380-445: projection along an approximate normal, then a
+      // radial return to the updated yield stress
+      const double svm2 = sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + RG_THREE * sn[2] * sn[2];
+      const double svm = std::sqrt(svm2);
+      const double yld2 = yld * yld;
+      if (svm2 > yld2 && off == RG_ONE) {
+        if (yld >= ymax)
+          h = RG_ZERO;
+        else
+          h = G.cn * cb * std::exp((G.cn - RG_ONE) * std::log(pla + RG_EM07));
+        const double aa = (svm2 - yld2) /
+                          (RG_FIVE * svm2 + RG_THREE * (-(sn[0] * sn[1]) + sn[2] * sn[2]));
+        const double s1 = (RG_ONE - RG_TWO * aa) * sn[0] + aa * sn[1];
+        const double s2 = aa * sn[0] + (RG_ONE - RG_TWO * aa) * sn[1];
+        const double s3 = (RG_ONE - RG_THREE * aa) * sn[2];
+        sn[0] = s1;
+        sn[1] = s2;
+        sn[2] = s3;
+        dpla = off * (svm - yld) / (RG_THREE * gg + h);
+        pla = pla + dpla;
+        yld = yld + h * dpla;
+        const double svmn =
+            std::sqrt(sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + RG_THREE * sn[2] * sn[2]);
+        const double r = dmin(RG_ONE, yld / dmax(RG_EM20, svmn));
+        sn[0] = sn[0] * r;
+        sn[1] = sn[1] * r;
+        sn[2] = sn[2] * r;
+        ezz = dpla * RG_HALF * (sn[0] + sn[1]) / yld;
       }
     } else {
       const double s1 = sn[0] + sn[1];
@@ -472,9 +552,22 @@ static void element(Shells *S, const Group &G, int e, const double *X,
         else
           h = G.cn * cb * std::exp((G.cn - RG_ONE) * std::log(pla + RG_EM07));
         double dpla_j = (svm - yld) / (RG_THREE * gg + h);
-        const double anu1 = A * nu1;
-        const double bnu2 = RG_THREE * B * nu2;
-        const double h2 = RG_TWO * h;
+        // isotropic Newton (FISOKIN = 0) or the kinematic / mixed one
+        // (m2cplr.F:289-363): modified NU1, NU2 and the isotropic part of H
+        double nu1k = nu1, nu2k = RG_THREE * nu2, h2 = RG_TWO * h, beta = RG_ONE;
+        double anu1 = A * nu1, bnu2 = RG_THREE * B * nu2;
+        if (fisokin > RG_ZERO) {
+          const double bh = h * fisokin;
+          const double hi = h - bh;
+          const double hk = RG_TWO_THIRD * bh;
+          const double aaa = RG_THREE * hk / young;
+          nu1k = nu1 + aaa;
+          nu2k = RG_THREE * nu2 + aaa;
+          anu1 = A * nu1k;
+          bnu2 = B * nu2k;
+          h2 = RG_TWO * hi;
+          beta = RG_ONE - fisokin;
+        }
         double dpla_i = 0, P = 1, Q = 1, dr = 0;
         for (int n = 0; n < 3; n++) {
           dpla_i = dpla_j;
@@ -482,11 +575,18 @@ static void element(Shells *S, const Group &G, int e, const double *X,
           double yld_i;
           if (pla_i == RG_ZERO)
             yld_i = dmin(ymax, ca);
+          else if (fisokin > RG_ZERO)
+            yld_i = dmin(ymax, ca + beta * cb * std::exp(G.cn * std::log(pla_i)));
           else
             yld_i = dmin(ymax, ca + cb * std::exp(G.cn * std::log(pla_i)));
           dr = RG_HALF * young * dpla_i / yld_i;
-          P = RG_ONE / (RG_ONE + dr * nu1);
-          Q = RG_ONE / (RG_ONE + RG_THREE * dr * nu2);
+          if (fisokin > RG_ZERO) {
+            P = RG_ONE / (RG_ONE + dr * nu1k);
+            Q = RG_ONE / (RG_ONE + dr * nu2k);
+          } else {
+            P = RG_ONE / (RG_ONE + dr * nu1);
+            Q = RG_ONE / (RG_ONE + RG_THREE * dr * nu2);
+          }
           const double p2 = P * P, q2 = Q * Q;
           const double f = A * p2 + B * q2 - yld_i * yld_i;
           const double df = -(anu1 * p2 * P + bnu2 * q2 * Q) * (young - dr * h2) / yld_i - h2 * yld_i;
@@ -495,6 +595,7 @@ static void element(Shells *S, const Group &G, int e, const double *X,
           else
             dpla_j = RG_ZERO;
         }
+        dpla = dpla_i;
         pla = pla + dpla_i;
         const double t1 = (sn[0] + sn[1]) * P;
         const double t2 = (sn[0] - sn[1]) * Q;
@@ -502,8 +603,30 @@ static void element(Shells *S, const Group &G, int e, const double *X,
         sn[1] = RG_HALF * (t1 - t2);
         sn[2] = sn[2] * Q;
         ezz = dr * t1 / young;
+        // kinematic: YLD from the new PLA, H kept (m2cplr.F:465-476)
+        if (fisokin > RG_ZERO) {
+          if (pla == RG_ZERO)
+            yld = ca;
+          else
+            yld = dmin(ymax, ca + beta * cb * std::exp(G.cn * std::log(pla)));
+        }
       }
     }
+    // kinematic / mixed hardening: back stress update, stress shifted back
+    // (m2cplr.F:477-490)
+    if (fisokin > RG_ZERO) {
+      const double hkin = fisokin * h;
+      const double alpha = hkin * dpla / yld;
+      for (int c = 0; c < 3; c++) {
+        SGB_(c, it, e) = SGB_(c, it, e) + alpha * sn[c];
+        sn[c] = sn[c] + SGB_(c, it, e);
+      }
+    }
+    // SIGEPS02C: SIGY accumulates YLD / NPT over the points so far, and the
+    // adiabatic heating of this point uses that running sum
+    // (sigeps02c.F:197-199, 226-229; SIGY zeroed per group, mulawc.F90:577)
+    sigy_acc = sigy_acc + yld / (double)npt;
+    if (G.thermal) TMP_(it, e) = TMP_(it, e) + sigy_acc * dpla / G.rhocp;
     // SIGEPS02C epilogue: thickness strain, thickness (INLOC = 0)
     ezz = -(depsxx + depsyy) * nuu - (RG_ONE - RG_TWO * nuu) * ezz;
     ezz = ezz / (RG_ONE - nuu);
@@ -715,6 +838,13 @@ void step(Shells *S, const double *X, const double *V, const double *VR,
   const int ne = S->numelc;
   if (ne == 0) return;
   const int ng = (int)S->groups.size();
+  if (!S->temp_init) {
+    // each point's temperature starts at its material's TREF (TINI)
+    for (const Group &G : S->groups)
+      for (int p = 0; p < 5; p++)
+        for (int i = 0; i < G.nel; i++) TMP_(p, G.nft + i) = G.tref;
+    S->temp_init = true;
+  }
   std::vector<double> gdt(ng, RG_EP06);
   std::vector<int> gel(ng, -1);
   RG_OPCOUNT_PHASE(2);
@@ -779,6 +909,16 @@ int get_state(const Shells *S, int which, double *out) {
       return 0;
     }
     case 7: std::copy(S->hour.begin(), S->hour.begin() + 5 * n, out); return 0;
+    case 8: {  // back stress per IP: [npt][3][n]
+      const int npt = S->groups.empty() ? 0 : S->groups[0].npt;
+      std::copy(S->sigbak.begin(), S->sigbak.begin() + 3 * npt * n, out);
+      return 0;
+    }
+    case 9: {  // temperature per IP: [npt][n]
+      const int npt = S->groups.empty() ? 0 : S->groups[0].npt;
+      std::copy(S->temp.begin(), S->temp.begin() + npt * n, out);
+      return 0;
+    }
   }
   return -1;
 }

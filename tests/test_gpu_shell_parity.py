@@ -125,3 +125,51 @@ def test_formulation_combinations(Engine, oracle_lib, ishfram, ithk, iplas, npt)
     assert rel(ng["VR"], no["VR"]) < 1e-10
     # thickness (updated in both ITHK modes by the material)
     assert rel(e.shell_state(2, m.numelc), o.shell_state(2, m.numelc)) < 1e-10
+
+
+@pytest.mark.parametrize("iplas,fisokin,rhocp,cc", [
+    (2, 0.0, 0.0, 0.022),      # IPLA = 2: normal projection + radial return
+    (0, 0.5, 0.0, 0.022),      # mixed hardening, radial return
+    (1, 0.5, 0.0, 0.022),      # mixed hardening, plane-stress Newton
+    (2, 1.0, 0.0, 0.0),        # kinematic hardening, IPLA = 2, no rate effect
+    (1, 0.0, 3.6e5, 0.022),    # adiabatic heating and thermal softening
+    (0, 0.3, 3.6e5, 0.0),      # heating without strain rate, with mixed hardening
+])
+def test_m2cplr_branches(Engine, oracle_lib, iplas, fisokin, rhocp, cc):
+    """The M2CPLR branches beyond the benchmark's (IPLA = 2, kinematic and
+    mixed hardening, Johnson-Cook thermal softening with adiabatic heating;
+    m2cplr.F:115-121, 146-180, 289-490, sigeps02c.F:125, 226-229) on a
+    deforming crash box against the oracle: first-cycle forces and moments
+    1e-12, 150-cycle trajectories, thickness, back stress and temperature
+    1e-10 (plastic strain 1e-8, as in the other shell tests)."""
+    m = M.crash_box(n_side=5, n_len=12, v0=40.0, vpert=3.0, npt=5)
+    g = m.shells[0]
+    g.mat = M.law2(7850.0, 210e9, 0.3, 350e6, 275e6, 0.36, c=cc, eps0=1.0,
+                   fisokin=fisokin, rhocp=rhocp, tmelt=800.0 if rhocp else 0.0)
+    g.geo[38] = iplas
+    e = Engine(m)
+    o = oracle_lib.OracleModel(m, nthreads=2)
+    e.cycle(1)
+    o.cycle(1)
+    fg, fo = e.forces(), o.nodes()
+    assert rel(fg["F"], fo["F"]) < 1e-12
+    assert rel(fg["FR"], fo["FR"]) < 1e-12
+    e.cycle(149)
+    o.cycle(149)
+    ng, no = e.nodes(), o.nodes()
+    nc = m.numelc
+    assert rel(ng["X"] - m.X, no["X"] - m.X) < 1e-10
+    assert rel(ng["VR"], no["VR"]) < 1e-10
+    assert rel(e.shell_state(2, nc), o.shell_state(2, nc)) < 1e-10
+    pg, po = e.shell_state(6, 5 * nc), o.shell_state(6, 5 * nc)
+    assert po.max() > 0.0, "the case must yield"
+    assert rel(pg, po) < 1e-8
+    if fisokin > 0.0:
+        bg, bo = e.shell_state(8, 15 * nc), o.shell_state(8, 15 * nc)
+        assert np.max(np.abs(bo)) > 0.0
+        assert rel(bg, bo) < 1e-10
+    if rhocp > 0.0:
+        tg, to = e.shell_state(9, 5 * nc), o.shell_state(9, 5 * nc)
+        assert to.max() > 300.0 + 1.0, "adiabatic heating must raise the temperature"
+        assert rel(tg - 300.0, to - 300.0) < 1e-10
+    assert e.status() == 0
