@@ -572,7 +572,7 @@ def run_ours(args, rank, world, local_rank):
         if model.shells:
             try:
                 line["reference_gpu_shell"] = reference_gpu_shell(model, args, local_rank,
-                                                                  res64["kt"]["shell"])
+                                                                  res64["kt"])
             except Exception as ex:  # the comparator is optional
                 line["reference_gpu_shell"] = {"unavailable": repr(ex)[:200]}
     return line
@@ -674,6 +674,7 @@ def run_sweep(args, njobs=SWEEP_JOBS, cycles=SWEEP_CYCLES_PER_JOB, device=0):
 SERVE_JOBS = 32
 SERVE_RATE = 4.0          # Poisson arrivals, jobs/s
 SERVE_BUDGET = 48 << 30   # HBM budget of the serving loop (bytes)
+SERVE_ELEMENTS = 400_000  # elements in flight of the least-work-first policy
 
 
 def run_serving(args, njobs=SERVE_JOBS, device=0):
@@ -706,9 +707,17 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
             free = start + t
             lat.append(free - float(a))
         return float(np.percentile(lat, 50)), float(np.percentile(lat, 99))
+    reqs = [(k, m, n, float(a)) for k, ((m, n), a) in enumerate(zip(jobs, arr))]
+    # every arrived job admitted at once (arrival order, HBM budget only)
     srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device)
+    st_all = srv.run(reqs)
+    srv.close()
+    # least work first, at most SERVE_ELEMENTS elements in flight (one large
+    # model already fills the GPU: more concurrency only shares it)
+    srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device,
+                 policy="sjf", max_elements=SERVE_ELEMENTS)
     with Clocks(device) as clk:
-        st = srv.run([(k, m, n, float(a)) for k, ((m, n), a) in enumerate(zip(jobs, arr))])
+        st = srv.run(reqs)
     bad = sum(1 for r in srv.done if r.result.get("status", 0)) + len(srv.failed)
     srv.close()
     seq_jobs_h = {p: 3600.0 * njobs / seq[p] for p in seq}
@@ -725,6 +734,7 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
                    "elements_per_job": [min(ne), max(ne)],
                    "cycles_per_job": [min(n for _, n in jobs), max(n for _, n in jobs)],
                    "hbm_budget_gb": SERVE_BUDGET / 2 ** 30, "step_cycles": 100,
+                   "policy": "least work first, at most %d elements in flight" % SERVE_ELEMENTS,
                    "sequential": "every job run alone at full length (device time)"},
         "completed": st["completed"], "failed": st["failed"],
         "p50_latency_s": st["p50_latency_s"],
@@ -735,6 +745,9 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
         "max_used_gb": st["max_used_bytes"] / 2 ** 30,
         "sequential_fp64_jobs_h": seq_jobs_h[0],
         "sequential_mixed_jobs_h": seq_jobs_h[1],
+        "admit_all_arrival_order": {"jobs_h": st_all["jobs_per_h"],
+                                    "p50_latency_s": st_all["p50_latency_s"],
+                                    "p99_latency_s": st_all["p99_latency_s"]},
         "fifo_one_at_a_time_latency_s": {
             "fp64": dict(zip(("p50", "p99"), fifo_latency(per_job[0]))),
             "mixed": dict(zip(("p50", "p99"), fifo_latency(per_job[1]))),
@@ -747,7 +760,7 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
     }
 
 
-def reference_gpu_shell(model, args, device, ours_kernel_ms):
+def reference_gpu_shell(model, args, device, ours_kt):
     """Baseline leg: the reference's own CUDA shell path (its unmodified
     shell_*_kernel.cu and shell_gpu_driver.cu, built for sm_103a in double
     precision; oracle/ref_gpu.py) timed on this GPU on the same shells and
@@ -820,8 +833,12 @@ def reference_gpu_shell(model, args, device, ours_kernel_ms):
              "ours_forint_step_ms": ours_ms,
              "speedup_full_step": ref["full_step_ms"] / ours_ms}
         if name == "window_state":
-            d["ours_shell_kernel_ms"] = ours_kernel_ms
-            d["speedup_kernels"] = ref["kernels_ms_per_step"] / ours_kernel_ms
+            # the reference's kernels include the (atomic) assembly; ours
+            # assembles in the node kernel, which also does the nodal update
+            both = ours_kt["shell"] + ours_kt["node"]
+            d["ours_shell_kernel_ms"] = ours_kt["shell"]
+            d["ours_shell_plus_node_kernel_ms"] = both
+            d["speedup_kernels"] = ref["kernels_ms_per_step"] / both
         out[name] = d
     return out
 
@@ -924,7 +941,7 @@ def main():
             line["serving"] = {k: sv[k] for k in (
                 "value", "unit", "completed", "failed", "p50_latency_s", "p99_latency_s",
                 "sequential_fp64_jobs_h", "sequential_mixed_jobs_h",
-                "fifo_one_at_a_time_latency_s",
+                "fifo_one_at_a_time_latency_s", "admit_all_arrival_order",
                 "speedup_vs_sequential_plain", "speedup_vs_sequential_mixed",
                 "element_updates_s", "makespan_s", "config", "jobs_with_device_status")}
     if rank == 0:

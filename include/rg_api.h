@@ -207,6 +207,21 @@ int rg_energy(rg_ctx *ctx, double *eint, double *ekin, double *ekinr,
 /* Device status word (RG_ST_* bits), cleared by the read. */
 int rg_status(rg_ctx *ctx);
 
+/* Checkpoint / restart of one model, the device-resident counterpart of the
+ * engine's restart file (WRRESTP, engine/source/output/restart/
+ * wrrestp.F:161): the snapshot holds every device array of the context --
+ * nodes, element and point state, PARITH/ON slots, the time-step record,
+ * link switches, status -- behind a header naming the model (counts,
+ * precision, allocation layout).  rg_snapshot copies after the cycles
+ * already queued (synchronous; a context in a batch: after
+ * rg_batch_synchronize).  rg_restore accepts a snapshot of the same model
+ * set up the same way (this context or a fresh one: a restart in another
+ * process) and refuses any other with RG_E_ARG; the run then resumes bit for
+ * bit.  Host buffers are plain memory of rg_snapshot_size bytes. */
+int rg_snapshot_size(rg_ctx *ctx, unsigned long long *bytes);
+int rg_snapshot(rg_ctx *ctx, void *buf, unsigned long long bytes);
+int rg_restore(rg_ctx *ctx, const void *buf, unsigned long long bytes);
+
 /* Inspection / benchmarking. */
 int rg_info(rg_ctx *ctx, int *numnod, int *numels, int *numelc, int *lsky,
             unsigned long long *device_bytes);

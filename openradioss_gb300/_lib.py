@@ -46,6 +46,9 @@ SIGNATURES = [
     ("rg_get_time", _ip, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("rg_energy", _ip, [_vp, _vp, _vp, _vp, _vp]),
     ("rg_status", _ip, [_vp]),
+    ("rg_snapshot_size", _ip, [_vp, _vp]),
+    ("rg_snapshot", _ip, [_vp, _vp, C.c_ulonglong]),
+    ("rg_restore", _ip, [_vp, _vp, C.c_ulonglong]),
     ("rg_info", _ip, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("rg_set_timing", _ip, [_vp, _ip]),
     ("rg_kernel_times", _ip, [_vp, _vp]),

@@ -67,6 +67,25 @@ def build(force=False, verbose=False, ptxas_info=False):
     return LIB
 
 
+def build_fortran(fc=None):
+    """Compile the Fortran ISO_C_BINDING module include/rg_api_mod.F90 (the
+    interface a Fortran engine uses) when asked (RG_FORTRAN=1) and a Fortran
+    compiler is present ($FC, else gfortran / flang / ifx / nvfortran).
+    Returns the object file, or None when skipped."""
+    if os.environ.get("RG_FORTRAN") != "1":
+        return None
+    fc = fc or os.environ.get("FC") or next(
+        (c for c in ("gfortran", "flang", "ifx", "nvfortran") if shutil.which(c)), None)
+    if not fc:
+        raise RuntimeError("RG_FORTRAN=1 but no Fortran compiler found")
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "..", "include", "rg_api_mod.F90")
+    obj = os.path.join(OUT, "rg_api_mod.o")
+    subprocess.run([fc, "-c", src, "-o", obj, "-J" if "gfortran" in fc else "-module", OUT],
+                   check=True)
+    return obj
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True,
                 ptxas_info="--ptxas" in sys.argv))

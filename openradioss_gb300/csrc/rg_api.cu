@@ -1499,6 +1499,97 @@ int rg_status(rg_ctx *c) {
   return s;
 }
 
+// ---- checkpoint / restart ------------------------------------------------
+// A snapshot is every device allocation of the context, in allocation order,
+// behind a header that ties it to the model it came from (counts, precision,
+// allocation sizes).  All of the model's state lives in those allocations
+// (nodes, element and point state, skyline slots, the time-step record, link
+// switches, status word), so restoring them resumes the run bit for bit.
+namespace {
+struct SnapHeader {
+  char magic[8];
+  unsigned long long nalloc, payload, layout;
+  int numnod, numels, numelc, prec;
+};
+unsigned long long snap_layout(const rg_ctx *c) {
+  // FNV-1a over the allocation sizes
+  unsigned long long h = 1469598103934665603ull;
+  for (size_t b : c->alloc_bytes) {
+    h ^= (unsigned long long)b;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+unsigned long long snap_payload(const rg_ctx *c) {
+  unsigned long long t = 0;
+  for (size_t b : c->alloc_bytes) t += b;
+  return t;
+}
+void snap_header(const rg_ctx *c, SnapHeader &h) {
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, "RGSNAP01", 8);
+  h.nalloc = c->allocs.size();
+  h.payload = snap_payload(c);
+  h.layout = snap_layout(c);
+  h.numnod = c->numnod;
+  h.numels = c->numels;
+  h.numelc = c->shells.numelc;
+  h.prec = c->prec;
+}
+}  // namespace
+
+int rg_snapshot_size(rg_ctx *c, unsigned long long *bytes) {
+  if (!c || !bytes) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  *bytes = sizeof(SnapHeader) + snap_payload(c);
+  return RG_OK;
+}
+
+int rg_snapshot(rg_ctx *c, void *buf, unsigned long long bytes) {
+  if (!c || !buf) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  const unsigned long long need = sizeof(SnapHeader) + snap_payload(c);
+  if (bytes < need) return fail(c, RG_E_ARG, "rg_snapshot: buffer smaller than rg_snapshot_size");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  SnapHeader h;
+  snap_header(c, h);
+  std::memcpy(buf, &h, sizeof(h));
+  char *q = (char *)buf + sizeof(h);
+  for (size_t i = 0; i < c->allocs.size(); i++) {
+    RG_CUDA(c, cudaMemcpyAsync(q, c->allocs[i], c->alloc_bytes[i], cudaMemcpyDeviceToHost,
+                               c->stream));
+    q += c->alloc_bytes[i];
+  }
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return RG_OK;
+}
+
+int rg_restore(rg_ctx *c, const void *buf, unsigned long long bytes) {
+  if (!c || !buf) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  if (bytes < sizeof(SnapHeader)) return fail(c, RG_E_ARG, "rg_restore: buffer too small");
+  SnapHeader h, mine;
+  std::memcpy(&h, buf, sizeof(h));
+  snap_header(c, mine);
+  if (std::memcmp(h.magic, mine.magic, 8) != 0)
+    return fail(c, RG_E_ARG, "rg_restore: not a snapshot of this library");
+  if (h.nalloc != mine.nalloc || h.payload != mine.payload || h.layout != mine.layout ||
+      h.numnod != mine.numnod || h.numels != mine.numels || h.numelc != mine.numelc ||
+      h.prec != mine.prec)
+    return fail(c, RG_E_ARG, "rg_restore: snapshot of a different model or precision");
+  if (bytes < sizeof(SnapHeader) + h.payload)
+    return fail(c, RG_E_ARG, "rg_restore: truncated snapshot");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  const char *q = (const char *)buf + sizeof(h);
+  for (size_t i = 0; i < c->allocs.size(); i++) {
+    RG_CUDA(c, cudaMemcpyAsync(c->allocs[i], q, c->alloc_bytes[i], cudaMemcpyHostToDevice,
+                               c->stream));
+    q += c->alloc_bytes[i];
+  }
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return RG_OK;
+}
+
 int rg_info(rg_ctx *c, int *numnod, int *numels, int *numelc, int *lsky,
             unsigned long long *device_bytes) {
   if (!c) return RG_E_ARG;

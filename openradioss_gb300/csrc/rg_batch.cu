@@ -668,6 +668,13 @@ int rg_batch_add(rg_batch *b, rg_ctx *c, int target_ncycle) {
   for (auto &g : c->hg)
     if (g.P.jcvt)
       return bfail(b, RG_E_UNSUP, "batch: co-rotational (JCVT=1) hexa jobs run alone (rg_cycle)");
+  // the batched kernel carries the lean shell material (no kinematic
+  // hardening, thermal softening or IPLA = 2: they run alone)
+  for (int g = 0; g < shell_group_count(c->shells); g++)
+    if (shell_mf(*shell_group_params(c->shells, g)) != 0)
+      return bfail(b, RG_E_UNSUP,
+                   "batch: shells with kinematic hardening, thermal softening or Iplas=2 run alone "
+                   "(rg_cycle)");
   bool any = false;
   for (auto *q : b->jobs) any = any || q;
   if (any && c->prec != b->prec)

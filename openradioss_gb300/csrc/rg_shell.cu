@@ -35,7 +35,7 @@ struct ShellDev {
 // The mixed form stages each element's state in shared memory (cp.async at
 // the start of the element, shell_element<..., STAGE>): the DRAM reads of the
 // state overlap the node gathers and the geometry without holding registers.
-template <typename ER, int NPT, int NT>
+template <typename ER, int NPT, int NT, int MF>
 __global__ void __launch_bounds__(NT, sizeof(ER) == 4 ? RG_SHELL_MIXED_MINB : 1)
 shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              typename SlotT<ER>::type *__restrict__ fsky,
@@ -73,8 +73,8 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     }
     const int il = t * 32 + lane;
     if (il < P.nel)
-      shell_element<ER, NPT, STG>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine, elmin,
-                                  DT1, dtinv, s_stg, s_stgd);
+      shell_element<ER, NPT, STG, MF>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine,
+                                      elmin, DT1, dtinv, s_stg, s_stgd);
   }
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
   if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
@@ -118,12 +118,23 @@ static void launch_shell(const ShellParams &P, const ShellArrays<ER> &A, const N
   const int nb = P.nblk;
   if (P.wtasks) cudaMemsetAsync(P.qctr, 0, sizeof(unsigned), s);
   ST *f = (ST *)fsky, *fr = (ST *)fskyr;
-  switch (P.npt) {
-    case 1: shell_kernel<ER, 1, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-    case 2: shell_kernel<ER, 2, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-    case 3: shell_kernel<ER, 3, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-    case 4: shell_kernel<ER, 4, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-    default: shell_kernel<ER, 5, SHELL_NT><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+  if (shell_mf(P) == 0) {
+    switch (P.npt) {
+      case 1: shell_kernel<ER, 1, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 2: shell_kernel<ER, 2, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 3: shell_kernel<ER, 3, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 4: shell_kernel<ER, 4, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      default: shell_kernel<ER, 5, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+    }
+  } else {
+    constexpr int MF = SHELL_MF_ALL;
+    switch (P.npt) {
+      case 1: shell_kernel<ER, 1, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 2: shell_kernel<ER, 2, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 3: shell_kernel<ER, 3, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 4: shell_kernel<ER, 4, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      default: shell_kernel<ER, 5, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+    }
   }
 }
 
@@ -324,11 +335,11 @@ static int shell_resident(int npt) {
   int r = 0;
   cudaError_t e;
   switch (npt) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 1, SHELL_NT>, SHELL_NT, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 2, SHELL_NT>, SHELL_NT, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 3, SHELL_NT>, SHELL_NT, 0); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 4, SHELL_NT>, SHELL_NT, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 5, SHELL_NT>, SHELL_NT, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 1, SHELL_NT, 0>, SHELL_NT, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 2, SHELL_NT, 0>, SHELL_NT, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 3, SHELL_NT, 0>, SHELL_NT, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 4, SHELL_NT, 0>, SHELL_NT, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, shell_kernel<ER, 5, SHELL_NT, 0>, SHELL_NT, 0); break;
   }
   return e == cudaSuccess && r > 0 ? r : 1;
 }

@@ -232,7 +232,17 @@ struct ShellStage {
   static constexpr int ndouble = 3;
 };
 
-template <typename ER, int NPT, bool STAGE = false>
+// Material branches compiled into a kernel variant (MF bits): 1 kinematic /
+// mixed hardening, 2 thermal softening, 4 IPLA = 2.  The lean variant (MF =
+// 0) serves groups that use none of them; the full one (SHELL_MF_ALL) the
+// others -- the extra live values of those branches would otherwise cost
+// every group registers and time.
+constexpr int SHELL_MF_ALL = 7;
+inline int shell_mf(const ShellParams &P) {
+  return (P.fisokin > 0.0 || P.thermal || P.ipla == 2) ? SHELL_MF_ALL : 0;
+}
+
+template <typename ER, int NPT, bool STAGE = false, int MF = 0>
 __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellArrays<ER> &S,
                                               const NodeView &N,
                                               typename SlotT<ER>::type *__restrict__ fsky,
@@ -568,17 +578,21 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       epsd_pg = sqrt(eps_k2 + eps_m2) * dtinv;
       S.epsdg[e] = epsd_pg;
     }
-    // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) and CDT3, ahead of MULAWC: they
-    // read no result of the material update, so the local velocities and
-    // rotation rates are dead before the through-thickness loop ----
+    // ---- CHVIS3 (ISMSTR = 4, IHBE = 1) and CDT3: they read no result of
+    // the material update.  The staged (mixed) kernel runs them ahead of
+    // MULAWC, so that the local velocities and rotation rates are dead before
+    // the through-thickness loop; the FP64 kernel, held by its FP64 pipe,
+    // keeps the reference's order.  Same operations either way. ----
+    R h11, h12, h13, h21, h22, h23, h31, h32, h33, hr4, hr5;
+    R sti_noda = (R)0, stir_noda = (R)0;
+    R inv_divm = (R)0;  // FP64 form: 1 / MAX(ALDT^2, EM20), formed with HH2
+    R sti;
+    auto hourglass_and_dt = [&]() {
     if constexpr (STAGE) {
 #pragma unroll
       for (int c = 0; c < 5; c++) st_hour[c] = stg[(SG_HOUR + c) * SHELL_STG_NT + tid];
       st_ehou = stgd[2 * SHELL_STG_NT + tid];
     }
-    R h11, h12, h13, h21, h22, h23, h31, h32, h33, hr4, hr5;
-    R sti_noda = (R)0, stir_noda = (R)0;
-    R inv_divm = (R)0;  // FP64 form: 1 / MAX(ALDT^2, EM20), formed with HH2
     {
       const R px1v = px1 * vhx, px2v = px2 * vhx, py1v = py1 * vhy, py2v = py2 * vhy;
       const R gama1 = off * ((R)RG_ONE - px1v - py1v);
@@ -669,7 +683,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       S.ehou[e] = st_ehou + (double)ehou;
     }
     // ---- CDT3 (not called under the nodal time step, cforc3.F:668) ----
-    R sti = sti_noda;
+    sti = sti_noda;
     if (!P.nodadt) {
       const R dt = aldt * PC(dtfac_ssp);
       if (offg > (R)0 && off != (R)0) {
@@ -685,6 +699,8 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       }
       sti = (R)RG_ZEP81 * sti * off;
     }
+    };
+    if constexpr (STAGE) hourglass_and_dt();
     // ---- MULAWC: through-thickness loop (SIGEPS02C / M2CPLR) ----
     R forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
     if constexpr (STAGE) {
@@ -762,10 +778,10 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       R ca = PC(ca), cb = PC(cb), ymax = PC(ymax);
       // T* of the point (sigeps02c.F:125), 0 without adiabatic heating
       R tstar = (R)0;
-      if (P.thermal) tstar = smax((R)0, (S.temp[it * nc + e] - PC(tref)) / (PC(tmelt) - PC(tref)));
+      if ((MF & 2) && P.thermal) tstar = smax((R)0, (S.temp[it * nc + e] - PC(tref)) / (PC(tmelt) - PC(tref)));
       // kinematic hardening: the predictor works on the shifted stress
       // (m2cplr.F:115-121)
-      const bool kin = P.fisokin > 0.0;
+      const bool kin = (MF & 1) && P.fisokin > 0.0;
       R sgb[3] = {(R)0, (R)0, (R)0};
       if (kin) {
 #pragma unroll
@@ -827,7 +843,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
           dpla_pt = dpla;
           if (kin && yld < ymax) h = PC(cn) * cb * exp((PC(cn) - (R)RG_ONE) * log(pla + (R)RG_EM07));
         }
-      } else if (P.ipla == 2) {
+      } else if ((MF & 4) && P.ipla == 2) {
         // m2cplr.F:380-445: projection along an approximate normal, then a
         // radial return to the yield stress advanced by H * DPLA
         const R svm2 = sn[0] * sn[0] + sn[1] * sn[1] - sn[0] * sn[1] + (R)RG_THREE * sn[2] * sn[2];
@@ -950,7 +966,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       // SIGEPS02C: SIGY accumulates YLD / NPT over the points so far, and
       // this point's adiabatic heating uses that running sum
       // (sigeps02c.F:197-199, 226-229; SIGY zeroed per group, mulawc.F90:577)
-      if (P.thermal) {
+      if ((MF & 2) && P.thermal) {
         sigy_acc = sigy_acc + yld / (R)NPT;
         S.temp[it * nc + e] = S.temp[it * nc + e] + sigy_acc * dpla_pt / PC(rhocp);
       }
@@ -994,6 +1010,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     for (int c = 0; c < 5; c++) S.forc[c * nc + e] = forn[c];
 #pragma unroll
     for (int c = 0; c < 3; c++) S.mom[c * nc + e] = momn[c];
+    if constexpr (!STAGE) hourglass_and_dt();
     // ---- CFINT3 ----
     R F[3][4], M[3][4];
     {

@@ -224,6 +224,21 @@ class Engine:
                   "rg_skyline_get")
         return adsky, iads[:8 * m.numels], iadc[:4 * m.numelc], lsky.value
 
+    def snapshot(self):
+        """The model's whole device state as bytes (rg_snapshot), after the
+        queued cycles."""
+        n = C.c_ulonglong()
+        self._chk(self.L.rg_snapshot_size(self.h, C.byref(n)), "rg_snapshot_size")
+        buf = np.empty(n.value, np.uint8)
+        self._chk(self.L.rg_snapshot(self.h, _p(buf), n.value), "rg_snapshot")
+        return buf
+
+    def restore(self, snap):
+        """Resume from a snapshot of the same model (this engine or another
+        one built from the same model and precision)."""
+        snap = np.ascontiguousarray(snap, np.uint8)
+        self._chk(self.L.rg_restore(self.h, _p(snap), snap.nbytes), "rg_restore")
+
     def info(self):
         a = [C.c_int() for _ in range(4)]
         b = C.c_ulonglong()

@@ -27,6 +27,14 @@ functions; the compiler may contract multiply-adds differently in the two
 kernels), and are bitwise the same whatever the batch's launch
 configuration or neighbours -- both of which the tests check.
 
+With preemption on, a request may carry a priority: when an arrived request
+does not fit (slot or budget) and jobs of lower priority are running, the
+lowest-priority running jobs (the most cycles left first) are preempted --
+their whole device state is snapshotted to host memory (rg_snapshot), their
+device memory released -- until it fits; a preempted job waits in the queue
+with its snapshot and resumes from it (rg_restore) bit for bit, the batched
+kernel's results not depending on what else is in the batch.
+
 The latency of a job is its completion time minus its arrival time; the
 loop reports jobs/h and the p50 / p99 latencies.
 """
@@ -74,6 +82,9 @@ class Request:
     key: int
     model: object = field(compare=False)
     ncycles: int = field(compare=False)
+    priority: int = field(default=0, compare=False)
+    snapshot: object = field(default=None, compare=False)   # preempted job's state
+    record: object = field(default=None, compare=False)     # its JobRecord
 
 
 @dataclass
@@ -88,6 +99,9 @@ class JobRecord:
     result: dict = field(default_factory=dict)
     failed: bool = False
     status: int = 0
+    priority: int = 0
+    preemptions: int = 0
+    ncycles_done: int = 0   # cycles done when last preempted
 
     @property
     def latency(self):
@@ -99,7 +113,13 @@ class Server:
 
     def __init__(self, hbm_budget_bytes, max_jobs=64, precision=RG_PREC_MIXED,
                  step_cycles=100, device=0, config=None, keep_results=False,
-                 result_fn=None):
+                 result_fn=None, preempt=False, policy="fifo", max_elements=None):
+        """policy: admission order among arrived requests of equal priority,
+        "fifo" (arrival) or "sjf" (least work first: elements x cycles
+        left).  max_elements: cap on the elements of the running jobs -- a
+        single large model already fills the GPU, and admitting more only
+        shares it (every job slower) where waiting would finish the first
+        ones sooner; a job is always admitted when nothing runs."""
         self.budget = int(hbm_budget_bytes)
         self.max_jobs = max_jobs
         self.precision = precision
@@ -111,46 +131,109 @@ class Server:
         self.keep_results = keep_results
         self.result_fn = result_fn
         self.used = 0
-        self.running = {}     # slot -> (Engine, JobRecord, reserved bytes)
-        self.waiting = []     # heap of Request (arrival order)
+        self.preempt = preempt
+        if policy not in ("fifo", "sjf"):
+            raise ValueError("policy must be 'fifo' or 'sjf'")
+        self.policy = policy
+        self.max_elements = max_elements
+        self.running = {}     # slot -> (Engine, JobRecord, reserved bytes, Request)
+        self.waiting = []     # heap of Request not yet arrived (arrival order)
+        self.queue = []       # heap of arrived requests: priority, then arrival
         self.done = []
         self.failed = []
         self.max_used = 0
 
-    def submit(self, key, model, ncycles, arrival):
-        heapq.heappush(self.waiting, Request(arrival, key, model, ncycles))
+    def submit(self, key, model, ncycles, arrival, priority=0):
+        heapq.heappush(self.waiting, Request(arrival, key, model, ncycles, priority))
+
+    def _enqueue(self, req):
+        work = 0.0
+        if self.policy == "sjf":
+            left = req.ncycles - (req.record.ncycles_done if req.record else 0)
+            work = float(req.model.numels + req.model.numelc) * max(left, 0)
+        heapq.heappush(self.queue, (-req.priority, work, req.arrival, req.key, req))
+
+    def _elements_running(self):
+        return sum(r[1].elements for r in self.running.values())
+
+    def _victims(self, req, need):
+        """Running jobs of lower priority than req whose preemption frees a
+        slot and enough budget for it (lowest priority, most cycles left
+        first), or None when that is not possible."""
+        cands = sorted((s for s, r in self.running.items() if r[3].priority < req.priority),
+                       key=lambda s: (self.running[s][3].priority,
+                                      -(self.running[s][1].ncycles -
+                                        self.running[s][0].time()["ncycle"])))
+        out, free, slots = [], self.budget - self.used, self.max_jobs - len(self.running)
+        for s in cands:
+            if free >= need and slots >= 1:
+                break
+            out.append(s)
+            free += self.running[s][2]
+            slots += 1
+        return out if (free >= need and slots >= 1) else None
+
+    def _preempt(self, slot):
+        """Snapshot a running job to host memory, release its device memory
+        and put it back in the queue."""
+        self.batch.sync()
+        e, rec, need, req = self.running.pop(slot)
+        self.batch.remove(slot)
+        req.snapshot = e.snapshot()
+        req.record = rec
+        rec.preemptions += 1
+        rec.ncycles_done = e.time()["ncycle"]
+        e.close()
+        self.used -= need
+        self._enqueue(req)
 
     def _admit(self, now):
         n = 0
-        while self.waiting and self.waiting[0].arrival <= now and \
-                len(self.running) < self.max_jobs:
-            req = self.waiting[0]
+        while self.waiting and self.waiting[0].arrival <= now:
+            self._enqueue(heapq.heappop(self.waiting))
+        while self.queue:
+            req = self.queue[0][-1]
             need = estimate_device_bytes(req.model, self.precision)
-            if self.used + need > self.budget:
-                if not self.running:
+            if self.running and self.max_elements is not None and \
+                    self._elements_running() + req.model.numels + req.model.numelc > \
+                    self.max_elements:
+                break
+            if self.used + need > self.budget or len(self.running) >= self.max_jobs:
+                if not self.running and self.used + need > self.budget:
                     raise RuntimeError("job %d needs %d bytes, more than the whole budget %d"
                                        % (req.key, need, self.budget))
-                break
-            heapq.heappop(self.waiting)
+                vict = self._victims(req, need) if self.preempt else None
+                if not vict:
+                    break
+                for s in vict:
+                    self._preempt(s)
+            heapq.heappop(self.queue)
             e = Engine(req.model, device=self.device, precision=self.precision)
-            rec = JobRecord(req.key, req.arrival, admitted=self._clock(), ncycles=req.ncycles,
-                            elements=req.model.numels + req.model.numelc,
-                            device_bytes=e.info()["device_bytes"])
+            if req.snapshot is not None:
+                e.restore(req.snapshot)   # resume where it was preempted
+                req.snapshot = None
+                rec = req.record
+            else:
+                rec = JobRecord(req.key, req.arrival, admitted=self._clock(),
+                                ncycles=req.ncycles,
+                                elements=req.model.numels + req.model.numelc,
+                                device_bytes=e.info()["device_bytes"], priority=req.priority)
             slot = self.batch.add(e, req.ncycles)
-            self.running[slot] = (e, rec, need)
+            self.running[slot] = (e, rec, need, req)
             self.used += need
             self.max_used = max(self.max_used, self.used)
             n += 1
         return n
 
     def _retire(self, prog):
-        fin = [s for s, (e, rec, need) in self.running.items() if prog.get(s, -1) >= rec.ncycles]
+        fin = [s for s, (e, rec, need, _) in self.running.items()
+               if prog.get(s, -1) >= rec.ncycles]
         if not fin:
             return 0
         self.batch.sync()
         now = self._clock()
         for s in fin:
-            e, rec, need = self.running.pop(s)
+            e, rec, need, _ = self.running.pop(s)
             self.batch.remove(s)
             rec.finished = now
             if self.result_fn is not None:
@@ -176,7 +259,7 @@ class Server:
         self.batch.sync()
         now = self._clock()
         for s in bad:
-            e, rec, need = self.running.pop(s)
+            e, rec, need, _ = self.running.pop(s)
             self.batch.remove(s)
             rec.finished = now
             rec.failed = True
@@ -194,8 +277,8 @@ class Server:
     def run(self, requests):
         """Serve ``requests`` -- (key, model, ncycles, arrival seconds) --
         arriving on the wall clock from now; returns the statistics."""
-        for (k, m, n, a) in requests:
-            self.submit(k, m, n, a)
+        for r in requests:
+            self.submit(*r)
         total = len(self.waiting)
         self.t0 = time.perf_counter()
         steps = 0
@@ -210,7 +293,7 @@ class Server:
                 self._retire_failed(self.batch.job_status(), st)
                 self._retire(prog)
             else:
-                if self.waiting and self.waiting[0].arrival > now:
+                if not self.queue and self.waiting and self.waiting[0].arrival > now:
                     time.sleep(min(0.05, self.waiting[0].arrival - now))
                 self._admit(self._clock())
         makespan = self._clock()
@@ -225,7 +308,7 @@ class Server:
                     element_updates=float(sum(r.elements * r.ncycles for r in self.done)))
 
     def close(self):
-        for s, (e, rec, need) in list(self.running.items()):
+        for s, (e, rec, need, _) in list(self.running.items()):
             self.batch.remove(s)
             e.close()
         self.running.clear()

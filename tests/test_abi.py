@@ -57,3 +57,13 @@ def test_engine_refuses_without_library(tmp_path):
     from openradioss_gb300 import _lib
     with pytest.raises(RuntimeError):
         _lib.lib(str(tmp_path / "missing.so"))
+
+
+def test_fortran_module_binds_every_entry_point():
+    """include/rg_api_mod.F90 (the ISO_C_BINDING module a Fortran engine
+    uses) binds every function the C header declares, by its C name."""
+    src = open(os.path.join(ROOT, "include", "rg_api_mod.F90")).read()
+    bound = set(re.findall(r"bind\(c,\s*name='(rg_[a-z0-9_]+)'\)", src))
+    missing = [s for s in declared() if s not in bound]
+    assert not missing, missing
+    assert bound <= set(declared()), sorted(bound - set(declared()))

@@ -32,6 +32,12 @@ class FakeEngine:
         w, self.word = self.word, 0
         return w
 
+    def snapshot(self):
+        return {"nc": self.nc}
+
+    def restore(self, snap):
+        self.nc = snap["nc"]
+
     def close(self):
         FakeEngine.live -= 1
 
@@ -56,8 +62,12 @@ class FakeBatch:
         self.slots.pop(s)
 
     bstatus = 0
+    step_s = 0.0   # wall time a step takes (arrivals during running steps)
 
     def cycle(self, n):
+        if FakeBatch.step_s:
+            import time
+            time.sleep(FakeBatch.step_s)
         for e, t in self.slots.values():
             e.nc = min(t, e.nc + n)
             f = FakeEngine.fail_at.get(e.model.name)
@@ -85,7 +95,9 @@ def fakes(monkeypatch):
     FakeEngine.live = 0
     FakeEngine.fail_at = {}
     FakeBatch.bstatus = 0
+    FakeBatch.step_s = 0.0
     yield
+    FakeBatch.step_s = 0.0
 
 
 def small_jobs():
@@ -155,6 +167,59 @@ def test_batch_failure_retires_the_running_jobs(fakes):
     assert all(r.status & 16 for r in srv.failed)
     assert [r.key for r in srv.done] == [9]
     assert st["completed"] == 1 and srv.used == 0 and FakeEngine.live == 0
+
+
+def test_priority_request_preempts_and_preempted_job_resumes(fakes):
+    """With preemption on, a high-priority request that does not fit the
+    budget evicts the lowest-priority running job with the most cycles
+    left: that job is snapshotted, its memory released, and it resumes from
+    the snapshot later, reaching exactly its cycle count (no work redone)."""
+    lo1 = M.crash_box(n_side=4, n_len=8, seed=1)
+    lo2 = M.crash_box(n_side=4, n_len=8, seed=2)
+    hi = M.crash_box(n_side=4, n_len=8, seed=3)
+    need = S.estimate_device_bytes(lo1, 1)
+    jobs = [(0, lo1, 2000, 0.0, 0), (1, lo2, 1500, 0.0, 0), (2, hi, 200, 0.05, 5)]
+    FakeBatch.step_s = 0.005
+    srv = S.Server(2 * need + need // 2, max_jobs=8, step_cycles=50, preempt=True)
+    st = srv.run(jobs)
+    assert st["completed"] == 3 and st["failed"] == 0
+    recs = {r.key: r for r in srv.done}
+    assert recs[0].preemptions == 1 and recs[1].preemptions == 0  # most cycles left
+    assert recs[2].finished < recs[0].finished
+    assert all(r.result["time"]["ncycle"] == jobs[r.key][2] for r in srv.done)
+    assert srv.used == 0 and FakeEngine.live == 0
+    # without preemption the high-priority job waits for a retirement
+    srv2 = S.Server(2 * need + need // 2, max_jobs=8, step_cycles=50, preempt=False)
+    srv2.run(jobs)
+    r2 = {r.key: r for r in srv2.done}
+    assert all(r.preemptions == 0 for r in srv2.done)
+    assert r2[2].finished > r2[1].finished
+
+
+def test_sjf_admits_least_work_first_under_an_element_cap(fakes):
+    """With policy sjf and an element cap, arrived requests are admitted in
+    order of their work (elements x cycles), never more elements at once than
+    the cap (except a single job), and every job completes."""
+    big = M.crash_box(n_side=6, n_len=20, seed=1)
+    small = [M.crash_box(n_side=3, n_len=4, seed=k) for k in range(2, 5)]
+    jobs = [(0, big, 3000, 0.0)] + [(k + 1, m, 200, 0.0) for k, m in enumerate(small)]
+    cap = big.numelc  # room for the big job alone, or for the small ones
+    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50, policy="sjf", max_elements=cap)
+    seen = []
+    orig = srv._admit
+
+    def spy(now):
+        n = orig(now)
+        seen.append(srv._elements_running())
+        return n
+    srv._admit = spy
+    st = srv.run(jobs)
+    assert st["completed"] == 4
+    assert max(seen) <= cap
+    adm = sorted(srv.done, key=lambda r: r.admitted)
+    assert adm[-1].key == 0  # the large job goes last
+    fin = {r.key: r.finished for r in srv.done}
+    assert max(fin[k] for k in (1, 2, 3)) < fin[0]
 
 
 def test_oversize_job_is_refused(fakes):
