@@ -204,6 +204,14 @@ int rg_get_time(rg_ctx *ctx, double *tt, double *dt1, double *dt2,
  * translational / rotational kinetic, accumulated hourglass. */
 int rg_energy(rg_ctx *ctx, double *eint, double *ekin, double *ekinr,
               double *ehour);
+/* Energy balance of the listing's cycle line (ECRIT, engine/source/output/
+ * ecrit.F:501-517), n <= 13 values: 0 TT, 1 internal energy, 2 kinetic,
+ * 3 rotational kinetic, 4 accumulated hourglass, 5 external work of the
+ * rigid walls (WFEXT), 6 ENTOT = IE + KE + KE-R, 7 energy error in percent
+ * 100 (ENTOT / (ENTOT0 + WFEXT) - 1) clamped to +-99 with ENTOT0 taken at
+ * rg_finalize, 8 total nodal mass, 9 mass error (M - M0) / M0, 10-12
+ * momentum x, y, z.  The node sums are fixed-order device reductions. */
+int rg_energy_balance(rg_ctx *ctx, double *out, int n);
 /* Device status word (RG_ST_* bits), cleared by the read. */
 int rg_status(rg_ctx *ctx);
 

@@ -45,6 +45,7 @@ SIGNATURES = [
     ("rg_download_shell_state", _ip, [_vp, _ip, _vp]),
     ("rg_get_time", _ip, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("rg_energy", _ip, [_vp, _vp, _vp, _vp, _vp]),
+    ("rg_energy_balance", _ip, [_vp, _vp, _ip]),
     ("rg_status", _ip, [_vp]),
     ("rg_snapshot_size", _ip, [_vp, _vp]),
     ("rg_snapshot", _ip, [_vp, _vp, C.c_ulonglong]),

@@ -330,6 +330,42 @@ __global__ void energy_final(const double *__restrict__ part, int nextra,
   for (int j = 0; j < nextra; j++) out[j] += extra[j];
 }
 
+// Node sums of the energy balance, fixed order like energy_kernel: mass,
+// momentum (x, y, z) and the rigid walls' external work.
+__global__ void __launch_bounds__(EN_NT)
+balance_kernel(NodeView N, double *__restrict__ part) {
+  double s[5] = {0, 0, 0, 0, 0};
+  const int stride = EN_BLOCKS * EN_NT;
+  for (int i = blockIdx.x * EN_NT + threadIdx.x; i < N.numnod; i += stride) {
+    const double m = N.D4[i].w;
+    const dbl4 v = N.V4[i];
+    s[0] += m;
+    s[1] += m * v.x;
+    s[2] += m * v.y;
+    s[3] += m * v.z;
+    if (N.wext) s[4] += N.wext[i];
+  }
+  __shared__ double sh[5][EN_NT];
+  for (int j = 0; j < 5; j++) sh[j][threadIdx.x] = s[j];
+  __syncthreads();
+  for (int o = EN_NT / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int j = 0; j < 5; j++) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int j = 0; j < 5; j++) part[j * EN_BLOCKS + blockIdx.x] = sh[j][0];
+}
+
+__global__ void balance_final(const double *__restrict__ part, double *__restrict__ out) {
+  if (threadIdx.x != 0) return;
+  for (int j = 0; j < 5; j++) {
+    double s = 0.0;
+    for (int b = 0; b < EN_BLOCKS; b++) s += part[j * EN_BLOCKS + b];
+    out[j] = s;
+  }
+}
+
 // AoS X(3,n) -> X4.xyz (keeps .w); same for V and VR.
 // FORINT-level upload: X, V and (shell models) VR, xyz interleaved, read
 // straight from registered host memory (or from the staging buffer) into the
@@ -1060,6 +1096,9 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
     if ((r = dalloc(c, &c->d_walls, 6 * c->nwalls))) return r;
     RG_CUDA(c, cudaMemcpy(c->d_wall, wn.data(), numnod * sizeof(int), cudaMemcpyHostToDevice));
     RG_CUDA(c, cudaMemcpy(c->d_walls, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice));
+    // external work of the walls, accumulated per node by the node kernel
+    if ((r = dalloc(c, &c->nv.wext, numnod))) return r;
+    RG_CUDA(c, cudaMemset(c->nv.wext, 0, numnod * sizeof(double)));
   }
   if (c->nlinks) {
     std::vector<int> ln, lo(1, 0);
@@ -1106,7 +1145,7 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   }
   if ((r = dalloc(c, &c->d_stage, 12 * (size_t)numnod + 16))) return r;
   RG_CUDA(c, cudaMallocHost((void **)&c->h_time, sizeof(Time)));
-  if ((r = dalloc(c, &c->d_epart, 4 * EN_BLOCKS + 8))) return r;
+  if ((r = dalloc(c, &c->d_epart, 9 * EN_BLOCKS + 8))) return r;
   RG_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));  // uploads complete
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
   // capture one cycle as a graph
@@ -1116,6 +1155,13 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   if (ce != cudaSuccess) return fail(c, RG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
   RG_CUDA(c, cudaGraphInstantiate(&c->gexec, c->graph, 0));
   c->finalized = true;
+  // cycle-0 totals of the energy balance (ECRIT's ENTOT0 and MASS0)
+  {
+    double b[13];
+    if ((r = rg_energy_balance(c, b, 13))) return r;
+    c->entot0 = b[6];
+    c->mass0 = b[8];
+  }
   return RG_OK;
 }
 
@@ -1484,6 +1530,36 @@ int rg_energy(rg_ctx *c, double *eint, double *ekin, double *ekinr, double *ehou
   if (ehour) *ehour = h[1];
   if (ekin) *ekin = h[2];
   if (ekinr) *ekinr = h[3];
+  return RG_OK;
+}
+
+// Energy balance of the listing's cycle line (ECRIT, engine/source/output/
+// ecrit.F:373-520): ENTOT = IE + KE + KE-R, ERROR = ENTOT / (ENTOT0 +
+// WFEXT) - 1 (in %, clamped to +-99), mass error against the cycle-0 mass.
+int rg_energy_balance(rg_ctx *c, double *out, int n) {
+  if (!c || !out || n < 0) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  double ei, ek, ekr, eh;
+  int r = rg_energy(c, &ei, &ek, &ekr, &eh);
+  if (r) return r;
+  double *part = c->d_epart + 4 * EN_BLOCKS;
+  double *dout = c->d_stage + 16;  // 5 doubles (staging holds >= 12 numnod + 16)
+  balance_kernel<<<EN_BLOCKS, EN_NT, 0, c->stream>>>(c->nv, part);
+  balance_final<<<1, 32, 0, c->stream>>>(part, dout);
+  double nb[5];
+  RG_CUDA(c, cudaMemcpyAsync(nb, dout, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  RG_CUDA(c, cudaMemcpyAsync(c->h_time, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost,
+                             c->stream));
+  RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  const double entot = ei + ek + ekr;
+  const double den = c->entot0 + nb[4];
+  double err = 0.0;
+  if (std::fabs(den) > RG_EM20) err = std::fmax(-99.0, std::fmin(99.0, (entot / den - 1.0) * 100.0));
+  const double mass0 = c->finalized && c->mass0 > 0.0 ? c->mass0 : nb[0];
+  const double emass = (nb[0] - mass0) / std::fmax(mass0, RG_EM20);
+  const double b[13] = {c->h_time->tt, ei, ek, ekr, eh, nb[4], entot, err, nb[0], emass,
+                        nb[1], nb[2], nb[3]};
+  for (int k = 0; k < n && k < 13; k++) out[k] = b[k];
   return RG_OK;
 }
 

@@ -111,6 +111,7 @@ struct rg_ctx {
   cudaEvent_t ev[8] = {};
   void *d_flush = nullptr;     // L2 flush buffer of rg_time_cycles_cold
   Time *h_time = nullptr;      // pinned host copy of the time-step record
+  double entot0 = 0.0, mass0 = 0.0;  // cycle-0 totals of the energy balance
   size_t flush_bytes = 0;
 };
 

@@ -56,6 +56,7 @@ struct NodeView {
   F8 *XF;     // mixed form: FP32 hi/lo position copies
   float4 *VF;   // mixed form: FP32 velocity copies
   float4 *VRF;  // mixed form: FP32 rotational velocity copies (shells)
+  double *wext; // external work of the rigid walls per node (null without walls)
   int numnod;
 };
 

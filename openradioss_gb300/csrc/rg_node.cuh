@@ -235,6 +235,21 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
                                     __dmul_rn(v.z, W[5]));
         const double da = __dadd_rn(__dadd_rn(__dmul_rn(a0, W[3]), __dmul_rn(a1, W[4])),
                                     __dmul_rn(a2, W[5]));
+        if (N.wext) {
+          // external work of the wall (rgwall.F:289-300, 515): the normal
+          // impulse force FN = (DV + DA*DT12)*MS*n against the velocity
+          // before the correction, TFXTN = -FACT*(V.FN), FACT = 1/DT12, and
+          // WFEXT += HALF*DT1*TFXTN (accumulated per node; explicit rounding)
+          const double ms = N.D4[n].w;
+          const double dvt = __dmul_rn(__dadd_rn(dv, __dmul_rn(da, dt12)), ms);
+          const double fact = dt12 != 0.0 ? __drcp_rn(dt12) : 0.0;
+          const double vfn =
+              __dadd_rn(__dadd_rn(__dmul_rn(v.x, __dmul_rn(dvt, W[3])),
+                                  __dmul_rn(v.y, __dmul_rn(dvt, W[4]))),
+                        __dmul_rn(v.z, __dmul_rn(dvt, W[5])));
+          const double dt1 = COH ? __ldcg(&T->dt1) : T->dt1;
+          N.wext[n] = __dadd_rn(N.wext[n], __dmul_rn(__dmul_rn(RG_HALF, dt1), -__dmul_rn(fact, vfn)));
+        }
         a0 = __dadd_rn(a0, -__dmul_rn(da, W[3]));
         a1 = __dadd_rn(a1, -__dmul_rn(da, W[4]));
         a2 = __dadd_rn(a2, -__dmul_rn(da, W[5]));

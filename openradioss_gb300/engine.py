@@ -214,6 +214,17 @@ class Engine:
         self._chk(self.L.rg_energy(self.h, *[C.byref(x) for x in v]), "rg_energy")
         return dict(eint=v[0].value, ekin=v[1].value, ekinr=v[2].value, ehour=v[3].value)
 
+    BALANCE_KEYS = ("tt", "eint", "ekin", "ekinr", "ehour", "wfext", "entot", "error_pct",
+                    "mass", "mass_error", "xmom", "ymom", "zmom")
+
+    def energy_balance(self):
+        """The listing cycle line's energy balance (ECRIT): energies, the
+        rigid walls' external work, ENTOT, the energy error in percent
+        against the cycle-0 total, mass, mass error and momentum."""
+        out = np.zeros(len(self.BALANCE_KEYS))
+        self._chk(self.L.rg_energy_balance(self.h, _p(out), len(out)), "rg_energy_balance")
+        return dict(zip(self.BALANCE_KEYS, out.tolist()))
+
     def skyline(self):
         m = self.model
         adsky = np.zeros(m.numnod + 1, np.int32)

@@ -81,6 +81,7 @@ def _declare(L):
         L.or_set_record.argtypes = [vp, C.c_int]
         L.or_set_nodal_dt.argtypes = [vp, C.c_double, C.c_double]
         L.or_get_record.argtypes = [vp, C.c_void_p, C.c_void_p]
+        L.or_get_wfext.argtypes = [vp, C.c_void_p]
         L.or_rbody_add.argtypes = [vp, C.c_int, C.c_int, _ip, _dp, _dp]
         L.or_set_forces.argtypes = [vp] + [C.c_void_p] * 4 + [C.c_double, C.c_int]
         L.or_cload_add.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
@@ -200,6 +201,12 @@ class OracleModel:
         v = [np.zeros(1) for _ in range(4)]
         self.L.or_energy(self.h, *[_ptr(a) for a in v])
         return dict(eint=v[0][0], ekin=v[1][0], ekinr=v[2][0], ehour=v[3][0])
+
+    def wfext(self):
+        """External work accumulated so far (loads, rigid walls)."""
+        out = np.zeros(1)
+        self.L.or_get_wfext(self.h, _ptr(out))
+        return float(out[0])
 
     def error(self):
         return self.L.or_error(self.h)

@@ -1416,6 +1416,10 @@ int or_cycle(void *m, int ncycle) {
     // sliding: a slave node whose predicted position X + (V + A*DT12)*DT2 is
     // on or behind the plane and which does not move away from it loses the
     // normal components of its acceleration and velocity.
+    // external work of the walls (rgwall.F:289-300, 515): TFXTN summed over
+    // the corrected nodes, WFEXT += HALF*DT1*TFXTN
+    double tfxtn = RG_ZERO;
+    const double fact = M.dt12 != RG_ZERO ? RG_ONE / M.dt12 : RG_ZERO;
     for (auto &W : w->walls) {
       for (int n : W.slaves) {
         const int n1 = 3 * n, n2 = n1 + 1, n3 = n1 + 2;
@@ -1433,6 +1437,12 @@ int or_cycle(void *m, int ncycle) {
         const double dv = (M.V[n1] - RG_ZERO) * W.n[0] + (M.V[n2] - RG_ZERO) * W.n[1] +
                           (M.V[n3] - RG_ZERO) * W.n[2];
         const double da = M.A[n1] * W.n[0] + M.A[n2] * W.n[1] + M.A[n3] * W.n[2];
+        {
+          const double dvt = (dv + da * M.dt12) * M.MS[n];
+          const double fnx = dvt * W.n[0], fny = dvt * W.n[1], fnz = dvt * W.n[2];
+          tfxtn = tfxtn - fact * ((M.V[n1] - RG_ZERO) * fnx + (M.V[n2] - RG_ZERO) * fny +
+                                  (M.V[n3] - RG_ZERO) * fnz);
+        }
         M.A[n1] = M.A[n1] - da * W.n[0];
         M.A[n2] = M.A[n2] - da * W.n[1];
         M.A[n3] = M.A[n3] - da * W.n[2];
@@ -1441,6 +1451,7 @@ int or_cycle(void *m, int ncycle) {
         M.V[n3] = M.V[n3] - dv * W.n[2];
       }
     }
+    if (!w->walls.empty()) M.wfext = M.wfext + RG_HALF * M.dt1 * tfxtn;
     // RLINK1 (constraints/general/rlink/rlink1.F): every node of a link
     // takes the mass-weighted mean acceleration of the link in the linked
     // directions (IC bits 4 = x, 2 = y, 1 = z), after the boundary
@@ -1740,6 +1751,12 @@ int or_rlink_clear(void *m) {
 
 int or_set_record(void *m, int on) {
   ((OrModelWrap *)m)->m.record = on != 0;
+  return 0;
+}
+
+// External work accumulated so far (loads and rigid walls).
+int or_get_wfext(void *m, double *out) {
+  *out = ((OrModelWrap *)m)->m.wfext;
   return 0;
 }
 

@@ -133,6 +133,7 @@ int or_set_forces(void *m, const double *f, const double *stifn, const double *f
  * V + DT1/2 A, hourglass energy, x/y/z momentum, mass, external work of the
  * concentrated loads.  Off by default. */
 int or_set_record(void *m, int on);
+int or_get_wfext(void *m, double *out);
 int or_get_record(void *m, double *out, int *neltst);
 /* Shell state: which = 0 FOR (5 x nc), 1 MOM (3 x nc), 2 THK, 3 EINT
  * (2 x nc), 4 OFF, 5 SIG (5 x npt x nc), 6 PLA (npt x nc), 7 HOUR (5 x nc). */
