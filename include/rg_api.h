@@ -129,6 +129,24 @@ int rg_rlink_set_active(rg_ctx *ctx, int link, int active);
  * rg_finalize; models with it run alone (not in a batch). */
 int rg_set_nodal_dt(rg_ctx *ctx, double dtfac, double dtmin);
 
+/* Time-step actions of /DT (IDTMIN, DTMIN1), before rg_finalize; a model
+ * with one runs alone (not in a batch).
+ * kind 3 -- shells, IDTMIN(3) in CDT3 (engine/source/elements/shell/coque/
+ *   cdt3.F:77-141): an element of OFF = 1 whose step is at or below dtmin
+ *   raises RG_ST_DTMIN (idtmin 1 or 5: the engine stops) or is deleted
+ *   (idtmin 2: OFF = 0 from that cycle on, out of the step minimum; its
+ *   forces of that cycle are still assembled, as CFINT3 does not read OFF).
+ * kind 11 -- nodal time step, IDTMIN(11) in DTNODA (dtnoda.F:258-305,
+ *   459-500), with rg_set_nodal_dt: a node whose step is below dtmin raises
+ *   RG_ST_DTMIN (idtmin 0, 1, 5) or takes the mass (inertia) of a step dtmin:
+ *   MS = 1/2 STIFN (dtmin/DTFAC1)^2 * 1.00001 (idtmin 3 or 8), used from
+ *   that cycle's ACCELE on; the added mass shows in rg_energy_balance.
+ * Other kinds and actions (IDTMIN(3) = 3 small-strain switch, IDTMIN(11) =
+ * 4 acceleration scaling) are refused with RG_E_UNSUP.  Solids: a hexa of
+ * non-positive volume is always deleted and flagged RG_ST_NEGVOL
+ * (SCHKJAB3); the engine stops on the flag or carries on (IDTMIN(1) = 2). */
+int rg_set_dtmin(rg_ctx *ctx, int kind, int idtmin, double dtmin);
+
 /* Local shell frame of CNVEC3 (cnvec3.F:117-170): ISHFRAM 0 (symmetric
  * convected frame, default) or 2 (the starter's /SHFRA/V4, contrl.F:495-498).
  * Before rg_finalize. */

@@ -182,6 +182,12 @@ module rg_api_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: eint, ekin, ekinr, ehour
     end function
+    integer(c_int) function rg_set_dtmin(ctx, kind, idtmin, dtmin) bind(c, name='rg_set_dtmin')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: kind, idtmin
+      real(c_double), value :: dtmin
+    end function
     integer(c_int) function rg_energy_balance(ctx, out, n) bind(c, name='rg_energy_balance')
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx

@@ -46,6 +46,7 @@ SIGNATURES = [
     ("rg_get_time", _ip, [_vp, _vp, _vp, _vp, _vp, _vp]),
     ("rg_energy", _ip, [_vp, _vp, _vp, _vp, _vp]),
     ("rg_energy_balance", _ip, [_vp, _vp, _ip]),
+    ("rg_set_dtmin", _ip, [_vp, _ip, _ip, _dp]),
     ("rg_status", _ip, [_vp]),
     ("rg_snapshot_size", _ip, [_vp, _vp]),
     ("rg_snapshot", _ip, [_vp, _vp, C.c_ulonglong]),

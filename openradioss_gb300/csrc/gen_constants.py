@@ -26,7 +26,7 @@ WANTED = [
     "EM30", "EP02", "EP06", "EP20", "EP30", "ZEP499", "FOUR_OVER_3",
     "FIVE", "SIX", "TWELVE", "ONE_OVER_6", "ONE_OVER_12", "EM04", "EP03",
     "ZEP81", "ZEP072169", "ONEP414", "ONE_OVER_9", "THREE_OVER_4",
-    "FOUR_OVER_5", "EM07", "NINE",
+    "FOUR_OVER_5", "EM07", "NINE", "ONEP00001",
 ]
 
 

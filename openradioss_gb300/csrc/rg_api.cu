@@ -98,8 +98,8 @@ template <bool F64, bool ROT>
 __global__ void __launch_bounds__(NODE_NT)
 nodal_dt_kernel(NodeView N, const int *__restrict__ adsky, const void *__restrict__ fsky_,
                 const void *__restrict__ fskyr_, const double dtfac, const double dtmin,
-                DtPartials dp, Time *__restrict__ T, int *__restrict__ status,
-                const DtFinish F) {
+                const int idtmin, DtPartials dp, Time *__restrict__ T,
+                int *__restrict__ status, const DtFinish F) {
   const int n = blockIdx.x * NODE_NT + threadIdx.x;
   const int numnod = N.numnod;
   double d = RG_EP06;
@@ -117,11 +117,28 @@ nodal_dt_kernel(NodeView N, const int *__restrict__ adsky, const void *__restric
       }
     }
     const double ms = N.D4[n].w;
+    // IDTMIN(11) = 3 / 8 (dtnoda.F:268-305, 466-500): a node whose step is
+    // below DTMIN1(11) takes the mass (inertia) of a step DTMIN1(11):
+    // 1/2 STIFN (DTMIN1/DTFAC1)^2 * 1.00001, used by this cycle's ACCELE;
+    // the step of this cycle stays the one computed before the scaling.
+    // 0, 1, 5: the step below DTMIN1(11) raises RG_ST_DTMIN (1, 5: stop).
+    const bool scale = idtmin == 3 || idtmin == 8;
     if (st <= 0.0) {
       atomicOr(status, RG_ST_NODSTIF);
     } else if (ms > 0.0) {
       const double dn = __dmul_rn(dtfac, sqrt(__dmul_rn(2.0, ms) / st));
-      if (dn < dtmin) atomicOr(status, RG_ST_DTMIN);
+      if (dn < dtmin) {
+        if (scale) {
+          const double dt2p = dtmin / dtfac;
+          const double mas = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(RG_HALF, st), dt2p), dt2p),
+                                       RG_ONEP00001);
+          N.D4[n].w = mas;
+          N.X4[n].w = 1.0 / mas;
+          if (!F64) N.XF[n].pad0 = (float)(1.0 / mas);
+        } else {
+          atomicOr(status, RG_ST_DTMIN);
+        }
+      }
       dt_pair_min(d, k, dn, 2 * numnod - 1 - n);
     }
     if (ROT) {
@@ -130,7 +147,19 @@ nodal_dt_kernel(NodeView N, const int *__restrict__ adsky, const void *__restric
         atomicOr(status, RG_ST_NODSTIF);
       } else if (in > 0.0) {
         const double dn = __dmul_rn(dtfac, sqrt(__dmul_rn(2.0, in) / sr));
-        if (dn < dtmin) atomicOr(status, RG_ST_DTMIN);
+        if (dn < dtmin) {
+          if (scale) {
+            const double dt2p = dtmin / dtfac;
+            const double iner = __dmul_rn(
+                __dmul_rn(__dmul_rn(__dmul_rn(RG_HALF, sr), dt2p), dt2p), RG_ONEP00001);
+            const double in2 = fmax(iner, in);
+            N.DR4[n].w = in2;
+            N.VR4[n].w = 1.0 / in2;
+            if (!F64) N.XF[n].pad1 = (float)(1.0 / in2);
+          } else {
+            atomicOr(status, RG_ST_DTMIN);
+          }
+        }
         dt_pair_min(d, k, dn, numnod - 1 - n);
       }
     }
@@ -613,8 +642,8 @@ void launch_nodes(rg_ctx *c) {
     F.advance = 1;
     F.ngl = c->d_ngl_nodes;
     nodal_dt_kernel<F64, ROT><<<nb, NODE_NT, 0, c->stream>>>(
-        c->nv, c->d_adsky, c->d_fsky, fr, c->dtfac_noda, c->dtmin_noda, c->ndp, c->d_time,
-        c->d_status, F);
+        c->nv, c->d_adsky, c->d_fsky, fr, c->dtfac_noda, c->dtmin_noda, c->idtmin_noda, c->ndp,
+        c->d_time, c->d_status, F);
   }
   if (c->nlinks)
     rlink_kernel<F64, ROT><<<c->nlinks, LINK_NT, 0, c->stream>>>(
@@ -886,6 +915,27 @@ int rg_set_nodal_dt(rg_ctx *c, double dtfac, double dtmin) {
   return RG_OK;
 }
 
+int rg_set_dtmin(rg_ctx *c, int kind, int idtmin, double dtmin) {
+  if (!c) return RG_E_ARG;
+  if (c->finalized) return fail(c, RG_E_STATE, "rg_set_dtmin after rg_finalize");
+  if (!(dtmin >= 0.0)) return fail(c, RG_E_ARG, "rg_set_dtmin: DTMIN must be >= 0");
+  if (kind == 3) {
+    if (idtmin != 0 && idtmin != 1 && idtmin != 2 && idtmin != 5)
+      return fail(c, RG_E_UNSUP, "shell IDTMIN must be 0, 1, 2 or 5 (3: small-strain switch not built)");
+    c->shells.idtmin = idtmin;
+    c->shells.dtmin = dtmin;
+    return RG_OK;
+  }
+  if (kind == 11) {
+    if (idtmin != 0 && idtmin != 1 && idtmin != 3 && idtmin != 5 && idtmin != 8)
+      return fail(c, RG_E_UNSUP, "nodal IDTMIN must be 0, 1, 3, 5 or 8 (4: acceleration scaling not built)");
+    c->idtmin_noda = idtmin;
+    c->dtmin_noda = dtmin;
+    return RG_OK;
+  }
+  return fail(c, RG_E_UNSUP, "rg_set_dtmin: kind must be 3 (shells) or 11 (nodal time step)");
+}
+
 int rg_set_shell_frame(rg_ctx *c, int ishfram) {
   if (!c) return RG_E_ARG;
   if (c->finalized) return fail(c, RG_E_STATE, "rg_set_shell_frame after rg_finalize");
@@ -1079,13 +1129,19 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   c->nwalls = (int)c->walls.size();
   if (c->nwalls) {
     std::vector<int> wn(numnod, -1);
-    std::vector<double> wd(6 * c->nwalls);
+    // device record: P0, N in FP64, then the same in FP32 (RG_WALL_STRIDE)
+    std::vector<double> wd(RG_WALL_STRIDE * c->nwalls);
     for (int w = 0; w < c->nwalls; w++) {
       const WallHost &W = c->walls[w];
+      double *rec = wd.data() + RG_WALL_STRIDE * w;
+      float f32[6];
       for (int i = 0; i < 3; i++) {
-        wd[6 * w + i] = W.p0[i];
-        wd[6 * w + 3 + i] = W.n[i];
+        rec[i] = W.p0[i];
+        rec[3 + i] = W.n[i];
+        f32[i] = (float)W.p0[i];
+        f32[3 + i] = (float)W.n[i];
       }
+      memcpy(rec + 6, f32, sizeof f32);
       for (int n = 0; n < numnod; n++) {
         const double d = (c->X[3 * n] - W.p0[0]) * W.n[0] + (c->X[3 * n + 1] - W.p0[1]) * W.n[1] +
                          (c->X[3 * n + 2] - W.p0[2]) * W.n[2];
@@ -1093,7 +1149,7 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
       }
     }
     if ((r = dalloc(c, &c->d_wall, numnod))) return r;
-    if ((r = dalloc(c, &c->d_walls, 6 * c->nwalls))) return r;
+    if ((r = dalloc(c, &c->d_walls, RG_WALL_STRIDE * c->nwalls))) return r;
     RG_CUDA(c, cudaMemcpy(c->d_wall, wn.data(), numnod * sizeof(int), cudaMemcpyHostToDevice));
     RG_CUDA(c, cudaMemcpy(c->d_walls, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice));
     // external work of the walls, accumulated per node by the node kernel

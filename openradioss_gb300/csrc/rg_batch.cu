@@ -665,6 +665,8 @@ int rg_batch_add(rg_batch *b, rg_ctx *c, int target_ncycle) {
   if (c->device != b->device) return bfail(b, RG_E_ARG, "batch: job on another device");
   if (c->nlinks) return bfail(b, RG_E_UNSUP, "batch: jobs with rigid links run alone (rg_cycle)");
   if (c->nodadt) return bfail(b, RG_E_UNSUP, "batch: jobs with the nodal time step run alone (rg_cycle)");
+  if (c->shells.idtmin)
+    return bfail(b, RG_E_UNSUP, "batch: jobs with an element time-step action run alone (rg_cycle)");
   for (auto &g : c->hg)
     if (g.P.jcvt)
       return bfail(b, RG_E_UNSUP, "batch: co-rotational (JCVT=1) hexa jobs run alone (rg_cycle)");

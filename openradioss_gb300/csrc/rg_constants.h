@@ -49,4 +49,5 @@
 #define RG_FOUR_OVER_5  (0x1.999999999999ap-1) /* 0.80000000000000004 */
 #define RG_EM07         (0x1.ad7f29abcaf48p-24) /* 9.9999999999999995e-08 */
 #define RG_NINE         (0x1.2000000000000p+3) /* 9 */
+#define RG_ONEP00001    (0x1.0000a7c5ac472p+0) /* 1.0000100000000001 */
 #define RG_SP_1P1       (0x1.19999a0000000p+0) /* 1.1000000238418579: REAL*4 literal 1.1 */

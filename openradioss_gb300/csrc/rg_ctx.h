@@ -93,6 +93,7 @@ struct rg_ctx {
   // last-block reduction, and the key -> node number table
   int nodadt = 0;
   double dtfac_noda = 0.9, dtmin_noda = 0.0;
+  int idtmin_noda = 0;  // IDTMIN(11): 0 flag only, 1/5 stop, 3/8 mass scaling
   int nnparts = 0;
   rg::DtPartials ndp{};
   unsigned *d_nctr = nullptr;

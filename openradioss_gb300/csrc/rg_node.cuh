@@ -3,6 +3,7 @@
 // functions, shared by the single-model kernels (rg_api.cu) and the batched
 // persistent kernel (rg_batch.cu).
 #include "../../include/rg_api.h"
+#include "rg_bits.h"
 #include "rg_device.cuh"
 
 namespace rg {
@@ -43,6 +44,38 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, const float d) {
   const float h2 = __fadd_rn(s, l);
   lo = __fsub_rn(l, __fsub_rn(h2, s));
   hi = h2;
+}
+
+// Rigid wall record on the device: P0 (3), unit normal N (3) in FP64, then
+// the same six values in FP32 (packed in the last three doubles) for the
+// FP32 screen of the wall test.
+constexpr int RG_WALL_STRIDE = 9;
+
+// FP32 screen of the sliding-wall test: true when the predicted distance
+// DP = (X - P0).N + DT2 (V + A DT12).N of the node is positive for certain,
+// so that the FP64 test below would leave the node alone.  Every FP32 value
+// here is within a few units of 2^-24 of the FP64 value it stands for, so
+// the estimate is off by less than 2^-20 of MAG (the sum of the magnitudes
+// it is formed from); the screen asks for a margin of 2^-14 MAG and sends
+// every closer node (and any NaN or overflow) to the FP64 test.
+__device__ __forceinline__ bool wall_clear(const double *__restrict__ W, const dbl4 &x,
+                                           const dbl4 &v, const double a0, const double a1,
+                                           const double a2, const double dt12,
+                                           const double dt2) {
+  const float *Wf = (const float *)(W + 6);
+  const float d12 = narrow_f64(dt12), d2 = narrow_f64(dt2);
+  const float nx = Wf[3], ny = Wf[4], nz = Wf[5];
+  const float ax = narrow_f64(a0), ay = narrow_f64(a1), az = narrow_f64(a2);
+  const float ux = narrow_f64(v.x), uy = narrow_f64(v.y), uz = narrow_f64(v.z);
+  const float vx = fmaf(ax, d12, ux), vy = fmaf(ay, d12, uy), vz = fmaf(az, d12, uz);
+  const float px = narrow_f64(x.x), py = narrow_f64(x.y), pz = narrow_f64(x.z);
+  const float vn = fmaf(vz, nz, fmaf(vy, ny, vx * nx));
+  const float dp0 = fmaf(pz - Wf[2], nz, fmaf(py - Wf[1], ny, (px - Wf[0]) * nx));
+  const float dp = fmaf(d2, vn, dp0);
+  const float mx = (fabsf(px) + fabsf(Wf[0]) + d2 * (fabsf(ux) + fabsf(ax) * d12)) * fabsf(nx);
+  const float my = (fabsf(py) + fabsf(Wf[1]) + d2 * (fabsf(uy) + fabsf(ay) * d12)) * fabsf(ny);
+  const float mz = (fabsf(pz) + fabsf(Wf[2]) + d2 * (fabsf(uz) + fabsf(az) * d12)) * fabsf(nz);
+  return dp > 0x1p-14f * (mx + my + mz);
 }
 
 // L2-coherent loads (ld.global.cg): used where the data was written by other
@@ -172,13 +205,13 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     xf = N.XF[n];
     // ACCELE on the FP32 force sums: F * (1/MS) rounded once in FP32, then
     // widened (the forces carry FP32 precision already)
-    a0 = (double)__fmul_rn(b0, xf.pad0);
-    a1 = (double)__fmul_rn(b1, xf.pad0);
-    a2 = (double)__fmul_rn(b2, xf.pad0);
+    a0 = widen_f32(__fmul_rn(b0, xf.pad0));
+    a1 = widen_f32(__fmul_rn(b1, xf.pad0));
+    a2 = widen_f32(__fmul_rn(b2, xf.pad0));
     if (ROT) {
-      r0 = (double)__fmul_rn(c0, xf.pad1);
-      r1 = (double)__fmul_rn(c1, xf.pad1);
-      r2 = (double)__fmul_rn(c2, xf.pad1);
+      r0 = widen_f32(__fmul_rn(c0, xf.pad1));
+      r1 = widen_f32(__fmul_rn(c1, xf.pad1));
+      r2 = widen_f32(__fmul_rn(c2, xf.pad1));
     }
   }
   dbl4 x = ld4(N.X4 + n);
@@ -197,7 +230,7 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
   }
   // node code: BCS bits 1/2/4 (x/y/z), 8/16/32 (rotations); above them the
   // 1-based index of the node's rigid link (0: none)
-  const int code = (int)v.w;
+  const int code = small_int_f64(v.w);
   if (code) {
     if (code & 1) a0 = 0.0;
     if (code & 2) a1 = 0.0;
@@ -219,8 +252,8 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
   // normal components of its acceleration and velocity.
   if (wall) {
     const int w = __ldg(wall + n);
-    if (w >= 0) {
-      const double *W = walls + 6 * w;
+    if (w >= 0 && !wall_clear(walls + RG_WALL_STRIDE * w, x, v, a0, a1, a2, dt12, dt2)) {
+      const double *W = walls + RG_WALL_STRIDE * w;
       // predicted normal velocity VN = (V + A*DT12).n and distance
       // DP = (X + (V + A*DT12)*DT2 - P0).n = (X - P0).n + DT2*VN, in fused
       // multiply-adds written out (the same bits in every kernel)
@@ -283,9 +316,8 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     // exact two-sum (no FP64 split of the new position)
     // increment DT2 * V formed in FP32 from the FP32 velocity copy (one
     // rounding more than the FP64 product: below the copy's resolution)
-    const float vfx = __double2float_rn(v.x), vfy = __double2float_rn(v.y),
-                vfz = __double2float_rn(v.z);
-    const float dt2f = __double2float_rn(dt2);
+    const float vfx = narrow_f64(v.x), vfy = narrow_f64(v.y), vfz = narrow_f64(v.z);
+    const float dt2f = narrow_f64(dt2);
     ff_add(xf.hx, xf.lx, __fmul_rn(dt2f, vfx));
     ff_add(xf.hy, xf.ly, __fmul_rn(dt2f, vfy));
     ff_add(xf.hz, xf.lz, __fmul_rn(dt2f, vfz));
@@ -325,8 +357,7 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     }
     st4(N.VR4 + n, vr);
     if constexpr (!F64)
-      N.VRF[n] = make_float4(__double2float_rn(vr.x), __double2float_rn(vr.y),
-                             __double2float_rn(vr.z), 0.f);
+      N.VRF[n] = make_float4(narrow_f64(vr.x), narrow_f64(vr.y), narrow_f64(vr.z), 0.f);
   }
 }
 

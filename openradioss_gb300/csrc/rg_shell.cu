@@ -26,17 +26,24 @@ struct ShellDev {
   double *epart = nullptr;  // energy partials
 };
 
-// Resident blocks per SM of the mixed kernel (its register budget); the
-// FP64 kernel takes as many as its ~250 registers allow.
+// Block size and resident blocks per SM of the mixed kernel (its register
+// budget); the FP64 kernel runs 128-thread blocks, as many as its ~250
+// registers allow.
+#ifndef RG_SHELL_MIXED_NT
+#define RG_SHELL_MIXED_NT 128
+#endif
 #ifndef RG_SHELL_MIXED_MINB
 #define RG_SHELL_MIXED_MINB 4
+#endif
+#ifndef RG_SHELL_F64_MINB
+#define RG_SHELL_F64_MINB 1
 #endif
 
 // The mixed form stages each element's state in shared memory (cp.async at
 // the start of the element, shell_element<..., STAGE>): the DRAM reads of the
 // state overlap the node gathers and the geometry without holding registers.
 template <typename ER, int NPT, int NT, int MF>
-__global__ void __launch_bounds__(NT, sizeof(ER) == 4 ? RG_SHELL_MIXED_MINB : 1)
+__global__ void __launch_bounds__(NT, sizeof(ER) == 4 ? RG_SHELL_MIXED_MINB : RG_SHELL_F64_MINB)
 shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              typename SlotT<ER>::type *__restrict__ fsky,
              typename SlotT<ER>::type *__restrict__ fskyr, DtPartials dp,
@@ -44,7 +51,6 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              const DtFinish F) {
   typedef ER R;
   constexpr bool STG = sizeof(ER) == 4;
-  static_assert(!STG || NT == SHELL_STG_NT, "staging slots are laid out for 128 threads");
   __shared__ float s_stg[STG ? ShellStage<NPT>::nfloat * NT : 1];
   __shared__ double s_stgd[STG ? ShellStage<NPT>::ndouble * NT : 1];
   R dtmine = (R)RG_EP06;
@@ -73,8 +79,8 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
     }
     const int il = t * 32 + lane;
     if (il < P.nel)
-      shell_element<ER, NPT, STG, MF>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine,
-                                      elmin, DT1, dtinv, s_stg, s_stgd);
+      shell_element<ER, NPT, STG, MF, NT>(P, S, N, fsky, fskyr, T, key0, nc_total, il, dtmine,
+                                          elmin, DT1, dtinv, s_stg, s_stgd, status);
   }
   block_dt_min<NT, R>(dtmine, elmin, dp.dt + P.part_off + blockIdx.x, dp.el + P.part_off + blockIdx.x);
   if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
@@ -109,6 +115,8 @@ __global__ void shell_energy_kernel(int nc, const double *__restrict__ eint,
 
 constexpr int SHELL_NT = 128;
 int shell_blocks(int nel) { return (nel + SHELL_NT - 1) / SHELL_NT; }
+template <typename ER>
+constexpr int shell_nt() { return sizeof(ER) == 4 ? RG_SHELL_MIXED_NT : SHELL_NT; }
 
 template <typename ER>
 static void launch_shell(const ShellParams &P, const ShellArrays<ER> &A, const NodeView &N,
@@ -118,22 +126,23 @@ static void launch_shell(const ShellParams &P, const ShellArrays<ER> &A, const N
   const int nb = P.nblk;
   if (P.wtasks) cudaMemsetAsync(P.qctr, 0, sizeof(unsigned), s);
   ST *f = (ST *)fsky, *fr = (ST *)fskyr;
+  constexpr int NTL = shell_nt<ER>();
   if (shell_mf(P) == 0) {
     switch (P.npt) {
-      case 1: shell_kernel<ER, 1, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      case 2: shell_kernel<ER, 2, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      case 3: shell_kernel<ER, 3, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      case 4: shell_kernel<ER, 4, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      default: shell_kernel<ER, 5, SHELL_NT, 0><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 1: shell_kernel<ER, 1, NTL, 0><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 2: shell_kernel<ER, 2, NTL, 0><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 3: shell_kernel<ER, 3, NTL, 0><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 4: shell_kernel<ER, 4, NTL, 0><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      default: shell_kernel<ER, 5, NTL, 0><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
     }
   } else {
     constexpr int MF = SHELL_MF_ALL;
     switch (P.npt) {
-      case 1: shell_kernel<ER, 1, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      case 2: shell_kernel<ER, 2, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      case 3: shell_kernel<ER, 3, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      case 4: shell_kernel<ER, 4, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
-      default: shell_kernel<ER, 5, SHELL_NT, MF><<<nb, SHELL_NT, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 1: shell_kernel<ER, 1, NTL, MF><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 2: shell_kernel<ER, 2, NTL, MF><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 3: shell_kernel<ER, 3, NTL, MF><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      case 4: shell_kernel<ER, 4, NTL, MF><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
+      default: shell_kernel<ER, 5, NTL, MF><<<nb, NTL, 0, s>>>(P, A, N, f, fr, dp, T, key0, nct, status, F); break;
     }
   }
 }
@@ -395,11 +404,14 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
     g->P.dtfac = dtfac;
     g->P.ishfram = S.ishfram;
     g->P.nodadt = S.nodadt;
+    g->P.idtmin = S.idtmin;
+    g->P.dtmin = S.dtmin;
     shell_params_mirror(g->P);
     // FP64 groups needing more than one wave of resident blocks: one wave
     // taking warp tasks from a counter (the mixed kernel, latency bound,
     // keeps one element per thread and the extra warps that hide latency)
-    g->P.nblk = shell_blocks(g->P.nel);
+    g->P.nblk = prec == RG_PREC_FP64 ? shell_blocks(g->P.nel)
+                                     : (g->P.nel + RG_SHELL_MIXED_NT - 1) / RG_SHELL_MIXED_NT;
     g->P.wtasks = 0;
     if (prec == RG_PREC_FP64) {
       int dev = 0, nsm = 0;

@@ -18,6 +18,8 @@ struct ShellModelHost {
   int key0 = 0;                         // dt-order key of the first shell
   int ishfram = 0;                      // local frame of every group (0 / 2)
   int nodadt = 0;                       // nodal time step (/DT/NODA)
+  int idtmin = 0;                       // element time-step action IDTMIN(3)
+  double dtmin = 0.0;                   // DTMIN1(3)
   void *dev = nullptr;                  // device arrays (rg_shell.cu)
 };
 

@@ -60,6 +60,10 @@ struct ShellParams {
   // point's temperature, sigeps02c.F:125, 226-229; thermal = rho*Cp > 0)
   double fisokin, m_exp, tref, tmelt, rhocp;
   int thermal;
+  // element time-step action (IDTMIN(3), DTMIN1(3), cdt3.F:77-141): 0 none,
+  // 1 or 5 stop the run (RG_ST_DTMIN), 2 delete the element
+  int idtmin;
+  double dtmin;
   // FP32 copies for the mixed form (converted once on the host) and the
   // branch flags CC /= 0, DM /= 0 evaluated on the FP64 values
   struct {
@@ -67,7 +71,7 @@ struct ShellParams {
     float ca, cb, cn, ymax, cc, eps0, pm9, dtfac;
     float a1, a2, inv1mnu, inv1pnu, inv_hmax, dtfac_ssp;
     float shf0, hA1, hA3, hA5, hA7, hA8;
-    float fisokin, m_exp, tref, tmelt, rhocp;
+    float fisokin, m_exp, tref, tmelt, rhocp, dtmin;
     int cc_nz, dm_nz;
   } f;
 };
@@ -92,6 +96,7 @@ inline void shell_params_mirror(ShellParams &P) {
     P.hA7 = P.h1 * r0e;
     P.hA8 = P.h2 * r0e * shfpr3;
   }
+  P.f.dtmin = (float)P.dtmin;
   P.f.a1 = (float)P.a1;
   P.f.a2 = (float)P.a2;
   P.f.inv1mnu = (float)P.inv1mnu;
@@ -219,7 +224,7 @@ __device__ __forceinline__ R sqrt_ratio(const R s1, const R s2) {
 }
 
 // Shared-memory staging of a block's element state (mixed form, single-model
-// kernel): per thread of a SHELL_STG_NT-thread block, the float components
+// kernel): per thread of an SNT-thread block, the float components
 // [forc 5 | mom 3 | hour 5 | gstr 8 | sig 5*NPT | pla NPT | epsd NPT] and the
 // doubles [eint 2 | ehou], component-major (slot = component * NT + thread).
 constexpr int SHELL_STG_NT = 128;
@@ -242,7 +247,7 @@ inline int shell_mf(const ShellParams &P) {
   return (P.fisokin > 0.0 || P.thermal || P.ipla == 2) ? SHELL_MF_ALL : 0;
 }
 
-template <typename ER, int NPT, bool STAGE = false, int MF = 0>
+template <typename ER, int NPT, bool STAGE = false, int MF = 0, int SNT = SHELL_STG_NT>
 __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellArrays<ER> &S,
                                               const NodeView &N,
                                               typename SlotT<ER>::type *__restrict__ fsky,
@@ -252,7 +257,8 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
                                               int &elmin, const double DT1in = -1.0,
                                               const ER dtinv_in = (ER)0,
                                               float *__restrict__ stg = nullptr,
-                                              double *__restrict__ stgd = nullptr) {
+                                              double *__restrict__ stgd = nullptr,
+                                              int *__restrict__ status_dt = nullptr) {
   typedef ER R;
   constexpr bool F64 = std::is_same<ER, double>::value;
   static_assert(!(STAGE && F64), "shared-memory staging is the mixed form's");
@@ -268,7 +274,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     // staged form: the whole element state is requested now, into this
     // thread's shared-memory slots, and waited for at its first use (CSTRA3)
     if constexpr (STAGE) {
-      constexpr int NT = SHELL_STG_NT;
+      constexpr int NT = SNT;
 #pragma unroll
       for (int c = 0; c < 5; c++) cp_async4(stg + (SG_FORC + c) * NT + tid, S.forc + c * nc + e);
 #pragma unroll
@@ -560,7 +566,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         cp_async_wait_all();
 #pragma unroll
         for (int c = 0; c < 8; c++)
-          S.gstr[c * nc + e] = stg[(SG_GSTR + c) * SHELL_STG_NT + tid] + inc[c];
+          S.gstr[c * nc + e] = stg[(SG_GSTR + c) * SNT + tid] + inc[c];
       } else {
 #pragma unroll
         for (int c = 0; c < 8; c++) S.gstr[c * nc + e] = S.gstr[c * nc + e] + inc[c];
@@ -587,11 +593,12 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     R sti_noda = (R)0, stir_noda = (R)0;
     R inv_divm = (R)0;  // FP64 form: 1 / MAX(ALDT^2, EM20), formed with HH2
     R sti;
+    bool kill = false;  // deleted by the element time-step action (CDT3)
     auto hourglass_and_dt = [&]() {
     if constexpr (STAGE) {
 #pragma unroll
-      for (int c = 0; c < 5; c++) st_hour[c] = stg[(SG_HOUR + c) * SHELL_STG_NT + tid];
-      st_ehou = stgd[2 * SHELL_STG_NT + tid];
+      for (int c = 0; c < 5; c++) st_hour[c] = stg[(SG_HOUR + c) * SNT + tid];
+      st_ehou = stgd[2 * SNT + tid];
     }
     {
       const R px1v = px1 * vhx, px2v = px2 * vhx, py1v = py1 * vhy, py2v = py2 * vhy;
@@ -686,7 +693,21 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     sti = sti_noda;
     if (!P.nodadt) {
       const R dt = aldt * PC(dtfac_ssp);
-      if (offg > (R)0 && off != (R)0) {
+      // IDTMIN(3) (cdt3.F:77-141), ahead of the step minimum: an element of
+      // OFF = 1 whose step is at or below DTMIN1(3) stops the run (1, 5) or
+      // is deleted (2): OFF = 0 from here on -- out of the minimum, STI = 0,
+      // OFFG = 0 kept by CUPDT3P; its forces of this cycle are still
+      // assembled (CFINT3 does not read OFF)
+      R offd = off;
+      if (P.idtmin && !(dt > PC(dtmin)) && off >= (R)RG_ONE && offg >= (R)0) {
+        if (P.idtmin == 2) {
+          offd = (R)0;
+          kill = true;
+        } else if (status_dt) {
+          atomicOr(status_dt, RG_ST_DTMIN);
+        }
+      }
+      if (offg > (R)0 && offd != (R)0) {
         // running minimum; reversed order key: the first element wins ties
         // (strict < in CDT3)
         dt_pair_min_t(dtmine, elmin, dt, key0 + (nc_total - 1 - e));
@@ -697,7 +718,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
         const R divm = smax(aldt * aldt, (R)RG_EM20);
         sti = (R)RG_HALF * vol0 * ym / divm;
       }
-      sti = (R)RG_ZEP81 * sti * off;
+      sti = (R)RG_ZEP81 * sti * offd;
     }
     };
     if constexpr (STAGE) hourglass_and_dt();
@@ -705,9 +726,9 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     R forn[5] = {0, 0, 0, 0, 0}, momn[3] = {0, 0, 0};
     if constexpr (STAGE) {
 #pragma unroll
-      for (int c = 0; c < 5; c++) st_forc[c] = stg[(SG_FORC + c) * SHELL_STG_NT + tid];
+      for (int c = 0; c < 5; c++) st_forc[c] = stg[(SG_FORC + c) * SNT + tid];
 #pragma unroll
-      for (int c = 0; c < 3; c++) st_mom[c] = stg[(SG_MOM + c) * SHELL_STG_NT + tid];
+      for (int c = 0; c < 3; c++) st_mom[c] = stg[(SG_MOM + c) * SNT + tid];
     }
     R degmb = st_forc[0] * exx + st_forc[1] * eyy + st_forc[2] * exy + st_forc[3] * eyz +
               st_forc[4] * exz;
@@ -742,9 +763,9 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       if constexpr (STAGE) {
         // the staged point state (shared memory, this thread's slots)
 #pragma unroll
-        for (int c = 0; c < 5; c++) sn[c] = stg[(SG_SIG + it * 5 + c) * SHELL_STG_NT + tid];
-        ep = stg[(SG::epsd + it) * SHELL_STG_NT + tid];
-        pla_in = stg[(SG::pla + it) * SHELL_STG_NT + tid];
+        for (int c = 0; c < 5; c++) sn[c] = stg[(SG_SIG + it * 5 + c) * SNT + tid];
+        ep = stg[(SG::epsd + it) * SNT + tid];
+        pla_in = stg[(SG::pla + it) * SNT + tid];
       } else {
 #pragma unroll
         for (int c = 0; c < 5; c++) sn[c] = nx_sig[c];
@@ -998,8 +1019,8 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     degmb = degmb + forn[0] * exx + forn[1] * eyy + forn[2] * exy + forn[3] * eyz + forn[4] * exz;
     degfx = degfx + momn[0] * kxx + momn[1] * kyy + momn[2] * kxy;
     if constexpr (STAGE) {
-      st_eint0 = stgd[0 * SHELL_STG_NT + tid];
-      st_eint1 = stgd[1 * SHELL_STG_NT + tid];
+      st_eint0 = stgd[0 * SNT + tid];
+      st_eint1 = stgd[1 * SNT + tid];
     }
     {
       const R vol2 = (R)RG_HALF * vol0;
@@ -1058,7 +1079,10 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     }
     // ---- CUPDT3P ----
     R offg_new = offg;
-    if (off < (R)RG_ONE) {
+    if (kill) {
+      offg_new = (R)0;
+      S.offg[e] = (R)0;
+    } else if (off < (R)RG_ONE) {
       offg_new = off;
       S.offg[e] = off;
     }

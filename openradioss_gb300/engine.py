@@ -99,6 +99,8 @@ class Engine:
         if getattr(m, "nodal_dt", None):
             dtfac, dtmin = m.nodal_dt
             self._chk(L.rg_set_nodal_dt(self.h, float(dtfac), float(dtmin)), "rg_set_nodal_dt")
+        for kind, (idtmin, dtmin) in sorted(getattr(m, "dtmin_actions", {}).items()):
+            self._chk(L.rg_set_dtmin(self.h, int(kind), int(idtmin), float(dtmin)), "rg_set_dtmin")
         if skyline is not None:
             adsky, iads, iadc = (np.ascontiguousarray(a, np.int32) for a in skyline)
             self._chk(L.rg_skyline_set(self.h, _p(adsky), _p(iads), _p(iadc)), "rg_skyline_set")

@@ -197,6 +197,9 @@ class Model:
     cloads: list = field(default_factory=list)
     ishfram: int = 0           # local shell frame: 0 symmetric, 2 /SHFRA/V4
     nodal_dt: tuple | None = None  # /DT/NODA: (DTFAC1(11), DTMIN1(11))
+    # /DT time-step actions {kind: (IDTMIN, DTMIN1)}: 3 shells (1/5 stop,
+    # 2 delete), 11 nodal step (3/8 mass scaling, else stop)
+    dtmin_actions: dict = field(default_factory=dict)
     dtfac_solid: float = 0.9
     dtfac_shell: float = 0.9
     dtmx: float = 1e30

@@ -80,6 +80,8 @@ def _declare(L):
         L.or_rlink_clear.argtypes = [vp]
         L.or_set_record.argtypes = [vp, C.c_int]
         L.or_set_nodal_dt.argtypes = [vp, C.c_double, C.c_double]
+        L.or_set_dtmin.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+        L.or_get_mass.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.or_get_record.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.or_get_wfext.argtypes = [vp, C.c_void_p]
         L.or_rbody_add.argtypes = [vp, C.c_int, C.c_int, _ip, _dp, _dp]
@@ -146,6 +148,9 @@ class OracleModel:
         if getattr(model, "nodal_dt", None):
             if L.or_set_nodal_dt(self.h, float(model.nodal_dt[0]), float(model.nodal_dt[1])) != 0:
                 raise RuntimeError("or_set_nodal_dt failed")
+        for kind, (idtmin, dtmin) in sorted(getattr(model, "dtmin_actions", {}).items()):
+            if L.or_set_dtmin(self.h, int(kind), int(idtmin), float(dtmin)) != 0:
+                raise RuntimeError("or_set_dtmin failed")
         nt = nthreads or os.cpu_count() or 1
         r = L.or_finalize(self.h, model.dtfac_solid, model.dtfac_shell, model.dtmx,
                           model.dt2old, nt)
@@ -201,6 +206,13 @@ class OracleModel:
         v = [np.zeros(1) for _ in range(4)]
         self.L.or_energy(self.h, *[_ptr(a) for a in v])
         return dict(eint=v[0][0], ekin=v[1][0], ekinr=v[2][0], ehour=v[3][0])
+
+    def mass(self):
+        """Nodal masses and inertias (MS, IN) after any mass scaling."""
+        n = self.model.numnod
+        ms, inn = np.zeros(n), np.zeros(n)
+        self.L.or_get_mass(self.h, _ptr(ms), _ptr(inn))
+        return ms, inn
 
     def wfext(self):
         """External work accumulated so far (loads, rigid walls)."""

@@ -86,6 +86,7 @@ struct Model {
   // nodal time step (/DT/NODA, DTNODA): DTFAC1(11), DTMIN1(11)
   int nodadt = 0;
   double dtfac_noda = RG_ZEP9, dtmin_noda = RG_ZERO;
+  int idtmin_noda = 0;  // IDTMIN(11): 3 / 8 mass scaling, else flag
 
   // rigid bodies (/RBODY; starter INIRBY done by the caller: the main node
   // sits at the centre of mass with MS = body mass, IN = smallest principal
@@ -844,6 +845,7 @@ void rwall_apply(Shells *, int numnod, const double *X, double *V,
 int get_state(const Shells *, int which, double *out);
 int set_frame(Shells *, int ishfram);
 void set_nodadt(Shells *, int on);
+void set_dtmin(Shells *, int idtmin, double dtmin);
 }  // namespace rg_oracle_shell
 
 struct OrModelWrap {
@@ -1342,13 +1344,25 @@ int or_cycle(void *m, int ncycle) {
     // rotational one DTFAC1(11)*SQRT(2*IN/STIFR); a node with non-positive
     // stiffness stops the run (flagged here).  Strict '<' scans: on ties the
     // first node of the translational pass, then of the rotational pass.
+    // IDTMIN(11) = 3 / 8 (dtnoda.F:268-305, 466-500): a node below
+    // DTMIN1(11) takes the mass (inertia) of a step DTMIN1(11),
+    // 1/2 STIFN (DTMIN1/DTFAC1)^2 * ONEP00001 (inertia: the larger of that
+    // and IN); the node's step of this cycle is the one computed before.
     if (M.nodadt) {
+      const bool scale = M.idtmin_noda == 3 || M.idtmin_noda == 8;
       for (int n = 0; n < numnod; n++) {
         if (M.STIFN[n] <= RG_ZERO) {
           M.error |= 32;
         } else if (M.MS[n] > RG_ZERO) {
           const double d = M.dtfac_noda * std::sqrt(RG_TWO * M.MS[n] / M.STIFN[n]);
-          if (d < M.dtmin_noda) M.error |= 8;
+          if (d < M.dtmin_noda) {
+            if (scale) {
+              const double dt2p = M.dtmin_noda / M.dtfac_noda;
+              M.MS[n] = RG_HALF * M.STIFN[n] * dt2p * dt2p * RG_ONEP00001;
+            } else {
+              M.error |= 8;
+            }
+          }
           if (d < dt2t) {
             dt2t = d;
             neltst = n + 1;
@@ -1361,7 +1375,15 @@ int or_cycle(void *m, int ncycle) {
             M.error |= 32;
           } else if (M.IN[n] > RG_ZERO) {
             const double d = M.dtfac_noda * std::sqrt(RG_TWO * M.IN[n] / M.STIFR[n]);
-            if (d < M.dtmin_noda) M.error |= 8;
+            if (d < M.dtmin_noda) {
+              if (scale) {
+                const double dt2p = M.dtmin_noda / M.dtfac_noda;
+                const double iner = RG_HALF * M.STIFR[n] * dt2p * dt2p * RG_ONEP00001;
+                M.IN[n] = std::max(iner, M.IN[n]);
+              } else {
+                M.error |= 8;
+              }
+            }
             if (d < dt2t) {
               dt2t = d;
               neltst = n + 1;
@@ -1658,6 +1680,20 @@ int or_energy(void *m, double *eint, double *ekin, double *ekinr,
 
 int or_error(void *m) { return ((OrModelWrap *)m)->m.error; }
 
+int or_set_dtmin(void *m, int kind, int idtmin, double dtmin) {
+  auto *w = (OrModelWrap *)m;
+  if (kind == 3) {
+    rg_oracle_shell::set_dtmin(w->sh, idtmin, dtmin);
+    return 0;
+  }
+  if (kind == 11) {
+    w->m.idtmin_noda = idtmin;
+    w->m.dtmin_noda = dtmin;
+    return 0;
+  }
+  return -1;
+}
+
 int or_set_nodal_dt(void *m, double dtfac, double dtmin) {
   auto *w = (OrModelWrap *)m;
   if (w->m.finalized || !(dtfac > 0.0)) return -1;
@@ -1755,6 +1791,15 @@ int or_set_record(void *m, int on) {
 }
 
 // External work accumulated so far (loads and rigid walls).
+int or_get_mass(void *m, double *ms, double *in) {
+  const auto &M = ((OrModelWrap *)m)->m;
+  for (size_t n = 0; n < M.MS.size(); n++) {
+    ms[n] = M.MS[n];
+    if (in) in[n] = n < M.IN.size() ? M.IN[n] : 0.0;
+  }
+  return 0;
+}
+
 int or_get_wfext(void *m, double *out) {
   *out = ((OrModelWrap *)m)->m.wfext;
   return 0;

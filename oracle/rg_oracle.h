@@ -97,6 +97,11 @@ int or_error(void *m);
  * dtfac*sqrt(2*MS/STIFN) (and 2*IN/STIFR for shell nodes).  Before
  * or_finalize.  Error bits: 8 below dtmin, 32 node without stiffness. */
 int or_set_nodal_dt(void *m, double dtfac, double dtmin);
+/* /DT time-step actions: kind 3 shells (IDTMIN(3) 1/5 stop flag, 2 delete),
+ * kind 11 nodal step (IDTMIN(11) 3/8 mass scaling, else stop flag). */
+int or_set_dtmin(void *m, int kind, int idtmin, double dtmin);
+/* Nodal masses and inertias (after any mass scaling). */
+int or_get_mass(void *m, double *ms, double *in);
 /* Local shell frame: 0 = symmetric convected frame (default), 2 = the
  * version-4 frame of /SHFRA/V4 (CNVEC3, cnvec3.F:143-170). */
 int or_shell_frame(void *m, int ishfram);

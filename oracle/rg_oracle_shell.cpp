@@ -11,6 +11,7 @@
 // Conventions: see rg_oracle.cpp.  Paths are relative to the OpenRadioss
 // source tree.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
@@ -79,10 +80,17 @@ struct Shells {
   int nptmax = 5;
   int ishfram = 0;                     // local frame (/SHFRA/V4: 2)
   int nodadt = 0;                      // nodal time step (/DT/NODA)
+  int idtmin = 0;                      // IDTMIN(3): 1, 5 stop; 2 delete
+  double dtmin = 0.0;                  // DTMIN1(3)
+  std::atomic<int> stop{0};            // IDTMIN(3) = 1 / 5 reached
 };
 
 Shells *create() { return new Shells(); }
 void set_nodadt(Shells *s, int on) { s->nodadt = on; }
+void set_dtmin(Shells *s, int idtmin, double dtmin) {
+  s->idtmin = idtmin;
+  s->dtmin = dtmin;
+}
 int set_frame(Shells *s, int ishfram) {
   if (ishfram != 0 && ishfram != 2) return -1;
   s->ishfram = ishfram;
@@ -756,6 +764,14 @@ static void element(Shells *S, const Group &G, int e, const double *X,
   if (!S->nodadt) {
     aldt = aldt * viscmx / std::sqrt(RG_ONE);
     const double dt = dtfac * aldt / ssp;
+    // IDTMIN(3) (cdt3.F:77-141), ahead of the minimum loop (cdt3.F:143-155):
+    // 1 / 5 flag the stop; 2 deletes the element (OFF = 0)
+    if (S->idtmin && !(dt > S->dtmin) && !(off < RG_ONE) && !(S->offg[e] < RG_ZERO)) {
+      if (S->idtmin == 2)
+        off = RG_ZERO;
+      else
+        S->stop = 1;
+    }
     if (S->offg[e] > RG_ZERO && off != RG_ZERO && dt < dt2t) {
       dt2t = dt;
       elmin = e;
@@ -871,7 +887,7 @@ void step(Shells *S, const double *X, const double *V, const double *VR,
     dt2t = bd;
     neltst = S->ixc[7 * (size_t)best + 6];
   }
-  (void)error;
+  if (S->stop.exchange(0)) error |= 8;
 }
 
 void energy(const Shells *S, double &eint, double &ehour) {

@@ -71,11 +71,16 @@ def test_restore_refuses_another_model():
 
 def test_preempted_served_job_equals_uninterrupted():
     from openradioss_gb300.serving import Server, estimate_device_bytes
+    # three jobs of about the same device footprint in a budget of 2.5 of
+    # them: the high-priority arrival finds both low-priority jobs running
+    # (each takes seconds) and can only start by preempting one of them
     lo0 = M.crash_box(n_side=5, n_len=10, seed=31)
-    lo1 = M.crash_box(n_side=5, n_len=12, seed=32)
-    hi = M.hexa_impact_block(2000, seed=33, law="law2")
-    need = max(estimate_device_bytes(x, 1) for x in (lo0, lo1, hi))
-    jobs = [(0, lo0, 20000, 0.0, 0), (1, lo1, 16000, 0.0, 0), (2, hi, 500, 0.3, 1)]
+    lo1 = M.crash_box(n_side=5, n_len=11, seed=32)
+    hi = M.crash_box(n_side=5, n_len=10, seed=33)
+    sizes = [estimate_device_bytes(x, 1) for x in (lo0, lo1, hi)]
+    need = max(sizes)
+    assert sum(sizes) > 2.5 * need and sizes[0] + sizes[1] <= 2.5 * need
+    jobs = [(0, lo0, 120000, 0.0, 0), (1, lo1, 100000, 0.0, 0), (2, hi, 3000, 0.2, 1)]
     res = {}
     for pre in (True, False):
         srv = Server(int(2.5 * need), max_jobs=8, precision=1, step_cycles=25,
