@@ -674,7 +674,8 @@ def run_sweep(args, njobs=SWEEP_JOBS, cycles=SWEEP_CYCLES_PER_JOB, device=0):
 SERVE_JOBS = 32
 SERVE_RATE = 4.0          # Poisson arrivals, jobs/s
 SERVE_BUDGET = 48 << 30   # HBM budget of the serving loop (bytes)
-SERVE_ELEMENTS = 400_000  # elements in flight of the least-work-first policy
+SERVE_ELEMENTS = 400_000  # elements in flight of the least-work-first batched policy
+SERVE_STREAM_ELEMENTS = 250_000  # elements in flight of the streams executor
 
 
 def run_serving(args, njobs=SERVE_JOBS, device=0):
@@ -720,6 +721,13 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
         st = srv.run(reqs)
     bad = sum(1 for r in srv.done if r.result.get("status", 0)) + len(srv.failed)
     srv.close()
+    # each job its own single-model graph and stream, first come first
+    # served, at most SERVE_STREAM_ELEMENTS elements in flight
+    srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device,
+                 policy="fifo", max_elements=SERVE_STREAM_ELEMENTS, executor="streams")
+    st_str = srv.run(reqs)
+    bad += sum(1 for r in srv.done if r.result.get("status", 0)) + len(srv.failed)
+    srv.close()
     seq_jobs_h = {p: 3600.0 * njobs / seq[p] for p in seq}
     ne = [m.numels + m.numelc for m, _ in jobs]
     return {
@@ -748,6 +756,12 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
         "admit_all_arrival_order": {"jobs_h": st_all["jobs_per_h"],
                                     "p50_latency_s": st_all["p50_latency_s"],
                                     "p99_latency_s": st_all["p99_latency_s"]},
+        "streams_fifo": {"jobs_h": st_str["jobs_per_h"],
+                         "p50_latency_s": st_str["p50_latency_s"],
+                         "p99_latency_s": st_str["p99_latency_s"],
+                         "element_updates_s": st_str["element_updates"] / st_str["makespan_s"],
+                         "policy": "each job its own graph and stream, first come first served, "
+                                   "at most %d elements in flight" % SERVE_STREAM_ELEMENTS},
         "fifo_one_at_a_time_latency_s": {
             "fp64": dict(zip(("p50", "p99"), fifo_latency(per_job[0]))),
             "mixed": dict(zip(("p50", "p99"), fifo_latency(per_job[1]))),

@@ -1120,7 +1120,10 @@ int rg_finalize(rg_ctx *c, double dtfac_solid, double dtfac_shell, double dtmx,
   t.dt2old = dt2old;
   t.dtmx = dtmx;
   t.dt2t = 0;
-  t.dtmin = c->nodadt ? c->dtmin_noda : 0.0;
+  // the nodal kernel flags a node step below DTMIN1(11) itself; with mass
+  // scaling (IDTMIN(11) = 3 / 8) the cycle of the scaling keeps its step
+  // below DTMIN1(11) and the run goes on (no flag)
+  t.dtmin = c->nodadt && c->idtmin_noda != 3 && c->idtmin_noda != 8 ? c->dtmin_noda : 0.0;
   if ((r = dalloc(c, &c->d_time, 1))) return r;
   RG_CUDA(c, cudaMemcpy(c->d_time, &t, sizeof(Time), cudaMemcpyHostToDevice));
   if ((r = dalloc(c, &c->d_status, 1))) return r;

@@ -35,6 +35,15 @@ device memory released -- until it fits; a preempted job waits in the queue
 with its snapshot and resumes from it (rg_restore) bit for bit, the batched
 kernel's results not depending on what else is in the batch.
 
+Two executors.  "batch" (the default) advances the running jobs together in
+one batched persistent kernel per cycle -- the gain is largest for many
+small jobs, each of which alone would leave most of the GPU idle.  "streams"
+advances each running job with its own single-model CUDA graph on its own
+stream (rg_cycle, asynchronous): jobs large enough to fill the GPU by
+themselves run at their solo speed, and the kernels of concurrent jobs
+overlap where one leaves SMs idle.  Admission, retirement, failure
+isolation and preemption are the same in both.
+
 The latency of a job is its completion time minus its arrival time; the
 loop reports jobs/h and the p50 / p99 latencies.
 """
@@ -113,21 +122,29 @@ class Server:
 
     def __init__(self, hbm_budget_bytes, max_jobs=64, precision=RG_PREC_MIXED,
                  step_cycles=100, device=0, config=None, keep_results=False,
-                 result_fn=None, preempt=False, policy="fifo", max_elements=None):
+                 result_fn=None, preempt=False, policy="fifo", max_elements=None,
+                 executor="batch"):
         """policy: admission order among arrived requests of equal priority,
         "fifo" (arrival) or "sjf" (least work first: elements x cycles
         left).  max_elements: cap on the elements of the running jobs -- a
         single large model already fills the GPU, and admitting more only
         shares it (every job slower) where waiting would finish the first
-        ones sooner; a job is always admitted when nothing runs."""
+        ones sooner; a job is always admitted when nothing runs.
+        executor: "batch" (one batched kernel for all running jobs) or
+        "streams" (each job its own graph and stream)."""
         self.budget = int(hbm_budget_bytes)
         self.max_jobs = max_jobs
         self.precision = precision
         self.step_cycles = step_cycles
         self.device = device
-        self.batch = Batch(device)
-        if config:
+        if executor not in ("batch", "streams"):
+            raise ValueError("executor must be 'batch' or 'streams'")
+        self.executor = executor
+        self.batch = Batch(device) if executor == "batch" else None
+        if config and self.batch is not None:
             self.batch.set_config(**config)
+        self.next_slot = 0
+        self.cycles_done = {}  # streams executor: slot -> cycles launched
         self.keep_results = keep_results
         self.result_fn = result_fn
         self.used = 0
@@ -156,6 +173,47 @@ class Server:
     def _elements_running(self):
         return sum(r[1].elements for r in self.running.values())
 
+    # ---- executor: the batched kernel or one graph per job ----
+    def _sync(self):
+        if self.batch is not None:
+            self.batch.sync()
+        else:
+            for e, _, _, _ in self.running.values():
+                e.sync()
+
+    def _join(self, e, req):
+        if self.batch is not None:
+            return self.batch.add(e, req.ncycles)
+        slot = self.next_slot
+        self.next_slot += 1
+        self.cycles_done[slot] = e.time()["ncycle"]
+        return slot
+
+    def _leave(self, slot):
+        if self.batch is not None:
+            self.batch.remove(slot)
+        else:
+            self.cycles_done.pop(slot, None)
+
+    def _step(self):
+        if self.batch is not None:
+            self.batch.cycle(self.step_cycles)
+            return
+        for s, (e, rec, _, _) in self.running.items():
+            n = min(self.step_cycles, rec.ncycles - self.cycles_done[s])
+            if n > 0:
+                e.cycle(n, sync=False)
+                self.cycles_done[s] += n
+
+    def _progress(self):
+        """({slot: cycles done}, {slot: job status}, batch status)."""
+        if self.batch is not None:
+            prog, st = self.batch.progress()
+            return prog, self.batch.job_status(), st
+        self._sync()
+        return (dict(self.cycles_done),
+                {s: e.status() for s, (e, _, _, _) in self.running.items()}, 0)
+
     def _victims(self, req, need):
         """Running jobs of lower priority than req whose preemption frees a
         slot and enough budget for it (lowest priority, most cycles left
@@ -176,9 +234,9 @@ class Server:
     def _preempt(self, slot):
         """Snapshot a running job to host memory, release its device memory
         and put it back in the queue."""
-        self.batch.sync()
+        self._sync()
         e, rec, need, req = self.running.pop(slot)
-        self.batch.remove(slot)
+        self._leave(slot)
         req.snapshot = e.snapshot()
         req.record = rec
         rec.preemptions += 1
@@ -218,7 +276,7 @@ class Server:
                                 ncycles=req.ncycles,
                                 elements=req.model.numels + req.model.numelc,
                                 device_bytes=e.info()["device_bytes"], priority=req.priority)
-            slot = self.batch.add(e, req.ncycles)
+            slot = self._join(e, req)
             self.running[slot] = (e, rec, need, req)
             self.used += need
             self.max_used = max(self.max_used, self.used)
@@ -230,11 +288,11 @@ class Server:
                if prog.get(s, -1) >= rec.ncycles]
         if not fin:
             return 0
-        self.batch.sync()
+        self._sync()
         now = self._clock()
         for s in fin:
             e, rec, need, _ = self.running.pop(s)
-            self.batch.remove(s)
+            self._leave(s)
             rec.finished = now
             if self.result_fn is not None:
                 rec.result = self.result_fn(e)
@@ -256,11 +314,11 @@ class Server:
         bad = [s for s in self.running if bstatus or jstat.get(s, 0)]
         if not bad:
             return 0
-        self.batch.sync()
+        self._sync()
         now = self._clock()
         for s in bad:
             e, rec, need, _ = self.running.pop(s)
-            self.batch.remove(s)
+            self._leave(s)
             rec.finished = now
             rec.failed = True
             rec.status = int(jstat.get(s, 0)) | int(bstatus)
@@ -286,11 +344,11 @@ class Server:
             now = self._clock()
             if self.running:
                 # launch a step; admissions prepared meanwhile overlap with it
-                self.batch.cycle(self.step_cycles)
+                self._step()
                 steps += 1
                 self._admit(self._clock())
-                prog, st = self.batch.progress()
-                self._retire_failed(self.batch.job_status(), st)
+                prog, jst, st = self._progress()
+                self._retire_failed(jst, st)
                 self._retire(prog)
             else:
                 if not self.queue and self.waiting and self.waiting[0].arrival > now:
@@ -309,10 +367,11 @@ class Server:
 
     def close(self):
         for s, (e, rec, need, _) in list(self.running.items()):
-            self.batch.remove(s)
+            self._leave(s)
             e.close()
         self.running.clear()
-        self.batch.close()
+        if self.batch is not None:
+            self.batch.close()
 
 
 def poisson_arrivals(n, rate, seed=7):

@@ -38,6 +38,19 @@ class FakeEngine:
     def restore(self, snap):
         self.nc = snap["nc"]
 
+    def cycle(self, n, sync=True):
+        # the streams executor's solo graph launches
+        if FakeBatch.step_s:
+            import time
+            time.sleep(FakeBatch.step_s / 4)
+        self.nc += n
+        f = FakeEngine.fail_at.get(self.model.name)
+        if f and self.nc >= f[0]:
+            self.word |= f[1]
+
+    def sync(self):
+        pass
+
     def close(self):
         FakeEngine.live -= 1
 
@@ -241,3 +254,38 @@ def test_poisson_arrivals_seeded():
     assert np.all(np.diff(a) > 0)
     assert abs(1000 / a[-1] - 4.0) < 0.4
     assert np.array_equal(a, S.poisson_arrivals(1000, 4.0, seed=7))
+
+
+def test_streams_executor(fakes):
+    """Each job on its own graph: the same admission by budget, every job
+    done with exactly its cycle count, a failed job retired alone."""
+    jobs = small_jobs()
+    FakeEngine.fail_at = {jobs[2][1].name: (60, 8)}
+    need = [S.estimate_device_bytes(m, 1) for _, m, _, _ in jobs]
+    budget = max(need) + min(need)
+    srv = S.Server(budget, max_jobs=8, step_cycles=40, executor="streams", keep_results=False)
+    assert srv.batch is None
+    st = srv.run(jobs)
+    assert st["completed"] == 5 and st["failed"] == 1
+    assert st["max_used_bytes"] <= budget
+    assert [r.key for r in srv.failed] == [2] and srv.failed[0].status == 8
+    for r in srv.done:
+        assert r.result["time"]["ncycle"] == r.ncycles
+    assert srv.used == 0 and FakeEngine.live == 0
+
+
+def test_streams_executor_preemption(fakes):
+    FakeBatch.step_s = 0.02
+    lo = [(0, M.crash_box(n_side=5, n_len=10, seed=1), 4000, 0.0, 0),
+          (1, M.crash_box(n_side=5, n_len=11, seed=2), 4000, 0.0, 0)]
+    hi = (2, M.crash_box(n_side=5, n_len=10, seed=3), 200, 0.05, 1)
+    need = max(S.estimate_device_bytes(j[1], 1) for j in lo + [hi])
+    srv = S.Server(int(2.5 * need), max_jobs=8, step_cycles=40, executor="streams",
+                   preempt=True)
+    st = srv.run(lo + [hi])
+    assert st["completed"] == 3
+    recs = {r.key: r for r in srv.done}
+    assert recs[0].preemptions + recs[1].preemptions >= 1
+    assert recs[2].finished < max(recs[0].finished, recs[1].finished)
+    for r in srv.done:
+        assert r.result["time"]["ncycle"] == r.ncycles
