@@ -675,16 +675,17 @@ SERVE_JOBS = 32
 SERVE_RATE = 4.0          # Poisson arrivals, jobs/s
 SERVE_BUDGET = 48 << 30   # HBM budget of the serving loop (bytes)
 SERVE_ELEMENTS = 400_000  # elements in flight of the least-work-first batched policy
-SERVE_STREAM_ELEMENTS = 250_000  # elements in flight of the streams executor
+SERVE_STREAM_ELEMENTS = 400_000  # elements in flight of the streams executor
 
 
 def run_serving(args, njobs=SERVE_JOBS, device=0):
-    """Serving stream: njobs seeded requests (50/50 shell crash boxes of
-    2k-150k elements and hexa impact blocks of 2k-200k elements, 2,000-20,000
-    cycles each) arriving as a Poisson process of SERVE_RATE jobs/s, admitted
-    by HBM budget into a continuously batched mixed-form run.  Beside it the
-    same jobs run alone one after another at full length, in the plain FP64
-    form and in the mixed form (device time of every job)."""
+    """Serving stream: njobs seeded requests (50/50 shell crash boxes and
+    hexa impact blocks of 21k-180k elements, 3,000-20,000 cycles each)
+    arriving as a Poisson process of SERVE_RATE jobs/s, admitted by HBM
+    budget and served in the mixed form -- each job on its own graph and
+    stream (the line's value), and by the batched kernel under two policies.
+    Beside it the same jobs run alone one after another at full length, in
+    the plain FP64 form and in the mixed form (device time of every job)."""
     from openradioss_gb300.engine import Engine
     from openradioss_gb300.serving import Server, poisson_arrivals
     jobs = [M.serving_job(k) for k in range(njobs)]
@@ -709,25 +710,25 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
             lat.append(free - float(a))
         return float(np.percentile(lat, 50)), float(np.percentile(lat, 99))
     reqs = [(k, m, n, float(a)) for k, ((m, n), a) in enumerate(zip(jobs, arr))]
-    # every arrived job admitted at once (arrival order, HBM budget only)
-    srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device)
-    st_all = srv.run(reqs)
-    srv.close()
-    # least work first, at most SERVE_ELEMENTS elements in flight (one large
-    # model already fills the GPU: more concurrency only shares it)
-    srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device,
-                 policy="sjf", max_elements=SERVE_ELEMENTS)
-    with Clocks(device) as clk:
+
+    def serve(**kw):
+        srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device,
+                     **kw)
         st = srv.run(reqs)
-    bad = sum(1 for r in srv.done if r.result.get("status", 0)) + len(srv.failed)
-    srv.close()
-    # each job its own single-model graph and stream, first come first
-    # served, at most SERVE_STREAM_ELEMENTS elements in flight
-    srv = Server(SERVE_BUDGET, max_jobs=64, precision=1, step_cycles=100, device=device,
-                 policy="fifo", max_elements=SERVE_STREAM_ELEMENTS, executor="streams")
-    st_str = srv.run(reqs)
-    bad += sum(1 for r in srv.done if r.result.get("status", 0)) + len(srv.failed)
-    srv.close()
+        st["bad"] = sum(1 for r in srv.done if r.result.get("status", 0)) + len(srv.failed)
+        srv.close()
+        return st
+    # the served line: each job its own single-model graph and stream (these
+    # jobs fill the GPU alone: the batched kernel gains them nothing), first
+    # come first served, at most SERVE_STREAM_ELEMENTS elements in flight
+    with Clocks(device) as clk:
+        st = serve(policy="fifo", max_elements=SERVE_STREAM_ELEMENTS, executor="streams")
+    # the batched executor on the same stream: every arrived job admitted
+    # (arrival order, HBM budget only), and least work first under an
+    # element cap
+    st_all = serve()
+    st_sjf = serve(policy="sjf", max_elements=SERVE_ELEMENTS)
+    bad = st["bad"] + st_all["bad"] + st_sjf["bad"]
     seq_jobs_h = {p: 3600.0 * njobs / seq[p] for p in seq}
     ne = [m.numels + m.numelc for m, _ in jobs]
     return {
@@ -742,7 +743,8 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
                    "elements_per_job": [min(ne), max(ne)],
                    "cycles_per_job": [min(n for _, n in jobs), max(n for _, n in jobs)],
                    "hbm_budget_gb": SERVE_BUDGET / 2 ** 30, "step_cycles": 100,
-                   "policy": "least work first, at most %d elements in flight" % SERVE_ELEMENTS,
+                   "policy": "each job its own graph and stream, first come first served, "
+                             "at most %d elements in flight" % SERVE_STREAM_ELEMENTS,
                    "sequential": "every job run alone at full length (device time)"},
         "completed": st["completed"], "failed": st["failed"],
         "p50_latency_s": st["p50_latency_s"],
@@ -753,15 +755,13 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
         "max_used_gb": st["max_used_bytes"] / 2 ** 30,
         "sequential_fp64_jobs_h": seq_jobs_h[0],
         "sequential_mixed_jobs_h": seq_jobs_h[1],
-        "admit_all_arrival_order": {"jobs_h": st_all["jobs_per_h"],
-                                    "p50_latency_s": st_all["p50_latency_s"],
-                                    "p99_latency_s": st_all["p99_latency_s"]},
-        "streams_fifo": {"jobs_h": st_str["jobs_per_h"],
-                         "p50_latency_s": st_str["p50_latency_s"],
-                         "p99_latency_s": st_str["p99_latency_s"],
-                         "element_updates_s": st_str["element_updates"] / st_str["makespan_s"],
-                         "policy": "each job its own graph and stream, first come first served, "
-                                   "at most %d elements in flight" % SERVE_STREAM_ELEMENTS},
+        "batched_admit_all_arrival_order": {"jobs_h": st_all["jobs_per_h"],
+                                            "p50_latency_s": st_all["p50_latency_s"],
+                                            "p99_latency_s": st_all["p99_latency_s"]},
+        "batched_least_work_first": {"jobs_h": st_sjf["jobs_per_h"],
+                                     "p50_latency_s": st_sjf["p50_latency_s"],
+                                     "p99_latency_s": st_sjf["p99_latency_s"],
+                                     "policy": "at most %d elements in flight" % SERVE_ELEMENTS},
         "fifo_one_at_a_time_latency_s": {
             "fp64": dict(zip(("p50", "p99"), fifo_latency(per_job[0]))),
             "mixed": dict(zip(("p50", "p99"), fifo_latency(per_job[1]))),

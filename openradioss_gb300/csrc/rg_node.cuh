@@ -12,10 +12,6 @@ namespace rg {
 // the 1-based rigid-link index
 constexpr int RG_LINK_SHIFT = 8;
 
-#ifndef RG_NODE_PREFETCH
-#define RG_NODE_PREFETCH 1
-#endif
-
 // ---------------------------------------------------------------------------
 // Node update: ASSPAR4 (asspar4.F:165-180) fixed-order slot sums, ACCELE
 // (accele.F:66-78), BCS10/BCS1V (bcs10.F:31), planar rigid wall, VELOCITY
@@ -199,15 +195,6 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
                                             int *__restrict__ status, const int n) {
   double a0, a1, a2, r0 = 0.0, r1 = 0.0, r2 = 0.0;
   F8 xf;  // mixed form: FP32 position copy; pad0 / pad1 = 1/MS, 1/IN in FP32
-#if RG_NODE_PREFETCH
-  // the node's own records, requested into L2 ahead of the slot gathers
-  // whose latency they then overlap
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(N.X4 + n));
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(N.V4 + n));
-  if (ROT) asm volatile("prefetch.global.L2 [%0];" ::"l"(N.VR4 + n));
-  if (F64) asm volatile("prefetch.global.L2 [%0];" ::"l"(N.D4 + n));
-  else asm volatile("prefetch.global.L2 [%0];" ::"l"(N.XF + n));
-#endif
   if constexpr (F64) {
     node_assemble<F64, ROT, COH, MLP>(adsky, fsky_, fskyr_, status, n, a0, a1, a2, r0, r1, r2);
   } else {

@@ -38,9 +38,6 @@ struct ShellDev {
 #ifndef RG_SHELL_F64_MINB
 #define RG_SHELL_F64_MINB 1
 #endif
-#ifndef RG_SHELL_PREFETCH
-#define RG_SHELL_PREFETCH 1
-#endif
 
 // The mixed form stages each element's state in shared memory (cp.async at
 // the start of the element, shell_element<..., STAGE>): the DRAM reads of the
@@ -64,27 +61,18 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
   // until none is left: the FP64 kernel is bound by the FP64 pipe, and
   // dynamic tasks keep every SM's share equal even when plastic elements
   // cost more.  Results do not depend on which warp takes which task.
-  // With warp tasks a warp takes its next task when it starts the current
-  // one and prefetches that task's streams into L2 (RG_SHELL_PREFETCH).
   const int lane = threadIdx.x & 31;
   int t = blockIdx.x * (NT / 32) + (int)(threadIdx.x >> 5);
   bool first = true;
   const double DT1 = T->dt2;
   const R dt1r = (R)DT1;
   const R dtinv = dt1r / smax(dt1r * dt1r, (R)RG_EM20);
-  auto take = [&]() {
-    int g = 0;
-    if (lane == 0) g = (int)atomicAdd(P.qctr, 1u);
-    return __shfl_sync(0xffffffffu, g, 0);
-  };
-  int tnext = P.wtasks ? take() : 0;
   for (;;) {
     if (P.wtasks) {
-      t = tnext;
+      int g = 0;
+      if (lane == 0) g = (int)atomicAdd(P.qctr, 1u);
+      t = __shfl_sync(0xffffffffu, g, 0);
       if (t >= P.wtasks) break;
-      tnext = take();
-      if (RG_SHELL_PREFETCH && tnext < P.wtasks)
-        shell_prefetch_task(S, NPT, P.nft + tnext * 32, min(32, P.nel - tnext * 32), lane);
     } else {
       if (!first) break;
       first = false;

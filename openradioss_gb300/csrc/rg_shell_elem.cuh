@@ -156,44 +156,6 @@ struct ShellArrays {
 };
 
 
-// L2 prefetch of one 32-element warp task's streams -- connectivity, slot
-// indices and element state, elements e0 .. e0 + n - 1 of every component
-// -- issued by the 32 lanes of a warp (one 128-byte line each per request).
-// The FP64 kernel requests the task it takes next while it computes the
-// current one, so that the state streams' DRAM latency overlaps FP64 work.
-// Only lines holding an element of the task are requested, so every address
-// lies inside its array.
-template <typename ER>
-__device__ __forceinline__ void shell_prefetch_task(const ShellArrays<ER> &S, const int npt,
-                                                    const int e0, const int n,
-                                                    const int lane) {
-  const int nc = S.nc;
-  auto pf = [&](const void *base, const int ncomp, const int esize) {
-    const int per_line = 128 / esize;
-    const int lines = (n + per_line - 1) / per_line;
-    for (int i = lane; i < ncomp * lines; i += 32) {
-      const int c = i / lines, l = i - c * lines;
-      const char *p = (const char *)base + ((size_t)c * nc + e0 + (size_t)l * per_line) * esize;
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-    }
-  };
-  pf(S.ix, 4, 4);
-  pf(S.iadc, 4, 4);
-  pf(S.offg, 1, sizeof(ER));
-  pf(S.thke, 1, sizeof(ER));
-  pf(S.thk, 1, 8);
-  pf(S.forc, 5, sizeof(ER));
-  pf(S.mom, 3, sizeof(ER));
-  pf(S.hour, 5, sizeof(ER));
-  pf(S.gstr, 8, sizeof(ER));
-  pf(S.epsdg, 1, sizeof(ER));
-  pf(S.eint, 2, 8);
-  pf(S.ehou, 1, 8);
-  pf(S.sig, 5 * npt, sizeof(ER));
-  pf(S.pla, npt, sizeof(ER));
-  pf(S.epsd, npt, sizeof(ER));
-}
-
 // COQINI tables (NPT = 1..5), single-precision DATA literals.
 static __constant__ float c_z0[5][5] = {{0.f, 0.f, 0.f, 0.f, 0.f},
                                  {-.5f, 0.5f, 0.f, 0.f, 0.f},
