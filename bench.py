@@ -955,7 +955,8 @@ def main():
             line["serving"] = {k: sv[k] for k in (
                 "value", "unit", "completed", "failed", "p50_latency_s", "p99_latency_s",
                 "sequential_fp64_jobs_h", "sequential_mixed_jobs_h",
-                "fifo_one_at_a_time_latency_s", "admit_all_arrival_order",
+                "fifo_one_at_a_time_latency_s", "batched_admit_all_arrival_order",
+                "batched_least_work_first",
                 "speedup_vs_sequential_plain", "speedup_vs_sequential_mixed",
                 "element_updates_s", "makespan_s", "config", "jobs_with_device_status")}
     if rank == 0:

@@ -37,7 +37,11 @@ namespace rg {
 constexpr int BNT = 128;  // threads per block, elements / nodes per sub-tile
 constexpr unsigned BAR_SPIN_LIMIT = 1u << 22;  // ~0.3-3 s of 64 ns naps
 
-enum { BK_HEXA1 = 0, BK_HEXA2 = 1, BK_SHELL = 2 /* + npt - 1 */ };
+// tile kinds: hexa LAW1 / LAW2 (Jaumann rate), shells of 1..5 points,
+// hexa LAW1 / LAW2 in the co-rotational frame (JCVT = 1); tiles run in
+// decreasing kind order, the costliest first
+enum { BK_HEXA1 = 0, BK_HEXA2 = 1, BK_SHELL = 2 /* + npt - 1 */, BK_HEXA1C = 7, BK_HEXA2C = 8 };
+__host__ __device__ inline bool bk_hexa(int kind) { return kind < BK_SHELL || kind >= BK_HEXA1C; }
 
 struct BatchTile {
   int kind, group, tile, part;
@@ -164,7 +168,7 @@ batch_kernel(const BatchDev<ER> B, const int phases) {
       const int t = next_item(B.ctr, &s_item);
       if (t >= B.ntiles) break;
       const BatchTile tl = B.tiles[t];
-      const bool hexa = tl.kind < BK_SHELL;
+      const bool hexa = bk_hexa(tl.kind);
       const int j = hexa ? B.hg[tl.group].job : B.sg[tl.group].job;
       if (__ldcg(&B.jobs[j].T->ncycle) >= B.jobs[j].target) continue;  // block-uniform
       copy_to_shared(&sJ, B.jobs + j);
@@ -186,6 +190,14 @@ batch_kernel(const BatchDev<ER> B, const int phases) {
           case BK_HEXA2:
             if (il < sP.h.nel)
               hexa_element<ER, 2>(sP.h, sJ.ha, sJ.nv, fs, sJ.T, sJ.status, il, dtmine, elmin);
+            break;
+          case BK_HEXA1C:
+            if (il < sP.h.nel)
+              hexa_element<ER, 1, 1>(sP.h, sJ.ha, sJ.nv, fs, sJ.T, sJ.status, il, dtmine, elmin);
+            break;
+          case BK_HEXA2C:
+            if (il < sP.h.nel)
+              hexa_element<ER, 2, 1>(sP.h, sJ.ha, sJ.nv, fs, sJ.T, sJ.status, il, dtmine, elmin);
             break;
           case BK_SHELL + 0:
             if (il < sP.s.nel)
@@ -436,7 +448,9 @@ int rebuild(rg_batch *b) {
       hg.push_back(G);
       const int ntl_g = (g.nel + et - 1) / et;
       for (int t = 0; t < ntl_g; t++)
-        tiles.push_back({g.P.mtn == 1 ? BK_HEXA1 : BK_HEXA2, gi, t, part + t});
+        tiles.push_back({g.P.jcvt ? (g.P.mtn == 1 ? BK_HEXA1C : BK_HEXA2C)
+                                  : (g.P.mtn == 1 ? BK_HEXA1 : BK_HEXA2),
+                         gi, t, part + t});
       part += ntl_g;
     }
     const int nsg = shell_group_count(c->shells);
@@ -668,8 +682,6 @@ int rg_batch_add(rg_batch *b, rg_ctx *c, int target_ncycle) {
   if (c->shells.idtmin)
     return bfail(b, RG_E_UNSUP, "batch: jobs with an element time-step action run alone (rg_cycle)");
   for (auto &g : c->hg)
-    if (g.P.jcvt)
-      return bfail(b, RG_E_UNSUP, "batch: co-rotational (JCVT=1) hexa jobs run alone (rg_cycle)");
   // the batched kernel carries the lean shell material (no kinematic
   // hardening, thermal softening or IPLA = 2: they run alone)
   for (int g = 0; g < shell_group_count(c->shells); g++)

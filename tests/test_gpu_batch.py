@@ -138,3 +138,28 @@ def test_autotune_leaves_state_unchanged():
     b.sync()
     for i, e in enumerate(es):
         assert bitwise(state(e), ref[i]), i
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batch_corotational_hexa(prec):
+    """Hexa jobs in the co-rotational frame (JCVT = 1, the starter's default
+    for Lagrangian bricks) share a batch with Jaumann-rate hexas and shells:
+    each agrees with the same model stepped alone, and the batch is bitwise
+    the same under another launch configuration."""
+    from openradioss_gb300.engine import Engine
+    corot = []
+    for seed, law in ((21, "law2"), (22, "law1")):
+        m = M.hexa_impact_block(2000, seed=seed, law=law)
+        for g in m.hexa:
+            g.jcvt = 1
+        corot.append(m)
+    ms = corot + [M.crash_box(n_side=5, n_len=10, seed=23), M.hexa_impact_block(1500, seed=24)]
+    n = 40
+    got = run_batch(ms, prec, n)
+    for i, m in enumerate(ms):
+        e = Engine(m, precision=prec)
+        e.cycle(n)
+        assert close(got[i], state(e), TOL[prec]), i
+    other = run_batch(ms, prec, n, (2, 4, 1, 1))
+    for i in range(len(ms)):
+        assert bitwise(other[i], got[i]), i
