@@ -37,13 +37,16 @@ class Engine:
 
     def __init__(self, model, device=0, precision=RG_PREC_FP64, skyline=None,
                  elements_only=False):
-        """elements_only: the model's rigid bodies and concentrated loads
-        (model.rbodies, model.cloads), which the CUDA path does not run, are
-        left to the caller's own nodal update, and only the FORINT-level
-        call (forint_step) is open; without it such a model is refused."""
-        if (getattr(model, "rbodies", None) or getattr(model, "cloads", None)) and not elements_only:
-            raise RgError("rigid bodies and concentrated loads are not on the CUDA path: "
-                          "use elements_only=True with forint_step")
+        """elements_only: the model's rigid bodies, rigid-material bodies,
+        concentrated loads and imposed velocities (model.rbodies, rmats,
+        cloads, impvels), which the CUDA path does not run, are left to the
+        caller's own nodal update, and only the FORINT-level call
+        (forint_step) is open; without it such a model is refused."""
+        if any(getattr(model, k, None) for k in ("rbodies", "rmats", "cloads", "impvels")) \
+                and not elements_only:
+            raise RgError("rigid bodies, rigid materials, concentrated loads and imposed "
+                          "velocities are not on the CUDA path: use elements_only=True with "
+                          "forint_step")
         self.elements_only = elements_only
         self.L = _lib.lib()
         self.model = model

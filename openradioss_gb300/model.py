@@ -195,6 +195,14 @@ class Model:
     # concentrated loads (/CLOAD): (1-based node, direction 0..5, abscissa
     # scale, ordinate scale, curve abscissae, curve ordinates)
     cloads: list = field(default_factory=list)
+    # rigid-material bodies (/MAT/RIGID, LAW13, the starter's RIGID_MAT):
+    # (1-based secondary nodes, centre of mass (3,), mass, principal axes as
+    # rows (3, 3), principal inertia (3,)) -- oracle only, like rbodies
+    rmats: list = field(default_factory=list)
+    # imposed velocities (/IMPVEL): (1-based node, direction 0..2, 1/abscissa
+    # scale, ordinate scale, start, stop, curve abscissae, curve ordinates)
+    # -- oracle only
+    impvels: list = field(default_factory=list)
     ishfram: int = 0           # local shell frame: 0 symmetric, 2 /SHFRA/V4
     nodal_dt: tuple | None = None  # /DT/NODA: (DTFAC1(11), DTMIN1(11))
     # /DT time-step actions {kind: (IDTMIN, DTMIN1)}: 3 shells (1/5 stop,
@@ -631,3 +639,128 @@ def hexa_model_from_deck(d, name="deck"):
     m.rbodies = rbodies
     m.cloads = cloads
     return m
+
+
+def rigid_mat_init(X, MS, IN, nodes):
+    """The starter's RIGID_MAT (starter/source/materials/mat/mat019/
+    rigid_mat.F) for one rigid-material body of 1-based secondary nodes: mass
+    = the nodes' masses, centre of mass, the inertia tensor about it (nodal
+    inertia plus the point masses), its principal inertia and axes (rows,
+    right-handed).  Returns (centre, mass, axes, inertia)."""
+    sec = np.asarray(nodes, np.int64) - 1
+    ms = MS[sec]
+    mass = float(ms.sum())
+    xg = (X[:, sec] * ms).sum(axis=1) / mass
+    J = np.zeros((3, 3))
+    for k, n in enumerate(sec):
+        r = X[:, n] - xg
+        J += IN[n] * np.eye(3) + ms[k] * (np.dot(r, r) * np.eye(3) - np.outer(r, r))
+    w, v = np.linalg.eigh(J)
+    axes = v.T.copy()
+    if np.linalg.det(axes) < 0:
+        axes[2] = -axes[2]
+    return xg, mass, axes, w
+
+
+def rigid_material_bodies(ixs_rigid):
+    """ININODE_RM (starter/source/materials/mat/mat019/ininode_rm.F): the
+    rigid-material bricks (1-based node columns, (8, n)) grouped into bodies
+    of bricks connected through shared nodes; each body's nodes, sorted."""
+    n = ixs_rigid.shape[1]
+    parent = list(range(n))
+
+    def root(i):
+        while parent[i] != i:
+            parent[i] = parent[parent[i]]
+            i = parent[i]
+        return i
+    owner = {}
+    for e in range(n):
+        for nd in ixs_rigid[:, e]:
+            nd = int(nd)
+            if nd in owner:
+                a, b = root(owner[nd]), root(e)
+                if a != b:
+                    parent[max(a, b)] = min(a, b)
+            else:
+                owner[nd] = e
+    groups = {}
+    for e in range(n):
+        groups.setdefault(root(e), set()).update(int(v) for v in ixs_rigid[:, e])
+    return [np.array(sorted(groups[k]), np.int32) for k in sorted(groups)]
+
+
+def rigid_jc_model_from_deck(d, name="deck"):
+    """Model of a hexa deck with Johnson-Cook and rigid-material parts held
+    as arrays (the layout written by tests/golden/make_loi13.py: nodes,
+    /BRICK parts, /MAT/PLAS_JOHNS, /MAT/RIGID, /PROP/SOLID, /BCS, /IMPVEL +
+    /FUNCT), with the starter's decisions for it:
+
+    * the Johnson-Cook part: Isolid = 1, Ismstr 0 -> 4, Iframe 2 -> the
+      co-rotational frame (JCVT = 1); LAW2 with the reader's defaults;
+    * masses: SMASS3 lumping rho V / 8 of every brick, rigid ones included;
+    * the rigid-material parts (LAW13) run no element (FORINT skips them):
+      their bricks form rigid-material bodies (ININODE_RM), set up by
+      rigid_mat_init (RIGID_MAT);
+    * /IMPVEL: abscissa scale 0 -> 1 (stored inverted), ordinate scale 0 ->
+      1, stop time 0 -> infinity.
+
+    Node ids are mapped to 1-based indices in the order of the /NODE card;
+    elements keep their user ids."""
+    node_id = np.asarray(d["node_id"])
+    index = {int(n): k + 1 for k, n in enumerate(node_id)}
+    to_idx = np.vectorize(lambda n: index[int(n)], otypes=[np.int32])
+    X = np.ascontiguousarray(np.asarray(d["X"], np.float64).T)
+    numnod = X.shape[1]
+    jc = dict(zip([str(c) for c in d["mat_jc_columns"]], np.asarray(d["mat_jc"])))
+    rigid = {int(r[0]): r for r in np.asarray(d["mat_rigid"])}
+    pr = dict(zip([str(c) for c in d["prop_columns"]], np.asarray(d["prop"])))
+    if int(pr["Isolid"]) not in (0, 1) or int(pr["Ismstr"]) not in (0, 4) or \
+            int(pr["Iframe"]) not in (1, 2):
+        raise ValueError("only Isolid = 1, Ismstr = 4 bricks are supported")
+    ms = np.zeros(numnod)
+    groups, rigid_cols = [], []
+    bid, bpart, bnodes = (np.asarray(d[k]) for k in ("brick_id", "brick_part", "brick_nodes"))
+    for p, mid, pid in zip(d["part_id"], d["part_mat"], d["part_prop"]):
+        sel = np.nonzero(bpart == p)[0]
+        ixs = np.zeros((11, len(sel)), np.int32)
+        ixs[0] = int(mid)
+        ixs[1:9] = to_idx(bnodes[sel]).T
+        ixs[9] = int(pid)
+        ixs[10] = bid[sel]
+        if int(mid) in rigid:
+            lumped_mass_hexa(X, ixs, float(rigid[int(mid)][1]), ms)
+            rigid_cols.append(ixs[1:9])
+            continue
+        if int(mid) != int(jc["id"]):
+            raise ValueError("unexpected material %d" % int(mid))
+        lumped_mass_hexa(X, ixs, float(jc["rho"]), ms)
+        mat = law2(float(jc["rho"]), float(jc["E"]), float(jc["nu"]), float(jc["a"]),
+                   float(jc["b"]), float(jc["n"]), c=float(jc["c"]), eps0=float(jc["eps0"]),
+                   epsmax=float(jc["epsmax"]), sigmax=float(jc["sigmax"]))
+        geo = solid_prop(qa=pr["qa"] or 1.1, qb=pr["qb"] or 0.05, qh=pr["h"] or 0.1)
+        groups.append(HexaGroupSpec(ixs, mat, geo, jcvt=1 if int(pr["Iframe"]) == 2 else 0))
+    icodt = np.zeros(numnod, np.int32)
+    off = np.asarray(d["bcs_offsets"])
+    bn = to_idx(np.asarray(d["bcs_nodes"]))
+    for k, (tra, rot) in enumerate(zip(d["bcs_tra"], d["bcs_rot"])):
+        icodt[bn[off[k]:off[k + 1]] - 1] |= _code_bits(str(tra), 1) | _code_bits(str(rot), 8)
+    inr = np.zeros(numnod)
+    rmats = []
+    if rigid_cols:
+        for nodes in rigid_material_bodies(np.concatenate(rigid_cols, axis=1)):
+            xg, mass, axes, inertia = rigid_mat_init(X, ms, inr, nodes)
+            rmats.append((nodes, xg, mass, axes, inertia))
+    fx, fy = np.asarray(d["funct1"], np.float64).T
+    xs, ys, t0, t1 = (float(v) for v in d["impvel_scale"])
+    facx = 1.0 / (xs or 1.0)
+    impvels = [(index[int(n)], int(d["impvel_dir"]), facx, ys or 1.0, t0, t1 or 1e30, fx, fy)
+               for n in d["impvel_nodes"]]
+    m = Model(name, X, np.zeros_like(X), ms, icodt, hexa=groups, IN=inr)
+    m.rmats = rmats
+    m.impvels = impvels
+    dt = np.asarray(d["run_dt"])
+    if dt[0] > 0:
+        m.dtfac_solid = float(dt[0])
+    return m
+

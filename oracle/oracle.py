@@ -81,6 +81,9 @@ def _declare(L):
         L.or_set_record.argtypes = [vp, C.c_int]
         L.or_set_nodal_dt.argtypes = [vp, C.c_double, C.c_double]
         L.or_set_dtmin.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+        L.or_rmat_add.argtypes = [vp, C.c_int, _ip, _dp, C.c_double, _dp, _dp]
+        L.or_impvel_add.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, C.c_int, _dp, _dp]
         L.or_get_mass.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.or_get_record.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.or_get_wfext.argtypes = [vp, C.c_void_p]
@@ -131,6 +134,19 @@ class OracleModel:
                                np.ascontiguousarray(inertia, np.float64))
             if r < 0:
                 raise RuntimeError("or_rbody_add failed %d" % r)
+        for (nodes, xg, mass, axes, inertia) in getattr(model, "rmats", []):
+            r = L.or_rmat_add(self.h, len(nodes), np.ascontiguousarray(nodes, np.int32),
+                              np.ascontiguousarray(xg, np.float64), float(mass),
+                              np.ascontiguousarray(axes, np.float64).reshape(-1),
+                              np.ascontiguousarray(inertia, np.float64))
+            if r < 0:
+                raise RuntimeError("or_rmat_add failed %d" % r)
+        for (node, dr, facx, fsc, t0, t1, xs, ys) in getattr(model, "impvels", []):
+            xs = np.ascontiguousarray(xs, np.float64)
+            r = L.or_impvel_add(self.h, int(node), int(dr), float(facx), float(fsc), float(t0),
+                                float(t1), len(xs), xs, np.ascontiguousarray(ys, np.float64))
+            if r < 0:
+                raise RuntimeError("or_impvel_add failed %d" % r)
         for (node, dr, fcx, fcy, xs, ys) in getattr(model, "cloads", []):
             xs = np.ascontiguousarray(xs, np.float64)
             r = L.or_cload_add(self.h, int(node), int(dr), float(fcx), float(fcy), len(xs), xs,

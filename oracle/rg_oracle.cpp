@@ -110,6 +110,33 @@ struct Model {
   std::vector<Load> loads;
   double wfext = 0;  // external work of the loads (OUTPUT%TH%WFEXT)
 
+  // rigid-material bodies (/MAT/RIGID, LAW13): the starter's RIGID_MAT
+  // record, set up by the caller (rigid_mat.F): mass RBYM(1), centre of mass
+  // RBYM(2:4) (never moved by the engine), principal axes as rows
+  // RBYM(5:13), principal inertia RBYM(14:16), smallest of them RBYM(17),
+  // global inertia tensor RBYM(18:26); the codes CONDRMAT moved from the
+  // secondary nodes, and the body's accelerations and velocities ARBYM,
+  // VRBYM, ARRBYM, VRRBYM.
+  struct RigidMat {
+    std::vector<int> nodes;  // secondary nodes, 0-based
+    double mass = 0, xg[3] = {}, R[9] = {}, I[3] = {}, in = 0, J[9] = {};
+    int icod[2] = {0, 0};    // rotational, translational (Radioss codes: 4 x, 2 y, 1 z)
+    double ar[3] = {}, vr[3] = {}, arr[3] = {}, vrr[3] = {};
+  };
+  std::vector<RigidMat> rmats;
+
+  // imposed velocities (/IMPVEL, FIXVEL with IDIS = 1, global direction):
+  // node (0-based), direction 0..2, 1/abscissa scale (FACX), ordinate scale,
+  // start / stop times, load curve, and the power carried to the next
+  // cycle's work (VEL(4))
+  struct ImpVel {
+    int node = 0, dir = 0;
+    double facx = 1, fscale = 1, tstart = 0, tstop = 1e30;
+    std::vector<double> x, y;
+    double vel4 = 0;
+  };
+  std::vector<ImpVel> impvels;
+
   // forces supplied from outside for the next cycle (or_set_forces): the
   // cycle then skips its element groups and assembly
   bool ext = false;
@@ -1218,6 +1245,206 @@ int rgbodv(Model &M, const Model::Body &B) {
   return err;
 }
 
+// RMATPON (materials/mat/mat013/rmatpon.F, IFLAG 1 then 2; called by
+// RMATFORP at resol.F:5774, after the assembly): the secondary nodes'
+// forces and their moments about the body's (initial) centre of mass are
+// summed (the reference's SUM_6_FLOAT: order-independent, here in node
+// order); without a rotational code the moment, taken to the principal
+// frame, gains the gyroscopic term of the body's angular velocity turned by
+// ROTBMR over DT1 (a local copy of the axes: RBYM(5:13) keeps its starter
+// value) and comes back scaled by IN / I_k; the inertia tensor RBYM(18:26)
+// is rebuilt from the turned axes.  Then ARBYM = F / mass, ARRBYM = M / IN,
+// the translational code zeroes components, and the secondary nodes' forces,
+// moments and stiffnesses are cleared.
+void rmatpon(Model &M, Model::RigidMat &B, bool rot) {
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int n : B.nodes) {
+    const double rx = M.X[3 * n] - B.xg[0], ry = M.X[3 * n + 1] - B.xg[1],
+                 rz = M.X[3 * n + 2] - B.xg[2];
+    const double f0 = M.A[3 * n], f1 = M.A[3 * n + 1], f2 = M.A[3 * n + 2];
+    const double m0 = rot ? M.AR[3 * n] : RG_ZERO, m1 = rot ? M.AR[3 * n + 1] : RG_ZERO,
+                 m2 = rot ? M.AR[3 * n + 2] : RG_ZERO;
+    s[0] = s[0] + f0;
+    s[1] = s[1] + f1;
+    s[2] = s[2] + f2;
+    s[3] = s[3] + (m0 + ry * f2 - rz * f1);
+    s[4] = s[4] + (m1 + rz * f0 - rx * f2);
+    s[5] = s[5] + (m2 + rx * f1 - ry * f0);
+  }
+  double *ar = B.ar, *arr = B.arr, *vrr = B.vrr, *J = B.J;
+  for (int k = 0; k < 3; k++) {
+    ar[k] = s[k];
+    arr[k] = s[3 + k];
+  }
+  double RB[9];
+  for (int k = 0; k < 9; k++) RB[k] = B.R[k];
+  const double *I = B.I;
+  auto rebuild_j = [&]() {
+    const double ii1 = I[0] * RB[0], ii2 = I[0] * RB[1], ii3 = I[0] * RB[2];
+    const double ii4 = I[1] * RB[3], ii5 = I[1] * RB[4], ii6 = I[1] * RB[5];
+    const double ii7 = I[2] * RB[6], ii8 = I[2] * RB[7], ii9 = I[2] * RB[8];
+    J[0] = RB[0] * ii1 + RB[3] * ii4 + RB[6] * ii7;
+    J[1] = RB[0] * ii2 + RB[3] * ii5 + RB[6] * ii8;
+    J[2] = RB[0] * ii3 + RB[3] * ii6 + RB[6] * ii9;
+    J[3] = RB[1] * ii1 + RB[4] * ii4 + RB[7] * ii7;
+    J[4] = RB[1] * ii2 + RB[4] * ii5 + RB[7] * ii8;
+    J[5] = RB[1] * ii3 + RB[4] * ii6 + RB[7] * ii9;
+    J[6] = RB[2] * ii1 + RB[5] * ii4 + RB[8] * ii7;
+    J[7] = RB[2] * ii2 + RB[5] * ii5 + RB[8] * ii8;
+    J[8] = RB[2] * ii3 + RB[5] * ii6 + RB[8] * ii9;
+  };
+  const int lcod = B.icod[0];
+  if (lcod > 0) {
+    double vi[3];
+    for (int k = 0; k < 3; k++)
+      vi[k] = RB[3 * k] * vrr[0] + RB[3 * k + 1] * vrr[1] + RB[3 * k + 2] * vrr[2];
+    rotbmr(vi, RB, M.dt1);
+    rebuild_j();
+    const double wa1 = J[0] * vrr[0] + J[1] * vrr[1] + J[2] * vrr[2];
+    const double wa2 = J[3] * vrr[0] + J[4] * vrr[1] + J[5] * vrr[2];
+    const double wa3 = J[6] * vrr[0] + J[7] * vrr[1] + J[8] * vrr[2];
+    arr[0] = arr[0] + (wa2 * vrr[2] - wa3 * vrr[1]);
+    arr[1] = arr[1] + (wa3 * vrr[0] - wa1 * vrr[2]);
+    arr[2] = arr[2] + (wa1 * vrr[1] - wa2 * vrr[0]);
+    if (lcod == 1) {
+      const double det = RG_ONE / (J[0] * J[4] - J[1] * J[3]);
+      const double w1 = arr[0], w2 = arr[1];
+      arr[0] = (J[4] * w1 - J[3] * w2) * det;
+      arr[1] = (-J[1] * w1 + J[0] * w2) * det;
+      arr[2] = RG_ZERO;
+      vrr[2] = RG_ZERO;
+    } else if (lcod == 2) {
+      const double det = RG_ONE / (J[0] * J[8] - J[2] * J[6]);
+      const double w1 = arr[0], w2 = arr[2];
+      arr[0] = (J[8] * w1 - J[6] * w2) * det;
+      arr[1] = RG_ZERO;
+      arr[2] = (-J[2] * w1 + J[0] * w2) * det;
+      vrr[1] = RG_ZERO;
+    } else if (lcod == 3) {
+      arr[0] = arr[0] / J[0];
+      arr[1] = arr[2] = RG_ZERO;
+      vrr[1] = vrr[2] = RG_ZERO;
+    } else if (lcod == 4) {
+      const double det = RG_ONE / (J[4] * J[8] - J[5] * J[7]);
+      const double w1 = arr[1], w2 = arr[2];
+      arr[0] = RG_ZERO;
+      arr[1] = (J[8] * w1 - J[7] * w2) * det;
+      arr[2] = (-J[5] * w1 + J[4] * w2) * det;
+      vrr[0] = RG_ZERO;
+    } else if (lcod == 5) {
+      arr[0] = RG_ZERO;
+      arr[1] = arr[1] / J[4];
+      arr[2] = RG_ZERO;
+      vrr[0] = vrr[2] = RG_ZERO;
+    } else if (lcod == 6) {
+      arr[0] = arr[1] = RG_ZERO;
+      arr[2] = arr[2] / J[8];
+      vrr[0] = vrr[1] = RG_ZERO;
+    } else if (lcod == 7) {
+      arr[0] = arr[1] = arr[2] = RG_ZERO;
+      vrr[0] = vrr[1] = vrr[2] = RG_ZERO;
+    }
+  } else {
+    const double wa[3] = {arr[0], arr[1], arr[2]};
+    for (int k = 0; k < 3; k++)
+      arr[k] = RB[3 * k] * wa[0] + RB[3 * k + 1] * wa[1] + RB[3 * k + 2] * wa[2];
+    double vi[3];
+    for (int k = 0; k < 3; k++)
+      vi[k] = RB[3 * k] * vrr[0] + RB[3 * k + 1] * vrr[1] + RB[3 * k + 2] * vrr[2];
+    rotbmr(vi, RB, M.dt1);
+    arr[0] = arr[0] + ((I[1] - I[2]) * vi[1] * vi[2]);
+    arr[1] = arr[1] + ((I[2] - I[0]) * vi[2] * vi[0]);
+    arr[2] = arr[2] + ((I[0] - I[1]) * vi[0] * vi[1]);
+    double w[3];
+    for (int k = 0; k < 3; k++) w[k] = arr[k] * B.in / I[k];
+    for (int k = 0; k < 3; k++) arr[k] = RB[k] * w[0] + RB[3 + k] * w[1] + RB[6 + k] * w[2];
+    rebuild_j();
+  }
+  for (int k = 0; k < 3; k++) {
+    ar[k] = B.mass > RG_ZERO ? ar[k] / B.mass : RG_ZERO;
+    arr[k] = B.in > RG_ZERO ? arr[k] / B.in : RG_ZERO;
+  }
+  const int tcod = B.icod[1];
+  if (tcod & 4) ar[0] = B.vr[0] = RG_ZERO;
+  if (tcod & 2) ar[1] = B.vr[1] = RG_ZERO;
+  if (tcod & 1) ar[2] = B.vr[2] = RG_ZERO;
+  for (int n : B.nodes) {
+    for (int k = 0; k < 3; k++) {
+      M.A[3 * n + k] = RG_ZERO;
+      if (rot) M.AR[3 * n + k] = RG_ZERO;
+    }
+    M.STIFN[n] = RG_EM20;
+    if (rot) M.STIFR[n] = RG_EM20;
+  }
+}
+
+// RMATACCE (materials/mat/mat013/rmatacce.F, resol.F:7879): the secondary
+// nodes take the accelerations that make VELOCITY give them the body's
+// motion about its (initial) centre of mass: VG = VRRBYM + ARRBYM*DT12,
+// AR = (VG - VR)/DT12, A = ARBYM + (VRBYM + VG x r + DT2/2 VG x (VG x r) -
+// V)/DT12; then VRBYM += ARBYM*DT12 and VRRBYM = VG.
+void rmatacce(Model &M, Model::RigidMat &B, bool rot) {
+  const double usdt = RG_ONE / M.dt12;
+  double vg[3];
+  for (int k = 0; k < 3; k++) vg[k] = B.vrr[k] + B.arr[k] * M.dt12;
+  for (int n : B.nodes) {
+    const double rx = M.X[3 * n] - B.xg[0], ry = M.X[3 * n + 1] - B.xg[1],
+                 rz = M.X[3 * n + 2] - B.xg[2];
+    if (rot)
+      for (int k = 0; k < 3; k++) M.AR[3 * n + k] = (vg[k] - M.VR[3 * n + k]) * usdt;
+    const double v1x2 = vg[0] * ry, v2x1 = vg[1] * rx, v2x3 = vg[1] * rz;
+    const double v3x2 = vg[2] * ry, v3x1 = vg[2] * rx, v1x3 = vg[0] * rz;
+    const double vx1 = v2x3 - v3x2, vx2 = v3x1 - v1x3, vx3 = v1x2 - v2x1;
+    M.A[3 * n] = B.ar[0] + usdt * (B.vr[0] + vx1 + RG_HALF * M.dt2 * (vg[1] * vx3 - vg[2] * vx2) -
+                                   M.V[3 * n]);
+    M.A[3 * n + 1] = B.ar[1] + usdt * (B.vr[1] + vx2 +
+                                       RG_HALF * M.dt2 * (vg[2] * vx1 - vg[0] * vx3) -
+                                       M.V[3 * n + 1]);
+    M.A[3 * n + 2] = B.ar[2] + usdt * (B.vr[2] + vx3 +
+                                       RG_HALF * M.dt2 * (vg[0] * vx2 - vg[1] * vx1) -
+                                       M.V[3 * n + 2]);
+  }
+  for (int k = 0; k < 3; k++) {
+    B.vr[k] = B.vr[k] + B.ar[k] * M.dt12;
+    B.vrr[k] = vg[k];
+  }
+}
+
+// VINTERDP (tools/curve/vinterdp.F): linear interpolation on the segment
+// holding t (the first one past the last abscissa below t), extended by the
+// end segments.
+double vinterdp(const std::vector<double> &x, const std::vector<double> &y, double t) {
+  const size_t n = x.size();
+  if (n == 1) return y[0];
+  size_t j = 0;
+  while (j + 2 < n && t > x[j + 1]) j++;
+  const double dydx = (y[j + 1] - y[j]) / (x[j + 1] - x[j]);
+  return y[j] + dydx * (t - x[j]);
+}
+
+// FIXVEL (constraints/general/impvel/fixvel.F:335-346, 367-379, 834-837),
+// imposed velocity (IDIS = 1) along a global direction: the velocity
+// F((TT + DT2/2) FACX) * FSCALE at mid-step is reached by the acceleration
+// (VIMP - V)/DT12; the power DW = 1/4 MS (A DT12 + 2 V)(A - A_before) is
+// counted DT1*DW now and DT2*DW at the next cycle.
+void fixvel(Model &M) {
+  for (auto &F : M.impvels) {
+    if (M.tt < F.tstart || M.tt > F.tstop) continue;
+    M.wfext = M.wfext + F.vel4;
+    F.vel4 = RG_ZERO;
+    const double tsc = (M.tt + RG_HALF * M.dt2) * F.facx;
+    double yc = vinterdp(F.x, F.y, tsc) * F.fscale;
+    const int i = F.node, j = F.dir;
+    yc = (yc - M.V[3 * i + j]) / M.dt12;
+    const double aold = M.A[3 * i + j];
+    M.A[3 * i + j] = yc;
+    const double dw = RG_FOURTH * M.MS[i] * (M.A[3 * i + j] * M.dt12 + RG_TWO * M.V[3 * i + j]) *
+                      (M.A[3 * i + j] - aold);
+    M.wfext = M.wfext + M.dt1 * dw;
+    F.vel4 = F.vel4 + M.dt2 * dw;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1339,6 +1566,9 @@ int or_cycle(void *m, int ncycle) {
     }
     // RBYFOR (resol.F:5714), before the nodal time step
     for (auto &B : M.bodies) rbyfor(M, B);
+    // RMATFORP (resol.F:5774): rigid-material bodies gather their nodes'
+    // forces
+    for (auto &B : M.rmats) rmatpon(M, B, rot);
     // DTNODA (time_step/dtnoda.F:213-345, 443-470), NODADT > 0: nodal time
     // step DTFAC1(11)*SQRT(2*MS/STIFN) over the nodes with mass, then the
     // rotational one DTFAC1(11)*SQRT(2*IN/STIFR); a node with non-positive
@@ -1518,9 +1748,14 @@ int or_cycle(void *m, int ncycle) {
         }
       }
     }
+    // FIXVEL (resol.F:7610): imposed velocities, after the boundary
+    // conditions
+    fixvel(M);
     // RBYVIT (resol.F:7849), after the boundary conditions
     for (auto &B : M.bodies)
       if (rgbodv(M, B)) M.error |= 64;
+    // RMATACCE (resol.F:7879): rigid-material bodies drive their nodes
+    for (auto &B : M.rmats) rmatacce(M, B, rot);
     // ECRIT (output/ecrit.F:193, 266-330): energies of the printout with the
     // velocities brought to the current time, V + DT1/2 * A.  RBYCOR /
     // RGBCOR (rbycor.F, rgbcor.F:213-380) take the secondary nodes of rigid
@@ -1746,6 +1981,78 @@ int or_rbody_add(void *m, int main, int nsn, const int *nodes, const double *axe
   M.secondary[B.main] = 2;
   M.bodies.push_back(B);
   return (int)M.bodies.size() - 1;
+}
+
+int or_rmat_add(void *m, int nsl, const int *nodes, const double *xg, double mass,
+                const double *axes, const double *inertia) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (M.finalized || nsl < 1 || !nodes || !xg || !axes || !inertia || !(mass > RG_ZERO))
+    return -1;
+  Model::RigidMat B;
+  for (int i = 0; i < nsl; i++) {
+    const int n = nodes[i] - 1;
+    if (n < 0 || n >= M.numnod) return -1;
+    B.nodes.push_back(n);
+  }
+  B.mass = mass;
+  for (int k = 0; k < 3; k++) {
+    B.xg[k] = xg[k];
+    B.I[k] = inertia[k];
+  }
+  for (int k = 0; k < 9; k++) B.R[k] = axes[k];
+  B.in = std::min(B.I[0], std::min(B.I[1], B.I[2]));
+  {
+    // RBYM(18:26) of rigid_mat.F
+    const double *RB = B.R, *I = B.I;
+    const double ii1 = I[0] * RB[0], ii2 = I[0] * RB[1], ii3 = I[0] * RB[2];
+    const double ii4 = I[1] * RB[3], ii5 = I[1] * RB[4], ii6 = I[1] * RB[5];
+    const double ii7 = I[2] * RB[6], ii8 = I[2] * RB[7], ii9 = I[2] * RB[8];
+    B.J[0] = RB[0] * ii1 + RB[3] * ii4 + RB[6] * ii7;
+    B.J[1] = RB[0] * ii2 + RB[3] * ii5 + RB[6] * ii8;
+    B.J[2] = RB[0] * ii3 + RB[3] * ii6 + RB[6] * ii9;
+    B.J[3] = RB[1] * ii1 + RB[4] * ii4 + RB[7] * ii7;
+    B.J[4] = RB[1] * ii2 + RB[4] * ii5 + RB[7] * ii8;
+    B.J[5] = RB[1] * ii3 + RB[4] * ii6 + RB[7] * ii9;
+    B.J[6] = RB[2] * ii1 + RB[5] * ii4 + RB[8] * ii7;
+    B.J[7] = RB[2] * ii2 + RB[5] * ii5 + RB[8] * ii8;
+    B.J[8] = RB[2] * ii3 + RB[5] * ii6 + RB[8] * ii9;
+  }
+  // CONDRMAT (materials/mat/mat013/condrmat.F): the secondary nodes'
+  // boundary codes move to the body (Radioss codes: 4 x, 2 y, 1 z)
+  int it = 0, ir = 0;
+  for (int n : B.nodes) {
+    const int c = M.icodt[n];
+    if (c & 1) it |= 4;
+    if (c & 2) it |= 2;
+    if (c & 4) it |= 1;
+    if (c & 8) ir |= 4;
+    if (c & 16) ir |= 2;
+    if (c & 32) ir |= 1;
+    M.icodt[n] = 0;
+  }
+  B.icod[0] = ir;
+  B.icod[1] = it;
+  M.rmats.push_back(B);
+  return (int)M.rmats.size() - 1;
+}
+
+int or_impvel_add(void *m, int node, int dir, double facx, double fscale, double tstart,
+                  double tstop, int npts, const double *x, const double *y) {
+  Model &M = ((OrModelWrap *)m)->m;
+  if (node < 1 || node > M.numnod || dir < 0 || dir > 2 || npts < 1 || !x || !y) return -1;
+  for (int i = 1; i < npts; i++)
+    if (!(x[i] > x[i - 1])) return -1;
+  Model::ImpVel F;
+  F.node = node - 1;
+  F.dir = dir;
+  F.facx = facx;
+  F.fscale = fscale;
+  F.tstart = tstart;
+  F.tstop = tstop;
+  F.x.assign(x, x + npts);
+  F.y.assign(y, y + npts);
+  M.impvels.push_back(F);
+  return (int)M.impvels.size() - 1;
 }
 
 int or_cload_add(void *m, int node, int dir, double fcx, double fcy, int npts,

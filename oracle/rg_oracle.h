@@ -100,6 +100,15 @@ int or_set_nodal_dt(void *m, double dtfac, double dtmin);
 /* /DT time-step actions: kind 3 shells (IDTMIN(3) 1/5 stop flag, 2 delete),
  * kind 11 nodal step (IDTMIN(11) 3/8 mass scaling, else stop flag). */
 int or_set_dtmin(void *m, int kind, int idtmin, double dtmin);
+/* Rigid-material body (/MAT/RIGID, LAW13) of the starter's RIGID_MAT:
+ * 1-based secondary nodes, centre of mass, mass, principal axes (rows, 3x3)
+ * and principal inertia.  Before or_finalize. */
+int or_rmat_add(void *m, int nsl, const int *nodes, const double *xg, double mass,
+                const double *axes, const double *inertia);
+/* Imposed velocity (/IMPVEL, IDIS = 1) on a 1-based node along x, y or z
+ * (0..2): F((TT + DT2/2) * facx) * fscale between tstart and tstop. */
+int or_impvel_add(void *m, int node, int dir, double facx, double fscale, double tstart,
+                  double tstop, int npts, const double *x, const double *y);
 /* Nodal masses and inertias (after any mass scaling). */
 int or_get_mass(void *m, double *ms, double *in);
 /* Local shell frame: 0 = symmetric convected frame (default), 2 = the
