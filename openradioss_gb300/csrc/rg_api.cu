@@ -347,16 +347,26 @@ energy_kernel(int ne, const double *__restrict__ eint,
     for (int j = 0; j < 4; j++) part[j * EN_BLOCKS + blockIdx.x] = sh[j][0];
 }
 
-__global__ void energy_final(const double *__restrict__ part, int nextra,
-                             const double *__restrict__ extra,
-                             double *__restrict__ out) {
-  if (threadIdx.x != 0) return;
-  for (int j = 0; j < 4; j++) {
+// Fixed-order sum of the NJ rows of EN_BLOCKS partials: thread t takes
+// partials t, t + EN_NT, ... in order, then a fixed tree (one block).
+template <int NJ>
+__device__ __forceinline__ void partials_final(const double *__restrict__ part,
+                                               double *__restrict__ out) {
+  __shared__ double sh[EN_NT];
+  for (int j = 0; j < NJ; j++) {
     double s = 0.0;
-    for (int b = 0; b < EN_BLOCKS; b++) s += part[j * EN_BLOCKS + b];
-    out[j] = s;
+    for (int b = threadIdx.x; b < EN_BLOCKS; b += EN_NT) s += part[j * EN_BLOCKS + b];
+    s = block_sum_fixed<EN_NT>(s, sh);
+    if (threadIdx.x == 0) out[j] = s;
   }
-  for (int j = 0; j < nextra; j++) out[j] += extra[j];
+}
+
+__global__ void __launch_bounds__(EN_NT)
+energy_final(const double *__restrict__ part, int nextra, const double *__restrict__ extra,
+             double *__restrict__ out) {
+  partials_final<4>(part, out);
+  if (threadIdx.x == 0)
+    for (int j = 0; j < nextra; j++) out[j] += extra[j];
 }
 
 // Node sums of the energy balance, fixed order like energy_kernel: mass,
@@ -386,13 +396,9 @@ balance_kernel(NodeView N, double *__restrict__ part) {
     for (int j = 0; j < 5; j++) part[j * EN_BLOCKS + blockIdx.x] = sh[j][0];
 }
 
-__global__ void balance_final(const double *__restrict__ part, double *__restrict__ out) {
-  if (threadIdx.x != 0) return;
-  for (int j = 0; j < 5; j++) {
-    double s = 0.0;
-    for (int b = 0; b < EN_BLOCKS; b++) s += part[j * EN_BLOCKS + b];
-    out[j] = s;
-  }
+__global__ void __launch_bounds__(EN_NT)
+balance_final(const double *__restrict__ part, double *__restrict__ out) {
+  partials_final<5>(part, out);
 }
 
 // AoS X(3,n) -> X4.xyz (keeps .w); same for V and VR.
@@ -1581,7 +1587,7 @@ int rg_energy(rg_ctx *c, double *eint, double *ekin, double *ekinr, double *ehou
   // shell element energies (fixed order) go to out[4..5] via the shell module
   double *extra = c->d_stage + 8;
   int nextra = shell_energy_enqueue(c->shells, c->prec, extra, c->stream);
-  energy_final<<<1, 32, 0, c->stream>>>(part, nextra, extra, out);
+  energy_final<<<1, EN_NT, 0, c->stream>>>(part, nextra, extra, out);
   double h[4];
   RG_CUDA(c, cudaMemcpyAsync(h, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1604,7 +1610,7 @@ int rg_energy_balance(rg_ctx *c, double *out, int n) {
   double *part = c->d_epart + 4 * EN_BLOCKS;
   double *dout = c->d_stage + 16;  // 5 doubles (staging holds >= 12 numnod + 16)
   balance_kernel<<<EN_BLOCKS, EN_NT, 0, c->stream>>>(c->nv, part);
-  balance_final<<<1, 32, 0, c->stream>>>(part, dout);
+  balance_final<<<1, EN_NT, 0, c->stream>>>(part, dout);
   double nb[5];
   RG_CUDA(c, cudaMemcpyAsync(nb, dout, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   RG_CUDA(c, cudaMemcpyAsync(c->h_time, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost,

@@ -85,6 +85,22 @@ __device__ __forceinline__ void st4(dbl4 *__restrict__ p, dbl4 v) { *p = v; }
 __device__ __forceinline__ F8 ldF8(const F8 *__restrict__ p) { return *p; }
 __device__ __forceinline__ float4 ldf4(const float4 *__restrict__ p) { return __ldg(p); }
 
+// Sum of one double per thread over a block of NT threads (a power of two)
+// in a fixed order: a shared-memory tree, the same additions every time.
+// The result is valid in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum_fixed(double v, double *sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = NT / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
 // Asynchronous global -> shared copies of one thread's own values (sm_80+
 // cp.async): issued early, they fetch element state while the thread
 // computes, without holding registers; cp_async_wait_all() makes them

@@ -12,6 +12,10 @@ namespace rg {
 // the 1-based rigid-link index
 constexpr int RG_LINK_SHIFT = 8;
 
+#ifndef RG_NODE_EARLY
+#define RG_NODE_EARLY 1
+#endif
+
 // ---------------------------------------------------------------------------
 // Node update: ASSPAR4 (asspar4.F:165-180) fixed-order slot sums, ACCELE
 // (accele.F:66-78), BCS10/BCS1V (bcs10.F:31), planar rigid wall, VELOCITY
@@ -195,6 +199,16 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
                                             int *__restrict__ status, const int n) {
   double a0, a1, a2, r0 = 0.0, r1 = 0.0, r2 = 0.0;
   F8 xf;  // mixed form: FP32 position copy; pad0 / pad1 = 1/MS, 1/IN in FP32
+#if RG_NODE_EARLY
+  // the node's own records are loaded ahead of the slot gathers (whose
+  // status atomic would otherwise keep them behind), so that both latencies
+  // overlap
+  dbl4 x = ld4(N.X4 + n);
+  dbl4 v = ld4(N.V4 + n);
+  dbl4 d;
+  if constexpr (F64) d = ld4(N.D4 + n);
+  else xf = N.XF[n];
+#endif
   if constexpr (F64) {
     node_assemble<F64, ROT, COH, MLP>(adsky, fsky_, fskyr_, status, n, a0, a1, a2, r0, r1, r2);
   } else {
@@ -202,7 +216,9 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
     node_sums_f32<ROT, COH, MLP>(__ldg(adsky + n), __ldg(adsky + n + 1),
                                  (const float4 *)fsky_, (const float4 *)fskyr_, status, b0, b1,
                                  b2, c0, c1, c2);
+#if !RG_NODE_EARLY
     xf = N.XF[n];
+#endif
     // ACCELE on the FP32 force sums: F * (1/MS) rounded once in FP32, then
     // widened (the forces carry FP32 precision already)
     a0 = widen_f32(__fmul_rn(b0, xf.pad0));
@@ -214,12 +230,14 @@ __device__ __forceinline__ void node_update(const NodeView &N, const int *__rest
       r2 = widen_f32(__fmul_rn(c2, xf.pad1));
     }
   }
-  dbl4 x = ld4(N.X4 + n);
-  dbl4 v = ld4(N.V4 + n);
   // FP64 form: D4 = displacement, MS.  Mixed form: D4 holds the initial
   // position and MS (D = X - X0 on download), so it is not touched here.
+#if !RG_NODE_EARLY
+  dbl4 x = ld4(N.X4 + n);
+  dbl4 v = ld4(N.V4 + n);
   dbl4 d;
   if constexpr (F64) d = ld4(N.D4 + n);
+#endif
   const double dt12 = COH ? __ldcg(&T->dt12) : T->dt12;
   const double dt2 = COH ? __ldcg(&T->dt2) : T->dt2;
   // ACCELE: A = A * (1/MS); X4.w holds 1/MS (0 when MS <= 0, giving A = 0)

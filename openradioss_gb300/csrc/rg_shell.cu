@@ -86,30 +86,35 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
   if (F.ctr) dt_finish_block<NT>(dp, F, P.part_off + blockIdx.x, T, status);
 }
 
-// Fixed-order shell energy partials: [0] internal (membrane + bending),
-// [1] hourglass.
-__global__ void shell_energy_kernel(int nc, const double *__restrict__ eint,
-                                    const double *__restrict__ ehou,
-                                    double *__restrict__ out) {
-  __shared__ double s0[256], s1[256];
+// Fixed-order shell energy sums, [0] internal (membrane + bending), [1]
+// hourglass: SHE_BLOCKS block partials (thread t of block b takes elements
+// b * 256 + t, then every SHE_BLOCKS * 256 further, in order; a fixed tree
+// per block), then one block adds the partials the same way.
+constexpr int SHE_BLOCKS = 152, SHE_NT = 256;
+__global__ void __launch_bounds__(SHE_NT)
+shell_energy_kernel(int nc, const double *__restrict__ eint, const double *__restrict__ ehou,
+                    double *__restrict__ part) {
+  __shared__ double sh[SHE_NT];
   double a = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < nc; i += 256) {
+  for (int i = blockIdx.x * SHE_NT + threadIdx.x; i < nc; i += SHE_BLOCKS * SHE_NT) {
     a += eint[i] + eint[nc + i];
     b += ehou[i];
   }
-  s0[threadIdx.x] = a;
-  s1[threadIdx.x] = b;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      s0[threadIdx.x] += s0[threadIdx.x + o];
-      s1[threadIdx.x] += s1[threadIdx.x + o];
-    }
-    __syncthreads();
-  }
+  a = block_sum_fixed<SHE_NT>(a, sh);
+  b = block_sum_fixed<SHE_NT>(b, sh);
   if (threadIdx.x == 0) {
-    out[0] = s0[0];
-    out[1] = s1[0];
+    part[blockIdx.x] = a;
+    part[SHE_BLOCKS + blockIdx.x] = b;
+  }
+}
+
+__global__ void __launch_bounds__(SHE_NT)
+shell_energy_final(const double *__restrict__ part, double *__restrict__ out) {
+  __shared__ double sh[SHE_NT];
+  for (int j = 0; j < 2; j++) {
+    const double v = (int)threadIdx.x < SHE_BLOCKS ? part[j * SHE_BLOCKS + threadIdx.x] : 0.0;
+    const double s = block_sum_fixed<SHE_NT>(v, sh);
+    if (threadIdx.x == 0) out[j] = s;
   }
 }
 
@@ -373,7 +378,7 @@ int shell_finalize(ShellModelHost &S, int prec, const double *X, const int *iadc
   if ((r = alloc((void **)&D->ix, ix.size() * sizeof(int)))) return r;
   if ((r = alloc((void **)&D->iadc, ia.size() * sizeof(int)))) return r;
   if ((r = alloc((void **)&D->degen, dg.size() * sizeof(int)))) return r;
-  if ((r = alloc((void **)&D->epart, 8 * sizeof(double)))) return r;
+  if ((r = alloc((void **)&D->epart, (2 * SHE_BLOCKS + 8) * sizeof(double)))) return r;
   if (cudaMemcpy(D->ix, ix.data(), ix.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(D->iadc, ia.data(), ia.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(D->degen, dg.data(), dg.size() * sizeof(int), cudaMemcpyHostToDevice)) {
@@ -447,7 +452,8 @@ int shell_energy_enqueue(ShellModelHost &S, int prec, double *out2, cudaStream_t
   auto *D = (ShellDev *)S.dev;
   const double *ei = prec == RG_PREC_FP64 ? D->a64.eint : D->a32.eint;
   const double *eh = prec == RG_PREC_FP64 ? D->a64.ehou : D->a32.ehou;
-  shell_energy_kernel<<<1, 256, 0, s>>>(S.numelc, ei, eh, out2);
+  shell_energy_kernel<<<SHE_BLOCKS, SHE_NT, 0, s>>>(S.numelc, ei, eh, D->epart);
+  shell_energy_final<<<1, SHE_NT, 0, s>>>(D->epart, out2);
   return 2;
 }
 
