@@ -25,16 +25,22 @@ hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
 }
 
 // ---------------------------------------------------------------------------
-template <typename ER, int LAW>
-static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
-                       const NodeView &N, typename SlotT<ER>::type *fsky,
-                       DtPartials dp, Time *T, int *status, const DtFinish &F,
-                       cudaStream_t s) {
-  constexpr int NT = 128;
-  // mixed form: 6 resident blocks per SM at 80 registers (about 100 bytes
-  // per thread spill to L1: measured faster than 4, 5 or 7 blocks); the FP64
-  // form needs its ~250 registers
-  constexpr int MINB = std::is_same<ER, float>::value ? 6 : 1;
+// Block size of a group: 128 threads, or 64 for a group of fewer than two
+// blocks of 128 per SM of a 152-SM GPU, whose 128-thread blocks would leave
+// SMs idle (the 8,000-hexa bar: 63 blocks of 128 on 152 SMs, each SM's
+// FP64 work then set by one block).
+constexpr int HEXA_SMALL = 2 * 152 * 128;
+static int hexa_nt(int nel) { return nel < HEXA_SMALL ? 64 : 128; }
+
+template <typename ER, int LAW, int NT>
+static void launch_nt(const HexaParams &P, const HexaArrays<ER> &A, const NodeView &N,
+                      typename SlotT<ER>::type *fsky, DtPartials dp, Time *T, int *status,
+                      const DtFinish &F, cudaStream_t s) {
+  // mixed form: 6 resident 128-thread blocks per SM at 80 registers (about
+  // 100 bytes per thread spill to L1: measured faster than 4, 5 or 7
+  // blocks; 64-thread blocks keep the same register budget); the FP64 form
+  // needs its ~250 registers
+  constexpr int MINB = std::is_same<ER, float>::value ? 6 * 128 / NT : 1;
   const int nb = (P.nel + NT - 1) / NT;
   if (P.jcvt)
     hexa_kernel<ER, LAW, 1, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);
@@ -42,7 +48,19 @@ static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
     hexa_kernel<ER, LAW, 0, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);
 }
 
-int hexa_blocks(int nel) { return (nel + 127) / 128; }
+template <typename ER, int LAW>
+static void launch_one(const HexaParams &P, const HexaArrays<ER> &A,
+                       const NodeView &N, typename SlotT<ER>::type *fsky,
+                       DtPartials dp, Time *T, int *status, const DtFinish &F,
+                       cudaStream_t s) {
+  if (hexa_nt(P.nel) == 64)
+    launch_nt<ER, LAW, 64>(P, A, N, fsky, dp, T, status, F, s);
+  else
+    launch_nt<ER, LAW, 128>(P, A, N, fsky, dp, T, status, F, s);
+}
+
+// time-step partials of a group: one per block of its launch
+int hexa_blocks(int nel) { return (nel + hexa_nt(nel) - 1) / hexa_nt(nel); }
 
 // Mixed form, FORINT-level call: the host supplies X and V for the cycle, so
 // the FP64 volume that the element kernel advances by its FP32 increment
