@@ -48,15 +48,18 @@ def test_forint_registered_equals_staged(kind, prec):
     assert a[4] == b[4] and a[5] == b[5]
 
 
+@pytest.mark.parametrize("registered", [True, False])
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("kind", ["shell", "hexa"])
-def test_cycle_host_equals_device_cycle(kind, prec):
+def test_cycle_host_equals_device_cycle(kind, prec, registered):
     """The whole-cycle call with host node buffers (rg_cycle_host), fed each
-    cycle with its own previous output from registered buffers, follows the
-    device-resident cycle: bitwise in the FP64 form (the upload writes back
-    the same values), within the mixed form's tolerance there (its element
-    volumes are re-anchored to the given coordinates), over 20 cycles, with
-    the same time step sequence (FP64)."""
+    cycle with its own previous output, follows the device-resident cycle:
+    bitwise in the FP64 form (the upload writes back the same values),
+    within the mixed form's tolerance there (its element volumes are
+    re-anchored to the given coordinates), over 20 cycles, with the same
+    time step sequence (FP64).  Registered buffers are read and written in
+    place by the upload and download kernels; pageable ones go through the
+    staging copies -- both give the same results."""
     from openradioss_gb300.engine import Engine
     m = (M.crash_box(n_side=5, n_len=10, vpert=1.0) if kind == "shell"
          else M.large_block(n=8, seed=2))
@@ -70,17 +73,16 @@ def test_cycle_host_equals_device_cycle(kind, prec):
     v = np.ascontiguousarray(nd["V"].T)
     vr = np.ascontiguousarray(nd["VR"].T) if kind == "shell" else None
     d = np.empty((n, 3))
-    for a in (x, v, vr, d):
-        if a is not None:
-            e2.host_register(a)
+    bufs = [a for a in (x, v, vr, d) if a is not None] if registered else []
+    for a in bufs:
+        e2.host_register(a)
     for _ in range(20):
         e1.cycle(1)
         dt2 = e2.cycle_host(x, v, vr, x_out=x, v_out=v, vr_out=vr, d_out=d)
         if prec == 0:
             assert dt2 == e1.time()["dt2"]
-    for a in (x, v, vr, d):
-        if a is not None:
-            e2.host_unregister(a)
+    for a in bufs:
+        e2.host_unregister(a)
     n1 = e1.nodes()
     if prec == 0:
         assert np.array_equal(x.T, n1["X"]) and np.array_equal(v.T, n1["V"])
