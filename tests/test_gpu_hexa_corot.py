@@ -7,8 +7,7 @@ co-rotational frame, built by repeated normalisations of a distorted
 element, adds round-off that the element kernel's multiply-add contraction
 does not reproduce bit for bit; measured 3.4e-12), trajectories over
 hundreds of cycles within 1e-10; mixed form within 1e-4 of the FP64
-oracle's displacement scale.  The batched kernel refuses JCVT=1 jobs (they
-run alone).
+oracle's displacement scale.  The batched kernel runs JCVT=1 jobs.
 """
 import numpy as np
 import pytest
@@ -72,13 +71,26 @@ def test_mixed_within_bound(oracle_lib, k):
     assert abs(e.energy()["eint"] - o.energy()["eint"]) <= 1e-4 * o.energy()["eint"]
 
 
-def test_batch_refuses_corotational():
+def test_batch_runs_corotational():
+    """The batched kernel takes JCVT=1 jobs: the spinning block and the bar
+    in one batch follow their solo runs within the mixed form's bound."""
     from openradioss_gb300.batch import Batch
     from openradioss_gb300.engine import Engine, RG_PREC_MIXED
 
-    e = Engine(models()[1], precision=RG_PREC_MIXED)
+    ms = models()
+    es = [Engine(m, precision=RG_PREC_MIXED) for m in ms]
     b = Batch()
-    with pytest.raises(Exception):
-        b.add(e, 10)
+    for e in es:
+        b.add(e, 60)
+    b.cycle(60)
+    b.sync()
+    for m, e in zip(ms, es):
+        alone = Engine(m, precision=RG_PREC_MIXED)
+        alone.cycle(60)
+        xa, xb = alone.nodes()["X"], e.nodes()["X"]
+        assert e.time()["ncycle"] == 60
+        assert np.max(np.abs(xb - xa)) <= 1e-4 * max(np.max(np.abs(xa - m.X)), 1e-30)
+        alone.close()
     b.close()
-    e.close()
+    for e in es:
+        e.close()
