@@ -65,9 +65,12 @@ int dalloc(rg_ctx *c, T **p, size_t n) {
 // Node kernels: one thread per node (node_update in rg_node.cuh); LINK:
 // the model has rigid links; the link-free variants are the hot path.
 // RG_NODE_MINB: resident 64-thread blocks per SM the register budget is cut
-// for (1: no cut).
+// for.  14 (72 registers) puts a 120k-node model's 1882 blocks in one wave
+// of 152 SMs (80 registers allowed 12 blocks per SM, two waves): mixed node
+// kernel 15.4 -> 14.3 us on the crash box, FP64 and the 2.1M-node block
+// unchanged or faster; 16 (64 registers, spills) is no better.
 #ifndef RG_NODE_MINB
-#define RG_NODE_MINB 1
+#define RG_NODE_MINB 14
 #endif
 template <bool F64, bool LINK>
 __global__ void __launch_bounds__(NODE_NT, RG_NODE_MINB)
@@ -743,6 +746,8 @@ int rg_ctx_create(int device, rg_ctx **out) {
     return RG_E_CUDA;
   }
   for (auto &e : c->ev) cudaEventCreate(&e);
+  for (auto &s : c->cstream) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  for (auto &e : c->cev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   *out = c;
   return RG_OK;
 }
@@ -759,6 +764,10 @@ int rg_ctx_destroy(rg_ctx *c) {
   if (c->h_time) cudaFreeHost(c->h_time);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (auto &e : c->cev)
+    if (e) cudaEventDestroy(e);
+  for (auto &s : c->cstream)
+    if (s) cudaStreamDestroy(s);
   cudaStreamDestroy(c->stream);
   delete c;
   return RG_OK;
@@ -1321,6 +1330,35 @@ namespace {
 // Device address of a host buffer the kernels may access in place: memory
 // registered with rg_host_register (or device / managed memory); null for
 // ordinary pageable memory, which is staged instead.
+// Device -> host copies of up to four staged arrays, each on its own
+// stream (the context's stream and three side streams) so that they run on
+// separate copy engines, all ordered after the work queued so far on the
+// context's stream, which then waits for all of them.
+#ifndef RG_COPY_FANOUT
+#define RG_COPY_FANOUT 1
+#endif
+int copy_out(rg_ctx *c, double *const dst[4], const double *const src[4],
+             const size_t bytes[4]) {
+  const bool fan = RG_COPY_FANOUT && c->cstream[0] && c->cev[0];
+  if (fan) RG_CUDA(c, cudaEventRecord(c->cev[0], c->stream));
+  int side = 0;
+  for (int k = 0; k < 4; k++) {
+    if (!dst[k]) continue;
+    cudaStream_t s = c->stream;
+    if (fan && side < 3 && k > 0) {
+      s = c->cstream[side];
+      RG_CUDA(c, cudaStreamWaitEvent(s, c->cev[0], 0));
+    }
+    RG_CUDA(c, cudaMemcpyAsync(dst[k], src[k], bytes[k], cudaMemcpyDeviceToHost, s));
+    if (s != c->stream) {
+      RG_CUDA(c, cudaEventRecord(c->cev[1 + side], s));
+      RG_CUDA(c, cudaStreamWaitEvent(c->stream, c->cev[1 + side], 0));
+      side++;
+    }
+  }
+  return RG_OK;
+}
+
 const double *device_view(const void *p) {
   cudaPointerAttributes a;
   if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -1375,15 +1413,13 @@ int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr
   double *of = st, *os = st + n3, *ofr = st + n3 + n, *osr = st + 2 * n3 + n;
   enqueue_assemble(c, f ? of : nullptr, stifn ? os : nullptr, fr ? ofr : nullptr,
                    stifr ? osr : nullptr);
-  if (f)
-    RG_CUDA(c, cudaMemcpyAsync(f, of, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  if (stifn)
-    RG_CUDA(c, cudaMemcpyAsync(stifn, os, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  if (fr)
-    RG_CUDA(c, cudaMemcpyAsync(fr, ofr, n3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  if (stifr)
-    RG_CUDA(c, cudaMemcpyAsync(stifr, osr, n * sizeof(double), cudaMemcpyDeviceToHost,
-                               c->stream));
+  {
+    double *dst[4] = {f, stifn, fr, stifr};
+    const double *src[4] = {of, os, ofr, osr};
+    const size_t bytes[4] = {n3 * sizeof(double), n * sizeof(double), n3 * sizeof(double),
+                             n * sizeof(double)};
+    if (int r = copy_out(c, dst, src, bytes)) return r;
+  }
   // the time-step record comes back through a pinned host copy
   RG_CUDA(c, cudaMemcpyAsync(c->h_time, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost,
                              c->stream));
@@ -1443,6 +1479,9 @@ int rg_cycle_host(rg_ctx *c, const double *x, const double *v, const double *vr,
   // link a copy engine writes host memory faster than kernel stores (one
   // kernel writing all four registered arrays in place measured 0.534 vs
   // 0.443 ms per crash-box cycle)
+  double *dst[4] = {nullptr, nullptr, nullptr, nullptr};
+  const double *src[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t bytes[4] = {0, 0, 0, 0};
   for (int k = 0; k < 4; k++) {
     if (!items[k].dst) continue;
     double *sk = st + k * n3;  // 12 * numnod doubles of staging: one slice per array
@@ -1452,9 +1491,11 @@ int rg_cycle_host(rg_ctx *c, const double *x, const double *v, const double *vr,
       unpack_disp_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, c->nv.X4, c->nv.D4, sk);
     else
       unpack3_kernel<<<nb, NODE_NT, 0, c->stream>>>(n, items[k].src, sk);
-    RG_CUDA(c, cudaMemcpyAsync(items[k].dst, sk, n3 * sizeof(double), cudaMemcpyDeviceToHost,
-                               c->stream));
+    dst[k] = items[k].dst;
+    src[k] = sk;
+    bytes[k] = n3 * sizeof(double);
   }
+  if (int r = copy_out(c, dst, src, bytes)) return r;
   RG_CUDA(c, cudaMemcpyAsync(c->h_time, c->d_time, sizeof(Time), cudaMemcpyDeviceToHost,
                              c->stream));
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
