@@ -626,6 +626,28 @@ def run_sweep(args, njobs=SWEEP_JOBS, cycles=SWEEP_CYCLES_PER_JOB, device=0):
         for e in es:
             e.close()
 
+    # the same jobs as concurrent single-model graphs, each on its own
+    # stream (the serving loop's streams executor), launched in interleaved
+    # chunks of 100 cycles; wall time from the first launch to the last
+    # job's completion
+    conc = {}
+    for prec in (0, 1):
+        es = [Engine(m, device=device, precision=prec) for m in models]
+        for e in es:
+            e.sync()
+        t0 = time.perf_counter()
+        for _ in range(cycles // 100):
+            for e in es:
+                e.cycle(100, sync=False)
+        for e in es:
+            e.cycle(cycles % 100, sync=False)
+        for e in es:
+            e.sync()
+        conc[prec] = (time.perf_counter() - t0) * 1e3
+        assert all(e.time()["ncycle"] == cycles and e.status() == 0 for e in es)
+        for e in es:
+            e.close()
+
     def jobs_h(ms):
         return njobs * 3600.0 / (ms * 1e-3)
 
@@ -658,6 +680,10 @@ def run_sweep(args, njobs=SWEEP_JOBS, cycles=SWEEP_CYCLES_PER_JOB, device=0):
                             "element_updates_s": ne * cycles / (seq[0] * 1e-3)},
         "sequential_mixed": {"jobs_h": jobs_h(seq[1]),
                              "element_updates_s": ne * cycles / (seq[1] * 1e-3)},
+        "concurrent_streams_fp64": {"jobs_h": jobs_h(conc[0]), "gain_vs_sequential": seq[0] / conc[0]},
+        "concurrent_streams_mixed": {"jobs_h": jobs_h(conc[1]), "gain_vs_sequential": seq[1] / conc[1],
+                                     "note": "each job its own graph and stream, launched in "
+                                             "interleaved chunks of 100 cycles; wall time"},
         "batching_gain_fp64": seq[0] / bat[0]["ms"],
         "batching_gain_mixed": seq[1] / bat[1]["ms"],
         "speedup_vs_sequential_plain": seq[0] / bat[1]["ms"],

@@ -746,8 +746,6 @@ int rg_ctx_create(int device, rg_ctx **out) {
     return RG_E_CUDA;
   }
   for (auto &e : c->ev) cudaEventCreate(&e);
-  for (auto &s : c->cstream) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  for (auto &e : c->cev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   *out = c;
   return RG_OK;
 }
@@ -764,10 +762,6 @@ int rg_ctx_destroy(rg_ctx *c) {
   if (c->h_time) cudaFreeHost(c->h_time);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
-  for (auto &e : c->cev)
-    if (e) cudaEventDestroy(e);
-  for (auto &s : c->cstream)
-    if (s) cudaStreamDestroy(s);
   cudaStreamDestroy(c->stream);
   delete c;
   return RG_OK;
@@ -1330,32 +1324,14 @@ namespace {
 // Device address of a host buffer the kernels may access in place: memory
 // registered with rg_host_register (or device / managed memory); null for
 // ordinary pageable memory, which is staged instead.
-// Device -> host copies of up to four staged arrays, each on its own
-// stream (the context's stream and three side streams) so that they run on
-// separate copy engines, all ordered after the work queued so far on the
-// context's stream, which then waits for all of them.
-#ifndef RG_COPY_FANOUT
-#define RG_COPY_FANOUT 1
-#endif
+// Device -> host copies of up to four staged arrays on the context's stream
+// (spreading them over side streams, one copy engine each, measured no
+// faster: the host link, not the engines, sets their pace).
 int copy_out(rg_ctx *c, double *const dst[4], const double *const src[4],
              const size_t bytes[4]) {
-  const bool fan = RG_COPY_FANOUT && c->cstream[0] && c->cev[0];
-  if (fan) RG_CUDA(c, cudaEventRecord(c->cev[0], c->stream));
-  int side = 0;
-  for (int k = 0; k < 4; k++) {
-    if (!dst[k]) continue;
-    cudaStream_t s = c->stream;
-    if (fan && side < 3 && k > 0) {
-      s = c->cstream[side];
-      RG_CUDA(c, cudaStreamWaitEvent(s, c->cev[0], 0));
-    }
-    RG_CUDA(c, cudaMemcpyAsync(dst[k], src[k], bytes[k], cudaMemcpyDeviceToHost, s));
-    if (s != c->stream) {
-      RG_CUDA(c, cudaEventRecord(c->cev[1 + side], s));
-      RG_CUDA(c, cudaStreamWaitEvent(c->stream, c->cev[1 + side], 0));
-      side++;
-    }
-  }
+  for (int k = 0; k < 4; k++)
+    if (dst[k])
+      RG_CUDA(c, cudaMemcpyAsync(dst[k], src[k], bytes[k], cudaMemcpyDeviceToHost, c->stream));
   return RG_OK;
 }
 

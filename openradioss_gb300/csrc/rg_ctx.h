@@ -110,10 +110,6 @@ struct rg_ctx {
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
   cudaEvent_t ev[8] = {};
-  // side streams and events for the host-buffer calls' output copies (each
-  // output array on its own copy engine)
-  cudaStream_t cstream[3] = {};
-  cudaEvent_t cev[4] = {};
   void *d_flush = nullptr;     // L2 flush buffer of rg_time_cycles_cold
   Time *h_time = nullptr;      // pinned host copy of the time-step record
   double entot0 = 0.0, mass0 = 0.0;  // cycle-0 totals of the energy balance
