@@ -976,6 +976,7 @@ def main():
             line["batched_sweep"] = {k: sw[k] for k in (
                 "value", "unit", "batched_mixed", "batched_fp64", "sequential_fp64",
                 "sequential_mixed", "batching_gain_fp64", "batching_gain_mixed",
+                "concurrent_streams_fp64", "concurrent_streams_mixed",
                 "speedup_vs_sequential_plain", "config", "device_status", "roofline")}
             sv = run_serving(args)
             line["serving"] = {k: sv[k] for k in (
