@@ -163,3 +163,22 @@ def test_batch_corotational_hexa(prec):
     other = run_batch(ms, prec, n, (2, 4, 1, 1))
     for i in range(len(ms)):
         assert bitwise(other[i], got[i]), i
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_run_concurrent_equals_alone_bitwise(prec):
+    """batch.run_concurrent advances every job on its own stream with its own
+    graph: each ends bit for bit where the job run alone ends, with exactly
+    its cycle count."""
+    from openradioss_gb300.batch import run_concurrent
+    from openradioss_gb300.engine import Engine
+    ms = models_mix()
+    es = [Engine(m, precision=prec) for m in ms]
+    run_concurrent(es, 130, chunk=40)
+    for m, e in zip(ms, es):
+        alone = Engine(m, precision=prec)
+        alone.cycle(130)
+        assert bitwise(state(e), state(alone))
+        assert e.status() == 0
+        alone.close()
+        e.close()
