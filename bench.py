@@ -750,8 +750,8 @@ def run_serving(args, njobs=SERVE_JOBS, device=0):
     # the batched executor on the same stream: every arrived job admitted
     # (arrival order, HBM budget only), and least work first under an
     # element cap
-    st_all = serve()
-    st_sjf = serve(policy="sjf", max_elements=SERVE_ELEMENTS)
+    st_all = serve(executor="batch")
+    st_sjf = serve(policy="sjf", max_elements=SERVE_ELEMENTS, executor="batch")
     bad = st["bad"] + st_all["bad"] + st_sjf["bad"]
     seq_jobs_h = {p: 3600.0 * njobs / seq[p] for p in seq}
     ne = [m.numels + m.numelc for m, _ in jobs]

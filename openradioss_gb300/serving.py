@@ -1,14 +1,13 @@
 """Serving loop: simulation jobs admitted by HBM budget and advanced together
 (continuous batching) on one GPU.
 
-Requests (a model plus a cycle count) arrive over time.  The loop keeps a
-:class:`~openradioss_gb300.batch.Batch` running; between two batched steps
-of ``step_cycles`` cycles it
+Requests (a model plus a cycle count) arrive over time.  Between two steps
+of ``step_cycles`` cycles the loop
 
 * admits waiting requests, in arrival order, while a job slot is free and
   the job's estimated device bytes fit the remaining HBM budget -- the job's
   model is uploaded to the device (its state then stays there) and it joins
-  the running batch with its own cycle target;
+  the running jobs with its own cycle target;
 * retires the jobs whose cycle count reached their target: their results are
   read back, their device memory is released, and the freed slot and bytes go
   to the next waiting requests;
@@ -21,11 +20,12 @@ of ``step_cycles`` cycles it
 
 While the GPU runs a step, the host prepares the next admissions (upload
 and set-up), so requests that arrive while others are on the GPU overlap
-with them.  Each job's results equal those of the same job run alone within
+with them.  With the streams executor each job's results are bit for bit
+those of the job run alone; with the batch executor they equal them within
 the parity tolerance (the batched kernel runs the same element and node
 functions; the compiler may contract multiply-adds differently in the two
-kernels), and are bitwise the same whatever the batch's launch
-configuration or neighbours -- both of which the tests check.
+kernels) and are bitwise the same whatever the batch's launch configuration
+or neighbours -- all of which the tests check.
 
 With preemption on, a request may carry a priority: when an arrived request
 does not fit (slot or budget) and jobs of lower priority are running, the
@@ -35,13 +35,12 @@ device memory released -- until it fits; a preempted job waits in the queue
 with its snapshot and resumes from it (rg_restore) bit for bit, the batched
 kernel's results not depending on what else is in the batch.
 
-Two executors.  "batch" (the default) advances the running jobs together in
-one batched persistent kernel per cycle -- the gain is largest for many
-small jobs, each of which alone would leave most of the GPU idle.  "streams"
-advances each running job with its own single-model CUDA graph on its own
-stream (rg_cycle, asynchronous): jobs large enough to fill the GPU by
-themselves run at their solo speed, and the kernels of concurrent jobs
-overlap where one leaves SMs idle.  Admission, retirement, failure
+Two executors.  "streams" (the default) advances each running job with its
+own single-model CUDA graph on its own stream (rg_cycle, asynchronous): jobs
+large enough to fill the GPU by themselves run at their solo speed, and the
+kernels of concurrent jobs overlap where one leaves SMs idle.  "batch"
+advances the running jobs together in one batched persistent kernel per
+cycle, a job's results then not depending on what else runs beside it.  Admission, retirement, failure
 isolation and preemption are the same in both.
 
 The latency of a job is its completion time minus its arrival time; the
@@ -123,15 +122,17 @@ class Server:
     def __init__(self, hbm_budget_bytes, max_jobs=64, precision=RG_PREC_MIXED,
                  step_cycles=100, device=0, config=None, keep_results=False,
                  result_fn=None, preempt=False, policy="fifo", max_elements=None,
-                 executor="batch"):
+                 executor="streams"):
         """policy: admission order among arrived requests of equal priority,
         "fifo" (arrival) or "sjf" (least work first: elements x cycles
         left).  max_elements: cap on the elements of the running jobs -- a
         single large model already fills the GPU, and admitting more only
         shares it (every job slower) where waiting would finish the first
         ones sooner; a job is always admitted when nothing runs.
-        executor: "batch" (one batched kernel for all running jobs) or
-        "streams" (each job its own graph and stream)."""
+        executor: "streams" (each job its own graph and stream; the faster
+        on GB300 for every measured workload) or "batch" (one batched
+        kernel for all running jobs: results independent of the batch's
+        composition bit for bit)."""
         self.budget = int(hbm_budget_bytes)
         self.max_jobs = max_jobs
         self.precision = precision

@@ -105,7 +105,8 @@ def test_serving_retires_failed_job_and_others_match_alone():
     jobs = [(0, M.crash_box(n_side=5, n_len=10, seed=21), 100, 0.0),
             (1, bad, 100, 0.0),
             (2, M.hexa_impact_block(1500, seed=23, law="law1"), 75, 0.0)]
-    srv = Server(1 << 34, max_jobs=8, precision=1, step_cycles=25, keep_results=True)
+    srv = Server(1 << 34, max_jobs=8, precision=1, step_cycles=25, keep_results=True,
+                 executor="batch")
     st = srv.run(jobs)
     srv.close()
     assert st["failed"] == 1 and st["completed"] == 2

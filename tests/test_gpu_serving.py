@@ -20,7 +20,8 @@ def test_served_results_equal_alone():
     # budget for about two jobs at a time: admission must wait for retirements
     need = sorted(estimate_device_bytes(m, 1) for _, m, _, _ in jobs)
     budget = need[-1] + need[-2]
-    srv = Server(budget, max_jobs=8, precision=1, step_cycles=25, keep_results=True)
+    srv = Server(budget, max_jobs=8, precision=1, step_cycles=25, keep_results=True,
+                 executor="batch")
     stats = srv.run(jobs)
     srv.close()
     assert stats["jobs"] == 5 and len(srv.done) == 5

@@ -84,7 +84,7 @@ def test_preempted_served_job_equals_uninterrupted():
     res = {}
     for pre in (True, False):
         srv = Server(int(2.5 * need), max_jobs=8, precision=1, step_cycles=25,
-                     keep_results=True, preempt=pre)
+                     keep_results=True, preempt=pre, executor="batch")
         st = srv.run(jobs)
         srv.close()
         assert st["completed"] == 3

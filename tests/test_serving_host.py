@@ -122,7 +122,7 @@ def test_admission_respects_budget(fakes):
     jobs = small_jobs()
     need = [S.estimate_device_bytes(m, 1) for _, m, _, _ in jobs]
     budget = max(need) + min(need)
-    srv = S.Server(budget, max_jobs=8, step_cycles=50)
+    srv = S.Server(budget, max_jobs=8, step_cycles=50, executor="batch")
     st = srv.run(jobs)
     assert st["jobs"] == 6 and len(srv.done) == 6
     assert st["max_used_bytes"] <= budget
@@ -132,7 +132,7 @@ def test_admission_respects_budget(fakes):
 
 def test_slot_limit_and_order(fakes):
     jobs = small_jobs()
-    srv = S.Server(1 << 40, max_jobs=2, step_cycles=50)
+    srv = S.Server(1 << 40, max_jobs=2, step_cycles=50, executor="batch")
     srv.run(jobs)
     assert srv.batch.max_live == 2
     adm = sorted(srv.done, key=lambda r: r.admitted)
@@ -147,7 +147,7 @@ def test_failed_job_is_retired_and_others_finish(fakes):
     for k, m, n, a in jobs:
         m.name = "job%d" % k
     FakeEngine.fail_at = {"job3": (100, 2)}
-    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50)
+    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50, executor="batch")
     st = srv.run(jobs)
     assert st["failed"] == 1 and st["completed"] == 5
     assert [r.key for r in srv.failed] == [3]
@@ -174,7 +174,7 @@ def test_batch_failure_retires_the_running_jobs(fakes):
                 FakeBatch.bstatus = 16
 
     S.Batch = OnceBatch
-    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50)
+    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50, executor="batch")
     st = srv.run(jobs)
     assert sorted(r.key for r in srv.failed) == [0, 1]
     assert all(r.status & 16 for r in srv.failed)
@@ -193,7 +193,8 @@ def test_priority_request_preempts_and_preempted_job_resumes(fakes):
     need = S.estimate_device_bytes(lo1, 1)
     jobs = [(0, lo1, 2000, 0.0, 0), (1, lo2, 1500, 0.0, 0), (2, hi, 200, 0.05, 5)]
     FakeBatch.step_s = 0.005
-    srv = S.Server(2 * need + need // 2, max_jobs=8, step_cycles=50, preempt=True)
+    srv = S.Server(2 * need + need // 2, max_jobs=8, step_cycles=50, preempt=True,
+                   executor="batch")
     st = srv.run(jobs)
     assert st["completed"] == 3 and st["failed"] == 0
     recs = {r.key: r for r in srv.done}
@@ -202,7 +203,8 @@ def test_priority_request_preempts_and_preempted_job_resumes(fakes):
     assert all(r.result["time"]["ncycle"] == jobs[r.key][2] for r in srv.done)
     assert srv.used == 0 and FakeEngine.live == 0
     # without preemption the high-priority job waits for a retirement
-    srv2 = S.Server(2 * need + need // 2, max_jobs=8, step_cycles=50, preempt=False)
+    srv2 = S.Server(2 * need + need // 2, max_jobs=8, step_cycles=50, preempt=False,
+                    executor="batch")
     srv2.run(jobs)
     r2 = {r.key: r for r in srv2.done}
     assert all(r.preemptions == 0 for r in srv2.done)
@@ -217,7 +219,8 @@ def test_sjf_admits_least_work_first_under_an_element_cap(fakes):
     small = [M.crash_box(n_side=3, n_len=4, seed=k) for k in range(2, 5)]
     jobs = [(0, big, 3000, 0.0)] + [(k + 1, m, 200, 0.0) for k, m in enumerate(small)]
     cap = big.numelc  # room for the big job alone, or for the small ones
-    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50, policy="sjf", max_elements=cap)
+    srv = S.Server(1 << 40, max_jobs=8, step_cycles=50, policy="sjf", max_elements=cap,
+                   executor="batch")
     seen = []
     orig = srv._admit
 
@@ -237,7 +240,7 @@ def test_sjf_admits_least_work_first_under_an_element_cap(fakes):
 
 def test_oversize_job_is_refused(fakes):
     jobs = small_jobs()[:1]
-    srv = S.Server(1000, max_jobs=2)
+    srv = S.Server(1000, max_jobs=2, executor="batch")
     with pytest.raises(RuntimeError):
         srv.run(jobs)
 
