@@ -230,6 +230,33 @@ int rg_energy(rg_ctx *ctx, double *eint, double *ekin, double *ekinr,
  * rg_finalize, 8 total nodal mass, 9 mass error (M - M0) / M0, 10-12
  * momentum x, y, z.  The node sums are fixed-order device reductions. */
 int rg_energy_balance(rg_ctx *ctx, double *out, int n);
+
+/* Per-part element sums, the PARTSAV accumulation of SBILAN (engine/source/
+ * elements/solid/solide/sbilan.F:118-160) and CBILAN (elements/shell/coque/
+ * cbilan.F:160-190) plus CHVIS3's hourglass energy (chvis3.F:355-395): the
+ * default /TH/PART variables (output/th/hist2.F:377-395) of each part,
+ * out[p * RG_PART_NQ + q] with q = 0 IE, 1 KE (element-based: the element
+ * mass times the mean square of its nodes' velocities), 2-4 momentum,
+ * 5 mass of the elements not switched off, 6 accumulated hourglass energy.
+ *
+ * rg_set_parts (after rg_finalize) gives every element's 0-based part
+ * number, in element order (the groups in the order added); without it
+ * each element group is a part (hexa groups first, then shell groups).
+ * rg_part_count gives the context's part count.  rg_part_sums_due asks
+ * the next cycle -- rg_cycle (its first cycle), rg_cycle_host or
+ * rg_forint_step -- to take the sums where the engine does when it prints
+ * (IPRI, resol.F): after the element pass, before the nodal update, from
+ * X(n), V(n-1/2) and the element state of that cycle.  rg_part_sums reads
+ * them (RG_E_STATE before any such cycle; the batched kernel does not take
+ * them).  Fixed-order device reductions: the sums do not depend on the
+ * launch layout. */
+#define RG_PART_NQ 7
+int rg_set_parts(rg_ctx *ctx, int npart, const int *hexa_part,
+                 const int *shell_part);
+int rg_part_count(rg_ctx *ctx, int *npart);
+int rg_part_sums_due(rg_ctx *ctx);
+int rg_part_sums(rg_ctx *ctx, double *out, int npart);
+
 /* Device status word (RG_ST_* bits), cleared by the read. */
 int rg_status(rg_ctx *ctx);
 

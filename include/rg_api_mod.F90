@@ -19,6 +19,7 @@ module rg_api_mod
   integer(c_int), parameter :: RG_ST_NEGVOL = 1, RG_ST_NAN = 2, RG_ST_SLOT = 4, &
        RG_ST_DTMIN = 8, RG_ST_BARRIER = 16, RG_ST_NODSTIF = 32
   integer(c_int), parameter :: RG_PREC_FP64 = 0, RG_PREC_MIXED = 1
+  integer(c_int), parameter :: RG_PART_NQ = 7
 
   interface
     ! ---- context ---------------------------------------------------------
@@ -193,6 +194,29 @@ module rg_api_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: out(*)
       integer(c_int), value :: n
+    end function
+    ! ---- per-part sums (SBILAN / CBILAN PARTSAV, /TH/PART) ------------------
+    integer(c_int) function rg_set_parts(ctx, npart, hexa_part, shell_part) &
+        bind(c, name='rg_set_parts')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: npart
+      integer(c_int), intent(in) :: hexa_part(*), shell_part(*)
+    end function
+    integer(c_int) function rg_part_count(ctx, npart) bind(c, name='rg_part_count')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), intent(out) :: npart
+    end function
+    integer(c_int) function rg_part_sums_due(ctx) bind(c, name='rg_part_sums_due')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function rg_part_sums(ctx, out, npart) bind(c, name='rg_part_sums')
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: out(*)
+      integer(c_int), value :: npart
     end function
     integer(c_int) function rg_status(ctx) bind(c, name='rg_status')
       import :: c_int, c_ptr

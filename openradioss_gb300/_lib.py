@@ -47,6 +47,10 @@ SIGNATURES = [
     ("rg_energy", _ip, [_vp, _vp, _vp, _vp, _vp]),
     ("rg_energy_balance", _ip, [_vp, _vp, _ip]),
     ("rg_set_dtmin", _ip, [_vp, _ip, _ip, _dp]),
+    ("rg_set_parts", _ip, [_vp, _ip, _vp, _vp]),
+    ("rg_part_count", _ip, [_vp, _vp]),
+    ("rg_part_sums_due", _ip, [_vp]),
+    ("rg_part_sums", _ip, [_vp, _vp, _ip]),
     ("rg_status", _ip, [_vp]),
     ("rg_snapshot_size", _ip, [_vp, _vp]),
     ("rg_snapshot", _ip, [_vp, _vp, C.c_ulonglong]),

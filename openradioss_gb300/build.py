@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librg.so")
-SOURCES = ["rg_api.cu", "rg_hexa.cu", "rg_shell.cu", "rg_batch.cu", "rg_noalloc.cu"]
+SOURCES = ["rg_api.cu", "rg_hexa.cu", "rg_shell.cu", "rg_batch.cu", "rg_noalloc.cu", "rg_parts.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]

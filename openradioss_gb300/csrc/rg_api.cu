@@ -719,10 +719,20 @@ int enqueue_assemble(rg_ctx *c, double *f, double *stifn, double *fr, double *st
   return RG_OK;
 }
 
-int enqueue_cycle(rg_ctx *c) {
+int enqueue_cycle(rg_ctx *c, bool parts = false) {
   enqueue_elements(c, 1);
+  if (parts) parts_enqueue(c);
   enqueue_nodes(c);
   return RG_OK;
+}
+
+// The graph of the next cycle: the one that also takes the per-part sums
+// when they are due (rg_part_sums_due), else the plain one.
+cudaGraphExec_t next_cycle_graph(rg_ctx *c) {
+  if (!c->parts_due) return c->gexec;
+  c->parts_due = false;
+  c->parts_valid = true;
+  return c->gexec_parts;
 }
 
 }  // namespace
@@ -756,6 +766,9 @@ int rg_ctx_destroy(rg_ctx *c) {
   cudaStreamSynchronize(c->stream);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->graph) cudaGraphDestroy(c->graph);
+  if (c->gexec_parts) cudaGraphExecDestroy(c->gexec_parts);
+  if (c->graph_parts) cudaGraphDestroy(c->graph_parts);
+  parts_free(c);
   shell_free(c->shells);
   for (void *p : c->allocs) cudaFree(p);
   if (c->d_flush) cudaFree(c->d_flush);
@@ -1254,7 +1267,7 @@ int rg_cycle(rg_ctx *c, int ncycle) {
   if (ncycle < 0) return fail(c, RG_E_ARG, "negative cycle count");
   RG_CUDA(c, cudaSetDevice(c->device));
   if (!c->timing) {
-    for (int i = 0; i < ncycle; i++) RG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+    for (int i = 0; i < ncycle; i++) RG_CUDA(c, cudaGraphLaunch(next_cycle_graph(c), c->stream));
     return RG_OK;
   }
   // timed path: the same launches, bracketed by events per kernel class
@@ -1287,6 +1300,11 @@ int rg_cycle(rg_ctx *c, int ncycle) {
     // nodal dt kernel, launched with the node phase)
     if (c->nparts == 0 && !c->nodadt)
       dt_kernel<<<1, DT_NT, 0, c->stream>>>(dp, 0, c->d_ngl_all, c->d_time, c->d_status, 1);
+    if (c->parts_due) {
+      parts_enqueue(c);
+      c->parts_due = false;
+      c->parts_valid = true;
+    }
     cudaEventRecord(c->ev[3], c->stream);
     enqueue_nodes(c);
     cudaEventRecord(c->ev[4], c->stream);
@@ -1383,6 +1401,11 @@ int rg_forint_step(rg_ctx *c, const double *x, const double *v, const double *vr
   if (c->prec == RG_PREC_MIXED && c->numels > 0)
     launch_hexa_prev_volume(c->h32, c->nv, c->d_time, c->stream);
   enqueue_elements(c, 0);
+  if (c->parts_due) {
+    parts_enqueue(c);
+    c->parts_due = false;
+    c->parts_valid = true;
+  }
   // outputs: assembled into the staging buffer, returned by DMA copies (on
   // the host link a copy engine writes host memory about twice as fast as
   // kernel stores do)
@@ -1445,7 +1468,7 @@ int rg_cycle_host(rg_ctx *c, const double *x, const double *v, const double *vr,
     if (c->prec == RG_PREC_MIXED && c->numels > 0)
       launch_hexa_prev_volume(c->h32, c->nv, c->d_time, c->stream);
   }
-  RG_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+  RG_CUDA(c, cudaGraphLaunch(next_cycle_graph(c), c->stream));
   struct {
     double *dst;
     dbl4 *src;
@@ -1654,6 +1677,26 @@ int rg_energy_balance(rg_ctx *c, double *out, int n) {
   return RG_OK;
 }
 
+int rg_part_sums_due(rg_ctx *c) {
+  if (!c) return RG_E_ARG;
+  if (!c->finalized) return fail(c, RG_E_STATE, "rg_finalize first");
+  RG_CUDA(c, cudaSetDevice(c->device));
+  if (int r = parts_prepare(c)) return r;
+  if (!c->gexec_parts) {
+    // the cycle graph with the part sums between the element pass and the
+    // nodal update, captured once
+    RG_CUDA(c, cudaStreamSynchronize(c->stream));
+    RG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_cycle(c, true);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &c->graph_parts);
+    if (ce != cudaSuccess)
+      return fail(c, RG_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    RG_CUDA(c, cudaGraphInstantiate(&c->gexec_parts, c->graph_parts, 0));
+  }
+  c->parts_due = true;
+  return RG_OK;
+}
+
 int rg_status(rg_ctx *c) {
   if (!c) return RG_E_ARG;
   if (!c->finalized) return 0;
@@ -1754,6 +1797,7 @@ int rg_restore(rg_ctx *c, const void *buf, unsigned long long bytes) {
     q += c->alloc_bytes[i];
   }
   RG_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->parts_valid = false;  // the part sums were of a cycle before the restore
   return RG_OK;
 }
 

@@ -27,6 +27,20 @@ struct LinkHost {
   int ic = 0, icr = 0;     // direction bits 4 = x, 2 = y, 1 = z
 };
 
+// Device tables of the per-part sums (rg_parts.cu): each part's elements in
+// element order, cut into chunks (start in perm, count, partial slot, part);
+// the density per entry; the slot range of each part.  Outside the
+// snapshot: derived from the model, not state.
+struct PartTables {
+  int npart = 0, nh_chunks = 0, ns_chunks = 0, nslots = 0;
+  int *hperm = nullptr, *sperm = nullptr;
+  double *hcoef = nullptr, *scoef = nullptr;
+  int4 *hchunk = nullptr, *schunk = nullptr;
+  int *poff = nullptr;        // [npart + 1]
+  double *partial = nullptr;  // [nslots][RG_PART_NQ]
+  double *out = nullptr;      // [npart][RG_PART_NQ]
+};
+
 }  // namespace rg
 
 struct rg_ctx {
@@ -114,5 +128,21 @@ struct rg_ctx {
   Time *h_time = nullptr;      // pinned host copy of the time-step record
   double entot0 = 0.0, mass0 = 0.0;  // cycle-0 totals of the energy balance
   size_t flush_bytes = 0;
+  // per-part sums: element -> part maps (empty: one part per element
+  // group), their tables, the request for the next cycle and the cycle
+  // graph that takes them between the element pass and the nodal update
+  int npart = 0;
+  std::vector<int> part_hexa, part_shell;
+  rg::PartTables pt{};
+  bool parts_ready = false, parts_due = false, parts_valid = false;
+  cudaGraphExec_t gexec_parts = nullptr;
+  cudaGraph_t graph_parts = nullptr;
 };
+
+namespace rg {
+// rg_parts.cu
+int parts_prepare(rg_ctx *c);  // tables and buffers (after rg_finalize)
+void parts_enqueue(rg_ctx *c); // the sums of the element pass just enqueued
+void parts_free(rg_ctx *c);
+}  // namespace rg
 

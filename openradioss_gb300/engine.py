@@ -230,6 +230,36 @@ class Engine:
         self._chk(self.L.rg_energy_balance(self.h, _p(out), len(out)), "rg_energy_balance")
         return dict(zip(self.BALANCE_KEYS, out.tolist()))
 
+    PART_KEYS = ("IE", "KE", "XMOM", "YMOM", "ZMOM", "MASS", "HE")
+
+    def set_parts(self, npart, hexa_part=None, shell_part=None):
+        """Every element's 0-based part number, in element order (groups in
+        the order added); without it each element group is a part."""
+        m = self.model
+        hp = np.ascontiguousarray(hexa_part if hexa_part is not None else np.zeros(0), np.int32)
+        sp = np.ascontiguousarray(shell_part if shell_part is not None else np.zeros(0), np.int32)
+        if hp.size != m.numels or sp.size != m.numelc:
+            raise ValueError("one part number per hexa and per shell")
+        self._chk(self.L.rg_set_parts(self.h, int(npart), _p(hp), _p(sp)), "rg_set_parts")
+
+    def part_count(self):
+        n = C.c_int()
+        self._chk(self.L.rg_part_count(self.h, C.byref(n)), "rg_part_count")
+        return n.value
+
+    def part_sums_due(self):
+        """The next cycle takes the per-part sums (between its element pass
+        and its nodal update)."""
+        self._chk(self.L.rg_part_sums_due(self.h), "rg_part_sums_due")
+
+    def part_sums(self):
+        """Per-part sums of the last cycle that took them: (npart, 7) array,
+        columns PART_KEYS."""
+        n = self.part_count()
+        out = np.zeros((n, len(self.PART_KEYS)))
+        self._chk(self.L.rg_part_sums(self.h, _p(out), n), "rg_part_sums")
+        return out
+
     def skyline(self):
         m = self.model
         adsky = np.zeros(m.numnod + 1, np.int32)

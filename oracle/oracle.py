@@ -91,6 +91,8 @@ def _declare(L):
         L.or_set_forces.argtypes = [vp] + [C.c_void_p] * 4 + [C.c_double, C.c_int]
         L.or_cload_add.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                    _dp, _dp]
+        L.or_set_parts.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p]
+        L.or_get_part_sums.argtypes = [vp, C.c_void_p, C.c_int]
     return L
 
 
@@ -254,6 +256,22 @@ class OracleModel:
 
     def set_record(self, on=True):
         self.L.or_set_record(self.h, 1 if on else 0)
+
+    def set_parts(self, npart, hexa_part=None, shell_part=None):
+        """Element -> part maps of the per-part sums (0-based, element
+        order); without them each element group is a part."""
+        hp = np.ascontiguousarray(hexa_part if hexa_part is not None else np.zeros(0), np.int32)
+        sp = np.ascontiguousarray(shell_part if shell_part is not None else np.zeros(0), np.int32)
+        if self.L.or_set_parts(self.h, int(npart), _ptr(hp), _ptr(sp)) != 0:
+            raise ValueError("or_set_parts: a part in [0, npart) for every element")
+
+    def part_sums(self):
+        """Per-part sums (SBILAN / CBILAN) of the last recorded cycle:
+        (npart, 7) array, columns IE KE XMOM YMOM ZMOM MASS HE."""
+        n = self.L.or_get_part_sums(self.h, None, 0)
+        out = np.zeros((n, 7))
+        self.L.or_get_part_sums(self.h, _ptr(out), n)
+        return out
 
     def record(self):
         """Listing quantities of the last cycle (ECRIT's point of the

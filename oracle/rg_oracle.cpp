@@ -148,6 +148,11 @@ struct Model {
   // kinematic conditions, before VELOCITY)
   bool record = false;
   double out[11] = {};
+  // per-part sums of the last recorded cycle (SBILAN / CBILAN): element ->
+  // part maps (empty: one part per element group, hexa groups first)
+  int npart = 0;
+  std::vector<int> part_hexa, part_shell;
+  std::vector<double> psum;  // [npart][7]
 };
 
 // ----------------------------------------------------------------------------
@@ -873,6 +878,9 @@ int get_state(const Shells *, int which, double *out);
 int set_frame(Shells *, int ishfram);
 void set_nodadt(Shells *, int on);
 void set_dtmin(Shells *, int idtmin, double dtmin);
+void part_sums(const Shells *, const double *X, const double *V, const int *part, int part0,
+               double *out);
+int group_count(const Shells *);
 }  // namespace rg_oracle_shell
 
 struct OrModelWrap {
@@ -885,6 +893,58 @@ struct OrModelWrap {
   };
   std::vector<Wall> walls;
 };
+
+// SBILAN (elements/solid/solide/sbilan.F:118-160) + the hexas' accumulated
+// hourglass energy: per element EI = EINT * VOL, XMAS = RHO * VNEW (= RHO0 *
+// VOL0: SRHO3 keeps the element mass), the nodes' mean velocity <v> and mean
+// square <v^2>, EK = XMAS <v^2> / 2, momentum XMAS <v>, mass if OFF >= 1;
+// then the shells (CBILAN).  Sequential over elements into M.psum.
+void part_sums(Model &M, rg_oracle_shell::Shells *sh) {
+  const int nhg = (int)M.hg.size();
+  const int npart = M.part_hexa.empty() && M.part_shell.empty()
+                        ? nhg + rg_oracle_shell::group_count(sh)
+                        : M.npart;
+  M.psum.assign(7 * (size_t)npart, 0.0);
+  for (int g = 0; g < nhg; g++) {
+    const HexaGroup &G = M.hg[g];
+    for (int i = 0; i < G.nel; i++) {
+      const int e = G.nft + i;
+      double vx[8], vy[8], vz[8];
+      for (int k = 0; k < 8; k++) {
+        const int n = M.ixs[11 * (size_t)e + 1 + k] - 1;
+        vx[k] = M.V[3 * (size_t)n];
+        vy[k] = M.V[3 * (size_t)n + 1];
+        vz[k] = M.V[3 * (size_t)n + 2];
+      }
+      double sx = vx[0], sy = vy[0], sz = vz[0];
+      for (int k = 1; k < 8; k++) {
+        sx = sx + vx[k];
+        sy = sy + vy[k];
+        sz = sz + vz[k];
+      }
+      double va2 = vx[0] * vx[0];
+      for (int k = 1; k < 8; k++) va2 = va2 + vx[k] * vx[k];
+      for (int k = 0; k < 8; k++) va2 = va2 + vy[k] * vy[k];
+      for (int k = 0; k < 8; k++) va2 = va2 + vz[k] * vz[k];
+      sx = sx * RG_ONE_OVER_8;
+      sy = sy * RG_ONE_OVER_8;
+      sz = sz * RG_ONE_OVER_8;
+      va2 = va2 * RG_ONE_OVER_8;
+      const double xmas = G.rho0 * M.vol[e];
+      double *o = &M.psum[7 * (size_t)(M.part_hexa.empty() ? g : M.part_hexa[e])];
+      o[0] += M.eint[e] * M.vol[e];
+      o[1] += xmas * va2 * RG_HALF;
+      o[2] += xmas * sx;
+      o[3] += xmas * sy;
+      o[4] += xmas * sz;
+      if (M.offg[e] >= RG_ONE) o[5] += xmas;
+      o[6] += M.ehou[e];
+    }
+  }
+  rg_oracle_shell::part_sums(sh, M.X.data(), M.V.data(),
+                             M.part_shell.empty() ? nullptr : M.part_shell.data(), nhg,
+                             M.psum.data());
+}
 
 extern "C" {
 
@@ -1519,6 +1579,9 @@ int or_cycle(void *m, int ncycle) {
         neltst = el;
       }
     }
+    // part sums of the element pass (SBILAN / CBILAN, taken in the cycles
+    // that print): X(n), V(n-1/2), the cycle's element state
+    if (M.record && !M.ext) part_sums(M, w->sh);
     // ASSPAR4 (asspar4.F:165-180): fixed-order slot sums
     RG_OPCOUNT_PHASE(3);
 #pragma omp parallel for schedule(static) num_threads(M.nthreads)
@@ -2117,6 +2180,33 @@ int or_get_record(void *m, double *out, int *neltst) {
   if (out) std::copy(M.out, M.out + 11, out);
   if (neltst) *neltst = M.neltst;
   return 0;
+}
+
+// Element -> part maps of the per-part sums (0-based parts < npart; null
+// maps: one part per element group, hexa groups first).
+int or_set_parts(void *m, int npart, const int *hexa_part, const int *shell_part) {
+  auto *w = (OrModelWrap *)m;
+  Model &M = w->m;
+  const int nc = rg_oracle_shell::numelc(w->sh);
+  if (npart <= 0) return -1;
+  for (int e = 0; e < M.numels; e++)
+    if (!hexa_part || hexa_part[e] < 0 || hexa_part[e] >= npart) return -1;
+  for (int e = 0; e < nc; e++)
+    if (!shell_part || shell_part[e] < 0 || shell_part[e] >= npart) return -1;
+  M.npart = npart;
+  M.part_hexa.assign(hexa_part, hexa_part + M.numels);
+  M.part_shell.assign(shell_part, shell_part + nc);
+  M.psum.clear();
+  return 0;
+}
+
+// Per-part sums of the last recorded cycle: out[p * 7 + q] (IE, KE, XMOM,
+// YMOM, ZMOM, MASS, HE); returns the part count (0 before any such cycle).
+int or_get_part_sums(void *m, double *out, int npart) {
+  const Model &M = ((OrModelWrap *)m)->m;
+  const int n = (int)(M.psum.size() / 7);
+  if (out) std::copy(M.psum.begin(), M.psum.begin() + 7 * (size_t)std::min(n, npart), out);
+  return n;
 }
 
 int or_get_shell_state(void *m, int which, double *out) {

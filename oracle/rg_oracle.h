@@ -152,6 +152,11 @@ int or_get_record(void *m, double *out, int *neltst);
 /* Shell state: which = 0 FOR (5 x nc), 1 MOM (3 x nc), 2 THK, 3 EINT
  * (2 x nc), 4 OFF, 5 SIG (5 x npt x nc), 6 PLA (npt x nc), 7 HOUR (5 x nc). */
 int or_get_shell_state(void *m, int which, double *out);
+/* Per-part sums (SBILAN / CBILAN) of the recorded cycles: element -> part
+ * maps (0-based) and the sums of the last recorded cycle, out[p * 7 + q]
+ * = IE, KE, XMOM, YMOM, ZMOM, MASS, HE; returns the part count. */
+int or_set_parts(void *m, int npart, const int *hexa_part, const int *shell_part);
+int or_get_part_sums(void *m, double *out, int npart);
 
 #ifdef __cplusplus
 }

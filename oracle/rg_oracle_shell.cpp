@@ -890,6 +890,51 @@ void step(Shells *S, const double *X, const double *V, const double *VR,
   if (S->stop.exchange(0)) error |= 8;
 }
 
+// CBILAN (elements/shell/coque/cbilan.F:160-190) + CHVIS3's PARTSAV(8)
+// (chvis3.F:355-395): per-part sums of the element pass just done, from the
+// cycle's X(n) and V(n-1/2): IE = EINT(1) + EINT(2), KE = XMAS sum v^2 / 8,
+// momentum XMAS / 4 sum v, mass of the elements not switched off, the
+// accumulated hourglass energy.  XMAS = RHO * AREA * THK with the area of
+// the cycle's coordinates (half the norm of the diagonals' cross product)
+// and the thickness after the cycle's update.  part: the shell's part, or
+// null for part0 + its group.  Adds into out[part][7].
+void part_sums(const Shells *S, const double *X, const double *V, const int *part, int part0,
+               double *out) {
+  for (size_t g = 0; g < S->groups.size(); g++) {
+    const Group &G = S->groups[g];
+    for (int i = 0; i < G.nel; i++) {
+      const int e = G.nft + i;
+      const int *ix = &S->ixc[7 * (size_t)e];
+      const double *x1 = &X[3 * (size_t)(ix[1] - 1)], *x2 = &X[3 * (size_t)(ix[2] - 1)];
+      const double *x3 = &X[3 * (size_t)(ix[3] - 1)], *x4 = &X[3 * (size_t)(ix[4] - 1)];
+      const double *v1 = &V[3 * (size_t)(ix[1] - 1)], *v2 = &V[3 * (size_t)(ix[2] - 1)];
+      const double *v3 = &V[3 * (size_t)(ix[3] - 1)], *v4 = &V[3 * (size_t)(ix[4] - 1)];
+      const double ax = x3[0] - x1[0], ay = x3[1] - x1[1], az = x3[2] - x1[2];
+      const double bx = x4[0] - x2[0], by = x4[1] - x2[1], bz = x4[2] - x2[2];
+      const double cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+      const double area = RG_HALF * std::sqrt(cx * cx + cy * cy + cz * cz);
+      const double xmas = G.rho * (area * S->thk[e]);
+      const double vxa = v1[0] + v2[0] + v3[0] + v4[0];
+      const double vya = v1[1] + v2[1] + v3[1] + v4[1];
+      const double vza = v1[2] + v2[2] + v3[2] + v4[2];
+      const double va2 = v1[0] * v1[0] + v2[0] * v2[0] + v3[0] * v3[0] + v4[0] * v4[0] +
+                         v1[1] * v1[1] + v2[1] * v2[1] + v3[1] * v3[1] + v4[1] * v4[1] +
+                         v1[2] * v1[2] + v2[2] * v2[2] + v3[2] * v3[2] + v4[2] * v4[2];
+      const double xmas25 = xmas * RG_FOURTH;
+      double *o = &out[7 * (size_t)(part ? part[e] : part0 + (int)g)];
+      o[0] += S->eint[e] + S->eint[(size_t)S->numelc + e];
+      o[1] += xmas * va2 * RG_ONE_OVER_8;
+      o[2] += xmas25 * vxa;
+      o[3] += xmas25 * vya;
+      o[4] += xmas25 * vza;
+      if (S->offg[e] != RG_ZERO) o[5] += xmas;
+      o[6] += S->ehou[e];
+    }
+  }
+}
+
+int group_count(const Shells *S) { return (int)S->groups.size(); }
+
 void energy(const Shells *S, double &eint, double &ehour) {
   eint = 0;
   ehour = 0;

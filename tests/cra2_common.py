@@ -93,6 +93,34 @@ def check_time_history(deck, recs, nodes, phase, tol=TH_TOL, dtol=5e-5, vtol=5e-
     assert len(th_t) == 50
 
 
+# per-part time history (the 7 sums SBILAN / CBILAN accumulate, relative;
+# momentum relative to the part's momentum norm): a few times the oracle's
+# differences (IE 8e-7, KE 1.3e-5, momentum 2.2e-5, MASS 3.4e-8, HE 3.7e-6)
+PART_TOL = dict(IE=3e-6, KE=5e-5, MOM=1e-4, MASS=1e-7, HE=1.5e-5)
+
+
+def check_part_history(deck, recs, phase, tol=PART_TOL, tmatch=1e-3):
+    """Every time-history output of the part variables IE, KE, XMOM, YMOM,
+    ZMOM, MASS, HE against rec["parts"] (npart x 7) of the matching cycle
+    (its time within tmatch time steps of the output's)."""
+    pre = "th1" if phase == 0 else "th2"
+    th_t, th_p = deck[pre + "_time"], deck[pre + "_part"]
+    tts = np.array([r["tt"] for r in recs[phase]])
+    for k, t in enumerate(th_t):
+        c = int(np.argmin(np.abs(tts - float(t))))
+        assert abs(tts[c] - float(t)) <= tmatch * recs[phase][c]["dt2"], (phase, k, t, tts[c])
+        ours = recs[phase][c]["parts"]
+        ref = th_p[k].astype(np.float64)
+        assert ours.shape == (ref.shape[0], 7)
+        for p in range(ref.shape[0]):
+            mom = np.abs(ref[p, 2:5]).max()
+            for q, name in enumerate(("IE", "KE", "XMOM", "YMOM", "ZMOM", "MASS", "HE")):
+                rel = tol["MOM"] if name.endswith("MOM") else tol[name]
+                scale = mom if name.endswith("MOM") else abs(ref[p, q])
+                assert abs(ours[p, q] - ref[p, q]) <= rel * scale + 1e-12, (phase, k, p, name,
+                                                                             ours[p, q], ref[p, q])
+
+
 def listing_from_velocities(MS, IN, V0, V1, VR0, VR1, dt1, dt2):
     """ECRIT's kinetic energies from the velocities before (V0 = V at
     t - DT1/2) and after (V1 = V at t + DT2/2) a cycle: the cycle's

@@ -20,8 +20,8 @@ gives the cycle's acceleration for ECRIT's V + DT1/2 A.
 import numpy as np
 import pytest
 
-from cra2_common import (check_printed, check_time_history, listing_from_velocities, load_deck,
-                         printed_ok, run_both)
+from cra2_common import (PART_TOL, check_part_history, check_printed, check_time_history,
+                         listing_from_velocities, load_deck, printed_ok, run_both)
 from openradioss_gb300 import model as M
 
 pytestmark = pytest.mark.gpu
@@ -45,6 +45,7 @@ def gpu_run(deck, precision):
         return nd["D"], nd["V"]
 
     def step():
+        e.part_sums_due()
         e.cycle(1)
         t = e.time()
         en = e.energy()
@@ -52,7 +53,7 @@ def gpu_run(deck, precision):
         rec = listing_from_velocities(m.MS, m.IN, state["V0"], nd["V"], state["VR0"], nd["VR"],
                                       t["dt1"], t["dt2"])
         rec.update(tt=t["tt"] - t["dt2"], dt2=t["dt2"], neltst=t["neltst"], eint=en["eint"],
-                   ehour=en["ehour"])
+                   ehour=en["ehour"], parts=e.part_sums())
         return rec
 
     try:
@@ -88,6 +89,25 @@ def test_fp64_time_history(deck, fp64, phase):
     check_time_history(deck, fp64[0], fp64[1], phase)
 
 
+@pytest.mark.parametrize("phase", [0, 1])
+def test_fp64_part_time_history(deck, fp64, phase):
+    """The device's per-part sums (rg_part_sums, taken every cycle here)
+    against the reference's /TH/PART outputs, within the oracle's
+    tolerances."""
+    check_part_history(deck, fp64[0], phase)
+
+
+@pytest.mark.parametrize("phase", [0, 1])
+def test_mixed_part_time_history(deck, mixed, phase):
+    """Mixed form: the per-part sums within the mixed form's bound (1e-4
+    relative, the mass to its FP64 accuracy: it depends on coordinates and
+    the FP64 thickness only).  The mixed run's cycle times stay within
+    1e-2 of a step of the reference's (3e-7 relative by t = 4.6)."""
+    tol = {k: max(v, 1e-4) for k, v in PART_TOL.items()}
+    tol["MASS"] = 1e-6
+    check_part_history(deck, mixed[0], phase, tol=tol, tmatch=1e-2)
+
+
 def test_fp64_cycle_count(deck, fp64):
     # run 1 stops at the same cycle as the reference: the restart's cycle 0
     # is printed at t = 2.501
@@ -112,8 +132,9 @@ def test_mixed_within_bound(deck, mixed, phase):
 
 def test_fp64_matches_oracle(deck, fp64):
     """Over the first 200 cycles (before the buckling amplifies round-off)
-    the FP64 form and the oracle agree to round-off: energies and time step
-    within 1e-12 relative, time-history node values within 1e-9."""
+    the FP64 form and the oracle agree to round-off: energies, time step and
+    the per-part sums within 1e-12 relative, time-history node values within
+    1e-9."""
     from oracle.oracle import OracleModel
 
     o = OracleModel(M.model_from_deck(deck, "cra2"))
@@ -124,7 +145,9 @@ def test_fp64_matches_oracle(deck, fp64):
         nd = o.nodes()
         nodes.append(np.concatenate([nd["D"][:, nid].T, nd["V"][:, nid].T], axis=1))
         o.cycle(1)
-        recs.append(o.record())
+        r = o.record()
+        r["parts"] = o.part_sums()
+        recs.append(r)
     g, gn = fp64[0][0], fp64[1][0]
     for c in range(200):
         for key in ("eint", "ekin", "dt2", "ehour", "tt"):
@@ -135,3 +158,7 @@ def test_fp64_matches_oracle(deck, fp64):
         if g[c]["neltst"] != recs[c]["neltst"]:
             assert abs(g[c]["dt2"] - recs[c]["dt2"]) <= 1e-13 * recs[c]["dt2"], c
         assert np.abs(gn[c] - nodes[c]).max() <= 1e-9, c
+        # per-part sums (chunked fixed-order tree vs sequential sums)
+        pg, po = g[c]["parts"], recs[c]["parts"]
+        scale = np.maximum(np.abs(po), np.abs(po[:, 2:5]).max(axis=1, keepdims=True))
+        assert (np.abs(pg - po) <= 1e-12 * scale + 1e-12).all(), (c, pg, po)

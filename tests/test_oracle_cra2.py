@@ -13,12 +13,14 @@ history files (float32, every 0.05).  The oracle must reproduce the printed
 table to the last printed digit, the controlling element of every printed
 cycle and the time histories to within the tolerances below, which are a few
 times the differences seen (IE 4e-7, KE 4e-8, DT 6e-7 relative; node
-displacements 1.3e-5, velocities 9e-4 absolute, on values of order 10).
+displacements 1.3e-5, velocities 9e-4 absolute, on values of order 10), and
+the per-part time histories of the three parts (PART_TOL in cra2_common).
 """
 import numpy as np
 import pytest
 
-from cra2_common import check_printed, check_time_history, load_deck, printed_ok, run_both
+from cra2_common import (check_part_history, check_printed, check_time_history, load_deck,
+                         printed_ok, run_both)
 from openradioss_gb300 import model as M
 
 
@@ -56,7 +58,9 @@ def run(deck):
     def step():
         o.cycle(1)
         assert o.error() == 0
-        return o.record()
+        r = o.record()
+        r["parts"] = o.part_sums()
+        return r
 
     def nodes_of():
         nd = o.nodes()
@@ -88,6 +92,39 @@ def test_printed_table(deck, run, phase):
 @pytest.mark.parametrize("phase", [0, 1])
 def test_time_history(deck, run, phase):
     check_time_history(deck, run[0], run[1], phase)
+
+
+@pytest.mark.parametrize("phase", [0, 1])
+def test_part_time_history(deck, run, phase):
+    """The per-part sums (CBILAN's PARTSAV with CHVIS3's hourglass energy)
+    against the reference's /TH/PART outputs of the three parts: IE, KE,
+    momentum, mass and hourglass energy at every time-history time."""
+    check_part_history(deck, run[0], phase)
+
+
+def test_part_history_detects_wrong_part_map(deck):
+    """Planted in the oracle on the CPU: the shells' part numbers rotated
+    (part p's elements counted in part p + 1) no longer match the
+    reference's per-part outputs."""
+    from oracle.oracle import OracleModel
+
+    m = M.model_from_deck(deck, "cra2")
+    o = OracleModel(m)
+    o.set_record(True)
+    part = np.concatenate([np.full(g.ixc.shape[1], (k + 1) % 3, np.int32)
+                           for k, g in enumerate(m.shells)])
+    o.set_parts(3, None, part)
+    th_t, th_p = deck["th1_time"], deck["th1_part"]
+    recs = []
+    while o.time()["tt"] < float(th_t[3]) + 1e-9:
+        o.cycle(1)
+        r = o.record()
+        r["parts"] = o.part_sums()
+        recs.append(r)
+    short = dict(deck)
+    short["th1_time"], short["th1_part"] = th_t[:4], th_p[:4]
+    with pytest.raises(AssertionError):
+        check_part_history(short, (recs, []), 0)
 
 
 def _printed_misses(deck, mutate, ncyc=1501):
