@@ -8,6 +8,13 @@
 
 namespace rg {
 
+// Resident 128-thread blocks per SM the FP32 hexa kernel's register budget
+// is cut for: 6 (80 registers) -- 2.1M-hexa block 0.249 ms, against 0.251
+// at 5 (96 registers) and 0.264 at 7 (72).
+#ifndef RG_HEXA_MIXED_BLK128
+#define RG_HEXA_MIXED_BLK128 6
+#endif
+
 template <typename ER, int LAW, int JCVT, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 hexa_kernel(const HexaParams P, const HexaArrays<ER> A, const NodeView N,
@@ -40,7 +47,7 @@ static void launch_nt(const HexaParams &P, const HexaArrays<ER> &A, const NodeVi
   // 100 bytes per thread spill to L1: measured faster than 4, 5 or 7
   // blocks; 64-thread blocks keep the same register budget); the FP64 form
   // needs its ~250 registers
-  constexpr int MINB = std::is_same<ER, float>::value ? 6 * 128 / NT : 1;
+  constexpr int MINB = std::is_same<ER, float>::value ? RG_HEXA_MIXED_BLK128 * 128 / NT : 1;
   const int nb = (P.nel + NT - 1) / NT;
   if (P.jcvt)
     hexa_kernel<ER, LAW, 1, NT, MINB><<<nb, NT, 0, s>>>(P, A, N, fsky, dp, T, status, F);
