@@ -175,8 +175,10 @@ def element_bytes(model, prec):
         ne = model.numels
         law = model.hexa[0].mat["mtn"]
         # reads NC, IADS (8 int32 each), OFF, SIG(6), QVIS (ER), EINT, RHO,
-        # VOL0, EHOU (FP64), [PLA, EPSD]; node X4, V4 (32 B each)
-        rd = 32 + 32 + er * (1 + 6 + 1) + 8 * 4 + (2 * er if law == 2 else 0) + 64.0 * nn / ne
+        # VOL0, EHOU (FP64), [PLA, EPSD]; node records X4, V4 (32 B each;
+        # mixed: the FP32 copies XF 32 B, VF 16 B)
+        gather = 64.0 if prec == 0 else 48.0
+        rd = 32 + 32 + er * (1 + 6 + 1) + 8 * 4 + (2 * er if law == 2 else 0) + gather * nn / ne
         # writes SIG, QVIS, EINT, RHO, EHOU, [PLA, EPSD], 8 slots
         wr = er * (6 + 1) + 8 * 3 + (2 * er if law == 2 else 0) + 8 * slot
         spn = 8.0 * ne / nn
@@ -188,8 +190,10 @@ def element_bytes(model, prec):
     npt = model.shells[0].npt
     # reads IX, IADC (4 int32 each), DEGEN, OFF, THKE (ER), THK (FP64),
     # FOR(5), MOM(3), HOUR(5), GSTR(8) (ER), EINT(2), EHOU (FP64),
-    # per point SIG(5), PLA, EPSD (ER); node X4, V4, VR4 (32 B each)
-    rd = 16 + 16 + 4 + 2 * er + 8 + 21 * er + 24 + npt * 7 * er + 96.0 * nn / nc
+    # per point SIG(5), PLA, EPSD (ER); node records X4, V4, VR4 (32 B
+    # each; mixed: the FP32 copies XF 32 B, VF and VRF 16 B)
+    gather = 96.0 if prec == 0 else 64.0
+    rd = 16 + 16 + 4 + 2 * er + 8 + 21 * er + 24 + npt * 7 * er + gather * nn / nc
     # writes GSTR(8), EPSDG, THK, EINT(2), FOR(5), MOM(3), HOUR(5), EHOU,
     # per point SIG(5), PLA, EPSD; 4 slots of forces + 4 of moments
     wr = 22 * er + 8 + 16 + 8 + npt * 7 * er + 4 * 2 * slot
