@@ -272,6 +272,11 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
     const double DT1 = DT1in >= 0.0 ? DT1in : T->dt2;
     const R dt1 = (R)DT1;
     const int tid = threadIdx.x;
+    // the connectivity first: its loads head the gather chain, and the
+    // staging below (asm with a memory clobber) would keep them behind it
+    int nn[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) nn[k] = __ldg(S.ix + k * nc + e);
     // staged form: the whole element state is requested now, into this
     // thread's shared-memory slots, and waited for at its first use (CSTRA3)
     if constexpr (STAGE) {
@@ -297,9 +302,6 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       cp_async_commit();
     }
     // ---- CCOOR3 ----
-    int nn[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) nn[k] = __ldg(S.ix + k * nc + e);
     R vl[4][3], vrl[4][3];
     const R offg = S.offg[e];
     const R off = smin((R)RG_ONE, fabs(offg));
