@@ -539,7 +539,9 @@ def run_ours(args, rank, world, local_rank):
                 "call": "rg_cycle_host: whole cycle (elements, PARITH/ON assembly, time step, "
                         "nodal update) with host node buffers",
                 "transfer": "inputs X, V, VR read in place from registered (pinned) host "
-                            "buffers by the upload kernel; outputs X, V, VR, D by DMA copies",
+                            "buffers by the upload kernel; outputs X, V, VR, D written in "
+                            "place into registered host buffers by one kernel (16-byte "
+                            "stores)",
                 "h2d_bytes_per_step": e2e[RG_PREC_FP64]["h2d"],
                 "d2h_bytes_per_step": e2e[RG_PREC_FP64]["d2h"],
                 "mixed": world * ne * args.steps / e2e[RG_PREC_MIXED]["s"],
