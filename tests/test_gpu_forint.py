@@ -1,8 +1,9 @@
 """FORINT-level call (rg_forint_step) with registered host buffers -- the
-inputs read in place by the upload kernel -- against the same call with
-ordinary pageable buffers (staged copies): bitwise equal forces, moments,
-stiffnesses and time step, for a shell model (rotational slots) and a hexa
-model, in both arithmetic forms."""
+inputs read in place by the upload kernel, the outputs written in place by
+the assembly -- against the same call with ordinary pageable buffers (staged
+copies): bitwise equal forces, moments, stiffnesses and time step, for a
+shell model (rotational slots) and a hexa model (its moments and rotational
+stiffness come back zero), in both arithmetic forms."""
 import numpy as np
 import pytest
 
@@ -28,8 +29,8 @@ def test_forint_registered_equals_staged(kind, prec):
         v = np.ascontiguousarray(nd["V"].T)
         vr = np.ascontiguousarray(nd["VR"].T) if kind == "shell" else None
         f, st = np.full((n, 3), np.nan), np.full(n, np.nan)
-        fr = np.full((n, 3), np.nan) if kind == "shell" else None
-        sr = np.full(n, np.nan) if kind == "shell" else None
+        fr = np.full((n, 3), np.nan)
+        sr = np.full(n, np.nan)
         bufs = [a for a in (x, v, vr, f, st, fr, sr) if a is not None]
         if register:
             for a in bufs:
@@ -46,6 +47,8 @@ def test_forint_registered_equals_staged(kind, prec):
         if a[i] is not None:
             assert np.array_equal(a[i], b[i]), i
     assert a[4] == b[4] and a[5] == b[5]
+    if kind == "hexa":
+        assert (a[2] == 0).all() and (a[3] == 0).all()
 
 
 @pytest.mark.parametrize("registered", [True, False])
