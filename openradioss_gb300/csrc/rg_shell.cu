@@ -51,8 +51,8 @@ shell_kernel(const ShellParams P, const ShellArrays<ER> S, const NodeView N,
              const DtFinish F) {
   typedef ER R;
   constexpr bool STG = sizeof(ER) == 4;
-  __shared__ float s_stg[STG ? ShellStage<NPT>::nfloat * NT : 1];
-  __shared__ double s_stgd[STG ? ShellStage<NPT>::ndouble * NT : 1];
+  __shared__ __align__(16) float s_stg[STG ? ShellStage<NPT>::nfloat * NT : 1];
+  __shared__ __align__(16) double s_stgd[STG ? ShellStage<NPT>::ndouble * NT : 1];
   R dtmine = (R)RG_EP06;
   int elmin = -1;
   // warp tasks of 32 consecutive elements.  wtasks = 0: each warp does the

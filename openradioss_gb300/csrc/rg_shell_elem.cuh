@@ -31,6 +31,11 @@
 #include <vector>
 
 
+// Cooperative 16-byte staging of full warps (see shell_element).
+#ifndef RG_SHELL_COOP_STAGE
+#define RG_SHELL_COOP_STAGE 1
+#endif
+
 namespace rg {
 
 struct ShellParams {
@@ -278,9 +283,46 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
 #pragma unroll
     for (int k = 0; k < 4; k++) nn[k] = __ldg(S.ix + k * nc + e);
     // staged form: the whole element state is requested now, into this
-    // thread's shared-memory slots, and waited for at its first use (CSTRA3)
+    // thread's shared-memory slots, and waited for at its first use (CSTRA3).
+    // A full warp whose 32 elements start on a 16-byte boundary copies them
+    // cooperatively: each component of its 32 elements is 128 contiguous
+    // bytes (SoA), 8 lanes x 16 bytes, so one instruction moves 4 components
+    // (15 + 2 copies per thread for NPT = 5 instead of 59 of 4 or 8 bytes).
+    const int lane = tid & 31;
+    const int e0 = e - lane;
+    const bool coop = STAGE && RG_SHELL_COOP_STAGE && ((e0 & 3) == 0) && ((nc & 3) == 0) &&
+                      il - lane + 32 <= P.nel;
     if constexpr (STAGE) {
       constexpr int NT = SNT;
+      if (coop) {
+        __syncwarp();  // the warp's slots are free: its previous task read them
+        const int wb = tid - lane;
+        const int sub = lane & 7, grp = lane >> 3;
+#pragma unroll
+        for (int k = 0; k < (SG::nfloat + 3) / 4; k++) {
+          const int q = 4 * k + grp;
+          if (q < SG::nfloat) {
+            const ER *b;
+            if (q < SG_MOM) b = S.forc + q * nc;
+            else if (q < SG_HOUR) b = S.mom + (q - SG_MOM) * nc;
+            else if (q < SG_GSTR) b = S.hour + (q - SG_HOUR) * nc;
+            else if (q < SG_SIG) b = S.gstr + (q - SG_GSTR) * nc;
+            else if (q < SG::pla) b = S.sig + (q - SG_SIG) * nc;
+            else if (q < SG::epsd) b = S.pla + (q - SG::pla) * nc;
+            else b = S.epsd + (q - SG::epsd) * nc;
+            cp_async16(stg + q * NT + wb + 4 * sub, b + e0 + 4 * sub);
+          }
+        }
+        const int sub2 = lane & 15, grp2 = lane >> 4;
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          const int q = 2 * k + grp2;
+          if (q < SG::ndouble) {
+            const double *b = q == 0 ? S.eint : (q == 1 ? S.eint + nc : S.ehou);
+            cp_async16(stgd + q * NT + wb + 2 * sub2, b + e0 + 2 * sub2);
+          }
+        }
+      } else {
 #pragma unroll
       for (int c = 0; c < 5; c++) cp_async4(stg + (SG_FORC + c) * NT + tid, S.forc + c * nc + e);
 #pragma unroll
@@ -299,6 +341,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       cp_async8(stgd + 0 * NT + tid, S.eint + e);
       cp_async8(stgd + 1 * NT + tid, S.eint + nc + e);
       cp_async8(stgd + 2 * NT + tid, S.ehou + e);
+      }
       cp_async_commit();
     }
     // ---- CCOOR3 ----
@@ -567,6 +610,7 @@ __device__ __forceinline__ void shell_element(const ShellParams &P, const ShellA
       const R inc[8] = {exx, eyy, exy, eyz, exz, kxx, kyy, kxy};
       if constexpr (STAGE) {
         cp_async_wait_all();
+        if (coop) __syncwarp();  // the lanes' copies are the warp's
 #pragma unroll
         for (int c = 0; c < 8; c++)
           S.gstr[c * nc + e] = stg[(SG_GSTR + c) * SNT + tid] + inc[c];
