@@ -38,6 +38,7 @@ constexpr int MVSIZ = 128;  // group length (engine/share/spe_inc/mvsiz_p.inc)
 
 struct HexaGroup {
   int nft = 0, nel = 0, mtn = 1;
+  int add = 0;  // index of the or_hexa_group_add call (the default part)
   int ismstr = 4, jhbe = 1, jcvt = 0;
   // material / property values used on the path
   double rho0 = 0, g = 0, c1 = 0;  // PM(1), PM(22), PM(32)
@@ -151,6 +152,7 @@ struct Model {
   // per-part sums of the last recorded cycle (SBILAN / CBILAN): element ->
   // part maps (empty: one part per element group, hexa groups first)
   int npart = 0;
+  int nhexa_adds = 0;  // or_hexa_group_add calls: the default parts of hexas
   std::vector<int> part_hexa, part_shell;
   std::vector<double> psum;  // [npart][7]
 };
@@ -902,7 +904,7 @@ struct OrModelWrap {
 void part_sums(Model &M, rg_oracle_shell::Shells *sh) {
   const int nhg = (int)M.hg.size();
   const int npart = M.part_hexa.empty() && M.part_shell.empty()
-                        ? nhg + rg_oracle_shell::group_count(sh)
+                        ? M.nhexa_adds + rg_oracle_shell::group_count(sh)
                         : M.npart;
   M.psum.assign(7 * (size_t)npart, 0.0);
   for (int g = 0; g < nhg; g++) {
@@ -931,7 +933,7 @@ void part_sums(Model &M, rg_oracle_shell::Shells *sh) {
       sz = sz * RG_ONE_OVER_8;
       va2 = va2 * RG_ONE_OVER_8;
       const double xmas = G.rho0 * M.vol[e];
-      double *o = &M.psum[7 * (size_t)(M.part_hexa.empty() ? g : M.part_hexa[e])];
+      double *o = &M.psum[7 * (size_t)(M.part_hexa.empty() ? G.add : M.part_hexa[e])];
       o[0] += M.eint[e] * M.vol[e];
       o[1] += xmas * va2 * RG_HALF;
       o[2] += xmas * sx;
@@ -942,8 +944,8 @@ void part_sums(Model &M, rg_oracle_shell::Shells *sh) {
     }
   }
   rg_oracle_shell::part_sums(sh, M.X.data(), M.V.data(),
-                             M.part_shell.empty() ? nullptr : M.part_shell.data(), nhg,
-                             M.psum.data());
+                             M.part_shell.empty() ? nullptr : M.part_shell.data(),
+                             M.nhexa_adds, M.psum.data());
 }
 
 extern "C" {
@@ -996,6 +998,7 @@ int or_hexa_group_add(void *m, int nel, const int *ixs, int mtn,
   // Split into MVSIZ-long groups like the starter (SGRTAILS).
   for (int s = 0; s < nel; s += MVSIZ) {
     HexaGroup G;
+    G.add = M.nhexa_adds;
     G.nft = M.numels + s;
     G.nel = std::min(MVSIZ, nel - s);
     G.mtn = mtn;
@@ -1044,6 +1047,7 @@ int or_hexa_group_add(void *m, int nel, const int *ixs, int mtn,
   M.epsd.resize(M.numels, 0.0);
   M.ehou.resize(M.numels, 0.0);
   (void)old;
+  M.nhexa_adds += 1;
   return (int)M.hg.size() - 1;
 }
 

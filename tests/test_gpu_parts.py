@@ -76,6 +76,16 @@ def test_hexa_block_interleaved_parts(precision):
     assert abs(res[-1][0][:, 5].sum() - res[-1][1][:, 5].sum()) <= 1e-12 * res[-1][1][:, 5].sum()
 
 
+def test_hexa_default_parts():
+    """Without a map each hexa group added is a part, in the oracle too
+    (whose groups are split into MVSIZ-long element groups internally)."""
+    m = M.hexa_impact_block(20000, seed=3, law="law2")
+    res = _run_pair(m, 0, [1, 30])
+    for g, o, en in res:
+        assert g.shape == o.shape == (len(m.hexa), 7)
+        assert _close(g, o, 1e-12).all(), (g, o)
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_crash_box_parts(precision):
     m = M.crash_box(n_side=10, n_len=60, v0=20.0, vpert=1.0)
