@@ -179,7 +179,10 @@ int rg_synchronize(rg_ctx *ctx);
  * shells, may be NULL) and the element time step dt2t (min of DTFAC*DTX).
  * This is the per-cycle call a Fortran engine makes in place of FORINT +
  * ASSPAR4 (resol.F:4138-4858); the engine keeps its own nodal update.
- * Host buffers may be pinned with rg_host_register for full copy speed. */
+ * Host buffers may be pinned with rg_host_register: registered inputs are
+ * read in place, and registered outputs (F, FR aligned to 16 bytes) are
+ * written in place by the device.  For a model without rotations FR and
+ * STIFR come back zero. */
 int rg_forint_step(rg_ctx *ctx, const double *x, const double *v,
                    const double *vr, double dt1, double *f, double *stifn,
                    double *fr, double *stifr, double *dt2t, int *neltst);
@@ -193,7 +196,8 @@ int rg_forint_step(rg_ctx *ctx, const double *x, const double *v,
  * cycle's step.  Synchronous.  The device keeps the time-step record and the
  * element state.  In the mixed form the element volumes are re-anchored to
  * the given coordinates, as in rg_forint_step.  Registered host buffers
- * (rg_host_register) are read in place.  The reference's GPU shell path
+ * (rg_host_register) are read in place, and registered outputs aligned to
+ * 16 bytes are written in place by the device.  The reference's GPU shell path
  * moves the same arrays each cycle (shell_gpu_global_upload_nodes,
  * shell_gpu_driver.cu:149-185) but leaves the nodal update on the host. */
 int rg_cycle_host(rg_ctx *ctx, const double *x, const double *v, const double *vr,
