@@ -51,7 +51,7 @@ def test_forint_registered_equals_staged(kind, prec):
         assert (a[2] == 0).all() and (a[3] == 0).all()
 
 
-@pytest.mark.parametrize("registered", [True, False])
+@pytest.mark.parametrize("registered", [True, False, "unaligned"])
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("kind", ["shell", "hexa"])
 def test_cycle_host_equals_device_cycle(kind, prec, registered):
@@ -62,7 +62,8 @@ def test_cycle_host_equals_device_cycle(kind, prec, registered):
     re-anchored to the given coordinates), over 20 cycles, with the same
     time step sequence (FP64).  Registered buffers are read and written in
     place by the upload and download kernels; pageable ones go through the
-    staging copies -- both give the same results."""
+    staging copies, and so do the outputs of registered buffers that are not
+    16-byte aligned -- all give the same results."""
     from openradioss_gb300.engine import Engine
     m = (M.crash_box(n_side=5, n_len=10, vpert=1.0) if kind == "shell"
          else M.large_block(n=8, seed=2))
@@ -72,10 +73,21 @@ def test_cycle_host_equals_device_cycle(kind, prec, registered):
     e1.cycle(5)
     e2.cycle(5)
     nd = e2.nodes()
-    x = np.ascontiguousarray(nd["X"].T)
-    v = np.ascontiguousarray(nd["V"].T)
-    vr = np.ascontiguousarray(nd["VR"].T) if kind == "shell" else None
-    d = np.empty((n, 3))
+    def buf(init):
+        if registered != "unaligned":
+            return np.ascontiguousarray(init)
+        raw = np.empty(3 * n + 2)
+        off = 1 if raw.ctypes.data % 16 == 0 else 0  # 8 bytes past a 16-byte boundary
+        a = raw[off:off + 3 * n].reshape(n, 3)
+        a[:] = init
+        return a
+
+    x = buf(nd["X"].T)
+    v = buf(nd["V"].T)
+    vr = buf(nd["VR"].T) if kind == "shell" else None
+    d = buf(np.zeros((n, 3)))
+    if registered == "unaligned":
+        assert x.ctypes.data % 16 == 8
     bufs = [a for a in (x, v, vr, d) if a is not None] if registered else []
     for a in bufs:
         e2.host_register(a)
