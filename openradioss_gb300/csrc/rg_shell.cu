@@ -27,13 +27,16 @@ struct ShellDev {
 };
 
 // Block size and resident blocks per SM of the mixed kernel (its register
-// budget); the FP64 kernel runs 128-thread blocks, as many as its ~250
-// registers allow.
+// budget: 128 registers either way); the FP64 kernel runs 128-thread blocks,
+// as many as its ~250 registers allow.  64-thread blocks, 8 per SM: a block
+// ends -- and frees its place for the next -- when its two warps are done,
+// not four (crash box 36.9 -> 36.7 us from a flushed L2, 38.9 -> 38.3 us per
+// warm cycle, the same bits).
 #ifndef RG_SHELL_MIXED_NT
-#define RG_SHELL_MIXED_NT 128
+#define RG_SHELL_MIXED_NT 64
 #endif
 #ifndef RG_SHELL_MIXED_MINB
-#define RG_SHELL_MIXED_MINB 4
+#define RG_SHELL_MIXED_MINB 8
 #endif
 #ifndef RG_SHELL_F64_MINB
 #define RG_SHELL_F64_MINB 1
